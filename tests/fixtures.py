@@ -1,0 +1,36 @@
+"""Loads the committed golden fixtures (tests/golden/), made by tests/golden/make_golden.py
+from the reference library compiled unmodified."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def known_answers():
+    with open(os.path.join(GOLDEN, "known_answers.json")) as f:
+        cases = json.load(f)
+    out = []
+    for c in cases:
+        d = dict(c)
+        d["indices"] = np.array(c["indices"], np.uint32)
+        d["positions"] = np.array(c["positions"], np.float32)
+        for k, dt in (("attributes", np.float32), ("weights", np.float32), ("lock", np.uint8), ("expect", np.uint32)):
+            d[k] = None if c[k] is None else np.array(c[k], dt)
+        d["ref_output"] = np.array(c["ref_output"], np.uint32)
+        out.append(d)
+    return out
+
+
+def seeded_cases():
+    z = np.load(os.path.join(GOLDEN, "seeded_cases.npz"))
+    meta = json.loads(str(z["meta"]))
+    out = []
+    for i, m in enumerate(meta):
+        d = dict(m)
+        for k in ("indices", "positions", "attributes", "weights", "expect"):
+            key = f"{i}_{k}"
+            d[k] = z[key] if key in z else None
+        out.append(d)
+    return out

@@ -1,0 +1,272 @@
+"""Generates the committed golden fixtures for the simplifier parity tests.
+
+Run here, where the reference sources exist:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+It writes two files next to this script:
+
+* ``known_answers.json`` -- the simplifier known-answer cases of the reference's own
+  unit tests (demo/tests.cpp, simplify* functions). The literal vertex/index/lock
+  arrays are read from that file as text; the call arguments are the ones its
+  asserts use. Each case is run through the reference library compiled unmodified
+  (oracle/_ref/libmeshopt_ref.so) and the expected output is recorded together with
+  the assertion the reference test makes (exact buffer, count or error bound).
+* ``seeded_cases.npz`` -- seeded synthetic meshes (heightfields, attribute spheres,
+  lock-border patches, random lattice soups) with the reference library's outputs.
+
+The GPU machine has no reference tree; these fixtures carry its results there.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle  # noqa: E402
+from meshoptimizer_gb300 import workloads as W  # noqa: E402
+
+REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+TESTS_CPP = os.path.join(REFERENCE_ROOT, "demo", "tests.cpp")
+
+
+def _function_body(src: str, name: str) -> str:
+    m = re.search(r"static void " + re.escape(name) + r"\s*\([^)]*\)\s*\{", src)
+    if not m:
+        raise KeyError(name)
+    i, depth = m.end(), 1
+    while depth:
+        depth += {"{": 1, "}": -1}.get(src[i], 0)
+        i += 1
+    return src[m.end():i - 1]
+
+
+def _eval_number(tok: str):
+    tok = tok.strip()
+    tok = re.sub(r"(?<=[0-9.])f\b", "", tok)
+    tok = re.sub(r"(?<=[0-9])u\b", "", tok)
+    return eval(tok, {"__builtins__": {}}, {})  # literal arithmetic like 0 | (9 << 28)
+
+
+def _arrays(body: str) -> dict:
+    """All `type name[...] = { ... };` literal arrays in a function body (flattened)."""
+    out = {}
+    for m in re.finditer(r"(?:const\s+)?(float|unsigned int|unsigned char)\s+(\w+)(?:\[[^\]]*\])+\s*=\s*\{", body):
+        i, depth = m.end(), 1
+        while depth:
+            depth += {"{": 1, "}": -1}.get(body[i], 0)
+            i += 1
+        text = body[m.end():i - 1]
+        text = re.sub(r"//[^\n]*", "", text).replace("{", " ").replace("}", " ")
+        try:
+            vals = [_eval_number(t) for t in text.split(",") if t.strip()]
+        except SyntaxError:
+            continue  # initialisers that are not literals (e.g. conditional weights) are restated by the caller
+        out[m.group(2)] = (m.group(1), vals)
+    return out
+
+
+def _np(arrs, name):
+    t, v = arrs[name]
+    return np.array(v, dtype={"float": np.float32, "unsigned int": np.uint32, "unsigned char": np.uint8}[t])
+
+
+def known_answer_cases():
+    src = open(TESTS_CPP).read()
+    cases = []
+
+    def add(fn, name, idx, pos, stride, target, error, options=0, attrs=None, astride=0, weights=None, lock=None,
+            expect=None, expect_count=None, expect_error_lt=None, expect_error_near=None):
+        cases.append(dict(source=f"demo/tests.cpp:{fn}", name=name, indices=idx, positions=pos, stride=stride,
+                          target=target, error=error, options=options, attributes=attrs, attr_stride=astride,
+                          weights=weights, lock=lock, expect=expect, expect_count=expect_count,
+                          expect_error_lt=expect_error_lt, expect_error_near=expect_error_near))
+
+    a = _arrays(_function_body(src, "simplify"))
+    add("simplify", "simplify", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-2, expect=_np(a, "expected"), expect_error_lt=1e-4)
+
+    a = _arrays(_function_body(src, "simplifyStuck"))
+    add("simplifyStuck", "stuck_tetra", _np(a, "ib1"), _np(a, "vb1"), 12, 6, 1e-3, expect_count=12)
+    add("simplifyStuck", "stuck_strip_ok", _np(a, "ib2"), _np(a, "vb2"), 12, 6, 1e-3, expect_count=6)
+    add("simplifyStuck", "stuck_strip_flipped", _np(a, "ib3"), _np(a, "vb2"), 12, 6, 1e-3, expect_count=9)
+    add("simplifyStuck", "stuck_quad_corner", _np(a, "ib4"), _np(a, "vb4"), 12, 3, 1e-3, expect_count=6)
+    add("simplifyStuck", "stuck_quad_split", _np(a, "ib5"), _np(a, "vb5"), 12, 3, 1e-3, expect_count=6)
+
+    a = _arrays(_function_body(src, "simplifyFlip"))
+    add("simplifyFlip", "flip", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-3, expect=_np(a, "expected"), expect_count=24)
+
+    a = _arrays(_function_body(src, "simplifyDegenerate"))
+    add("simplifyDegenerate", "degenerate", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-3, expect=_np(a, "expected"), expect_count=6)
+
+    a = _arrays(_function_body(src, "simplifyLockBorder"))
+    add("simplifyLockBorder", "lock_border", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-3, options=1,
+        expect=_np(a, "expected"), expect_count=18)
+
+    # simplifyAttr builds its 8x3 grid with loops; the same construction, restated
+    body = _function_body(src, "simplifyAttr")
+    expected = _np(_arrays(body), "expected")
+    vb = np.zeros((24, 6), np.float32)
+    for y in range(8):
+        r = np.float32(0.8) + np.float32(y) * np.float32(0.05) if y < 4 else np.float32(0)
+        b = np.float32(0) if y < 4 else np.float32(0.8) + np.float32(7 - y) * np.float32(0.05)
+        for x in range(3):
+            vb[y * 3 + x] = [x, y, np.float32(0.03) * x + np.float32(0.03) * (y % 2) + (x == 2 and y == 7) * np.float32(0.03), r, r, b]
+    ib = []
+    for y in range(7):
+        for x in range(2):
+            ib += [(y + 0) * 3 + (x + 0), (y + 0) * 3 + (x + 1), (y + 1) * 3 + (x + 0),
+                   (y + 1) * 3 + (x + 0), (y + 0) * 3 + (x + 1), (y + 1) * 3 + (x + 1)]
+    ib = np.array(ib, np.uint32)
+    for skip_g in (False, True):
+        w = np.array([0.5, 0.0 if skip_g else 0.5, 0.5], np.float32)
+        add("simplifyAttr", f"attr_skip_g{int(skip_g)}", ib, vb.reshape(-1), 24, 18, 1e-2,
+            attrs=vb.reshape(-1)[3:].copy(), astride=24, weights=w, expect=expected, expect_count=18)
+
+    a = _arrays(_function_body(src, "simplifyLockFlags"))
+    add("simplifyLockFlags", "lock_flags", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-3, lock=_np(a, "lock"),
+        expect=_np(a, "expected"), expect_count=18)
+
+    a = _arrays(_function_body(src, "simplifyLockFlagsSeam"))
+    add("simplifyLockFlagsSeam", "lock_seam_none", _np(a, "ib"), _np(a, "vb"), 12, 0, 1.0, expect_count=0)
+    for name, cnt in (("lock0", 12), ("lock1", 18), ("lock2", 24), ("lock3", 24)):
+        add("simplifyLockFlagsSeam", f"lock_seam_{name}", _np(a, "ib"), _np(a, "vb"), 12, 0, 1.0, lock=_np(a, name), expect_count=cnt)
+
+    a = _arrays(_function_body(src, "simplifySparse"))
+    add("simplifySparse", "sparse", _np(a, "ib"), _np(a, "vb"), 12, 6, 1e-3, options=2, expect=_np(a, "expected"), expect_count=6)
+    add("simplifySparse", "sparse_attr", _np(a, "ib"), _np(a, "vb"), 12, 6, 1e-1, options=2, attrs=_np(a, "vba"), astride=4,
+        weights=_np(a, "aw"), lock=_np(a, "lock"), expect=_np(a, "expecteda"), expect_count=6)
+
+    a = _arrays(_function_body(src, "simplifyErrorAbsolute"))
+    add("simplifyErrorAbsolute", "error_absolute", _np(a, "ib"), _np(a, "vb"), 12, 18, 2.0, options=1 | 4,
+        expect_count=18, expect_error_near=(0.85, 0.01))
+
+    a = _arrays(_function_body(src, "simplifySeam"))
+    vb = _np(a, "vb")
+    add("simplifySeam", "seam", _np(a, "ib"), vb, 16, 12, 1.0, expect=_np(a, "expected"), expect_count=12,
+        expect_error_near=(0.1, 0.01))
+    add("simplifySeam", "seam_attr", _np(a, "ib"), vb, 16, 12, 2.0, attrs=vb[3:].copy(), astride=16,
+        weights=np.array([1.0], np.float32), expect=_np(a, "expected"), expect_count=12, expect_error_near=(0.1, 0.01))
+
+    a = _arrays(_function_body(src, "simplifySeamFake"))
+    add("simplifySeamFake", "seam_fake", _np(a, "ib"), _np(a, "vb"), 16, 0, 1.0, expect_count=6)
+
+    a = _arrays(_function_body(src, "simplifySeamAttr"))
+    vb = _np(a, "vb")
+    add("simplifySeamAttr", "seam_attr_lockborder", _np(a, "ib"), vb, 16, 12, 2.0, options=1, attrs=vb[3:].copy(), astride=16,
+        weights=np.array([1.0], np.float32), expect=_np(a, "expected"), expect_count=18, expect_error_near=(0.35, 0.01))
+
+    a = _arrays(_function_body(src, "simplifyDebug"))
+    add("simplifyDebug", "debug_kinds", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-2, options=1 << 30,
+        expect=_np(a, "expected"), expect_count=3, expect_error_lt=1e-4)
+    return cases
+
+
+def _run_ref(c):
+    """Calls the reference library with the case's exact buffers and strides."""
+    import ctypes as C
+    o = oracle.load("ref")
+    idx = np.ascontiguousarray(c["indices"], np.uint32)
+    pos = np.ascontiguousarray(c["positions"], np.float32)
+    vcount = len(pos) * 4 // c["stride"]
+    out = np.zeros(max(len(idx), 1), np.uint32)
+    err = C.c_float(0)
+    attrs = c["attributes"]
+    weights = c["weights"]
+    lock = c["lock"]
+    acount = 0 if weights is None else len(weights)
+    p = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    if attrs is None and lock is None:
+        n = o._simplify(p(out), p(idx), len(idx), p(pos), vcount, c["stride"], c["target"], c["error"], c["options"], C.byref(err))
+    else:
+        attrs = None if attrs is None else np.ascontiguousarray(attrs, np.float32)
+        n = o._simplify_attr(p(out), p(idx), len(idx), p(pos), vcount, c["stride"], p(attrs), c["attr_stride"],
+                             p(weights), acount, p(lock), c["target"], c["error"], c["options"], C.byref(err))
+    return out[:n].copy(), float(err.value)
+
+
+def _check_expectation(c, out, err):
+    if c["expect"] is not None:
+        assert np.array_equal(out[:len(c["expect"])], c["expect"]), c["name"]
+    if c["expect_count"] is not None:
+        assert len(out) == c["expect_count"], (c["name"], len(out))
+    if c["expect_error_lt"] is not None:
+        assert err < c["expect_error_lt"], c["name"]
+    if c["expect_error_near"] is not None:
+        v, tol = c["expect_error_near"]
+        assert abs(err - v) < tol, (c["name"], err)
+
+
+def _listify(v):
+    if isinstance(v, np.ndarray):
+        if v.dtype == np.float32:
+            return [float(x) for x in v]
+        return [int(x) for x in v]
+    return v
+
+
+def seeded_cases():
+    rng = np.random.default_rng(20261203)
+    cases = []
+    for n, amp, opt in ((9, 0.05, 0), (17, 0.05, 0), (33, 0.1, 1), (24, 0.0, 0)):
+        idx, pos = W.heightfield(n, seed=n, amp=amp)
+        cases.append(dict(name=f"heightfield_{n}_{opt}", indices=idx, positions=pos, target=W.target_count(len(idx), 0.25),
+                          error=1e-2, options=opt))
+    for lv in (2, 3, 4):
+        idx, pos, attr, w = W.octa_sphere(lv, seed=lv)
+        cases.append(dict(name=f"sphere_attr_{lv}", indices=idx, positions=pos, attributes=attr, weights=w,
+                          target=W.target_count(len(idx), 0.10), error=5e-3, options=0))
+        cases.append(dict(name=f"sphere_pos_{lv}", indices=idx, positions=pos, target=W.target_count(len(idx), 0.2),
+                          error=5e-2, options=0))
+    for g, (idx, pos) in enumerate(W.sphere_patches(6, seed=11, levels=5)):
+        cases.append(dict(name=f"patch_{g}", indices=idx, positions=pos, target=W.target_count(len(idx), 0.5),
+                          error=2e-2, options=1))
+    for s in range(8):
+        v = rng.integers(0, 10, size=(100, 3)).astype(np.float32)
+        idx = rng.integers(0, 100, size=3 * int(rng.integers(10, 120))).astype(np.uint32)
+        cases.append(dict(name=f"lattice_soup_{s}", indices=idx, positions=v, target=0, error=float(np.finfo(np.float32).max),
+                          options=int([0, 1, 4, 16][s % 4])))
+    for c in cases:
+        out, err = oracle.simplify("ref", c["indices"], c["positions"], c["target"], c["error"], c["options"],
+                                   attributes=c.get("attributes"), weights=c.get("weights"))
+        c["expect"], c["expect_error"] = out, err
+    return cases
+
+
+def main():
+    ka = known_answer_cases()
+    js = []
+    for c in ka:
+        out, err = _run_ref(c)
+        _check_expectation(c, out, err)
+        d = {k: _listify(v) for k, v in c.items()}
+        d["ref_output"] = [int(x) for x in out]
+        d["ref_error"] = err
+        js.append(d)
+    with open(os.path.join(HERE, "known_answers.json"), "w") as f:
+        json.dump(js, f, indent=None, separators=(",", ":"))
+    print(f"known answers: {len(js)} cases")
+
+    sc = seeded_cases()
+    blob = {}
+    meta = []
+    for i, c in enumerate(sc):
+        for k in ("indices", "positions", "attributes", "weights", "expect"):
+            if c.get(k) is not None:
+                blob[f"{i}_{k}"] = np.asarray(c[k])
+        meta.append(dict(name=c["name"], target=c["target"], error=c["error"], options=c["options"],
+                         expect_error=c["expect_error"], has_attr=c.get("attributes") is not None))
+    blob["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "seeded_cases.npz"), **blob)
+    print(f"seeded cases: {len(sc)}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,69 @@
+"""The CPU oracle (oracle/mo_oracle.c) pinned against the reference's own results:
+the known-answer cases of demo/tests.cpp and seeded meshes run through the reference
+library, both committed as fixtures under tests/golden/."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import fixtures
+
+
+def _run_port_raw(oracle, c):
+    """Calls the port with the case's exact buffers and strides (interleaved layouts kept)."""
+    o = oracle.load("port")
+    idx = np.ascontiguousarray(c["indices"])
+    pos = np.ascontiguousarray(c["positions"])
+    vcount = len(pos) * 4 // c["stride"]
+    out = np.zeros(max(len(idx), 1), np.uint32)
+    err = C.c_float(0)
+    p = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    attrs, weights, lock = c["attributes"], c["weights"], c["lock"]
+    acount = 0 if weights is None else len(weights)
+    n = o._simplify_attr(p(out), p(idx), len(idx), p(pos), vcount, c["stride"], p(attrs), c["attr_stride"],
+                         p(weights), acount, p(lock), c["target"], c["error"], c["options"], C.byref(err))
+    return out[:n].copy(), float(err.value)
+
+
+@pytest.mark.parametrize("case", fixtures.known_answers(), ids=lambda c: c["name"])
+def test_port_known_answers(port, case):
+    out, err = _run_port_raw(port, case)
+    assert np.array_equal(out, case["ref_output"])
+    assert err == np.float32(case["ref_error"])
+    if case["expect"] is not None:
+        assert np.array_equal(out[:len(case["expect"])], case["expect"])
+    if case["expect_count"] is not None:
+        assert len(out) == case["expect_count"]
+    if case["expect_error_lt"] is not None:
+        assert err < case["expect_error_lt"]
+    if case["expect_error_near"] is not None:
+        assert abs(err - case["expect_error_near"][0]) < case["expect_error_near"][1]
+
+
+@pytest.mark.parametrize("case", fixtures.seeded_cases(), ids=lambda c: c["name"])
+def test_port_seeded(port, case):
+    out, err = port.simplify("port", case["indices"], case["positions"], case["target"], case["error"], case["options"],
+                             attributes=case["attributes"], weights=case["weights"])
+    assert np.array_equal(out, case["expect"])
+    assert np.float32(err) == np.float32(case["expect_error"])
+
+
+def test_port_scale(port):
+    vb = np.array([0, 0, 0, 1, 0, 0, 0, 2, 0, 0, 0, 3], np.float32).reshape(-1, 3)
+    assert port.simplify_scale("port", vb) == 3.0  # demo/tests.cpp simplifyScale
+
+
+def test_port_fp64_close(port):
+    """The FP64 oracle stays within a small relative distance of the FP32 result error."""
+    from meshoptimizer_gb300 import workloads as W
+
+    idx, pos = W.heightfield(33, seed=3, amp=0.05)
+    t = W.target_count(len(idx), 0.25)
+    _, e32 = port.simplify("port", idx, pos, t, 1e-2, 0)
+    _, e64, _ = port.simplify("port", idx, pos, t, 1e-2, 0, fp64=True)
+    assert abs(e32 - e64) <= 0.05 * e64
+
+
+def test_port_empty(port):
+    out, err = port.simplify("port", np.zeros(0, np.uint32), np.zeros((3, 3), np.float32), 0, 1e-2, 0)
+    assert len(out) == 0 and err == 0
