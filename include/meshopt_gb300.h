@@ -1,0 +1,114 @@
+/*
+ * meshopt_gb300.h - C ABI of the GB300 (sm_103a) edge-collapse simplifier.
+ *
+ * The first group of entry points keeps the exact signatures of meshoptimizer.h, so a
+ * program linked against libmeshopt_gb300.so instead of libmeshoptimizer gets the same
+ * results (bit-identical index buffers) computed on the GPU. Pointers are HOST pointers,
+ * caller-owned, with the reference's rules for strides, aliasing and result_error == NULL.
+ *
+ * Errors: the reference has no error return (invalid input is an assert). Here a call that
+ * cannot run (unsupported option, CUDA error, invalid index) writes the input indices
+ * unchanged to destination, returns index_count, prints one line to stderr and records a
+ * nonzero status, queryable per thread with meshoptgpu_getLastStatus(). It never aborts
+ * the process and never falls back to a CPU implementation.
+ */
+#ifndef MESHOPT_GB300_H
+#define MESHOPT_GB300_H
+
+#include <stddef.h>
+
+#ifndef MESHOPTGPU_API
+#define MESHOPTGPU_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C"
+{
+#endif
+
+/* Option bits: same values as meshoptimizer.h:466-482. */
+enum
+{
+	meshopt_SimplifyLockBorder = 1 << 0,
+	meshopt_SimplifySparse = 1 << 1,
+	meshopt_SimplifyErrorAbsolute = 1 << 2,
+	meshopt_SimplifyPrune = 1 << 3,
+	meshopt_SimplifyRegularize = 1 << 4,
+	meshopt_SimplifyPermissive = 1 << 5,
+	meshopt_SimplifyRegularizeLight = 1 << 6,
+};
+
+/* vertex_lock flags: same values as meshoptimizer.h:488-495. */
+enum
+{
+	meshopt_SimplifyVertex_Lock = 1 << 0,
+	meshopt_SimplifyVertex_Protect = 1 << 1,
+	meshopt_SimplifyVertex_Priority = 1 << 2,
+};
+
+/* Replaces meshopt_simplify, meshoptimizer.h:513 (implementation src/simplifier.cpp:2628). */
+MESHOPTGPU_API size_t meshopt_simplify(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions,
+    size_t vertex_count, size_t vertex_positions_stride, size_t target_index_count, float target_error, unsigned int options, float* result_error);
+
+/* Replaces meshopt_simplifyWithAttributes, meshoptimizer.h:537 (src/simplifier.cpp:2635). */
+MESHOPTGPU_API size_t meshopt_simplifyWithAttributes(unsigned int* destination, const unsigned int* indices, size_t index_count,
+    const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, const float* vertex_attributes,
+    size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
+    size_t target_index_count, float target_error, unsigned int options, float* result_error);
+
+/* Replaces meshopt_simplifyScale, meshoptimizer.h:611 (src/simplifier.cpp:2938). */
+MESHOPTGPU_API float meshopt_simplifyScale(const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride);
+
+/* ---- additions with no counterpart in meshoptimizer.h ---- */
+
+enum
+{
+	meshoptgpu_StatusOk = 0,
+	meshoptgpu_StatusUnsupported = 1, /* an option this build does not implement on the GPU */
+	meshoptgpu_StatusInvalidArgument = 2,
+	meshoptgpu_StatusCudaError = 3,
+	meshoptgpu_StatusOutOfMemory = 4,
+};
+
+/* Status and message of the calling thread's last simplifier call. */
+MESHOPTGPU_API int meshoptgpu_getLastStatus(void);
+MESHOPTGPU_API const char* meshoptgpu_getLastMessage(void);
+
+/* Per-pass counters of the calling thread's last call: the quantities the reference
+ * prints under TRACE (src/simplifier.cpp:1625-1633). stop: 0 out of collapses,
+ * 1 error limit, 2 count limit, 3 error goal. */
+typedef struct meshoptgpu_PassStats
+{
+	unsigned int triangles, candidates, evaluated, done, skipped, invalid, stop, rounds;
+} meshoptgpu_PassStats;
+
+/* Copies up to max_passes entries; returns the number of passes of the last call. */
+MESHOPTGPU_API int meshoptgpu_getLastPassStats(meshoptgpu_PassStats* out, int max_passes);
+
+/* Device time (ms, CUDA events) of the phases of the calling thread's last call, when
+ * timing was enabled with meshoptgpu_setTiming(1): setup, adjacency, pick, rank, sort,
+ * perform, apply, total. Returns the number of values written (8). */
+MESHOPTGPU_API void meshoptgpu_setTiming(int enabled);
+MESHOPTGPU_API int meshoptgpu_getLastPhaseTimes(float* out8);
+
+/* Device-resident form of meshopt_simplifyWithAttributes: every array pointer is a DEVICE
+ * pointer on the current device, except attribute_weights (host, at most 32 floats).
+ * destination must hold index_count indices and may alias indices. Work is queued on
+ * `stream` (a cudaStream_t, or NULL for the legacy default stream) and the call returns
+ * once the result count is known. */
+MESHOPTGPU_API size_t meshoptgpu_simplifyDevice(unsigned int* destination, const unsigned int* indices, size_t index_count,
+    const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, const float* vertex_attributes,
+    size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
+    size_t target_index_count, float target_error, unsigned int options, float* result_error, void* stream);
+
+/* Bytes of device scratch one call on a mesh of this shape needs (for admission control). */
+MESHOPTGPU_API size_t meshoptgpu_workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count);
+
+/* Releases the calling thread's device scratch and streams. */
+MESHOPTGPU_API void meshoptgpu_releaseThreadResources(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

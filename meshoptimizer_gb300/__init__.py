@@ -1,0 +1,198 @@
+"""GB300-native quadric edge-collapse simplifier (meshopt_simplify / meshopt_simplifyWithAttributes).
+
+The product is the C ABI in ``include/meshopt_gb300.h``, implemented by the in-tree CUDA
+library ``meshoptimizer_gb300/libmeshopt_gb300.so`` (built by ``meshoptimizer_gb300.build``).
+This module is a thin ctypes mirror of that ABI for Python callers, tests and the
+benchmark: same function names, same argument meaning (numpy arrays in place of host
+pointers), same error behaviour (a nonzero status instead of an exception, plus
+``check=True`` to raise). There is no CPU implementation behind it: if the library is
+missing, ``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmeshopt_gb300.so")
+
+# option bits (meshoptimizer.h:466-482)
+SimplifyLockBorder = 1 << 0
+SimplifySparse = 1 << 1
+SimplifyErrorAbsolute = 1 << 2
+SimplifyPrune = 1 << 3
+SimplifyRegularize = 1 << 4
+SimplifyPermissive = 1 << 5
+SimplifyRegularizeLight = 1 << 6
+
+# vertex_lock flags (meshoptimizer.h:488-495)
+SimplifyVertex_Lock = 1 << 0
+SimplifyVertex_Protect = 1 << 1
+SimplifyVertex_Priority = 1 << 2
+
+STATUS_OK = 0
+STATUS_UNSUPPORTED = 1
+STATUS_INVALID_ARGUMENT = 2
+STATUS_CUDA_ERROR = 3
+STATUS_OUT_OF_MEMORY = 4
+
+# every symbol include/meshopt_gb300.h declares
+EXPORTS = [
+    "meshopt_simplify", "meshopt_simplifyWithAttributes", "meshopt_simplifyScale",
+    "meshoptgpu_getLastStatus", "meshoptgpu_getLastMessage", "meshoptgpu_getLastPassStats",
+    "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
+    "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources",
+]
+
+
+class PassStats(C.Structure):
+    _fields_ = [(n, C.c_uint) for n in ("triangles", "candidates", "evaluated", "done", "skipped", "invalid", "stop", "rounds")]
+
+
+class SimplifyError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load():
+    """Loads the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.isfile(LIB_PATH):
+        raise FileNotFoundError(f"{LIB_PATH} is not built; run meshoptimizer_gb300.build.build()")
+    lib = C.CDLL(LIB_PATH)
+    vp, sz, f32, u32 = C.c_void_p, C.c_size_t, C.c_float, C.c_uint
+    lib.meshopt_simplify.restype = sz
+    lib.meshopt_simplify.argtypes = [vp, vp, sz, vp, sz, sz, sz, f32, u32, vp]
+    lib.meshopt_simplifyWithAttributes.restype = sz
+    lib.meshopt_simplifyWithAttributes.argtypes = [vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp]
+    lib.meshopt_simplifyScale.restype = f32
+    lib.meshopt_simplifyScale.argtypes = [vp, sz, sz]
+    lib.meshoptgpu_getLastStatus.restype = C.c_int
+    lib.meshoptgpu_getLastMessage.restype = C.c_char_p
+    lib.meshoptgpu_getLastPassStats.restype = C.c_int
+    lib.meshoptgpu_getLastPassStats.argtypes = [vp, C.c_int]
+    lib.meshoptgpu_setTiming.argtypes = [C.c_int]
+    lib.meshoptgpu_getLastPhaseTimes.restype = C.c_int
+    lib.meshoptgpu_getLastPhaseTimes.argtypes = [vp]
+    lib.meshoptgpu_simplifyDevice.restype = sz
+    lib.meshoptgpu_simplifyDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp, vp]
+    lib.meshoptgpu_workspaceBytes.restype = sz
+    lib.meshoptgpu_workspaceBytes.argtypes = [sz, sz, sz]
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def last_status():
+    lib = load()
+    return int(lib.meshoptgpu_getLastStatus()), lib.meshoptgpu_getLastMessage().decode()
+
+
+def _check(check):
+    if check:
+        st, msg = last_status()
+        if st != STATUS_OK:
+            raise SimplifyError(st, msg)
+
+
+def simplify(indices, positions, target_index_count, target_error, options=0, attributes=None, weights=None, lock=None,
+             destination=None, check=True):
+    """meshopt_simplify / meshopt_simplifyWithAttributes on host arrays.
+
+    indices uint32 [I]; positions float32 [V, k>=3] (stride k*4 bytes); attributes float32 [V, a]
+    (or None) with weights float32 [a]; lock uint8 [V] or None. Returns (indices, result_error).
+    """
+    lib = load()
+    indices = np.ascontiguousarray(indices, dtype=np.uint32)
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    if positions.ndim == 1:
+        positions = positions.reshape(-1, 3)
+    out = destination if destination is not None else np.empty(max(len(indices), 1), np.uint32)
+    err = C.c_float(0)
+    V, pstride = positions.shape[0], positions.shape[1] * 4
+    if attributes is None and lock is None:
+        n = lib.meshopt_simplify(_p(out), _p(indices), len(indices), _p(positions), V, pstride, int(target_index_count),
+                                 float(target_error), int(options), C.byref(err))
+    else:
+        a = 0
+        astride = 0
+        if attributes is not None:
+            attributes = np.ascontiguousarray(attributes, dtype=np.float32)
+            weights = np.ascontiguousarray(weights, dtype=np.float32)
+            a, astride = attributes.shape[1], attributes.shape[1] * 4
+        if lock is not None:
+            lock = np.ascontiguousarray(lock, dtype=np.uint8)
+        n = lib.meshopt_simplifyWithAttributes(_p(out), _p(indices), len(indices), _p(positions), V, pstride,
+                                               _p(attributes), astride, _p(weights), a, _p(lock), int(target_index_count),
+                                               float(target_error), int(options), C.byref(err))
+    _check(check)
+    return out[:n].copy(), float(err.value)
+
+
+def simplify_raw(destination, indices, index_count, positions, vertex_count, positions_stride, target_index_count, target_error,
+                 options=0, attributes=None, attributes_stride=0, weights=None, attribute_count=0, lock=None, check=True):
+    """The C signature as is (numpy buffers with explicit counts and byte strides)."""
+    lib = load()
+    err = C.c_float(0)
+    n = lib.meshopt_simplifyWithAttributes(_p(destination), _p(indices), index_count, _p(positions), vertex_count, positions_stride,
+                                           _p(attributes), attributes_stride, _p(weights), attribute_count, _p(lock),
+                                           int(target_index_count), float(target_error), int(options), C.byref(err))
+    _check(check)
+    return int(n), float(err.value)
+
+
+def simplify_scale(positions):
+    lib = load()
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    return float(lib.meshopt_simplifyScale(_p(positions), positions.shape[0], positions.shape[1] * 4))
+
+
+def simplify_device(d_destination, d_indices, index_count, d_positions, vertex_count, positions_stride, target_index_count, target_error,
+                    options=0, d_attributes=0, attributes_stride=0, weights=None, d_lock=0, stream=0, check=True):
+    """meshoptgpu_simplifyDevice with raw device pointers (ints), e.g. from torch tensors' data_ptr()."""
+    lib = load()
+    err = C.c_float(0)
+    a = 0
+    if weights is not None:
+        weights = np.ascontiguousarray(weights, dtype=np.float32)
+        a = len(weights)
+    n = lib.meshoptgpu_simplifyDevice(C.c_void_p(d_destination), C.c_void_p(d_indices), index_count, C.c_void_p(d_positions), vertex_count,
+                                      positions_stride, C.c_void_p(d_attributes or None), attributes_stride, _p(weights), a,
+                                      C.c_void_p(d_lock or None), int(target_index_count), float(target_error), int(options), C.byref(err),
+                                      C.c_void_p(stream or None))
+    _check(check)
+    return int(n), float(err.value)
+
+
+def last_pass_stats():
+    lib = load()
+    buf = (PassStats * 128)()
+    n = lib.meshoptgpu_getLastPassStats(C.cast(buf, C.c_void_p), 128)
+    keys = [f[0] for f in PassStats._fields_]
+    return [{k: int(getattr(buf[i], k)) for k in keys} for i in range(min(n, 128))]
+
+
+def set_timing(enabled: bool):
+    load().meshoptgpu_setTiming(1 if enabled else 0)
+
+
+def last_phase_times():
+    out = (C.c_float * 8)()
+    load().meshoptgpu_getLastPhaseTimes(C.cast(out, C.c_void_p))
+    keys = ["setup", "adjacency", "pick", "rank", "sort", "perform", "apply", "total"]
+    return dict(zip(keys, [float(x) for x in out]))
+
+
+def workspace_bytes(index_count, vertex_count, attribute_count=0):
+    return int(load().meshoptgpu_workspaceBytes(index_count, vertex_count, attribute_count))

@@ -1,0 +1,233 @@
+// mo_prims.cu - device-wide exclusive scan and stable LSD radix sort.
+//
+// Both are plain HBM-streaming integer kernels: the scan reads each element twice and
+// writes it once (reduce pass + apply pass, with a small recursive scan of tile sums in
+// between); each radix pass reads the pairs twice (histogram + scatter) and writes them
+// once. Tiles are sized so that a grid of a few thousand blocks covers the 152 SMs.
+#include "mo_common.cuh"
+#include "mo_prims.cuh"
+
+namespace mogpu
+{
+
+namespace
+{
+
+__device__ __forceinline__ uint4 loadTile4(const unsigned int* in, size_t n, size_t i, bool aligned)
+{
+	if (aligned && i + 3 < n)
+		return *reinterpret_cast<const uint4*>(in + i);
+	uint4 r;
+	r.x = i + 0 < n ? in[i + 0] : 0u;
+	r.y = i + 1 < n ? in[i + 1] : 0u;
+	r.z = i + 2 < n ? in[i + 2] : 0u;
+	r.w = i + 3 < n ? in[i + 3] : 0u;
+	return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) kScanReduce(const unsigned int* __restrict__ in, size_t n, unsigned int* __restrict__ sums, bool aligned)
+{
+	__shared__ unsigned int smem[kScanThreads / 32 + 1];
+	size_t i = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+	uint4 v = loadTile4(in, n, i, aligned);
+	unsigned int s = v.x + v.y + v.z + v.w;
+	unsigned int total;
+	blockExclusiveScan<kScanThreads>(s, smem, &total);
+	if (threadIdx.x == 0)
+		sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) kScanApply(const unsigned int* in, unsigned int* out, size_t n, const unsigned int* __restrict__ tileoffs,
+    unsigned int* total, bool aligned)
+{
+	__shared__ unsigned int smem[kScanThreads / 32 + 1];
+	size_t i = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+	uint4 v = loadTile4(in, n, i, aligned);
+	unsigned int s = v.x + v.y + v.z + v.w;
+	unsigned int btotal;
+	unsigned int pre = blockExclusiveScan<kScanThreads>(s, smem, &btotal);
+	unsigned int base = tileoffs ? tileoffs[blockIdx.x] : 0u;
+	pre += base;
+	uint4 o;
+	o.x = pre;
+	o.y = o.x + v.x;
+	o.z = o.y + v.y;
+	o.w = o.z + v.z;
+	if (aligned && i + 3 < n)
+		*reinterpret_cast<uint4*>(out + i) = o;
+	else
+	{
+		if (i + 0 < n)
+			out[i + 0] = o.x;
+		if (i + 1 < n)
+			out[i + 1] = o.y;
+		if (i + 2 < n)
+			out[i + 2] = o.z;
+		if (i + 3 < n)
+			out[i + 3] = o.w;
+	}
+	if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+		*total = base + btotal;
+}
+
+size_t roundWords(size_t w)
+{
+	return (w + 63) & ~size_t(63);
+}
+
+void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream)
+{
+	size_t tiles = (n + kScanTile - 1) / kScanTile;
+	bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
+	if (tiles <= 1)
+	{
+		kScanApply<<<1, kScanThreads, 0, stream>>>(in, out, n, nullptr, total, aligned);
+		return;
+	}
+	unsigned int* sums = scratch;
+	kScanReduce<<<(unsigned)tiles, kScanThreads, 0, stream>>>(in, n, sums, aligned);
+	scanLevel(sums, sums, tiles, nullptr, scratch + roundWords(tiles), stream);
+	kScanApply<<<(unsigned)tiles, kScanThreads, 0, stream>>>(in, out, n, sums, total, aligned);
+}
+
+__global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* __restrict__ keys, size_t n, int shift, unsigned int* __restrict__ hist, unsigned int tiles)
+{
+	__shared__ unsigned int sh[kSortBins];
+	sh[threadIdx.x] = 0;
+	__syncthreads();
+	size_t base = (size_t)blockIdx.x * kSortTile + threadIdx.x;
+#pragma unroll 4
+	for (int j = 0; j < kSortItems; ++j)
+	{
+		size_t i = base + (size_t)j * kSortThreads;
+		if (i < n)
+			atomicAdd(&sh[(__ldg(keys + i) >> shift) & 0xFFu], 1u);
+	}
+	__syncthreads();
+	hist[(size_t)threadIdx.x * tiles + blockIdx.x] = sh[threadIdx.x];
+}
+
+// Stable scatter: elements are ranked in index order (sub-round j holds elements
+// j*256 .. j*256+255 of the tile; within it, warp w and lane l give the order), so equal
+// digits keep their input order; tiles are laid out by the digit-major scanned histogram.
+__global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
+    unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, size_t n, int shift, const unsigned int* __restrict__ hist, unsigned int tiles)
+{
+	// vin == nullptr stands for the identity values 0..n-1
+	__shared__ unsigned int base[kSortBins];
+	__shared__ unsigned int wcnt[2][kSortThreads / 32][kSortBins];
+
+	const unsigned int t = threadIdx.x, w = t >> 5, lane = t & 31;
+	base[t] = hist[(size_t)t * tiles + blockIdx.x];
+#pragma unroll
+	for (int q = 0; q < kSortThreads / 32; ++q)
+	{
+		wcnt[0][q][t] = 0;
+		wcnt[1][q][t] = 0;
+	}
+	__syncthreads();
+
+	size_t tile0 = (size_t)blockIdx.x * kSortTile;
+	for (int j = 0; j < kSortItems; ++j)
+	{
+		const int b = j & 1;
+		size_t i = tile0 + (size_t)j * kSortThreads + t;
+		bool valid = i < n;
+		unsigned int k = valid ? __ldg(kin + i) : 0u;
+		unsigned int v = valid ? (vin ? __ldg(vin + i) : (unsigned int)i) : 0u;
+		unsigned int d = valid ? ((k >> shift) & 0xFFu) : (0x100u + lane);
+		unsigned int peers = __match_any_sync(0xffffffffu, d);
+		unsigned int rank = __popc(peers & ((1u << lane) - 1u));
+		if (valid && lane == (unsigned)(__ffs(peers) - 1))
+			wcnt[b][w][d] = __popc(peers);
+		__syncthreads();
+		{
+			unsigned int run = base[t];
+#pragma unroll
+			for (int q = 0; q < kSortThreads / 32; ++q)
+			{
+				unsigned int c = wcnt[b][q][t];
+				wcnt[b][q][t] = run;
+				run += c;
+				wcnt[b ^ 1][q][t] = 0;
+			}
+			base[t] = run;
+		}
+		__syncthreads();
+		if (valid)
+		{
+			unsigned int pos = wcnt[b][w][d] + rank;
+			kout[pos] = k;
+			vout[pos] = v;
+		}
+	}
+}
+
+} // namespace
+
+size_t scanScratchWords(size_t n)
+{
+	size_t words = 64;
+	size_t tiles = (n + kScanTile - 1) / kScanTile;
+	while (tiles > 1)
+	{
+		words += roundWords(tiles);
+		tiles = (tiles + kScanTile - 1) / kScanTile;
+	}
+	return words;
+}
+
+void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream)
+{
+	if (n == 0)
+	{
+		if (total)
+			MO_CUDA_CHECK(cudaMemsetAsync(total, 0, sizeof(unsigned int), stream));
+		return;
+	}
+	scanLevel(in, out, n, total, scratch, stream);
+	MO_CUDA_CHECK(cudaGetLastError());
+}
+
+size_t radixScratchWords(size_t n)
+{
+	size_t tiles = (n + kSortTile - 1) / kSortTile;
+	size_t h = roundWords(tiles * kSortBins);
+	return h + scanScratchWords(tiles * kSortBins);
+}
+
+void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
+    unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream)
+{
+	if (n == 0)
+		return;
+	int passes = (bits + 7) / 8;
+	if (passes == 0)
+	{
+		MO_CUDA_CHECK(cudaMemcpyAsync(keys_out, keys_in, n * 4, cudaMemcpyDeviceToDevice, stream));
+		MO_CUDA_CHECK(cudaMemcpyAsync(vals_out, vals_in, n * 4, cudaMemcpyDeviceToDevice, stream));
+		return;
+	}
+	unsigned int tiles = unsigned((n + kSortTile - 1) / kSortTile);
+	unsigned int* hist = scratch;
+	unsigned int* sscratch = scratch + roundWords(size_t(tiles) * kSortBins);
+
+	const unsigned int* ks = keys_in;
+	const unsigned int* vs = vals_in;
+	for (int p = 0; p < passes; ++p)
+	{
+		// the last pass must land in *_out: pick the destination by parity from the end
+		bool to_out = ((passes - 1 - p) % 2) == 0;
+		unsigned int* kd = to_out ? keys_out : keys_tmp;
+		unsigned int* vd = to_out ? vals_out : vals_tmp;
+		int shift = p * 8;
+		kRadixHist<<<tiles, kSortThreads, 0, stream>>>(ks, n, shift, hist, tiles);
+		scanExclusive(hist, hist, size_t(tiles) * kSortBins, nullptr, sscratch, stream);
+		kRadixScatter<<<tiles, kSortThreads, 0, stream>>>(ks, vs, kd, vd, n, shift, hist, tiles);
+		ks = kd;
+		vs = vd;
+	}
+	MO_CUDA_CHECK(cudaGetLastError());
+}
+
+} // namespace mogpu

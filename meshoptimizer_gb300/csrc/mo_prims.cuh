@@ -1,0 +1,100 @@
+// mo_prims.cuh - integer primitives for the simplifier: block scans, a device-wide
+// exclusive scan, and a stable LSD radix sort of (key, value) pairs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+
+namespace mogpu
+{
+
+struct CudaError : std::runtime_error
+{
+	cudaError_t code;
+	CudaError(cudaError_t e, const char* expr, const char* file, int line)
+	    : std::runtime_error(std::string(cudaGetErrorString(e)) + " at " + file + ":" + std::to_string(line) + " (" + expr + ")"), code(e)
+	{
+	}
+};
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;                               // one uint4 per thread
+constexpr int kScanTile = kScanThreads * kScanItems;        // 1024 elements per block
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;        // 4096 pairs per block
+constexpr int kSortBins = 256;
+
+__device__ __forceinline__ unsigned int laneId()
+{
+	return threadIdx.x & 31;
+}
+
+__device__ __forceinline__ unsigned int warpInclusiveScan(unsigned int v)
+{
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1)
+	{
+		unsigned int n = __shfl_up_sync(0xffffffffu, v, o);
+		if (laneId() >= (unsigned)o)
+			v += n;
+	}
+	return v;
+}
+
+// Exclusive scan of one value per thread across a block of NT threads (NT multiple of 32,
+// at most 1024). Returns the exclusive prefix; *total receives the block sum. Uses `smem`
+// (NT/32 words) and synchronises the block twice.
+template <int NT>
+__device__ __forceinline__ unsigned int blockExclusiveScan(unsigned int v, unsigned int* smem, unsigned int* total)
+{
+	const int warps = NT / 32;
+	unsigned int inc = warpInclusiveScan(v);
+	unsigned int w = threadIdx.x >> 5;
+	if (laneId() == 31)
+		smem[w] = inc;
+	__syncthreads();
+	if (w == 0)
+	{
+		unsigned int s = laneId() < (unsigned)warps ? smem[laneId()] : 0;
+		unsigned int si = warpInclusiveScan(s);
+		if (laneId() < (unsigned)warps)
+			smem[laneId()] = si - s;
+		if (laneId() == warps - 1)
+			smem[warps] = si;
+	}
+	__syncthreads();
+	unsigned int r = smem[w] + inc - v;
+	*total = smem[warps];
+	return r;
+}
+
+// scratch words needed by scanExclusive for n elements
+size_t scanScratchWords(size_t n);
+
+// out[i] = sum(in[0..i)) for i < n; if total != nullptr, *total (device) = sum(in[0..n)).
+// in and out may alias. scratch: scanScratchWords(n) words of device memory.
+void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream);
+
+// scratch words needed by radixSortPairs for n pairs
+size_t radixScratchWords(size_t n);
+
+// Stable LSD radix sort of (keys, vals) on key bits [0, bits); vals_in == nullptr means
+// the values 0..n-1. Sorted result ends in
+// (keys_out, vals_out); keys_tmp/vals_tmp are ping-pong buffers of n elements. Input
+// arrays are left unchanged only when the pass count is even; callers treat them as scratch.
+void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
+    unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream);
+
+inline unsigned int gridFor(size_t n, int threads)
+{
+	size_t g = (n + threads - 1) / threads;
+	return unsigned(g ? g : 1);
+}
+
+} // namespace mogpu

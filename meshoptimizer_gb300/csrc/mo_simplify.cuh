@@ -1,0 +1,119 @@
+// mo_simplify.cuh - host interface of the device-resident edge-collapse simplifier.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <vector>
+
+#include "mo_prims.cuh"
+
+namespace mogpu
+{
+
+constexpr int kMaxAttributes = 32;   // src/simplifier.cpp:665
+constexpr int kMaxPassStats = 128;
+
+// One mesh to simplify; all array pointers are DEVICE pointers (except weights, which
+// live on the host: at most 32 floats, folded into kernel arguments).
+struct MeshDesc
+{
+	const unsigned int* indices = nullptr;
+	size_t index_count = 0;
+	const float* positions = nullptr;
+	size_t vertex_count = 0;
+	size_t positions_stride = 12; // bytes
+	const float* attributes = nullptr;
+	size_t attributes_stride = 0; // bytes
+	const float* weights = nullptr; // host
+	size_t attribute_count = 0;
+	const unsigned char* lock = nullptr;
+	size_t target_index_count = 0;
+	float target_error = 0.f;
+	unsigned int options = 0;
+};
+
+// Per-pass counters, the same quantities the reference prints under TRACE
+// (src/simplifier.cpp:1625-1633). stop: 0 out of collapses, 1 error limit, 2 count
+// limit, 3 error goal.
+struct PassStats
+{
+	unsigned int triangles;
+	unsigned int candidates;
+	unsigned int evaluated;
+	unsigned int done;
+	unsigned int skipped;
+	unsigned int invalid;
+	unsigned int stop;
+	unsigned int rounds;
+};
+
+struct RunResult
+{
+	size_t index_count = 0;
+	float result_error = 0.f;   // linear, scaled like the reference's *result_error
+	float result_error_sq = 0.f;
+	float scale = 0.f;
+	int passes = 0;
+	PassStats pass[kMaxPassStats];
+};
+
+// Device timings of the phases of one run (milliseconds, from CUDA events).
+struct PhaseTimes
+{
+	float setup = 0, adjacency = 0, pick = 0, rank = 0, sort = 0, perform = 0, apply = 0, total = 0;
+};
+
+// Debug copies of setup arrays (device -> host) for per-phase comparison with the oracle.
+struct SetupDump
+{
+	std::vector<unsigned int> remap, wedge, loop, loopback;
+	std::vector<unsigned char> kind;
+	std::vector<float> positions; // 3 per vertex
+	std::vector<float> quadrics;  // 11 per vertex
+	std::vector<float> attr_quadrics, attr_gradients;
+	size_t capacity = 0;
+	float scale = 0;
+};
+
+// Grow-only device arena; one per Simplifier.
+class DeviceArena
+{
+public:
+	~DeviceArena();
+	void reserve(size_t bytes);
+	char* base() const { return base_; }
+	size_t capacity() const { return cap_; }
+	void release();
+
+private:
+	char* base_ = nullptr;
+	size_t cap_ = 0;
+};
+
+class Simplifier
+{
+public:
+	explicit Simplifier(int device);
+	~Simplifier();
+
+	// Simplifies `mesh` on `stream`, writing the result index buffer to d_out (device,
+	// room for mesh.index_count indices). Blocks until the result count is known.
+	RunResult run(const MeshDesc& mesh, unsigned int* d_out, cudaStream_t stream, PhaseTimes* times = nullptr, SetupDump* dump = nullptr);
+
+	// meshopt_simplifyScale on device positions
+	float scale(const float* d_positions, size_t vertex_count, size_t stride, cudaStream_t stream);
+
+	int device() const { return device_; }
+	size_t arenaBytes() const { return arena_.capacity(); }
+
+	// Bytes of device scratch a run on this mesh shape needs (used by admission control).
+	static size_t workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count);
+
+private:
+	int device_;
+	DeviceArena arena_;
+	unsigned int* pinned_ = nullptr; // small pinned readback buffer
+};
+
+} // namespace mogpu

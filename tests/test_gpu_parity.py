@@ -1,0 +1,182 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the reference's results.
+
+Bar: the output index buffer and its count are bit-exact; result_error matches within
+1e-6 relative (it is in fact compared bit for bit where the pipeline is exact). The
+per-pass counters (triangles, candidates, evaluated, committed, skipped, flip-rejected,
+stop reason) are compared with the oracle's as a phase-level check.
+"""
+import numpy as np
+import pytest
+
+import fixtures
+import meshoptimizer_gb300 as mg
+from meshoptimizer_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-6
+GPU_OPTIONS = mg.SimplifyLockBorder | mg.SimplifyErrorAbsolute | mg.SimplifyRegularize | mg.SimplifyRegularizeLight
+
+
+def close(a, b):
+    return a == b or abs(a - b) <= REL_TOL * max(abs(a), abs(b))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from meshoptimizer_gb300 import build
+
+    build.build()
+    mg.load()
+
+
+def supported(options):
+    return (options & ~GPU_OPTIONS) == 0
+
+
+@pytest.mark.parametrize("case", fixtures.known_answers(), ids=lambda c: c["name"])
+def test_known_answers(case):
+    if not supported(case["options"]):
+        pytest.skip("option not implemented on the GPU path")
+    idx = case["indices"]
+    pos = case["positions"]
+    vcount = len(pos) * 4 // case["stride"]
+    out = np.zeros(max(len(idx), 1), np.uint32)
+    attrs, weights, lock = case["attributes"], case["weights"], case["lock"]
+    n, err = mg.simplify_raw(out, idx, len(idx), pos, vcount, case["stride"], case["target"], case["error"], case["options"],
+                             attributes=attrs, attributes_stride=case["attr_stride"], weights=weights,
+                             attribute_count=0 if weights is None else len(weights), lock=lock)
+    assert np.array_equal(out[:n], case["ref_output"])
+    assert close(err, case["ref_error"])
+
+
+@pytest.mark.parametrize("case", fixtures.seeded_cases(), ids=lambda c: c["name"])
+def test_seeded_fixtures(case):
+    out, err = mg.simplify(case["indices"], case["positions"], case["target"], case["error"], case["options"],
+                           attributes=case["attributes"], weights=case["weights"])
+    assert np.array_equal(out, case["expect"])
+    assert close(err, case["expect_error"])
+
+
+def _compare_with_oracle(port, idx, pos, target, error, options=0, attributes=None, weights=None, lock=None, stats=True):
+    ref_out, ref_err, ref_st = port.simplify("port", idx, pos, target, error, options, attributes=attributes, weights=weights,
+                                              lock=lock, stats=True)
+    out, err = mg.simplify(idx, pos, target, error, options, attributes=attributes, weights=weights, lock=lock)
+    st = mg.last_pass_stats()
+    assert len(out) == len(ref_out)
+    assert np.array_equal(out, ref_out)
+    assert close(err, ref_err)
+    if stats:
+        assert len(st) == ref_st["passes"]
+        for p, s in enumerate(st):
+            got = (s["triangles"], s["candidates"], s["evaluated"], s["done"], s["skipped"], s["invalid"], s["stop"])
+            want = tuple(ref_st[k][p] for k in ("tri", "cand", "evaluated", "done", "skipped", "invalid", "stop"))
+            assert got == want, f"pass {p}: {got} != {want}"
+    return out, err
+
+
+@pytest.mark.parametrize("n,opt", [(16, 0), (64, 0), (64, mg.SimplifyLockBorder), (256, 0)])
+def test_heightfield(port, n, opt):
+    idx, pos = W.heightfield(n, seed=n + opt, amp=0.05)
+    _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.25), 1e-2, opt)
+
+
+@pytest.mark.parametrize("levels", [3, 5, 7])
+def test_sphere_attributes(port, levels):
+    idx, pos, attr, w = W.octa_sphere(levels, seed=levels)
+    _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.1), 5e-3, 0, attributes=attr, weights=w)
+
+
+def test_sphere_attributes_2m(port):
+    """The 2,097,152-triangle attribute sphere (normals w=0.5, UV w=1.0, 10%, 5e-3)."""
+    c = W.config_sphere_attr(9)
+    _compare_with_oracle(port, c["indices"], c["positions"], c["target"], c["error"], 0, attributes=c["attributes"],
+                         weights=c["weights"])
+
+
+def test_fractal_heightfield(port):
+    c = W.config_fractal_3163(1024)
+    _compare_with_oracle(port, c["indices"], c["positions"], c["target"], c["error"], 0)
+
+
+def test_patches_lock_border(port):
+    for g, (idx, pos) in enumerate(W.sphere_patches(24, seed=5, levels=5)):
+        _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.5), 2e-2, mg.SimplifyLockBorder)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_lattice_soup(port, seed):
+    rng = np.random.default_rng(seed)
+    pos = rng.integers(0, 10, size=(100, 3)).astype(np.float32)
+    idx = rng.integers(0, 100, size=3 * int(rng.integers(1, 150))).astype(np.uint32)
+    opt = int(rng.choice([0, mg.SimplifyLockBorder, mg.SimplifyErrorAbsolute, mg.SimplifyRegularize]))
+    attrs = weights = lock = None
+    if seed % 2:
+        attrs = rng.random((100, 3)).astype(np.float32)
+        weights = np.array([0.5, 0.0, 1.0], np.float32)
+    if seed % 3 == 0:
+        lock = rng.choice([0, 0, 1, 4], size=100).astype(np.uint8)
+    _compare_with_oracle(port, idx, pos, 0, float(np.finfo(np.float32).max), opt, attributes=attrs, weights=weights, lock=lock)
+
+
+def test_seams_and_duplicates(port):
+    """Grid with duplicated vertices on a seam and random extra wedges."""
+    rng = np.random.default_rng(7)
+    idx, pos = W.heightfield(40, seed=7, amp=0.02)
+    V = len(pos)
+    dup = rng.choice(V, size=V // 5, replace=False)
+    newid = {int(v): V + i for i, v in enumerate(dup)}
+    pos2 = np.concatenate([pos, pos[dup]])
+    tri = idx.reshape(-1, 3).copy()
+    flip = rng.random(len(tri)) < 0.4
+    for t in np.nonzero(flip)[0]:
+        tri[t] = [newid.get(int(v), int(v)) for v in tri[t]]
+    idx2 = tri.reshape(-1).astype(np.uint32)
+    attrs = rng.random((len(pos2), 2)).astype(np.float32)
+    _compare_with_oracle(port, idx2, pos2, W.target_count(len(idx2), 0.3), 2e-2, 0)
+    _compare_with_oracle(port, idx2, pos2, W.target_count(len(idx2), 0.3), 2e-2, 0, attributes=attrs,
+                         weights=np.array([1.0, 0.5], np.float32))
+
+
+def test_empty_and_trivial(port):
+    pos = np.zeros((3, 3), np.float32)
+    out, err = mg.simplify(np.zeros(0, np.uint32), pos, 0, 1e-2)
+    assert len(out) == 0 and err == 0
+    idx, pos = W.heightfield(8, seed=1)
+    out, err = mg.simplify(idx, pos, len(idx), 1e-2)   # target >= input: no pass runs
+    assert np.array_equal(out, idx) and err == 0
+
+
+def test_special_values(port):
+    """NaN positions never weld, -0 welds with +0, degenerate and duplicate triangles."""
+    idx, pos = W.heightfield(20, seed=3, amp=0.05)
+    pos = pos.copy()
+    pos[5] = [np.nan, 0.2, 0.1]
+    pos[50, 0] = -0.0
+    z = pos[:, 2] == 0
+    pos[z, 2] = -0.0
+    tri = idx.reshape(-1, 3)
+    extra = np.array([[1, 1, 2], [3, 4, 3], tri[10], tri[11]], np.uint32)
+    idx2 = np.concatenate([tri, extra]).reshape(-1).astype(np.uint32)
+    _compare_with_oracle(port, idx2, pos, W.target_count(len(idx2), 0.25), 5e-2, 0)
+
+
+def test_strided_positions_and_alias(port):
+    idx, pos = W.heightfield(48, seed=9, amp=0.05)
+    wide = np.concatenate([pos, np.ones((len(pos), 5), np.float32)], axis=1)  # 32-byte stride
+    ref_out, ref_err = port.simplify("port", idx, wide, W.target_count(len(idx), 0.25), 1e-2, 0)
+    buf = idx.copy()
+    n, err = mg.simplify_raw(buf, buf, len(buf), wide, len(wide), 32, W.target_count(len(idx), 0.25), 1e-2, 0)
+    assert np.array_equal(buf[:n], ref_out) and close(err, ref_err)
+
+
+def test_scale():
+    vb = np.array([0, 0, 0, 1, 0, 0, 0, 2, 0, 0, 0, 3], np.float32).reshape(-1, 3)
+    assert mg.simplify_scale(vb) == 3.0
+
+
+def test_unsupported_option_reports_status():
+    idx, pos = W.heightfield(8, seed=1)
+    out, err = mg.simplify(idx, pos, 0, 1e-2, mg.SimplifyPermissive, check=False)
+    st, msg = mg.last_status()
+    assert st == mg.STATUS_UNSUPPORTED and np.array_equal(out, idx)
