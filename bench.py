@@ -1,0 +1,356 @@
+"""Benchmark of the GB300 edge-collapse simplifier.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload NAME]
+
+Default workload: meshopt_simplifyWithAttributes on the 2,097,152-triangle displaced
+octahedron sphere (normals w=0.5, equirectangular UV w=1.0 with the seam split, 10% target,
+target_error 5e-3). A step is one complete simplification of that mesh.
+
+* value: input Mtris/s with the mesh resident in HBM (meshoptgpu_simplifyDevice), device
+  time from CUDA events on the launching stream; L2 is flushed between steps (outside the
+  events) by writing a 512 MiB buffer.
+* e2e: the same metric through the drop-in C ABI (meshopt_simplifyWithAttributes) with
+  pinned host buffers: host->device copies of the step's inputs, the simplification and the
+  device->host copy of the result are inside the timed region.
+* roofline: the dominant kernel's algorithmic bytes per launch over its CUDA-event time.
+* cpu_baseline: the CPU oracle (plain-C restatement of the reference) on the same mesh,
+  single thread (the reference simplifier is single-threaded), on this host.
+* --impl reference: the reference's CPU implementation on this host (oracle/_ref when it was
+  compiled here, else the oracle port), same metric and workload.
+
+Multi-GPU: a single mesh does not shard without changing the result (one global greedy
+order), so N>1 runs N independent replicas and reports the aggregate ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from meshoptimizer_gb300 import workloads as W  # noqa: E402
+
+# Algorithmic bytes per unit for the kernels that can dominate a run:
+#   per active candidate for the decision-round kernels, per candidate for rank/gather,
+#   per pair per pass for the radix passes, per corner for the setup folds.
+KERNEL_BYTES = {
+    "kDecide": ("active candidates", 29),       # active id 4 + record 16 + status 1 + 2 touched + list append 4 + pad
+    "kMark": ("active candidates", 20),         # active id 4 + record 16 (atomics land in L2)
+    "kRank": ("candidates", 24),                # v0, v1, bidi/err in 12 + v0, v1, err, key out 16 (-4 overlap)
+    "kRadixScatter": ("pairs", 16),             # key+value in 8, key+value out 8
+    "kFillQuadrics": ("vertices", 48 + 16 + 8), # quadric out, position, CSR offsets
+}
+
+WORKLOADS = {
+    "sphere_attr_2m": lambda: W.config_sphere_attr(9),
+    "sphere_attr_524k": lambda: W.config_sphere_attr(8),
+    "heightfield_256": W.config_heightfield_256,
+    "fractal_3163": lambda: W.config_fractal_3163(3163),
+    "fractal_1024": lambda: W.config_fractal_3163(1024),
+}
+
+
+def load_workload(name):
+    c = WORKLOADS[name]()
+    c["tris"] = len(c["indices"]) // 3
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+                                          "-i", str(self.device_index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(c, min_seconds=8.0, max_runs=4):
+    """Oracle port (single thread) on the same mesh; returns (Mtris/s, runs, seconds, output, error)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    if not oracle.available("port"):
+        oracle.build(with_reference=False)
+    runs, t0 = 0, time.perf_counter()
+    out = err = None
+    while runs < max_runs and (runs == 0 or time.perf_counter() - t0 < min_seconds):
+        out, err = oracle.simplify("port", c["indices"], c["positions"], c["target"], c["error"], c["options"],
+                                   attributes=c.get("attributes"), weights=c.get("weights"))
+        runs += 1
+    dt = time.perf_counter() - t0
+    return c["tris"] * runs / dt / 1e6, runs, dt, out, err
+
+
+def run_reference(args):
+    """--impl reference: the reference's own CPU implementation of the path on this host."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    kind = "ref" if oracle.available("ref") else "port"
+    if kind == "port" and not oracle.available("port"):
+        oracle.build(with_reference=False)
+    c = load_workload(args.workload)
+    call = lambda: oracle.simplify(kind, c["indices"], c["positions"], c["target"], c["error"], c["options"],  # noqa: E731
+                                   attributes=c.get("attributes"), weights=c.get("weights"))
+    for _ in range(min(args.warmup, 1)):
+        call()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = c["tris"] * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": "input Mtris/s simplified (bit-exact)", "value": round(value, 4), "unit": "Mtris/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": c["name"], "input_tris": c["tris"], "target_index_count": c["target"], "target_error": c["error"],
+                   "options": c["options"]},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mtris/s", "cores": 1,
+                         "kind": "reference" if kind == "ref" else "port",
+                         "sample": f"{args.steps} full simplifications of {c['name']} (single thread: the simplifier has no threading)"},
+        "e2e": {"value": round(value, 4), "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sphere_attr_2m", choices=sorted(WORKLOADS))
+    ap.add_argument("--kernel", default="kDecide", help="kernel whose CUDA-event time gives the roofline line")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    import meshoptimizer_gb300 as mg
+    from meshoptimizer_gb300 import build as mgbuild
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    mgbuild.build()
+    mg.load()
+    c = load_workload(args.workload)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    idx = torch.from_numpy(c["indices"].view(np.int32)).to(dev)
+    pos = torch.from_numpy(c["positions"]).to(dev)
+    has_attr = c.get("attributes") is not None
+    attr = torch.from_numpy(c["attributes"]).to(dev) if has_attr else None
+    out = torch.empty_like(idx)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    V = pos.shape[0]
+    ac = attr.shape[1] if has_attr else 0
+
+    def step():
+        return mg.simplify_device(out.data_ptr(), idx.data_ptr(), idx.numel(), pos.data_ptr(), V, 12, c["target"], c["error"], c["options"],
+                                  d_attributes=attr.data_ptr() if has_attr else 0, attributes_stride=4 * ac,
+                                  weights=c.get("weights"), stream=stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 0)):
+        n_out, err = step()
+
+    mg.set_kernel_profile(args.kernel)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = mg.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            n_out, err = step()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = mg.launch_count() - launches0
+    k_launches, k_ms = mg.kernel_profile()
+    mg.set_kernel_profile(None)
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * c["tris"] * args.steps / (total_ms / 1e3) / 1e6
+    gpu_out = out[:n_out].cpu().numpy().view(np.uint32)
+
+    # per-pass and per-phase view of one more run (not timed for the value)
+    mg.set_timing(True)
+    step()
+    phases = mg.last_phase_times()
+    passes = mg.last_pass_stats()
+    mg.set_timing(False)
+
+    # end to end through the drop-in C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_idx = torch.from_numpy(c["indices"].view(np.int32)).pin_memory()
+        h_pos = torch.from_numpy(c["positions"]).pin_memory()
+        h_attr = torch.from_numpy(c["attributes"]).pin_memory() if has_attr else None
+        h_out = torch.empty(len(c["indices"]), dtype=torch.int32).pin_memory()
+        n_idx, n_pos = h_idx.numpy().view(np.uint32), h_pos.numpy()
+        n_attr = h_attr.numpy() if has_attr else None
+        n_outb = h_out.numpy().view(np.uint32)
+
+        def e2e_step():
+            if has_attr:
+                return mg.simplify_raw(n_outb, n_idx, len(n_idx), n_pos, V, 12, c["target"], c["error"], c["options"], attributes=n_attr,
+                                       attributes_stride=4 * ac, weights=c["weights"], attribute_count=ac)
+            return mg.simplify_raw(n_outb, n_idx, len(n_idx), n_pos, V, 12, c["target"], c["error"], c["options"])
+
+        for _ in range(max(args.warmup, 0)):
+            e2e_step()
+        tt = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            n_e2e, _ = e2e_step()
+            tt += time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([tt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tt = float(t.item())
+        assert np.array_equal(n_outb[:n_e2e], gpu_out), "drop-in and device-resident results differ"
+        h2d = c["indices"].nbytes + c["positions"].nbytes + (c["attributes"].nbytes if has_attr else 0)
+        d2h = n_e2e * 4
+        e2e = {"value": round(world * c["tris"] * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * tt / args.steps, 3)}
+
+    if rank != 0:
+        return
+
+    # roofline of the selected kernel: algorithmic bytes over its measured launch time
+    peak, peak_kind = measured_peak()
+    unit_name, per_unit = KERNEL_BYTES.get(args.kernel, ("units", 0))
+    roofline = None
+    if k_launches:
+        avg_ms = k_ms / k_launches
+        # units one launch processes, from the per-pass counters of one run
+        if args.kernel in ("kDecide", "kMark"):
+            units_per_launch = sum(p["active"] for p in passes) / max(sum(p["rounds"] for p in passes), 1)
+        elif args.kernel == "kRank":
+            units_per_launch = sum(p["candidates"] for p in passes) / max(len(passes), 1)
+        else:
+            units_per_launch = 0
+        bytes_per_launch = units_per_launch * per_unit
+        achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0
+        roofline = {"bound": "hbm", "kernel": args.kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
+                    "avg_launch_us": round(1e3 * avg_ms, 2), "launches": k_launches,
+                    "algorithmic_bytes_per_launch": int(bytes_per_launch), "unit_definition": f"{per_unit} B per {unit_name}",
+                    "share_of_step": round(k_ms / total_ms, 4)}
+
+    cpu = None
+    bit_exact = None
+    if not args.no_cpu_baseline:
+        mt, runs, secs, ref_out, ref_err = cpu_baseline(c)
+        bit_exact = bool(np.array_equal(ref_out, gpu_out)) and abs(ref_err - err) <= 1e-6 * max(abs(ref_err), 1e-30)
+        cpu = {"value": round(mt, 4), "unit": "Mtris/s", "cores": 1, "kind": "port",
+               "sample": f"{runs} full simplification(s) of {c['name']} in {secs:.1f} s, single thread (the simplifier has no threading)"}
+
+    line = {
+        "metric": "input Mtris/s simplified (bit-exact)", "value": round(value, 4), "unit": "Mtris/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": c["name"], "input_tris": c["tris"], "output_tris": int(n_out) // 3, "target_index_count": c["target"],
+                   "target_error": c["error"], "options": c["options"], "attributes": ac, "result_error": err,
+                   "l2": "flushed between steps (512 MiB write, outside the timed events)", "parallelism": f"replicas{world}"},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact,
+        "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "phases_ms": {k: round(v, 3) for k, v in phases.items()},
+        "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active")} for p in passes],
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

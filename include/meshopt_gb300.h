@@ -76,10 +76,11 @@ MESHOPTGPU_API const char* meshoptgpu_getLastMessage(void);
 
 /* Per-pass counters of the calling thread's last call: the quantities the reference
  * prints under TRACE (src/simplifier.cpp:1625-1633). stop: 0 out of collapses,
- * 1 error limit, 2 count limit, 3 error goal. */
+ * 1 error limit, 2 count limit, 3 error goal. rounds: decision rounds of the pass;
+ * active: candidates processed by the decision kernels, summed over its rounds. */
 typedef struct meshoptgpu_PassStats
 {
-	unsigned int triangles, candidates, evaluated, done, skipped, invalid, stop, rounds;
+	unsigned int triangles, candidates, evaluated, done, skipped, invalid, stop, rounds, active;
 } meshoptgpu_PassStats;
 
 /* Copies up to max_passes entries; returns the number of passes of the last call. */
@@ -100,6 +101,14 @@ MESHOPTGPU_API size_t meshoptgpu_simplifyDevice(unsigned int* destination, const
     const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, const float* vertex_attributes,
     size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
     size_t target_index_count, float target_error, unsigned int options, float* result_error, void* stream);
+
+/* Kernel launch accounting for the calling thread: the number of kernels this library has
+ * launched, and optional CUDA-event timing of every launch of one kernel (selected by its
+ * name prefix, e.g. "kDecide"; NULL disables). The events are recorded on the launching
+ * stream and read after each call's final synchronisation. */
+MESHOPTGPU_API unsigned long long meshoptgpu_getLaunchCount(void);
+MESHOPTGPU_API void meshoptgpu_setKernelProfile(const char* kernel_name);
+MESHOPTGPU_API void meshoptgpu_getKernelProfile(unsigned long long* launches, double* total_ms);
 
 /* Bytes of device scratch one call on a mesh of this shape needs (for admission control). */
 MESHOPTGPU_API size_t meshoptgpu_workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count);

@@ -43,12 +43,13 @@ EXPORTS = [
     "meshopt_simplify", "meshopt_simplifyWithAttributes", "meshopt_simplifyScale",
     "meshoptgpu_getLastStatus", "meshoptgpu_getLastMessage", "meshoptgpu_getLastPassStats",
     "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
-    "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources",
+    "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
+    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile",
 ]
 
 
 class PassStats(C.Structure):
-    _fields_ = [(n, C.c_uint) for n in ("triangles", "candidates", "evaluated", "done", "skipped", "invalid", "stop", "rounds")]
+    _fields_ = [(n, C.c_uint) for n in ("triangles", "candidates", "evaluated", "done", "skipped", "invalid", "stop", "rounds", "active")]
 
 
 class SimplifyError(RuntimeError):
@@ -86,6 +87,9 @@ def load():
     lib.meshoptgpu_simplifyDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp, vp]
     lib.meshoptgpu_workspaceBytes.restype = sz
     lib.meshoptgpu_workspaceBytes.argtypes = [sz, sz, sz]
+    lib.meshoptgpu_getLaunchCount.restype = C.c_ulonglong
+    lib.meshoptgpu_setKernelProfile.argtypes = [C.c_char_p]
+    lib.meshoptgpu_getKernelProfile.argtypes = [vp, vp]
     _lib = lib
     return lib
 
@@ -196,3 +200,21 @@ def last_phase_times():
 
 def workspace_bytes(index_count, vertex_count, attribute_count=0):
     return int(load().meshoptgpu_workspaceBytes(index_count, vertex_count, attribute_count))
+
+
+def launch_count():
+    """Kernels this library has launched from the calling thread."""
+    return int(load().meshoptgpu_getLaunchCount())
+
+
+def set_kernel_profile(name):
+    """Times every launch of the kernel whose name starts with `name` (None disables)."""
+    load().meshoptgpu_setKernelProfile(None if name is None else name.encode())
+
+
+def kernel_profile():
+    """(launches, total_ms) of the kernel selected with set_kernel_profile since selection."""
+    n = C.c_ulonglong(0)
+    ms = C.c_double(0)
+    load().meshoptgpu_getKernelProfile(C.byref(n), C.byref(ms))
+    return int(n.value), float(ms.value)

@@ -7,6 +7,7 @@
 #include "../../include/meshopt_gb300.h"
 
 #include "mo_common.cuh"
+#include "mo_probe.cuh"
 #include "mo_simplify.cuh"
 
 #include <cstdio>
@@ -288,7 +289,7 @@ int meshoptgpu_getLastPassStats(meshoptgpu_PassStats* out, int max_passes)
 	for (int i = 0; i < n && i < max_passes; ++i)
 	{
 		const PassStats& p = s.last.pass[i];
-		out[i] = meshoptgpu_PassStats{p.triangles, p.candidates, p.evaluated, p.done, p.skipped, p.invalid, p.stop, p.rounds};
+		out[i] = meshoptgpu_PassStats{p.triangles, p.candidates, p.evaluated, p.done, p.skipped, p.invalid, p.stop, p.rounds, p.active};
 	}
 	return s.last.passes;
 }
@@ -352,6 +353,28 @@ size_t meshoptgpu_simplifyDevice(unsigned int* destination, const unsigned int* 
 	{
 		return fail(statusOf(e), e.what());
 	}
+}
+
+void meshoptgpu_setKernelProfile(const char* kernel_name)
+{
+	LaunchProbe& p = probe();
+	p.selected = kernel_name ? kernel_name : "";
+	p.timed_launches = 0;
+	p.timed_ms = 0;
+}
+
+void meshoptgpu_getKernelProfile(unsigned long long* launches, double* total_ms)
+{
+	LaunchProbe& p = probe();
+	if (launches)
+		*launches = p.timed_launches;
+	if (total_ms)
+		*total_ms = p.timed_ms;
+}
+
+unsigned long long meshoptgpu_getLaunchCount(void)
+{
+	return probe().launches;
 }
 
 size_t meshoptgpu_workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count)

@@ -6,6 +6,7 @@
 // once. Tiles are sized so that a grid of a few thousand blocks covers the 152 SMs.
 #include "mo_common.cuh"
 #include "mo_prims.cuh"
+#include "mo_probe.cuh"
 
 namespace mogpu
 {
@@ -81,13 +82,13 @@ void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int
 	bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
 	if (tiles <= 1)
 	{
-		kScanApply<<<1, kScanThreads, 0, stream>>>(in, out, n, nullptr, total, aligned);
+		MO_LAUNCH(kScanApply, 1, kScanThreads, 0, stream, in, out, n, nullptr, total, aligned);
 		return;
 	}
 	unsigned int* sums = scratch;
-	kScanReduce<<<(unsigned)tiles, kScanThreads, 0, stream>>>(in, n, sums, aligned);
+	MO_LAUNCH(kScanReduce, (unsigned)tiles, kScanThreads, 0, stream, in, n, sums, aligned);
 	scanLevel(sums, sums, tiles, nullptr, scratch + roundWords(tiles), stream);
-	kScanApply<<<(unsigned)tiles, kScanThreads, 0, stream>>>(in, out, n, sums, total, aligned);
+	MO_LAUNCH(kScanApply, (unsigned)tiles, kScanThreads, 0, stream, in, out, n, sums, total, aligned);
 }
 
 __global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* __restrict__ keys, size_t n, int shift, unsigned int* __restrict__ hist, unsigned int tiles)
@@ -221,13 +222,61 @@ void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, un
 		unsigned int* kd = to_out ? keys_out : keys_tmp;
 		unsigned int* vd = to_out ? vals_out : vals_tmp;
 		int shift = p * 8;
-		kRadixHist<<<tiles, kSortThreads, 0, stream>>>(ks, n, shift, hist, tiles);
+		MO_LAUNCH(kRadixHist, tiles, kSortThreads, 0, stream, ks, n, shift, hist, tiles);
 		scanExclusive(hist, hist, size_t(tiles) * kSortBins, nullptr, sscratch, stream);
-		kRadixScatter<<<tiles, kSortThreads, 0, stream>>>(ks, vs, kd, vd, n, shift, hist, tiles);
+		MO_LAUNCH(kRadixScatter, tiles, kSortThreads, 0, stream, ks, vs, kd, vd, n, shift, hist, tiles);
 		ks = kd;
 		vs = vd;
 	}
 	MO_CUDA_CHECK(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- launch probe
+
+LaunchProbe::~LaunchProbe()
+{
+	for (auto& pr : pending)
+	{
+		cudaEventDestroy(pr.first);
+		cudaEventDestroy(pr.second);
+	}
+	for (cudaEvent_t e : pool)
+		cudaEventDestroy(e);
+}
+
+cudaEvent_t LaunchProbe::take()
+{
+	if (!pool.empty())
+	{
+		cudaEvent_t e = pool.back();
+		pool.pop_back();
+		return e;
+	}
+	cudaEvent_t e = nullptr;
+	cudaEventCreate(&e);
+	return e;
+}
+
+void LaunchProbe::collect()
+{
+	for (auto& pr : pending)
+	{
+		float ms = 0;
+		if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess)
+		{
+			timed_ms += ms;
+			timed_launches++;
+		}
+		pool.push_back(pr.first);
+		pool.push_back(pr.second);
+	}
+	pending.clear();
+}
+
+LaunchProbe& probe()
+{
+	static thread_local LaunchProbe p;
+	return p;
 }
 
 } // namespace mogpu

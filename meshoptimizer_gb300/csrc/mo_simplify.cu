@@ -18,6 +18,7 @@
 //    decisions; the stop rules are then applied as a prefix scan over sorted order.
 #include "mo_common.cuh"
 #include "mo_prims.cuh"
+#include "mo_probe.cuh"
 #include "mo_simplify.cuh"
 
 #include <algorithm>
@@ -1445,15 +1446,16 @@ float Simplifier::scale(const float* d_positions, size_t vertex_count, size_t st
 	layout(w, arena_.base(), 0, vertex_count, 0);
 	size_t V = vertex_count;
 	if (V)
-		kGatherPositions<<<gridFor(V, kThreads), kThreads, 0, stream>>>(d_positions, stride / 4, V, w.pos_raw);
+		MO_LAUNCH(kGatherPositions, gridFor(V, kThreads), kThreads, 0, stream, d_positions, stride / 4, V, w.pos_raw);
 	size_t per = (V + 4096 * kMinMaxThreads - 1) / (4096 * kMinMaxThreads);
 	per = per ? per : 1;
 	unsigned int mmb = gridFor((V + per - 1) / per, kMinMaxThreads);
-	kMinMaxPartial<<<mmb, kMinMaxThreads, 0, stream>>>(w.pos_raw, V, per, w.partial);
-	kMinMaxFinal<<<1, 32, 0, stream>>>(w.partial, mmb, w.sc);
+	MO_LAUNCH(kMinMaxPartial, mmb, kMinMaxThreads, 0, stream, w.pos_raw, V, per, w.partial);
+	MO_LAUNCH(kMinMaxFinal, 1, 32, 0, stream, w.partial, mmb, w.sc);
 	Scalars* h = reinterpret_cast<Scalars*>(pinned_);
 	MO_CUDA_CHECK(cudaMemcpyAsync(h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
 	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
+	probe().collect();
 	return h->extent;
 }
 
@@ -1508,16 +1510,16 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// ---- setup
 	const unsigned int gV = gridFor(V, kThreads), gI = gridFor(I, kThreads);
 	if (I)
-		kValidateIndices<<<gI, kThreads, 0, stream>>>(w.res0, I, V, &w.sc->bad_index);
+		MO_LAUNCH(kValidateIndices, gI, kThreads, 0, stream, w.res0, I, V, &w.sc->bad_index);
 	if (V)
-		kGatherPositions<<<gV, kThreads, 0, stream>>>(m.positions, m.positions_stride / 4, V, w.pos_raw);
+		MO_LAUNCH(kGatherPositions, gV, kThreads, 0, stream, m.positions, m.positions_stride / 4, V, w.pos_raw);
 
 	// position remap + wedges
 	MO_CUDA_CHECK(cudaMemsetAsync(w.table, 0xFF, size_t(w.hash_mask + 1) * 4, stream));
 	if (V)
 	{
-		kHashInsert<<<gV, kThreads, 0, stream>>>(w.pos_raw, V, w.table, w.hash_mask, w.slot, &w.sc->probe_fail);
-		kHashRemap<<<gV, kThreads, 0, stream>>>(w.table, w.slot, V, w.remap, w.wedge, w.flags);
+		MO_LAUNCH(kHashInsert, gV, kThreads, 0, stream, w.pos_raw, V, w.table, w.hash_mask, w.slot, &w.sc->probe_fail);
+		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.flags);
 		scanExclusive(w.flags, w.flags, V, &w.sc->dup_count, w.scratch, stream);
 	}
 	// flags now hold offsets; recompute flags from remap in the compaction kernel
@@ -1530,10 +1532,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	if (D)
 	{
 		// rebuild the dup flags (the scan consumed them) into cnt, then compact
-		kHashRemap<<<gV, kThreads, 0, stream>>>(w.table, w.slot, V, w.remap, w.wedge, w.cnt);
-		kCompactFlagged<<<gV, kThreads, 0, stream>>>(w.cnt, w.flags, w.remap, V, w.keys_b, w.vals_b);
+		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.cnt);
+		MO_LAUNCH(kCompactFlagged, gV, kThreads, 0, stream, w.cnt, w.flags, w.remap, V, w.keys_b, w.vals_b);
 		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.ckey, w.cv0, D, bitsFor(V), w.scratch, stream);
-		kWedgeLink<<<gridFor(D, kThreads), kThreads, 0, stream>>>(w.keys_a, w.vals_a, D, w.wedge);
+		MO_LAUNCH(kWedgeLink, gridFor(D, kThreads), kThreads, 0, stream, w.keys_a, w.vals_a, D, w.wedge);
 	}
 
 	// vertex -> corner lists in corner order: raw (classification, attribute quadrics) and
@@ -1541,7 +1543,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	const int vbits = bitsFor(V ? V - 1 : 0);
 	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 	if (I)
-		kCountKeys<<<gI, kThreads, 0, stream>>>(w.res0, nullptr, I, w.cnt);
+		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt);
 	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream);
 	radixSortPairs(w.res0, nullptr, w.keys_a, w.csr_raw, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
 	if (D)
@@ -1549,8 +1551,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 		if (I)
 		{
-			kCountKeys<<<gI, kThreads, 0, stream>>>(w.res0, w.remap, I, w.cnt);
-			kRemapKeys<<<gI, kThreads, 0, stream>>>(w.res0, w.remap, I, w.ckey);
+			MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt);
+			MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.ckey);
 		}
 		scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream);
 		radixSortPairs(w.ckey, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
@@ -1561,46 +1563,46 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// classification
 	if (V)
 	{
-		kOpenEdges<<<gV, kThreads, 0, stream>>>(w.res0, w.off_raw, w.csr_raw, V, w.loop, w.loopback);
-		kClassify<<<gV, kThreads, 0, stream>>>(V, w.remap, w.wedge, w.loop, w.loopback, w.kind);
+		MO_LAUNCH(kOpenEdges, gV, kThreads, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.loop, w.loopback);
+		MO_LAUNCH(kClassify, gV, kThreads, 0, stream, V, w.remap, w.wedge, w.loop, w.loopback, w.kind);
 		if (m.lock)
 		{
-			kLockMark<<<gV, kThreads, 0, stream>>>(V, m.lock, w.remap, w.kind);
-			kLockSpread<<<gV, kThreads, 0, stream>>>(V, w.remap, w.kind);
+			MO_LAUNCH(kLockMark, gV, kThreads, 0, stream, V, m.lock, w.remap, w.kind);
+			MO_LAUNCH(kLockSpread, gV, kThreads, 0, stream, V, w.remap, w.kind);
 		}
 		if (m.options & kOptLockBorder)
-			kLockBorder<<<gV, kThreads, 0, stream>>>(V, w.kind);
+			MO_LAUNCH(kLockBorder, gV, kThreads, 0, stream, V, w.kind);
 	}
 
 	// rescale
 	size_t per = (V + 4096 * kMinMaxThreads - 1) / (4096 * kMinMaxThreads);
 	per = per ? per : 1;
 	unsigned int mmb = gridFor((V + per - 1) / per, kMinMaxThreads);
-	kMinMaxPartial<<<mmb, kMinMaxThreads, 0, stream>>>(w.pos_raw, V, per, w.partial);
-	kMinMaxFinal<<<1, 32, 0, stream>>>(w.partial, mmb, w.sc);
+	MO_LAUNCH(kMinMaxPartial, mmb, kMinMaxThreads, 0, stream, w.pos_raw, V, per, w.partial);
+	MO_LAUNCH(kMinMaxFinal, 1, 32, 0, stream, w.partial, mmb, w.sc);
 	if (V)
-		kRescale<<<gV, kThreads, 0, stream>>>(w.pos_raw, V, w.sc, w.pos);
+		MO_LAUNCH(kRescale, gV, kThreads, 0, stream, w.pos_raw, V, w.sc, w.pos);
 	if (ac && V)
-		kRescaleAttributes<<<gV, kThreads, 0, stream>>>(m.attributes, m.attributes_stride / 4, V, am, w.attr);
+		MO_LAUNCH(kRescaleAttributes, gV, kThreads, 0, stream, m.attributes, m.attributes_stride / 4, V, am, w.attr);
 
 	// quadrics
 	float factor = (m.options & kOptRegularizeLight) ? 1e-2f : ((m.options & kOptRegularize) ? 1e-1f : 1e-7f);
 	if (V)
-		kFillQuadrics<<<gV, kThreads, 0, stream>>>(w.res0, off_rm, csr_rm, V, w.pos, w.remap, w.kind, w.loop, w.loopback, m.lock, factor, w.vq);
+		MO_LAUNCH(kFillQuadrics, gV, kThreads, 0, stream, w.res0, off_rm, csr_rm, V, w.pos, w.remap, w.kind, w.loop, w.loopback, m.lock, factor, w.vq);
 	if (ac && V)
 	{
 		if (ac <= 4)
-			kFillAttributeQuadrics<4><<<gridFor(V, 128), 128, 0, stream>>>(w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
+			MO_LAUNCH(kFillAttributeQuadrics<4>, gridFor(V, 128), 128, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
 		else if (ac <= 8)
-			kFillAttributeQuadrics<8><<<gridFor(V, 128), 128, 0, stream>>>(w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
+			MO_LAUNCH(kFillAttributeQuadrics<8>, gridFor(V, 128), 128, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
 		else if (ac <= 16)
-			kFillAttributeQuadrics<16><<<gridFor(V, 128), 128, 0, stream>>>(w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
+			MO_LAUNCH(kFillAttributeQuadrics<16>, gridFor(V, 128), 128, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
 		else
-			kFillAttributeQuadrics<32><<<gridFor(V, 64), 64, 0, stream>>>(w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
+			MO_LAUNCH(kFillAttributeQuadrics<32>, gridFor(V, 64), 64, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
 	}
 	if (V)
-		kDualCount<<<gV, kThreads, 0, stream>>>(w.off_raw, w.kind, V, &w.sc->dual);
-	kCapacity<<<1, 32, 0, stream>>>(I, w.sc);
+		MO_LAUNCH(kDualCount, gV, kThreads, 0, stream, w.off_raw, w.kind, V, &w.sc->dual);
+	MO_LAUNCH(kCapacity, 1, 32, 0, stream, I, w.sc);
 	MO_CUDA_CHECK(cudaGetLastError());
 	readScalars();
 	const float vertex_scale = hs->extent;
@@ -1667,17 +1669,17 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		// adjacency of the current result, welded by remap
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 		MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
-		kCountKeys<<<gridFor(result_count, kThreads), kThreads, 0, stream>>>(res, w.remap, result_count, w.cnt);
+		MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
 		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream);
-		kAdjFill<<<gT, kThreads, 0, stream>>>(res, T, w.remap, w.adj_off, w.fill, w.adj);
+		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[3], stream));
 
 		// pick
-		kPickCount<<<gT, kThreads, 0, stream>>>(res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt);
+		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt);
 		scanExclusive(w.tcnt, w.tcnt, T, &w.sc->pick_total, w.scratch, stream);
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, stream));
-		kPickEmit<<<gT, kThreads, 0, stream>>>(res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr);
+		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr);
 		readScalars();
 		const size_t C = std::min<size_t>(hs->pick_total, hs->pick_trunc);
 		if (timed)
@@ -1687,30 +1689,32 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		const unsigned int gC = gridFor(C, kThreads);
 
 		// rank + sort
-		kRank<<<gC, kThreads, 0, stream>>>(C, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback, w.attr, w.aq,
+		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback, w.attr, w.aq,
 		    w.ag, ac);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
 		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream);
-		kGatherSorted<<<gC, kThreads, 0, stream>>>(C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.srec, w.serr, w.skind, w.status);
+		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.srec, w.serr, w.skind, w.status);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
 		// perform: decision rounds
-		kPerformInit<<<gV, kThreads, 0, stream>>>(V, w.touched, w.moved_by, w.cr, w.minT, w.minS);
+		MO_LAUNCH(kPerformInit, gV, kThreads, 0, stream, V, w.touched, w.moved_by, w.cr, w.minT, w.minS);
 		const unsigned int* active = nullptr;
 		unsigned int* next = w.act0;
 		size_t act_count = C;
 		unsigned int round = 0;
+		unsigned long long active_sum = 0;
 		while (act_count)
 		{
+			active_sum += act_count;
 			++round;
 			if (round > C + 1)
 				throw std::runtime_error("collapse decision rounds did not converge");
 			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->active_count, 0, 4, stream));
 			unsigned int gA = gridFor(act_count, kThreads);
-			kMark<<<gA, kThreads, 0, stream>>>(active, act_count, w.srec, round, w.minT, w.minS);
-			kDecide<<<gA, kThreads, 0, stream>>>(active, act_count, round, w.srec, w.skind, w.minT, w.minS, w.touched, w.moved_by, w.moved_to, w.status,
+			MO_LAUNCH(kMark, gA, kThreads, 0, stream, active, act_count, w.srec, round, w.minT, w.minS);
+			MO_LAUNCH(kDecide, gA, kThreads, 0, stream, active, act_count, round, w.srec, w.skind, w.minT, w.minS, w.touched, w.moved_by, w.moved_to, w.status,
 			    w.adj_off, w.adj, w.pos, w.remap, w.wedge, w.loop, w.loopback, next, &w.sc->active_count);
 			readScalars();
 			if (hs->active_count >= act_count)
@@ -1723,10 +1727,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		// stop rules
 		const size_t goal = (result_count - m.target_index_count) / 3;
 		const unsigned int nblk = unsigned((C + kStopTile - 1) / kStopTile);
-		kStopReduce<<<nblk, 256, 0, stream>>>(C, w.status, w.skind, w.serr, w.blk);
-		kStopScanBlocks<<<1, 1024, 0, stream>>>(w.blk, nblk);
+		MO_LAUNCH(kStopReduce, nblk, 256, 0, stream, C, w.status, w.skind, w.serr, w.blk);
+		MO_LAUNCH(kStopScanBlocks, 1, 1024, 0, stream, w.blk, nblk);
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->cut, 0xFF, 8, stream));
-		kStopFind<<<nblk, 256, 0, stream>>>(C, w.status, w.skind, w.serr, w.blk, result_error_bits, error_limit, goal, &w.sc->cut);
+		MO_LAUNCH(kStopFind, nblk, 256, 0, stream, C, w.status, w.skind, w.serr, w.blk, result_error_bits, error_limit, goal, &w.sc->cut);
 		readScalars();
 		const unsigned long long cutv = hs->cut;
 		const size_t cut = cutv == ~0ull ? C : size_t(cutv >> 2);
@@ -1738,7 +1742,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->done, 0, 12, stream));
 		MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->result_error_bits, &result_error_bits, 4, cudaMemcpyHostToDevice, stream));
 		if (cut)
-			kApply<<<gridFor(cut, kThreads), kThreads, 0, stream>>>(cut, w.srec, w.skind, w.status, w.serr, w.remap, w.wedge, w.loop, w.loopback, w.cr, w.vq,
+			MO_LAUNCH(kApply, gridFor(cut, kThreads), kThreads, 0, stream, cut, w.srec, w.skind, w.status, w.serr, w.remap, w.wedge, w.loop, w.loopback, w.cr, w.vq,
 			    w.pos, w.aq, w.ag, ac, w.sc);
 		readScalars();
 		if (passes < kMaxPassStats)
@@ -1752,6 +1756,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			ps.invalid = hs->invalid;
 			ps.stop = reason;
 			ps.rounds = round;
+			ps.active = unsigned(active_sum);
 		}
 		passes++;
 		const unsigned int done = hs->done;
@@ -1763,10 +1768,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			break;
 		}
 
-		kRemapLoops<<<gV, kThreads, 0, stream>>>(V, w.cr, w.loop, w.loopback);
-		kCompactCount<<<gT, kThreads, 0, stream>>>(res, T, w.cr, w.remap, w.blkcnt);
+		MO_LAUNCH(kRemapLoops, gV, kThreads, 0, stream, V, w.cr, w.loop, w.loopback);
+		MO_LAUNCH(kCompactCount, gT, kThreads, 0, stream, res, T, w.cr, w.remap, w.blkcnt);
 		scanExclusive(w.blkcnt, w.blkcnt, gT, &w.sc->tri_total, w.scratch, stream);
-		kCompactEmit<<<gT, kThreads, 0, stream>>>(res, T, w.cr, w.remap, w.blkcnt, res_next);
+		MO_LAUNCH(kCompactEmit, gT, kThreads, 0, stream, res, T, w.cr, w.remap, w.blkcnt, res_next);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[8], stream));
 		readScalars();
@@ -1789,6 +1794,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaEventRecord(ev[9], stream));
 	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
 	MO_CUDA_CHECK(cudaGetLastError());
+	probe().collect();
 
 	float rerr;
 	memcpy(&rerr, &result_error_bits, 4);

@@ -46,6 +46,7 @@ struct PassStats
 	unsigned int invalid;
 	unsigned int stop;
 	unsigned int rounds;
+	unsigned int active; // candidates processed by the decision kernels, summed over rounds
 };
 
 struct RunResult
