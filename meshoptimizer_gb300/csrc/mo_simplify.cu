@@ -19,6 +19,7 @@
 #include "mo_common.cuh"
 #include "mo_prims.cuh"
 #include "mo_probe.cuh"
+#include "mo_grid.cuh"
 #include "mo_simplify.cuh"
 
 #include <algorithm>
@@ -55,7 +56,11 @@ struct Scalars
 	unsigned int invalid;
 	unsigned int result_error_bits;
 	unsigned int vertex_error_bits;
-	unsigned int pad[3];
+	unsigned int bar[2];          // grid barrier (arrivals, generation)
+	unsigned int grid_error;      // a grid barrier gave up waiting
+	unsigned int rounds;          // decision rounds of the last pass
+	unsigned int act_count[2];    // active candidates of the current / next round
+	unsigned long long active_sum; // candidates processed by the rounds of the last pass
 };
 
 __device__ __forceinline__ size_t gtid()
@@ -95,6 +100,7 @@ __device__ __forceinline__ float foldMax(float l, float r)
 }
 
 constexpr int kMinMaxThreads = 256;
+constexpr size_t kMinMaxMaxThreads = 152 * 4 * kMinMaxThreads; // threads of the partial pass, at most
 
 __global__ void __launch_bounds__(kMinMaxThreads) kMinMaxPartial(const float4* __restrict__ pos, size_t n, size_t per_thread, float* __restrict__ partial)
 {
@@ -148,24 +154,55 @@ __global__ void __launch_bounds__(kMinMaxThreads) kMinMaxPartial(const float4* _
 	}
 }
 
-__global__ void kMinMaxFinal(const float* __restrict__ partial, int blocks, Scalars* sc)
+// folds the per-block partials in block order: thread t takes a contiguous run of blocks,
+// then lanes and warps are combined left to right as in kMinMaxPartial
+__global__ void __launch_bounds__(kMinMaxThreads) kMinMaxFinal(const float* __restrict__ partial, int blocks, Scalars* sc)
 {
-	if (threadIdx.x != 0 || blockIdx.x != 0)
-		return;
 	float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
 	float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-	for (int b = 0; b < blocks; ++b)
+	int per = (blocks + kMinMaxThreads - 1) / kMinMaxThreads;
+	int b0 = threadIdx.x * per, b1 = min(b0 + per, blocks);
+	for (int b = b0; b < b1; ++b)
 		for (int j = 0; j < 3; ++j)
 		{
 			mn[j] = foldMin(mn[j], partial[b * 6 + j]);
 			mx[j] = foldMax(mx[j], partial[b * 6 + 3 + j]);
 		}
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1)
+	{
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			float a = __shfl_down_sync(0xffffffffu, mn[j], o);
+			float b = __shfl_down_sync(0xffffffffu, mx[j], o);
+			if ((threadIdx.x & 31) + o < 32 && ((threadIdx.x & (2 * o - 1)) == 0))
+			{
+				mn[j] = foldMin(mn[j], a);
+				mx[j] = foldMax(mx[j], b);
+			}
+		}
+	}
+	__shared__ float sm[kMinMaxThreads / 32][6];
+	int w = threadIdx.x >> 5;
+	if ((threadIdx.x & 31) == 0)
+		for (int j = 0; j < 3; ++j)
+			sm[w][j] = mn[j], sm[w][3 + j] = mx[j];
+	__syncthreads();
+	if (threadIdx.x != 0)
+		return;
+	for (int q = 1; q < kMinMaxThreads / 32; ++q)
+		for (int j = 0; j < 3; ++j)
+		{
+			sm[0][j] = foldMin(sm[0][j], sm[q][j]);
+			sm[0][3 + j] = foldMax(sm[0][3 + j], sm[q][3 + j]);
+		}
 	float extent = 0.f;
-	extent = (mx[0] - mn[0]) < extent ? extent : (mx[0] - mn[0]);
-	extent = (mx[1] - mn[1]) < extent ? extent : (mx[1] - mn[1]);
-	extent = (mx[2] - mn[2]) < extent ? extent : (mx[2] - mn[2]);
+	extent = (sm[0][3] - sm[0][0]) < extent ? extent : (sm[0][3] - sm[0][0]);
+	extent = (sm[0][4] - sm[0][1]) < extent ? extent : (sm[0][4] - sm[0][1]);
+	extent = (sm[0][5] - sm[0][2]) < extent ? extent : (sm[0][5] - sm[0][2]);
 	for (int j = 0; j < 3; ++j)
-		sc->minv[j] = mn[j], sc->maxv[j] = mx[j];
+		sc->minv[j] = sm[0][j], sc->maxv[j] = sm[0][3 + j];
 	sc->extent = extent;
 	sc->scale = extent == 0 ? 0.f : 1.f / extent;
 }
@@ -785,37 +822,9 @@ __global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ ord
 
 // ---------------------------------------------------------------- pass: perform (rounds)
 
-__global__ void kPerformInit(size_t n, unsigned char* __restrict__ touched, unsigned int* __restrict__ moved_by, unsigned int* __restrict__ cr,
-    unsigned long long* __restrict__ minT, unsigned long long* __restrict__ minS)
-{
-	size_t i = gtid();
-	if (i >= n)
-		return;
-	touched[i] = 0;
-	moved_by[i] = ~0u;
-	cr[i] = (unsigned int)i;
-	minT[i] = ~0ull;
-	minS[i] = ~0ull;
-}
-
 __device__ __forceinline__ unsigned long long roundTag(unsigned int round)
 {
 	return (unsigned long long)(0xFFFFFFFFu - round) << 32;
-}
-
-// every undecided candidate registers itself on its endpoints (minT) and on its source (minS)
-__global__ void kMark(const unsigned int* __restrict__ active, size_t count, const uint4* __restrict__ srec, unsigned int round,
-    unsigned long long* __restrict__ minT, unsigned long long* __restrict__ minS)
-{
-	size_t a = gtid();
-	if (a >= count)
-		return;
-	unsigned int k = active ? active[a] : (unsigned int)a;
-	uint4 rec = srec[k];
-	unsigned long long key = roundTag(round) | k;
-	atomicMin(&minT[rec.z], key);
-	atomicMin(&minT[rec.w], key);
-	atomicMin(&minS[rec.z], key);
 }
 
 __device__ __forceinline__ bool earlierThan(unsigned long long v, unsigned long long tag, unsigned int k)
@@ -823,99 +832,181 @@ __device__ __forceinline__ bool earlierThan(unsigned long long v, unsigned long 
 	return (v >> 32) == (tag >> 32) && (unsigned int)v < k;
 }
 
-// Decides candidate k once nothing earlier can change its outcome:
+// Decision rule of the rounds (performEdgeCollapses :1511-1623 made order-free): candidate k
+// is decided once nothing earlier in sorted order can change its outcome:
 //  * an earlier candidate already committed on one of its endpoints -> locked (final: any
 //    commit seen on an endpoint has a smaller sorted index);
 //  * otherwise it waits until it is the earliest undecided candidate on both endpoints and no
 //    undecided earlier candidate moves a vertex of its one-ring; then the flip test runs
 //    against the one-ring as moved by earlier commits only (moved_by < k).
-__global__ void kDecide(const unsigned int* __restrict__ active, size_t count, unsigned int round, const uint4* __restrict__ srec,
-    const unsigned char* __restrict__ skind, const unsigned long long* __restrict__ minT, const unsigned long long* __restrict__ minS,
-    unsigned char* touched, unsigned int* moved_by, unsigned int* moved_to, unsigned char* __restrict__ status, const unsigned int* __restrict__ adj_off,
-    const uint2* __restrict__ adj, const float4* __restrict__ pos, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge,
-    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ next_active, unsigned int* next_count)
+struct RoundsArgs
 {
-	size_t a = gtid();
-	bool keep = false;
-	unsigned int k = 0;
-	if (a < count)
+	size_t count;
+	size_t vcount;
+	const uint4* srec;
+	const unsigned char* skind;
+	unsigned long long* minT;
+	unsigned long long* minS;
+	unsigned char* touched;
+	unsigned int* moved_by;
+	unsigned int* moved_to;
+	unsigned int* cr;
+	unsigned char* status;
+	const unsigned int* adj_off;
+	const uint2* adj;
+	const float4* pos;
+	const unsigned int* remap;
+	const unsigned int* wedge;
+	const unsigned int* loop;
+	const unsigned int* loopback;
+	unsigned int* list[2];
+	Scalars* sc;
+};
+
+// One decision of the rounds below for candidate k; returns true if k stays undecided.
+// Arrays written during the rounds (minT, minS, touched, moved_by, moved_to) are read
+// through L2 (ld.global.cg): other blocks write them between grid barriers.
+__device__ __forceinline__ bool decideOne(const RoundsArgs& a, unsigned int k, unsigned int round)
+{
+	uint4 rec = __ldg(a.srec + k);
+	unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
+	const unsigned long long tag = roundTag(round);
+	const unsigned long long mine = tag | k;
+	if (__ldcg(a.touched + r0) | __ldcg(a.touched + r1))
 	{
-		k = active ? active[a] : (unsigned int)a;
-		uint4 rec = srec[k];
-		unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
-		const unsigned long long tag = roundTag(round);
-		const unsigned long long mine = tag | k;
-		if (*(volatile unsigned char*)&touched[r0] | *(volatile unsigned char*)&touched[r1])
+		a.status[k] = kSkipLocked;
+		return false;
+	}
+	if (__ldcg(a.minT + r0) != mine || __ldcg(a.minT + r1) != mine)
+		return true;
+	unsigned int b = __ldg(a.adj_off + r0), e = __ldg(a.adj_off + r0 + 1);
+	for (unsigned int j = b; j < e; ++j)
+	{
+		uint2 ed = __ldg(a.adj + j);
+		if (earlierThan(__ldcg(a.minS + ed.x), tag, k) || earlierThan(__ldcg(a.minS + ed.y), tag, k))
+			return true;
+	}
+	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
+	for (unsigned int j = b; j < e; ++j)
+	{
+		uint2 ed = __ldg(a.adj + j);
+		unsigned int mx = __ldcg(a.moved_by + ed.x), my = __ldcg(a.moved_by + ed.y);
+		unsigned int va = mx < k ? __ldcg(a.moved_to + ed.x) : ed.x;
+		unsigned int vb = my < k ? __ldcg(a.moved_to + ed.y) : ed.y;
+		if (va == r1 || vb == r1 || va == vb)
+			continue;
+		if (triFlip(ldpos(a.pos, va), ldpos(a.pos, vb), v0, v1))
 		{
-			status[k] = kSkipLocked;
-		}
-		else if (minT[r0] != mine || minT[r1] != mine)
-		{
-			keep = true;
-		}
-		else
-		{
-			unsigned int b = adj_off[r0], e = adj_off[r0 + 1];
-			bool ready = true;
-			for (unsigned int j = b; j < e && ready; ++j)
-			{
-				uint2 ed = adj[j];
-				ready = !earlierThan(minS[ed.x], tag, k) && !earlierThan(minS[ed.y], tag, k);
-			}
-			if (!ready)
-				keep = true;
-			else
-			{
-				V3 v0 = ldpos(pos, r0), v1 = ldpos(pos, r1);
-				bool flip = false;
-				for (unsigned int j = b; j < e && !flip; ++j)
-				{
-					uint2 ed = adj[j];
-					unsigned int mx = moved_by[ed.x], my = moved_by[ed.y];
-					unsigned int va = mx < k ? moved_to[ed.x] : ed.x;
-					unsigned int vb = my < k ? moved_to[ed.y] : ed.y;
-					if (va == r1 || vb == r1 || va == vb)
-						continue;
-					flip = triFlip(ldpos(pos, va), ldpos(pos, vb), v0, v1);
-				}
-				if (flip)
-					status[k] = kSkipFlip;
-				else
-				{
-					unsigned char kd = skind[k];
-					unsigned int target;
-					if (kd == kComplex)
-						target = complexTarget(r0, i1, remap, loop, loopback);
-					else if (kd == kSeam)
-					{
-						unsigned int s0 = wedge[i0];
-						unsigned int s1 = loop[i0] == i1 ? loopback[s0] : loop[s0];
-						s1 = (s1 != ~0u) ? s1 : wedge[i1];
-						target = (s0 == r0) ? s1 : i1;
-					}
-					else
-						target = i1;
-					moved_to[r0] = target;
-					moved_by[r0] = k;
-					touched[r0] = 1;
-					touched[r1] = 1;
-					status[k] = kCommit;
-				}
-			}
+			a.status[k] = kSkipFlip;
+			return false;
 		}
 	}
-	// warp-aggregated append of the candidates that stay undecided
-	unsigned int m = __ballot_sync(0xffffffffu, keep);
-	if (m)
+	unsigned char kd = __ldg(a.skind + k);
+	unsigned int target;
+	if (kd == kComplex)
+		target = complexTarget(r0, i1, a.remap, a.loop, a.loopback);
+	else if (kd == kSeam)
 	{
-		unsigned int lane = threadIdx.x & 31;
-		unsigned int leader = __ffs(m) - 1;
-		unsigned int base = 0;
-		if (lane == leader)
-			base = atomicAdd(next_count, __popc(m));
-		base = __shfl_sync(0xffffffffu, base, leader);
-		if (keep)
-			next_active[base + __popc(m & ((1u << lane) - 1u))] = k;
+		unsigned int s0 = a.wedge[i0];
+		unsigned int s1 = a.loop[i0] == i1 ? a.loopback[s0] : a.loop[s0];
+		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
+		target = (s0 == r0) ? s1 : i1;
+	}
+	else
+		target = i1;
+	a.moved_to[r0] = target;
+	a.moved_by[r0] = k;
+	a.touched[r0] = 1;
+	a.touched[r1] = 1;
+	a.status[k] = kCommit;
+	return false;
+}
+
+// All decision rounds of one pass in one cooperative launch. Round r reads the candidates
+// left undecided by round r-1 (round 1: every candidate, in sorted order) and appends the
+// ones that stay undecided to the other list; grid barriers separate the phases. Each round
+// decides at least the earliest undecided candidate, so the loop ends after at most
+// `count` rounds; a round without progress is reported as an error.
+__global__ void __launch_bounds__(kThreads) kRounds(RoundsArgs a)
+{
+	Scalars* sc = a.sc;
+	const size_t gthreads = (size_t)gridDim.x * blockDim.x;
+	const unsigned int lane = threadIdx.x & 31;
+	const size_t wbase = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+
+	for (size_t i = gtid(); i < a.vcount; i += gthreads)
+	{
+		a.touched[i] = 0;
+		a.moved_by[i] = ~0u;
+		a.cr[i] = (unsigned int)i;
+		a.minT[i] = ~0ull;
+		a.minS[i] = ~0ull;
+	}
+	gridBarrier(sc->bar, &sc->grid_error);
+
+	unsigned long long active_sum = 0;
+	unsigned int n = (unsigned int)a.count;
+	unsigned int round = 0;
+	while (n)
+	{
+		++round;
+		if (round > a.count + 1 || __ldcg(&sc->grid_error))
+			break;
+		active_sum += n;
+		const unsigned int* list = round == 1 ? nullptr : a.list[round & 1];
+		unsigned int* next = a.list[(round + 1) & 1];
+		unsigned int* next_count = &sc->act_count[(round + 1) & 1];
+		const unsigned long long key_tag = roundTag(round);
+
+		for (size_t x = gtid(); x < n; x += gthreads)
+		{
+			unsigned int k = list ? __ldcg(list + x) : (unsigned int)x;
+			uint4 rec = __ldg(a.srec + k);
+			unsigned long long key = key_tag | k;
+			atomicMin(&a.minT[rec.z], key);
+			atomicMin(&a.minT[rec.w], key);
+			atomicMin(&a.minS[rec.z], key);
+		}
+		if (gtid() == 0)
+			*next_count = 0;
+		gridBarrier(sc->bar, &sc->grid_error);
+
+		for (size_t base = wbase; base < n; base += gthreads)
+		{
+			size_t x = base + lane;
+			bool keep = false;
+			unsigned int k = 0;
+			if (x < n)
+			{
+				k = list ? __ldcg(list + x) : (unsigned int)x;
+				keep = decideOne(a, k, round);
+			}
+			unsigned int m = __ballot_sync(0xffffffffu, keep);
+			if (m)
+			{
+				unsigned int leader = __ffs(m) - 1;
+				unsigned int o = 0;
+				if (lane == leader)
+					o = atomicAdd(next_count, __popc(m));
+				o = __shfl_sync(0xffffffffu, o, leader);
+				if (keep)
+					next[o + __popc(m & ((1u << lane) - 1u))] = k;
+			}
+		}
+		gridBarrier(sc->bar, &sc->grid_error);
+		unsigned int nn = __ldcg(next_count);
+		if (nn >= n)
+		{
+			if (gtid() == 0)
+				atomicOr(&sc->grid_error, 2u);
+			break;
+		}
+		n = nn;
+	}
+	if (gtid() == 0)
+	{
+		sc->rounds = round;
+		sc->active_sum = active_sum;
 	}
 }
 
@@ -1104,99 +1195,126 @@ __global__ void __launch_bounds__(256) kStopFind(size_t count, const unsigned ch
 // quadric merges of updateQuadrics (:1638-1673); every target receives at most one source
 // position quadric per pass (endpoints of commits are disjoint), and attribute sources of one
 // commit are merged in vertex order
-__global__ void kApply(size_t cut, const uint4* __restrict__ srec, const unsigned char* __restrict__ skind, const unsigned char* __restrict__ status,
-    const unsigned int* __restrict__ serr, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge,
-    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ cr, Quadric* vq, const float4* __restrict__ pos,
-    Quadric* aq, float4* ag, int ac, Scalars* sc)
+__device__ __forceinline__ unsigned int blockMaxU32(unsigned int v, unsigned int* smem)
 {
+	for (int o = 16; o > 0; o >>= 1)
+		v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+	if ((threadIdx.x & 31) == 0)
+		smem[threadIdx.x >> 5] = v;
+	__syncthreads();
+	unsigned int r = 0;
+	if (threadIdx.x == 0)
+		for (unsigned int q = 0; q < blockDim.x / 32; ++q)
+			r = max(r, smem[q]);
+	return r;
+}
+
+// error bits usable by the max reductions (errors are non-negative; NaN never raises them)
+__device__ __forceinline__ unsigned int maxableBits(float v)
+{
+	return v == v ? __float_as_uint(v) : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) kApply(size_t cut, const uint4* __restrict__ srec, const unsigned char* __restrict__ skind,
+    const unsigned char* __restrict__ status, const unsigned int* __restrict__ serr, const unsigned int* __restrict__ remap,
+    const unsigned int* __restrict__ wedge, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ cr,
+    Quadric* vq, const float4* __restrict__ pos, Quadric* aq, float4* ag, int ac, Scalars* sc)
+{
+	__shared__ unsigned int smem[kThreads / 32];
 	size_t k = gtid();
 	unsigned int st = k < cut ? status[k] : 0;
-	unsigned int lane = threadIdx.x & 31;
-	unsigned int mc = __ballot_sync(0xffffffffu, st == kCommit), ml = __ballot_sync(0xffffffffu, st == kSkipLocked),
-	             mf = __ballot_sync(0xffffffffu, st == kSkipFlip);
-	if (lane == 0)
+	unsigned int nc = __syncthreads_count(st == kCommit), nl = __syncthreads_count(st == kSkipLocked), nf = __syncthreads_count(st == kSkipFlip);
+	if (threadIdx.x == 0)
 	{
-		if (mc)
-			atomicAdd(&sc->done, __popc(mc));
-		if (ml)
-			atomicAdd(&sc->skipped, __popc(ml));
-		if (mf)
-			atomicAdd(&sc->invalid, __popc(mf));
+		if (nc)
+			atomicAdd(&sc->done, nc);
+		if (nl)
+			atomicAdd(&sc->skipped, nl);
+		if (nf)
+			atomicAdd(&sc->invalid, nf);
 	}
-	if (st != kCommit)
-		return;
-	uint4 rec = srec[k];
-	unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
-	unsigned char kd = skind[k];
-
-	unsigned int moved[kMaxAttributes];
-	int nm = 0;
-	if (kd == kComplex)
+	unsigned int errbits = 0, derrbits = 0;
+	if (st == kCommit)
 	{
-		unsigned int v = i0;
-		do
+		uint4 rec = srec[k];
+		unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
+		unsigned char kd = skind[k];
+
+		unsigned int moved[kMaxAttributes];
+		int nm = 0;
+		if (kd == kComplex)
 		{
-			cr[v] = complexTarget(v, i1, remap, loop, loopback);
-			if (nm < kMaxAttributes)
-				moved[nm++] = v;
-			v = wedge[v];
-		} while (v != i0);
-	}
-	else if (kd == kSeam)
-	{
-		unsigned int s0 = wedge[i0];
-		unsigned int s1 = loop[i0] == i1 ? loopback[s0] : loop[s0];
-		s1 = (s1 != ~0u) ? s1 : wedge[i1];
-		cr[i0] = i1;
-		cr[s0] = s1;
-		moved[nm++] = i0;
-		if (s0 != i0)
-			moved[nm++] = s0;
-	}
-	else
-	{
-		cr[i0] = i1;
-		moved[nm++] = i0;
-	}
-
-	Quadric Q1 = ldquadric(vq, r1);
-	Quadric Q0 = ldquadric(vq, r0);
-	qadd(Q1, Q0);
-	stquadric(vq, r1, Q1);
-
-	atomicMaxNonNegFloat(&sc->result_error_bits, __uint_as_float(serr[k]));
-
-	if (ac)
-	{
-		// merge in increasing vertex order (insertion sort of the few moved wedges)
-		for (int a = 1; a < nm; ++a)
-		{
-			unsigned int x = moved[a];
-			int b = a - 1;
-			while (b >= 0 && moved[b] > x)
+			unsigned int v = i0;
+			do
 			{
-				moved[b + 1] = moved[b];
-				--b;
-			}
-			moved[b + 1] = x;
+				cr[v] = complexTarget(v, i1, remap, loop, loopback);
+				if (nm < kMaxAttributes)
+					moved[nm++] = v;
+				v = wedge[v];
+			} while (v != i0);
 		}
-		for (int m = 0; m < nm; ++m)
+		else if (kd == kSeam)
 		{
-			unsigned int v = moved[m];
-			unsigned int t = cr[v];
-			Quadric A = ldquadric(aq, t);
-			qadd(A, ldquadric(aq, v));
-			stquadric(aq, t, A);
-			for (int q = 0; q < ac; ++q)
-			{
-				float4 g = ag[(size_t)t * ac + q], h = ag[(size_t)v * ac + q];
-				g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
-				ag[(size_t)t * ac + q] = g;
-			}
+			unsigned int s0 = wedge[i0];
+			unsigned int s1 = loop[i0] == i1 ? loopback[s0] : loop[s0];
+			s1 = (s1 != ~0u) ? s1 : wedge[i1];
+			cr[i0] = i1;
+			cr[s0] = s1;
+			moved[nm++] = i0;
+			if (s0 != i0)
+				moved[nm++] = s0;
 		}
-		float derr = qerror(Q0, ldpos(pos, remap[cr[r0]]));
-		atomicMaxNonNegFloat(&sc->vertex_error_bits, derr);
+		else
+		{
+			cr[i0] = i1;
+			moved[nm++] = i0;
+		}
+
+		Quadric Q1 = ldquadric(vq, r1);
+		Quadric Q0 = ldquadric(vq, r0);
+		qadd(Q1, Q0);
+		stquadric(vq, r1, Q1);
+
+		errbits = maxableBits(__uint_as_float(serr[k]));
+
+		if (ac)
+		{
+			// merge in increasing vertex order (insertion sort of the few moved wedges)
+			for (int x = 1; x < nm; ++x)
+			{
+				unsigned int v = moved[x];
+				int y = x - 1;
+				while (y >= 0 && moved[y] > v)
+				{
+					moved[y + 1] = moved[y];
+					--y;
+				}
+				moved[y + 1] = v;
+			}
+			for (int m = 0; m < nm; ++m)
+			{
+				unsigned int v = moved[m];
+				unsigned int t = cr[v];
+				Quadric A = ldquadric(aq, t);
+				qadd(A, ldquadric(aq, v));
+				stquadric(aq, t, A);
+				for (int q = 0; q < ac; ++q)
+				{
+					float4 g = ag[(size_t)t * ac + q], h = ag[(size_t)v * ac + q];
+					g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
+					ag[(size_t)t * ac + q] = g;
+				}
+			}
+			derrbits = maxableBits(qerror(Q0, ldpos(pos, remap[cr[r0]])));
+		}
 	}
+	unsigned int bm = blockMaxU32(errbits, smem);
+	if (threadIdx.x == 0 && bm)
+		atomicMax(&sc->result_error_bits, bm);
+	__syncthreads();
+	unsigned int bd = blockMaxU32(derrbits, smem);
+	if (threadIdx.x == 0 && bd)
+		atomicMax(&sc->vertex_error_bits, bd);
 }
 
 // remapEdgeLoops :1845-1864 for loop and loopback; the in-place parallel form reads the
@@ -1423,6 +1541,10 @@ Simplifier::Simplifier(int device) : device_(device)
 {
 	MO_CUDA_CHECK(cudaSetDevice(device));
 	MO_CUDA_CHECK(cudaMallocHost(&pinned_, 4096));
+	int sms = 0, per_sm = 0;
+	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kRounds, kThreads, 0));
+	coop_blocks_ = unsigned(std::max(1, sms * std::max(per_sm, 1)));
 }
 
 Simplifier::~Simplifier()
@@ -1447,11 +1569,11 @@ float Simplifier::scale(const float* d_positions, size_t vertex_count, size_t st
 	size_t V = vertex_count;
 	if (V)
 		MO_LAUNCH(kGatherPositions, gridFor(V, kThreads), kThreads, 0, stream, d_positions, stride / 4, V, w.pos_raw);
-	size_t per = (V + 4096 * kMinMaxThreads - 1) / (4096 * kMinMaxThreads);
+	size_t per = (V + kMinMaxMaxThreads - 1) / kMinMaxMaxThreads;
 	per = per ? per : 1;
 	unsigned int mmb = gridFor((V + per - 1) / per, kMinMaxThreads);
 	MO_LAUNCH(kMinMaxPartial, mmb, kMinMaxThreads, 0, stream, w.pos_raw, V, per, w.partial);
-	MO_LAUNCH(kMinMaxFinal, 1, 32, 0, stream, w.partial, mmb, w.sc);
+	MO_LAUNCH(kMinMaxFinal, 1, kMinMaxThreads, 0, stream, w.partial, mmb, w.sc);
 	Scalars* h = reinterpret_cast<Scalars*>(pinned_);
 	MO_CUDA_CHECK(cudaMemcpyAsync(h, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
 	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
@@ -1575,11 +1697,11 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	}
 
 	// rescale
-	size_t per = (V + 4096 * kMinMaxThreads - 1) / (4096 * kMinMaxThreads);
+	size_t per = (V + kMinMaxMaxThreads - 1) / kMinMaxMaxThreads;
 	per = per ? per : 1;
 	unsigned int mmb = gridFor((V + per - 1) / per, kMinMaxThreads);
 	MO_LAUNCH(kMinMaxPartial, mmb, kMinMaxThreads, 0, stream, w.pos_raw, V, per, w.partial);
-	MO_LAUNCH(kMinMaxFinal, 1, 32, 0, stream, w.partial, mmb, w.sc);
+	MO_LAUNCH(kMinMaxFinal, 1, kMinMaxThreads, 0, stream, w.partial, mmb, w.sc);
 	if (V)
 		MO_LAUNCH(kRescale, gV, kThreads, 0, stream, w.pos_raw, V, w.sc, w.pos);
 	if (ac && V)
@@ -1698,32 +1820,37 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
-		// perform: decision rounds
-		MO_LAUNCH(kPerformInit, gV, kThreads, 0, stream, V, w.touched, w.moved_by, w.cr, w.minT, w.minS);
-		const unsigned int* active = nullptr;
-		unsigned int* next = w.act0;
-		size_t act_count = C;
-		unsigned int round = 0;
-		unsigned long long active_sum = 0;
-		while (act_count)
+		// perform: all decision rounds in one cooperative launch
 		{
-			active_sum += act_count;
-			++round;
-			if (round > C + 1)
-				throw std::runtime_error("collapse decision rounds did not converge");
-			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->active_count, 0, 4, stream));
-			unsigned int gA = gridFor(act_count, kThreads);
-			MO_LAUNCH(kMark, gA, kThreads, 0, stream, active, act_count, w.srec, round, w.minT, w.minS);
-			MO_LAUNCH(kDecide, gA, kThreads, 0, stream, active, act_count, round, w.srec, w.skind, w.minT, w.minS, w.touched, w.moved_by, w.moved_to, w.status,
-			    w.adj_off, w.adj, w.pos, w.remap, w.wedge, w.loop, w.loopback, next, &w.sc->active_count);
-			readScalars();
-			if (hs->active_count >= act_count)
-				throw std::runtime_error("collapse decision round made no progress");
-			act_count = hs->active_count;
-			active = next;
-			next = (next == w.act0) ? w.act1 : w.act0;
+			RoundsArgs ra;
+			ra.count = C;
+			ra.vcount = V;
+			ra.srec = w.srec;
+			ra.skind = w.skind;
+			ra.minT = w.minT;
+			ra.minS = w.minS;
+			ra.touched = w.touched;
+			ra.moved_by = w.moved_by;
+			ra.moved_to = w.moved_to;
+			ra.cr = w.cr;
+			ra.status = w.status;
+			ra.adj_off = w.adj_off;
+			ra.adj = w.adj;
+			ra.pos = w.pos;
+			ra.remap = w.remap;
+			ra.wedge = w.wedge;
+			ra.loop = w.loop;
+			ra.loopback = w.loopback;
+			ra.list[0] = w.act0;
+			ra.list[1] = w.act1;
+			ra.sc = w.sc;
+			MO_CUDA_CHECK(cudaMemsetAsync(w.sc->bar, 0, sizeof(unsigned int) * 3, stream));
+			unsigned int blocks = std::max(1u, std::min(coop_blocks_, gridFor(std::max(C, V), kThreads)));
+			void* params[] = {&ra};
+			cudaEvent_t e0 = probeBegin("kRounds", stream);
+			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kRounds, dim3(blocks), dim3(kThreads), params, 0, stream));
+			probeEnd(e0, stream);
 		}
-
 		// stop rules
 		const size_t goal = (result_count - m.target_index_count) / 3;
 		const unsigned int nblk = unsigned((C + kStopTile - 1) / kStopTile);
@@ -1732,6 +1859,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->cut, 0xFF, 8, stream));
 		MO_LAUNCH(kStopFind, nblk, 256, 0, stream, C, w.status, w.skind, w.serr, w.blk, result_error_bits, error_limit, goal, &w.sc->cut);
 		readScalars();
+		if (hs->grid_error)
+			throw std::runtime_error(hs->grid_error & 2 ? "collapse decision round made no progress" : "grid barrier wait limit reached");
+		const unsigned int round = hs->rounds;
+		const unsigned long long active_sum = hs->active_sum;
 		const unsigned long long cutv = hs->cut;
 		const size_t cut = cutv == ~0ull ? C : size_t(cutv >> 2);
 		const unsigned int reason = cutv == ~0ull ? 0 : unsigned(cutv & 3);

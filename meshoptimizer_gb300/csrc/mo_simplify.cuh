@@ -115,6 +115,7 @@ private:
 	int device_;
 	DeviceArena arena_;
 	unsigned int* pinned_ = nullptr; // small pinned readback buffer
+	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative rounds kernel
 };
 
 } // namespace mogpu
