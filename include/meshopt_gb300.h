@@ -113,6 +113,21 @@ MESHOPTGPU_API void meshoptgpu_getKernelProfile(unsigned long long* launches, do
 /* Bytes of device scratch one call on a mesh of this shape needs (for admission control). */
 MESHOPTGPU_API size_t meshoptgpu_workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count);
 
+/* Allocation-free mesh extent. No counterpart in the reference: it is the device-pointer
+ * form of meshopt_simplifyScale for callers that must not allocate device memory while they
+ * run (work recorded into a CUDA graph, a frame loop with a fixed memory budget, a plugin
+ * whose host owns all allocations). It writes the extent (the value meshopt_simplifyScale
+ * returns) to the device float *extent, reading positions that are already on the device,
+ * enqueued on `stream` without synchronising; it calls no cudaMalloc/cudaFree.
+ * Its scratch is a fixed 512 KiB device array inside the library (held on every GPU that
+ * loads it until exit), which limits vertex_count to 67,108,864; larger counts return
+ * meshoptgpu_StatusInvalidArgument. The first call on each device looks up that array's
+ * device address: make it before any stream capture. All calls share the array, so calls
+ * that overlap on the GPU race; order them (e.g. one stream). Returns a meshoptgpu_Status*
+ * value (this call does not update meshoptgpu_getLastStatus). */
+MESHOPTGPU_API int meshoptgpu_simplifyScaleNoAlloc(float* extent, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
+    void* stream);
+
 /* Releases the calling thread's device scratch and streams. */
 MESHOPTGPU_API void meshoptgpu_releaseThreadResources(void);
 

@@ -44,7 +44,7 @@ EXPORTS = [
     "meshoptgpu_getLastStatus", "meshoptgpu_getLastMessage", "meshoptgpu_getLastPassStats",
     "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
     "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
-    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile",
+    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc",
 ]
 
 
@@ -90,6 +90,8 @@ def load():
     lib.meshoptgpu_getLaunchCount.restype = C.c_ulonglong
     lib.meshoptgpu_setKernelProfile.argtypes = [C.c_char_p]
     lib.meshoptgpu_getKernelProfile.argtypes = [vp, vp]
+    lib.meshoptgpu_simplifyScaleNoAlloc.restype = C.c_int
+    lib.meshoptgpu_simplifyScaleNoAlloc.argtypes = [vp, vp, sz, sz, vp]
     _lib = lib
     return lib
 
@@ -218,3 +220,15 @@ def kernel_profile():
     ms = C.c_double(0)
     load().meshoptgpu_getKernelProfile(C.byref(n), C.byref(ms))
     return int(n.value), float(ms.value)
+
+
+def simplify_scale_noalloc(d_extent, d_positions, vertex_count, positions_stride=12, stream=0):
+    """meshoptgpu_simplifyScaleNoAlloc: writes the extent to the device float at d_extent.
+
+    For callers that must not allocate device memory while they run (graph capture, fixed
+    budgets); it reads device positions and uses only the library's fixed 512 KiB scratch,
+    which limits vertex_count to 67,108,864. Enqueued on `stream` without synchronising.
+    Returns the status code (0 on success).
+    """
+    return int(load().meshoptgpu_simplifyScaleNoAlloc(C.c_void_p(d_extent), C.c_void_p(d_positions or None), vertex_count,
+                                                      positions_stride, C.c_void_p(stream or None)))
