@@ -39,16 +39,18 @@ sys.path.insert(0, ROOT)
 
 from meshoptimizer_gb300 import workloads as W  # noqa: E402
 
-# Algorithmic bytes per unit for the kernels that can dominate a run:
-#   per active candidate for the decision-round kernels, per candidate for rank/gather,
-#   per pair per pass for the radix passes, per corner for the setup folds.
-KERNEL_BYTES = {
-    "kDecide": ("active candidates", 29),       # active id 4 + record 16 + status 1 + 2 touched + list append 4 + pad
-    "kMark": ("active candidates", 20),         # active id 4 + record 16 (atomics land in L2)
-    "kRank": ("candidates", 24),                # v0, v1, bidi/err in 12 + v0, v1, err, key out 16 (-4 overlap)
-    "kRadixScatter": ("pairs", 16),             # key+value in 8, key+value out 8
-    "kFillQuadrics": ("vertices", 48 + 16 + 8), # quadric out, position, CSR offsets
-}
+# Algorithmic bytes of the dominant kernel, kPerform (one cooperative launch per pass), from
+# the per-pass counters the library reports:
+#   decision rounds   29 B per active candidate (id 4, record 16, status 1, touched 2, append 4, pad 2)
+#   stop-rule scan    12 B per evaluated candidate (status, kind, error bits, read twice)
+#   per-vertex init   9 B per vertex (touched, moved_by, collapse_remap)
+#   apply             164 B per committed collapse (record 16, two quadrics read 96, one written 48, remap 4)
+#   loop remap        16 B per vertex (loop and loopback read and written)
+#   compaction        24 B per input triangle (indices read twice) + 12 B per kept triangle
+def kperform_bytes(p, vertices, next_triangles):
+    return (29 * p["active"] + 12 * p["evaluated"] + 9 * vertices + 164 * p["done"] + 16 * vertices
+            + 24 * p["triangles"] + 12 * next_triangles)
+
 
 WORKLOADS = {
     "sphere_attr_2m": lambda: W.config_sphere_attr(9),
@@ -188,7 +190,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sphere_attr_2m", choices=sorted(WORKLOADS))
-    ap.add_argument("--kernel", default="kDecide", help="kernel whose CUDA-event time gives the roofline line")
+    ap.add_argument("--kernel", default="kPerform", help="kernel whose CUDA-event time gives the roofline line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -308,23 +310,19 @@ def main():
 
     # roofline of the selected kernel: algorithmic bytes over its measured launch time
     peak, peak_kind = measured_peak()
-    unit_name, per_unit = KERNEL_BYTES.get(args.kernel, ("units", 0))
     roofline = None
     if k_launches:
         avg_ms = k_ms / k_launches
-        # units one launch processes, from the per-pass counters of one run
-        if args.kernel in ("kDecide", "kMark"):
-            units_per_launch = sum(p["active"] for p in passes) / max(sum(p["rounds"] for p in passes), 1)
-        elif args.kernel == "kRank":
-            units_per_launch = sum(p["candidates"] for p in passes) / max(len(passes), 1)
-        else:
-            units_per_launch = 0
-        bytes_per_launch = units_per_launch * per_unit
+        nxt = [p["triangles"] for p in passes[1:]] + [int(n_out) // 3]
+        bytes_run = sum(kperform_bytes(p, V, t) for p, t in zip(passes, nxt))
+        bytes_per_launch = bytes_run / max(len(passes), 1)
         achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0
         roofline = {"bound": "hbm", "kernel": args.kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
                     "avg_launch_us": round(1e3 * avg_ms, 2), "launches": k_launches,
-                    "algorithmic_bytes_per_launch": int(bytes_per_launch), "unit_definition": f"{per_unit} B per {unit_name}",
+                    "algorithmic_bytes_per_launch": int(bytes_per_launch),
+                    "unit_definition": "kperform_bytes(): rounds 29 B/active candidate, stop 12 B/evaluated, apply 164 B/commit, "
+                                       "25 B/vertex, 24 B/triangle + 12 B/kept triangle",
                     "share_of_step": round(k_ms / total_ms, 4)}
 
     cpu = None
@@ -345,7 +343,7 @@ def main():
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact,
         "clocks": clocks.summary(), "gpu_launches": int(launches),
         "phases_ms": {k: round(v, 3) for k, v in phases.items()},
-        "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active")} for p in passes],
+        "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active", "windows")} for p in passes],
     }
     print(json.dumps(line))
     if dist:

@@ -77,10 +77,11 @@ MESHOPTGPU_API const char* meshoptgpu_getLastMessage(void);
 /* Per-pass counters of the calling thread's last call: the quantities the reference
  * prints under TRACE (src/simplifier.cpp:1625-1633). stop: 0 out of collapses,
  * 1 error limit, 2 count limit, 3 error goal. rounds: decision rounds of the pass;
- * active: candidates processed by the decision kernels, summed over its rounds. */
+ * active: candidates processed by the decision rounds, summed over its rounds; windows:
+ * sorted-order windows decided before the stop cut was found. */
 typedef struct meshoptgpu_PassStats
 {
-	unsigned int triangles, candidates, evaluated, done, skipped, invalid, stop, rounds, active;
+	unsigned int triangles, candidates, evaluated, done, skipped, invalid, stop, rounds, active, windows;
 } meshoptgpu_PassStats;
 
 /* Copies up to max_passes entries; returns the number of passes of the last call. */

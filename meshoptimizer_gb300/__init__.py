@@ -49,7 +49,7 @@ EXPORTS = [
 
 
 class PassStats(C.Structure):
-    _fields_ = [(n, C.c_uint) for n in ("triangles", "candidates", "evaluated", "done", "skipped", "invalid", "stop", "rounds", "active")]
+    _fields_ = [(n, C.c_uint) for n in ("triangles", "candidates", "evaluated", "done", "skipped", "invalid", "stop", "rounds", "active", "windows")]
 
 
 class SimplifyError(RuntimeError):

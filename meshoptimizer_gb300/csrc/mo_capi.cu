@@ -289,7 +289,7 @@ int meshoptgpu_getLastPassStats(meshoptgpu_PassStats* out, int max_passes)
 	for (int i = 0; i < n && i < max_passes; ++i)
 	{
 		const PassStats& p = s.last.pass[i];
-		out[i] = meshoptgpu_PassStats{p.triangles, p.candidates, p.evaluated, p.done, p.skipped, p.invalid, p.stop, p.rounds, p.active};
+		out[i] = meshoptgpu_PassStats{p.triangles, p.candidates, p.evaluated, p.done, p.skipped, p.invalid, p.stop, p.rounds, p.active, p.windows};
 	}
 	return s.last.passes;
 }

@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace mogpu
@@ -59,8 +60,10 @@ struct Scalars
 	unsigned int bar[2];          // grid barrier (arrivals, generation)
 	unsigned int grid_error;      // a grid barrier gave up waiting
 	unsigned int rounds;          // decision rounds of the last pass
-	unsigned int act_count[2];    // active candidates of the current / next round
+	unsigned int act_count[3];    // appended candidates, rotating by round (round r appends to [(r+1)%3])
 	unsigned long long active_sum; // candidates processed by the rounds of the last pass
+	unsigned int carry[3];        // stop-rule prefix (triangles, flips, max error) after a window
+	unsigned int windows;         // sorted-order windows the last pass needed
 };
 
 __device__ __forceinline__ size_t gtid()
@@ -820,7 +823,15 @@ __global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ ord
 	status[k] = kUndecided;
 }
 
-// ---------------------------------------------------------------- pass: perform (rounds)
+// ---------------------------------------------------------------- pass: perform
+//
+// kPerform runs, in one cooperative launch per pass, everything from the sorted candidates
+// to the next pass's index buffer: the decision rounds (performEdgeCollapses :1498-1636 made
+// order-free), the stop rules as a prefix scan over sorted order, the collapse_remap writes
+// and quadric merges of the committed prefix (:1574-1616, updateQuadrics :1638-1673), the
+// loop remap (:1845-1864) and the order-preserving index compaction (:1811-1843). Phases are
+// separated by grid barriers (mo_grid.cuh); data written by other blocks in an earlier phase
+// is read through L2 (ld.global.cg).
 
 __device__ __forceinline__ unsigned long long roundTag(unsigned int round)
 {
@@ -832,58 +843,77 @@ __device__ __forceinline__ bool earlierThan(unsigned long long v, unsigned long 
 	return (v >> 32) == (tag >> 32) && (unsigned int)v < k;
 }
 
-// Decision rule of the rounds (performEdgeCollapses :1511-1623 made order-free): candidate k
-// is decided once nothing earlier in sorted order can change its outcome:
-//  * an earlier candidate already committed on one of its endpoints -> locked (final: any
-//    commit seen on an endpoint has a smaller sorted index);
-//  * otherwise it waits until it is the earliest undecided candidate on both endpoints and no
-//    undecided earlier candidate moves a vertex of its one-ring; then the flip test runs
-//    against the one-ring as moved by earlier commits only (moved_by < k).
-struct RoundsArgs
+struct PerformArgs
 {
-	size_t count;
-	size_t vcount;
+	// sorted candidates
+	unsigned int count;
 	const uint4* srec;
 	const unsigned char* skind;
-	unsigned long long* minT;
-	unsigned long long* minS;
+	const unsigned int* serr;
+	unsigned char* status;
+	// per-vertex decision state; marks alternate by round parity
+	unsigned int vcount;
+	unsigned long long* minT[2];
+	unsigned long long* minS[2];
 	unsigned char* touched;
 	unsigned int* moved_by;
 	unsigned int* moved_to;
 	unsigned int* cr;
-	unsigned char* status;
+	unsigned int* list[2];
+	// mesh
 	const unsigned int* adj_off;
 	const uint2* adj;
 	const float4* pos;
 	const unsigned int* remap;
 	const unsigned int* wedge;
-	const unsigned int* loop;
-	const unsigned int* loopback;
-	unsigned int* list[2];
+	unsigned int* loop;
+	unsigned int* loopback;
+	Quadric* vq;
+	Quadric* aq;
+	float4* ag;
+	int ac;
+	// stop rules
+	unsigned int prev_err_bits;
+	float error_limit;
+	unsigned long long goal;
+	unsigned int first_window;
+	unsigned int round_base;
+	// compaction
+	const unsigned int* res;
+	unsigned int* res_next;
+	unsigned int tris;
+	uint4* blk;
 	Scalars* sc;
 };
 
-// One decision of the rounds below for candidate k; returns true if k stays undecided.
-// Arrays written during the rounds (minT, minS, touched, moved_by, moved_to) are read
-// through L2 (ld.global.cg): other blocks write them between grid barriers.
-__device__ __forceinline__ bool decideOne(const RoundsArgs& a, unsigned int k, unsigned int round)
+// Decision rule: candidate k is decided once nothing earlier in sorted order can change its
+// outcome:
+//  * an earlier candidate already committed on one of its endpoints -> locked (final: any
+//    commit seen on an endpoint has a smaller sorted index);
+//  * otherwise it waits until it is the earliest undecided candidate on both endpoints (minT)
+//    and no undecided earlier candidate moves a vertex of its one-ring (minS); then the flip
+//    test runs against the one-ring as moved by earlier commits only (moved_by < k).
+// Returns true if k stays undecided.
+__device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, unsigned int round)
 {
 	uint4 rec = __ldg(a.srec + k);
 	unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
 	const unsigned long long tag = roundTag(round);
 	const unsigned long long mine = tag | k;
+	const unsigned long long* minT = a.minT[round & 1];
+	const unsigned long long* minS = a.minS[round & 1];
 	if (__ldcg(a.touched + r0) | __ldcg(a.touched + r1))
 	{
 		a.status[k] = kSkipLocked;
 		return false;
 	}
-	if (__ldcg(a.minT + r0) != mine || __ldcg(a.minT + r1) != mine)
+	if (__ldcg(minT + r0) != mine || __ldcg(minT + r1) != mine)
 		return true;
 	unsigned int b = __ldg(a.adj_off + r0), e = __ldg(a.adj_off + r0 + 1);
 	for (unsigned int j = b; j < e; ++j)
 	{
 		uint2 ed = __ldg(a.adj + j);
-		if (earlierThan(__ldcg(a.minS + ed.x), tag, k) || earlierThan(__ldcg(a.minS + ed.y), tag, k))
+		if (earlierThan(__ldcg(minS + ed.x), tag, k) || earlierThan(__ldcg(minS + ed.y), tag, k))
 			return true;
 	}
 	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
@@ -922,95 +952,14 @@ __device__ __forceinline__ bool decideOne(const RoundsArgs& a, unsigned int k, u
 	return false;
 }
 
-// All decision rounds of one pass in one cooperative launch. Round r reads the candidates
-// left undecided by round r-1 (round 1: every candidate, in sorted order) and appends the
-// ones that stay undecided to the other list; grid barriers separate the phases. Each round
-// decides at least the earliest undecided candidate, so the loop ends after at most
-// `count` rounds; a round without progress is reported as an error.
-__global__ void __launch_bounds__(kThreads) kRounds(RoundsArgs a)
+__device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int k, unsigned int round)
 {
-	Scalars* sc = a.sc;
-	const size_t gthreads = (size_t)gridDim.x * blockDim.x;
-	const unsigned int lane = threadIdx.x & 31;
-	const size_t wbase = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
-
-	for (size_t i = gtid(); i < a.vcount; i += gthreads)
-	{
-		a.touched[i] = 0;
-		a.moved_by[i] = ~0u;
-		a.cr[i] = (unsigned int)i;
-		a.minT[i] = ~0ull;
-		a.minS[i] = ~0ull;
-	}
-	gridBarrier(sc->bar, &sc->grid_error);
-
-	unsigned long long active_sum = 0;
-	unsigned int n = (unsigned int)a.count;
-	unsigned int round = 0;
-	while (n)
-	{
-		++round;
-		if (round > a.count + 1 || __ldcg(&sc->grid_error))
-			break;
-		active_sum += n;
-		const unsigned int* list = round == 1 ? nullptr : a.list[round & 1];
-		unsigned int* next = a.list[(round + 1) & 1];
-		unsigned int* next_count = &sc->act_count[(round + 1) & 1];
-		const unsigned long long key_tag = roundTag(round);
-
-		for (size_t x = gtid(); x < n; x += gthreads)
-		{
-			unsigned int k = list ? __ldcg(list + x) : (unsigned int)x;
-			uint4 rec = __ldg(a.srec + k);
-			unsigned long long key = key_tag | k;
-			atomicMin(&a.minT[rec.z], key);
-			atomicMin(&a.minT[rec.w], key);
-			atomicMin(&a.minS[rec.z], key);
-		}
-		if (gtid() == 0)
-			*next_count = 0;
-		gridBarrier(sc->bar, &sc->grid_error);
-
-		for (size_t base = wbase; base < n; base += gthreads)
-		{
-			size_t x = base + lane;
-			bool keep = false;
-			unsigned int k = 0;
-			if (x < n)
-			{
-				k = list ? __ldcg(list + x) : (unsigned int)x;
-				keep = decideOne(a, k, round);
-			}
-			unsigned int m = __ballot_sync(0xffffffffu, keep);
-			if (m)
-			{
-				unsigned int leader = __ffs(m) - 1;
-				unsigned int o = 0;
-				if (lane == leader)
-					o = atomicAdd(next_count, __popc(m));
-				o = __shfl_sync(0xffffffffu, o, leader);
-				if (keep)
-					next[o + __popc(m & ((1u << lane) - 1u))] = k;
-			}
-		}
-		gridBarrier(sc->bar, &sc->grid_error);
-		unsigned int nn = __ldcg(next_count);
-		if (nn >= n)
-		{
-			if (gtid() == 0)
-				atomicOr(&sc->grid_error, 2u);
-			break;
-		}
-		n = nn;
-	}
-	if (gtid() == 0)
-	{
-		sc->rounds = round;
-		sc->active_sum = active_sum;
-	}
+	uint4 rec = __ldg(a.srec + k);
+	unsigned long long key = roundTag(round) | k;
+	atomicMin(&a.minT[round & 1][rec.z], key);
+	atomicMin(&a.minT[round & 1][rec.w], key);
+	atomicMin(&a.minS[round & 1][rec.z], key);
 }
-
-// ---------------------------------------------------------------- pass: stop rules
 
 // per sorted candidate: triangles removed if committed, flip rejection, committed error
 __device__ __forceinline__ void stopTerms(unsigned char st, unsigned char kd, unsigned int errbits, unsigned int& tri, unsigned int& flip, unsigned int& errc)
@@ -1022,363 +971,408 @@ __device__ __forceinline__ void stopTerms(unsigned char st, unsigned char kd, un
 	errc = (commit && e == e) ? errbits : 0u; // NaN never raises result_error
 }
 
-__global__ void __launch_bounds__(256) kStopReduce(size_t count, const unsigned char* __restrict__ status, const unsigned char* __restrict__ skind,
-    const unsigned int* __restrict__ serr, uint4* __restrict__ blk)
+// block-wide exclusive scan of (sum, sum, max) triples; returns the block totals
+__device__ __forceinline__ uint3 blockScan3(unsigned int& t, unsigned int& f, unsigned int& m, unsigned int (*sm)[33])
 {
-	__shared__ unsigned int smem[3][8];
-	unsigned int st = 0, sf = 0, sm = 0;
-	size_t base = (size_t)blockIdx.x * kStopTile + threadIdx.x * 4;
-	for (int j = 0; j < 4; ++j)
-	{
-		size_t k = base + j;
-		if (k < count)
-		{
-			unsigned int t, f, e;
-			stopTerms(status[k], skind[k], serr[k], t, f, e);
-			st += t, sf += f, sm = max(sm, e);
-		}
-	}
-	for (int o = 16; o > 0; o >>= 1)
-	{
-		st += __shfl_down_sync(0xffffffffu, st, o);
-		sf += __shfl_down_sync(0xffffffffu, sf, o);
-		sm = max(sm, __shfl_down_sync(0xffffffffu, sm, o));
-	}
-	int w = threadIdx.x >> 5;
-	if ((threadIdx.x & 31) == 0)
-		smem[0][w] = st, smem[1][w] = sf, smem[2][w] = sm;
-	__syncthreads();
-	if (threadIdx.x == 0)
-	{
-		unsigned int a = 0, b = 0, c = 0;
-		for (int q = 0; q < 8; ++q)
-			a += smem[0][q], b += smem[1][q], c = max(c, smem[2][q]);
-		blk[blockIdx.x] = make_uint4(a, b, c, 0);
-	}
-}
-
-// exclusive scan of the block aggregates (sum, sum, max), single block, in place
-__global__ void __launch_bounds__(1024) kStopScanBlocks(uint4* blk, unsigned int nblk)
-{
-	__shared__ unsigned int sm[3][33];
-	unsigned int carryT = 0, carryF = 0, carryM = 0;
-	for (unsigned int base = 0; base < nblk; base += 1024)
-	{
-		unsigned int i = base + threadIdx.x;
-		uint4 v = i < nblk ? blk[i] : make_uint4(0, 0, 0, 0);
-		unsigned int t = v.x, f = v.y, m = v.z;
-		unsigned int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-		unsigned int it = t, iff = f, im = m;
-		for (int o = 1; o < 32; o <<= 1)
-		{
-			unsigned int a = __shfl_up_sync(0xffffffffu, it, o), b = __shfl_up_sync(0xffffffffu, iff, o), c = __shfl_up_sync(0xffffffffu, im, o);
-			if (lane >= (unsigned)o)
-				it += a, iff += b, im = max(im, c);
-		}
-		if (lane == 31)
-			sm[0][w] = it, sm[1][w] = iff, sm[2][w] = im;
-		__syncthreads();
-		if (w == 0)
-		{
-			unsigned int a = sm[0][lane], b = sm[1][lane], c = sm[2][lane];
-			unsigned int ia = a, ib = b, ic = c;
-			for (int o = 1; o < 32; o <<= 1)
-			{
-				unsigned int x = __shfl_up_sync(0xffffffffu, ia, o), y = __shfl_up_sync(0xffffffffu, ib, o), z = __shfl_up_sync(0xffffffffu, ic, o);
-				if (lane >= (unsigned)o)
-					ia += x, ib += y, ic = max(ic, z);
-			}
-			// exclusive warp prefixes, shifted by one lane
-			unsigned int ea = __shfl_up_sync(0xffffffffu, ia, 1), eb = __shfl_up_sync(0xffffffffu, ib, 1), ec = __shfl_up_sync(0xffffffffu, ic, 1);
-			sm[0][lane] = lane ? ea : 0;
-			sm[1][lane] = lane ? eb : 0;
-			sm[2][lane] = lane ? ec : 0;
-			if (lane == 31)
-				sm[0][32] = ia, sm[1][32] = ib, sm[2][32] = ic;
-		}
-		__syncthreads();
-		unsigned int et = carryT + sm[0][w] + it - t;
-		unsigned int ef = carryF + sm[1][w] + iff - f;
-		// exclusive max: max of the warps before and lanes before
-		unsigned int prevLane = __shfl_up_sync(0xffffffffu, im, 1);
-		unsigned int em = max(carryM, max(sm[2][w], lane ? prevLane : 0u));
-		if (i < nblk)
-			blk[i] = make_uint4(et, ef, em, 0);
-		unsigned int tT = sm[0][32], tF = sm[1][32], tM = sm[2][32];
-		__syncthreads();
-		carryT += tT, carryF += tF, carryM = max(carryM, tM);
-	}
-}
-
-// evaluates the three stop rules of performEdgeCollapses (:1517-1539) at every sorted
-// position with the prefix state of the decisions before it; the cut is the first hit
-__global__ void __launch_bounds__(256) kStopFind(size_t count, const unsigned char* __restrict__ status, const unsigned char* __restrict__ skind,
-    const unsigned int* __restrict__ serr, const uint4* __restrict__ blk, unsigned int prev_err_bits, float error_limit, unsigned long long goal,
-    unsigned long long* cut)
-{
-	__shared__ unsigned int smem[3][9];
-	size_t base = (size_t)blockIdx.x * kStopTile + threadIdx.x * 4;
-	unsigned int tt[4], ff[4], ee[4];
-	unsigned int st = 0, sf = 0, sm = 0;
-	for (int j = 0; j < 4; ++j)
-	{
-		size_t k = base + j;
-		tt[j] = ff[j] = ee[j] = 0;
-		if (k < count)
-			stopTerms(status[k], skind[k], serr[k], tt[j], ff[j], ee[j]);
-		st += tt[j], sf += ff[j], sm = max(sm, ee[j]);
-	}
-	// block exclusive scans of (sum, sum, max) over thread aggregates
 	unsigned int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-	unsigned int it = st, iff = sf, im = sm;
+	unsigned int it = t, iff = f, im = m;
 	for (int o = 1; o < 32; o <<= 1)
 	{
-		unsigned int a = __shfl_up_sync(0xffffffffu, it, o), b = __shfl_up_sync(0xffffffffu, iff, o), c = __shfl_up_sync(0xffffffffu, im, o);
+		unsigned int x = __shfl_up_sync(0xffffffffu, it, o), y = __shfl_up_sync(0xffffffffu, iff, o), z = __shfl_up_sync(0xffffffffu, im, o);
 		if (lane >= (unsigned)o)
-			it += a, iff += b, im = max(im, c);
+			it += x, iff += y, im = max(im, z);
 	}
+	unsigned int pm = __shfl_up_sync(0xffffffffu, im, 1);
 	if (lane == 31)
-		smem[0][w] = it, smem[1][w] = iff, smem[2][w] = im;
+		sm[0][w] = it, sm[1][w] = iff, sm[2][w] = im;
 	__syncthreads();
 	if (threadIdx.x == 0)
 	{
-		unsigned int a = 0, b = 0, c = 0;
-		for (int q = 0; q < 8; ++q)
-		{
-			unsigned int x = smem[0][q], y = smem[1][q], z = smem[2][q];
-			smem[0][q] = a, smem[1][q] = b, smem[2][q] = c;
-			a += x, b += y, c = max(c, z);
-		}
-	}
-	__syncthreads();
-	unsigned int prevLaneM = __shfl_up_sync(0xffffffffu, im, 1);
-	uint4 bb = blk[blockIdx.x];
-	unsigned long long T = (unsigned long long)bb.x + smem[0][w] + (it - st);
-	unsigned long long G = (unsigned long long)bb.y + smem[1][w] + (iff - sf);
-	unsigned int M = max(max(bb.z, smem[2][w]), lane ? prevLaneM : 0u);
-	M = max(M, prev_err_bits);
-
-	const unsigned long long egoal0 = goal / 2;
-	for (int j = 0; j < 4; ++j)
-	{
-		size_t k = base + j;
-		if (k >= count)
-			break;
-		float e = __uint_as_float(serr[k]);
-		unsigned int reason = 0;
-		if (e > error_limit)
-			reason = 1;
-		else if (T >= goal)
-			reason = 2;
-		else
-		{
-			unsigned long long eg = egoal0 + G;
-			float error_goal = eg < count ? 1.5f * __uint_as_float(serr[eg]) : FLT_MAX;
-			float R = __uint_as_float(M);
-			if (e > error_goal && e > R && T > goal / 6)
-				reason = 3;
-		}
-		if (reason)
-		{
-			atomicMin(cut, ((unsigned long long)k << 2) | reason);
-			break;
-		}
-		T += tt[j];
-		G += ff[j];
-		M = max(M, ee[j]);
-	}
-}
-
-// ---------------------------------------------------------------- pass: apply
-
-// commits before the cut: collapse_remap writes (performEdgeCollapses :1574-1616) and the
-// quadric merges of updateQuadrics (:1638-1673); every target receives at most one source
-// position quadric per pass (endpoints of commits are disjoint), and attribute sources of one
-// commit are merged in vertex order
-__device__ __forceinline__ unsigned int blockMaxU32(unsigned int v, unsigned int* smem)
-{
-	for (int o = 16; o > 0; o >>= 1)
-		v = max(v, __shfl_down_sync(0xffffffffu, v, o));
-	if ((threadIdx.x & 31) == 0)
-		smem[threadIdx.x >> 5] = v;
-	__syncthreads();
-	unsigned int r = 0;
-	if (threadIdx.x == 0)
+		unsigned int x = 0, y = 0, z = 0;
 		for (unsigned int q = 0; q < blockDim.x / 32; ++q)
-			r = max(r, smem[q]);
-	return r;
-}
-
-// error bits usable by the max reductions (errors are non-negative; NaN never raises them)
-__device__ __forceinline__ unsigned int maxableBits(float v)
-{
-	return v == v ? __float_as_uint(v) : 0u;
-}
-
-__global__ void __launch_bounds__(kThreads) kApply(size_t cut, const uint4* __restrict__ srec, const unsigned char* __restrict__ skind,
-    const unsigned char* __restrict__ status, const unsigned int* __restrict__ serr, const unsigned int* __restrict__ remap,
-    const unsigned int* __restrict__ wedge, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ cr,
-    Quadric* vq, const float4* __restrict__ pos, Quadric* aq, float4* ag, int ac, Scalars* sc)
-{
-	__shared__ unsigned int smem[kThreads / 32];
-	size_t k = gtid();
-	unsigned int st = k < cut ? status[k] : 0;
-	unsigned int nc = __syncthreads_count(st == kCommit), nl = __syncthreads_count(st == kSkipLocked), nf = __syncthreads_count(st == kSkipFlip);
-	if (threadIdx.x == 0)
-	{
-		if (nc)
-			atomicAdd(&sc->done, nc);
-		if (nl)
-			atomicAdd(&sc->skipped, nl);
-		if (nf)
-			atomicAdd(&sc->invalid, nf);
+		{
+			unsigned int a = sm[0][q], b = sm[1][q], c = sm[2][q];
+			sm[0][q] = x, sm[1][q] = y, sm[2][q] = z;
+			x += a, y += b, z = max(z, c);
+		}
+		sm[0][32] = x, sm[1][32] = y, sm[2][32] = z;
 	}
-	unsigned int errbits = 0, derrbits = 0;
-	if (st == kCommit)
-	{
-		uint4 rec = srec[k];
-		unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
-		unsigned char kd = skind[k];
-
-		unsigned int moved[kMaxAttributes];
-		int nm = 0;
-		if (kd == kComplex)
-		{
-			unsigned int v = i0;
-			do
-			{
-				cr[v] = complexTarget(v, i1, remap, loop, loopback);
-				if (nm < kMaxAttributes)
-					moved[nm++] = v;
-				v = wedge[v];
-			} while (v != i0);
-		}
-		else if (kd == kSeam)
-		{
-			unsigned int s0 = wedge[i0];
-			unsigned int s1 = loop[i0] == i1 ? loopback[s0] : loop[s0];
-			s1 = (s1 != ~0u) ? s1 : wedge[i1];
-			cr[i0] = i1;
-			cr[s0] = s1;
-			moved[nm++] = i0;
-			if (s0 != i0)
-				moved[nm++] = s0;
-		}
-		else
-		{
-			cr[i0] = i1;
-			moved[nm++] = i0;
-		}
-
-		Quadric Q1 = ldquadric(vq, r1);
-		Quadric Q0 = ldquadric(vq, r0);
-		qadd(Q1, Q0);
-		stquadric(vq, r1, Q1);
-
-		errbits = maxableBits(__uint_as_float(serr[k]));
-
-		if (ac)
-		{
-			// merge in increasing vertex order (insertion sort of the few moved wedges)
-			for (int x = 1; x < nm; ++x)
-			{
-				unsigned int v = moved[x];
-				int y = x - 1;
-				while (y >= 0 && moved[y] > v)
-				{
-					moved[y + 1] = moved[y];
-					--y;
-				}
-				moved[y + 1] = v;
-			}
-			for (int m = 0; m < nm; ++m)
-			{
-				unsigned int v = moved[m];
-				unsigned int t = cr[v];
-				Quadric A = ldquadric(aq, t);
-				qadd(A, ldquadric(aq, v));
-				stquadric(aq, t, A);
-				for (int q = 0; q < ac; ++q)
-				{
-					float4 g = ag[(size_t)t * ac + q], h = ag[(size_t)v * ac + q];
-					g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
-					ag[(size_t)t * ac + q] = g;
-				}
-			}
-			derrbits = maxableBits(qerror(Q0, ldpos(pos, remap[cr[r0]])));
-		}
-	}
-	unsigned int bm = blockMaxU32(errbits, smem);
-	if (threadIdx.x == 0 && bm)
-		atomicMax(&sc->result_error_bits, bm);
 	__syncthreads();
-	unsigned int bd = blockMaxU32(derrbits, smem);
-	if (threadIdx.x == 0 && bd)
-		atomicMax(&sc->vertex_error_bits, bd);
+	unsigned int et = sm[0][w] + it - t, ef = sm[1][w] + iff - f, em = max(sm[2][w], lane ? pm : 0u);
+	uint3 tot = make_uint3(sm[0][32], sm[1][32], sm[2][32]);
+	__syncthreads();
+	t = et, f = ef, m = em;
+	return tot;
 }
 
-// remapEdgeLoops :1845-1864 for loop and loopback; the in-place parallel form reads the
-// same values as the serial loop because collapse targets are fixed points of collapse_remap
-__global__ void kRemapLoops(size_t n, const unsigned int* __restrict__ cr, unsigned int* loop, unsigned int* loopback)
-{
-	size_t i = gtid();
-	if (i >= n)
-		return;
-	unsigned int* arrs[2] = {loop, loopback};
-#pragma unroll
-	for (int a = 0; a < 2; ++a)
-	{
-		unsigned int* L = arrs[a];
-		unsigned int l = L[i];
-		if (l == ~0u)
-			continue;
-		unsigned int r = cr[l];
-		if (i == r)
-		{
-			unsigned int ll = L[l];
-			L[i] = ll != ~0u ? cr[ll] : ~0u;
-		}
-		else
-			L[i] = r;
-	}
-}
-
-// remapIndexBuffer :1811-1843 as an order-preserving compaction: per-block counts, scan, emit
-__device__ __forceinline__ bool keepTriangle(const unsigned int* __restrict__ res, size_t t, const unsigned int* __restrict__ cr, const unsigned int* __restrict__ remap,
+__device__ __forceinline__ bool keepTriangle(const unsigned int* __restrict__ res, size_t t, const unsigned int* cr, const unsigned int* __restrict__ remap,
     uint3& out)
 {
-	unsigned int v0 = cr[res[t * 3 + 0]], v1 = cr[res[t * 3 + 1]], v2 = cr[res[t * 3 + 2]];
+	unsigned int v0 = __ldcg(cr + res[t * 3 + 0]), v1 = __ldcg(cr + res[t * 3 + 1]), v2 = __ldcg(cr + res[t * 3 + 2]);
 	unsigned int r0 = remap[v0], r1 = remap[v1], r2 = remap[v2];
 	out = make_uint3(v0, v1, v2);
 	return r0 != r1 && r0 != r2 && r1 != r2;
 }
 
-__global__ void __launch_bounds__(kThreads) kCompactCount(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ cr,
-    const unsigned int* __restrict__ remap, unsigned int* __restrict__ blkcnt)
+// the collapse_remap writes and quadric merges of one committed candidate
+__device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& errbits, unsigned int& derrbits)
 {
-	size_t t = gtid();
-	uint3 o;
-	bool keep = t < tris && keepTriangle(res, t, cr, remap, o);
-	unsigned int c = __syncthreads_count(keep);
-	if (threadIdx.x == 0)
-		blkcnt[blockIdx.x] = c;
+	uint4 rec = __ldg(a.srec + k);
+	unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
+	unsigned char kd = __ldg(a.skind + k);
+
+	unsigned int moved[kMaxAttributes];
+	int nm = 0;
+	if (kd == kComplex)
+	{
+		unsigned int v = i0;
+		do
+		{
+			a.cr[v] = complexTarget(v, i1, a.remap, a.loop, a.loopback);
+			if (nm < kMaxAttributes)
+				moved[nm++] = v;
+			v = a.wedge[v];
+		} while (v != i0);
+	}
+	else if (kd == kSeam)
+	{
+		unsigned int s0 = a.wedge[i0];
+		unsigned int s1 = a.loop[i0] == i1 ? a.loopback[s0] : a.loop[s0];
+		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
+		a.cr[i0] = i1;
+		a.cr[s0] = s1;
+		moved[nm++] = i0;
+		if (s0 != i0)
+			moved[nm++] = s0;
+	}
+	else
+	{
+		a.cr[i0] = i1;
+		moved[nm++] = i0;
+	}
+
+	Quadric Q1 = ldquadric(a.vq, r1);
+	Quadric Q0 = ldquadric(a.vq, r0);
+	qadd(Q1, Q0);
+	stquadric(a.vq, r1, Q1);
+
+	float e = __uint_as_float(__ldg(a.serr + k));
+	errbits = e == e ? __float_as_uint(e) : 0u;
+
+	if (a.ac)
+	{
+		// attribute sources of one commit merge in increasing vertex order (:1642-1671)
+		for (int x = 1; x < nm; ++x)
+		{
+			unsigned int v = moved[x];
+			int y = x - 1;
+			while (y >= 0 && moved[y] > v)
+			{
+				moved[y + 1] = moved[y];
+				--y;
+			}
+			moved[y + 1] = v;
+		}
+		const int ac = a.ac;
+		for (int m = 0; m < nm; ++m)
+		{
+			unsigned int v = moved[m];
+			unsigned int t = a.cr[v];
+			Quadric A = ldquadric(a.aq, t);
+			qadd(A, ldquadric(a.aq, v));
+			stquadric(a.aq, t, A);
+			for (int q = 0; q < ac; ++q)
+			{
+				float4 g = a.ag[(size_t)t * ac + q], h = a.ag[(size_t)v * ac + q];
+				g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
+				a.ag[(size_t)t * ac + q] = g;
+			}
+		}
+		float d = qerror(Q0, ldpos(a.pos, a.remap[a.cr[r0]]));
+		derrbits = d == d ? __float_as_uint(d) : 0u;
+	}
 }
 
-__global__ void __launch_bounds__(kThreads) kCompactEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ cr,
-    const unsigned int* __restrict__ remap, const unsigned int* __restrict__ blkoff, unsigned int* __restrict__ out)
+__global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 {
-	__shared__ unsigned int smem[kThreads / 32 + 1];
-	size_t t = gtid();
-	uint3 o = make_uint3(0, 0, 0);
-	bool keep = t < tris && keepTriangle(res, t, cr, remap, o);
-	unsigned int total;
-	unsigned int pre = blockExclusiveScan<kThreads>(keep ? 1u : 0u, smem, &total);
-	if (keep)
+	__shared__ unsigned int sm[3][33];
+	Scalars* sc = a.sc;
+	const unsigned int G = gridDim.x;
+	const size_t gthreads = (size_t)G * blockDim.x;
+	const unsigned int lane = threadIdx.x & 31;
+	const size_t wbase = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+
+	for (size_t i = gtid(); i < a.vcount; i += gthreads)
 	{
-		size_t w = (size_t)(blkoff[blockIdx.x] + pre) * 3;
-		out[w + 0] = o.x;
-		out[w + 1] = o.y;
-		out[w + 2] = o.z;
+		a.touched[i] = 0;
+		a.moved_by[i] = ~0u;
+		a.cr[i] = (unsigned int)i;
+	}
+
+	unsigned int round = a.round_base;
+	unsigned long long active_sum = 0;
+	unsigned int K0 = 0, K1 = min(a.count, a.first_window);
+	unsigned int carryT = 0, carryF = 0, carryM = a.prev_err_bits;
+	unsigned int windows = 0;
+
+	for (;;)
+	{
+		// ---- decision rounds over the window [K0, K1)
+		++windows;
+		for (size_t x = gtid(); x < K1 - K0; x += gthreads)
+			markCandidate(a, K0 + (unsigned int)x, round + 1);
+		if (gtid() == 0)
+			sc->act_count[(round + 2) % 3] = 0; // appended to by the window's first round
+		gridBarrier(sc->bar, &sc->grid_error);
+
+		unsigned int n = K1 - K0;
+		bool first = true;
+		unsigned int guard = 0;
+		while (n)
+		{
+			++round;
+			if (++guard > a.count + 1 || __ldcg(&sc->grid_error))
+				break;
+			active_sum += n;
+			const unsigned int* list = first ? nullptr : a.list[round & 1];
+			unsigned int* next = a.list[(round + 1) & 1];
+			unsigned int* next_count = &sc->act_count[(round + 1) % 3];
+			// the count round+1 appends to; every thread read it (as round-2's result) before the
+			// barrier that ended round-1
+			if (gtid() == 0)
+				sc->act_count[(round + 2) % 3] = 0;
+			for (size_t base = wbase; base < n; base += gthreads)
+			{
+				size_t x = base + lane;
+				bool keep = false;
+				unsigned int k = 0;
+				if (x < n)
+				{
+					k = list ? __ldcg(list + x) : K0 + (unsigned int)x;
+					keep = decideOne(a, k, round);
+					if (keep)
+						markCandidate(a, k, round + 1);
+				}
+				unsigned int m = __ballot_sync(0xffffffffu, keep);
+				if (m)
+				{
+					unsigned int leader = __ffs(m) - 1;
+					unsigned int o = 0;
+					if (lane == leader)
+						o = atomicAdd(next_count, __popc(m));
+					o = __shfl_sync(0xffffffffu, o, leader);
+					if (keep)
+						next[o + __popc(m & ((1u << lane) - 1u))] = k;
+				}
+			}
+			gridBarrier(sc->bar, &sc->grid_error);
+			unsigned int nn = __ldcg(next_count);
+			if (nn >= n)
+			{
+				if (gtid() == 0)
+					atomicOr(&sc->grid_error, 2u);
+				break;
+			}
+			n = nn;
+			first = false;
+		}
+		if (__ldcg(&sc->grid_error))
+			break;
+
+		// ---- stop rules over [K0, K1): block chunks, thread sub-chunks, carried prefix
+		const unsigned int len = K1 - K0;
+		const unsigned int per_block = (len + G - 1) / G;
+		const unsigned int c0 = min(K1, K0 + blockIdx.x * per_block), c1 = min(K1, c0 + per_block);
+		const unsigned int per_thread = (c1 - c0 + blockDim.x - 1) / blockDim.x;
+		const unsigned int t0 = min(c1, c0 + threadIdx.x * per_thread), t1 = min(c1, t0 + per_thread);
+		unsigned int sT = 0, sF = 0, sM = 0;
+		for (unsigned int k = t0; k < t1; ++k)
+		{
+			unsigned int tt, ff, ee;
+			stopTerms(__ldcg(a.status + k), __ldg(a.skind + k), __ldg(a.serr + k), tt, ff, ee);
+			sT += tt, sF += ff, sM = max(sM, ee);
+		}
+		unsigned int eT = sT, eF = sF, eM = sM;
+		uint3 tot = blockScan3(eT, eF, eM, sm);
+		if (threadIdx.x == 0)
+			a.blk[blockIdx.x] = make_uint4(tot.x, tot.y, tot.z, 0);
+		gridBarrier(sc->bar, &sc->grid_error);
+		if (blockIdx.x == 0)
+		{
+			// exclusive prefix over the block totals with the carry of earlier windows
+			unsigned int rT = carryT, rF = carryF, rM = carryM;
+			for (unsigned int q0 = 0; q0 < G; q0 += blockDim.x)
+			{
+				unsigned int q = q0 + threadIdx.x;
+				uint4 v = q < G ? __ldcg(a.blk + q) : make_uint4(0, 0, 0, 0);
+				unsigned int x = v.x, y = v.y, z = v.z;
+				uint3 ct = blockScan3(x, y, z, sm);
+				if (q < G)
+					a.blk[q] = make_uint4(rT + x, rF + y, max(rM, z), 0);
+				rT += ct.x, rF += ct.y, rM = max(rM, ct.z);
+			}
+			if (threadIdx.x == 0)
+				sc->carry[0] = rT, sc->carry[1] = rF, sc->carry[2] = rM;
+		}
+		gridBarrier(sc->bar, &sc->grid_error);
+		{
+			uint4 bb = __ldcg(a.blk + blockIdx.x);
+			unsigned long long T = (unsigned long long)bb.x + eT;
+			unsigned long long F = (unsigned long long)bb.y + eF;
+			unsigned int M = max(bb.z, eM);
+			const unsigned long long egoal0 = a.goal / 2;
+			for (unsigned int k = t0; k < t1; ++k)
+			{
+				float e = __uint_as_float(__ldg(a.serr + k));
+				unsigned int reason = 0;
+				if (e > a.error_limit)
+					reason = 1;
+				else if (T >= a.goal)
+					reason = 2;
+				else
+				{
+					unsigned long long eg = egoal0 + F;
+					float error_goal = eg < a.count ? 1.5f * __uint_as_float(__ldg(a.serr + eg)) : FLT_MAX;
+					if (e > error_goal && e > __uint_as_float(M) && T > a.goal / 6)
+						reason = 3;
+				}
+				if (reason)
+				{
+					atomicMin(&sc->cut, ((unsigned long long)k << 2) | reason);
+					break;
+				}
+				unsigned int tt, ff, ee;
+				stopTerms(__ldcg(a.status + k), __ldg(a.skind + k), __ldg(a.serr + k), tt, ff, ee);
+				T += tt, F += ff, M = max(M, ee);
+			}
+		}
+		gridBarrier(sc->bar, &sc->grid_error);
+		if (__ldcg(&sc->cut) != ~0ull || K1 == a.count || __ldcg(&sc->grid_error))
+			break;
+		carryT = __ldcg(&sc->carry[0]);
+		carryF = __ldcg(&sc->carry[1]);
+		carryM = __ldcg(&sc->carry[2]);
+		K0 = K1;
+		K1 = (unsigned int)min((unsigned long long)a.count, 2ull * K1);
+	}
+	if (__ldcg(&sc->grid_error))
+		return;
+
+	// ---- apply the committed prefix
+	const unsigned long long cutv = __ldcg(&sc->cut);
+	const unsigned int cut = cutv == ~0ull ? a.count : (unsigned int)(cutv >> 2);
+	unsigned int nd = 0, ns = 0, ni = 0, em = 0, dm = 0;
+	for (size_t k = gtid(); k < cut; k += gthreads)
+	{
+		unsigned char st = __ldcg(a.status + k);
+		nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
+		if (st == kCommit)
+		{
+			unsigned int eb = 0, db = 0;
+			applyCommit(a, (unsigned int)k, eb, db);
+			em = max(em, eb), dm = max(dm, db);
+		}
+	}
+	{
+		unsigned int x = nd, y = ns, z = em;
+		uint3 t1 = blockScan3(x, y, z, sm);
+		unsigned int p = ni, q = 0, r = dm;
+		uint3 t2 = blockScan3(p, q, r, sm);
+		if (threadIdx.x == 0)
+		{
+			if (t1.x)
+				atomicAdd(&sc->done, t1.x);
+			if (t1.y)
+				atomicAdd(&sc->skipped, t1.y);
+			if (t2.x)
+				atomicAdd(&sc->invalid, t2.x);
+			if (t1.z)
+				atomicMax(&sc->result_error_bits, t1.z);
+			if (t2.z)
+				atomicMax(&sc->vertex_error_bits, t2.z);
+		}
+	}
+	gridBarrier(sc->bar, &sc->grid_error);
+	if (__ldcg(&sc->done) == 0 || __ldcg(&sc->grid_error))
+	{
+		if (gtid() == 0)
+		{
+			sc->rounds = round - a.round_base;
+			sc->active_sum = active_sum;
+			sc->windows = windows;
+		}
+		return;
+	}
+
+	// ---- loop remap (in place: targets are fixed points of collapse_remap) and kept-triangle counts
+	for (size_t i = gtid(); i < a.vcount; i += gthreads)
+	{
+		unsigned int* arrs[2] = {a.loop, a.loopback};
+		for (int q = 0; q < 2; ++q)
+		{
+			unsigned int* L = arrs[q];
+			unsigned int l = L[i];
+			if (l == ~0u)
+				continue;
+			unsigned int r = __ldcg(a.cr + l);
+			if (i == r)
+			{
+				unsigned int ll = __ldcg(L + l);
+				L[i] = ll != ~0u ? __ldcg(a.cr + ll) : ~0u;
+			}
+			else
+				L[i] = r;
+		}
+	}
+	const unsigned int tper_block = (a.tris + G - 1) / G;
+	const unsigned int tb0 = min(a.tris, blockIdx.x * tper_block), tb1 = min(a.tris, tb0 + tper_block);
+	const unsigned int tper_thread = (tb1 - tb0 + blockDim.x - 1) / blockDim.x;
+	const unsigned int tt0 = min(tb1, tb0 + threadIdx.x * tper_thread), tt1 = min(tb1, tt0 + tper_thread);
+	unsigned int kept = 0;
+	for (unsigned int t = tt0; t < tt1; ++t)
+	{
+		uint3 o;
+		kept += keepTriangle(a.res, t, a.cr, a.remap, o);
+	}
+	unsigned int ek = kept, d1 = 0, d2 = 0;
+	uint3 ktot = blockScan3(ek, d1, d2, sm);
+	if (threadIdx.x == 0)
+		a.blk[blockIdx.x] = make_uint4(ktot.x, 0, 0, 0);
+	gridBarrier(sc->bar, &sc->grid_error);
+	if (blockIdx.x == 0)
+	{
+		unsigned int run = 0;
+		for (unsigned int q0 = 0; q0 < G; q0 += blockDim.x)
+		{
+			unsigned int q = q0 + threadIdx.x;
+			unsigned int x = q < G ? __ldcg(&a.blk[q].x) : 0u, y = 0, z = 0;
+			uint3 ct = blockScan3(x, y, z, sm);
+			if (q < G)
+				a.blk[q].y = run + x;
+			run += ct.x;
+		}
+		if (threadIdx.x == 0)
+		{
+			sc->tri_total = run;
+			sc->rounds = round - a.round_base;
+			sc->active_sum = active_sum;
+			sc->windows = windows;
+		}
+	}
+	gridBarrier(sc->bar, &sc->grid_error);
+	{
+		unsigned int w = __ldcg(&a.blk[blockIdx.x].y) + ek;
+		for (unsigned int t = tt0; t < tt1; ++t)
+		{
+			uint3 o;
+			if (keepTriangle(a.res, t, a.cr, a.remap, o))
+			{
+				a.res_next[(size_t)w * 3 + 0] = o.x;
+				a.res_next[(size_t)w * 3 + 1] = o.y;
+				a.res_next[(size_t)w * 3 + 2] = o.z;
+				w++;
+			}
+		}
 	}
 }
 
@@ -1487,13 +1481,13 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 	w.status = c.take<unsigned char>(cap);
 	w.act0 = c.take<unsigned int>(cap);
 	w.act1 = c.take<unsigned int>(cap);
-	w.minT = c.take<unsigned long long>(Vp);
-	w.minS = c.take<unsigned long long>(Vp);
+	w.minT = c.take<unsigned long long>(2 * Vp);
+	w.minS = c.take<unsigned long long>(2 * Vp);
 	w.touched = c.take<unsigned char>(Vp);
 	w.moved_by = c.take<unsigned int>(Vp);
 	w.moved_to = c.take<unsigned int>(Vp);
 	w.cr = c.take<unsigned int>(Vp);
-	w.blk = c.take<uint4>(cap / kStopTile + 2);
+	w.blk = c.take<uint4>(std::max<size_t>(cap / kStopTile + 2, 8192)); // >= blocks of any cooperative launch
 	w.blkcnt = c.take<unsigned int>(T / kThreads + 2);
 	size_t sw = std::max(std::max(scanScratchWords(I + Vp + 2), radixScratchWords(big)), scanScratchWords(T + 2));
 	w.scratch = c.take<unsigned int>(sw);
@@ -1509,6 +1503,18 @@ int bitsFor(size_t maxval)
 }
 
 } // namespace
+
+// ---------------------------------------------------------------- tuning
+
+Tuning Tuning::fromEnvironment()
+{
+	Tuning t;
+	if (const char* v = getenv("MESHOPTGPU_PERFORM_BLOCKS_PER_SM"))
+		t.perform_blocks_per_sm = std::max(1, atoi(v));
+	if (const char* v = getenv("MESHOPTGPU_WINDOW_FACTOR"))
+		t.window_factor = std::max(0.0, atof(v));
+	return t;
+}
 
 // ---------------------------------------------------------------- arena
 
@@ -1543,8 +1549,11 @@ Simplifier::Simplifier(int device) : device_(device)
 	MO_CUDA_CHECK(cudaMallocHost(&pinned_, 4096));
 	int sms = 0, per_sm = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kRounds, kThreads, 0));
+	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
+	sms_ = sms;
 	coop_blocks_ = unsigned(std::max(1, sms * std::max(per_sm, 1)));
+	tuning_ = Tuning::fromEnvironment();
+	perform_blocks_ = std::min(coop_blocks_, unsigned(std::max(1, sms * tuning_.perform_blocks_per_sm)));
 }
 
 Simplifier::~Simplifier()
@@ -1780,6 +1789,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	unsigned int* res_next = w.res1;
 	unsigned int result_error_bits = 0;
 	int passes = 0;
+	unsigned int round_base = 0; // decision rounds are numbered across the run (mark tags never repeat)
+	MO_CUDA_CHECK(cudaMemsetAsync(w.minT, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
+	MO_CUDA_CHECK(cudaMemsetAsync(w.minS, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
 
 	while (result_count > m.target_index_count)
 	{
@@ -1820,62 +1832,68 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
-		// perform: all decision rounds in one cooperative launch
+		// perform: decisions, stop rules, apply, loop remap and compaction in one cooperative launch
+		const size_t goal = (result_count - m.target_index_count) / 3;
 		{
-			RoundsArgs ra;
-			ra.count = C;
-			ra.vcount = V;
-			ra.srec = w.srec;
-			ra.skind = w.skind;
-			ra.minT = w.minT;
-			ra.minS = w.minS;
-			ra.touched = w.touched;
-			ra.moved_by = w.moved_by;
-			ra.moved_to = w.moved_to;
-			ra.cr = w.cr;
-			ra.status = w.status;
-			ra.adj_off = w.adj_off;
-			ra.adj = w.adj;
-			ra.pos = w.pos;
-			ra.remap = w.remap;
-			ra.wedge = w.wedge;
-			ra.loop = w.loop;
-			ra.loopback = w.loopback;
-			ra.list[0] = w.act0;
-			ra.list[1] = w.act1;
-			ra.sc = w.sc;
+			PerformArgs pa;
+			pa.count = unsigned(C);
+			pa.srec = w.srec;
+			pa.skind = w.skind;
+			pa.serr = w.serr;
+			pa.status = w.status;
+			pa.vcount = unsigned(V);
+			pa.minT[0] = w.minT;
+			pa.minT[1] = w.minT + (V + 1);
+			pa.minS[0] = w.minS;
+			pa.minS[1] = w.minS + (V + 1);
+			pa.touched = w.touched;
+			pa.moved_by = w.moved_by;
+			pa.moved_to = w.moved_to;
+			pa.cr = w.cr;
+			pa.list[0] = w.act0;
+			pa.list[1] = w.act1;
+			pa.adj_off = w.adj_off;
+			pa.adj = w.adj;
+			pa.pos = w.pos;
+			pa.remap = w.remap;
+			pa.wedge = w.wedge;
+			pa.loop = w.loop;
+			pa.loopback = w.loopback;
+			pa.vq = w.vq;
+			pa.aq = w.aq;
+			pa.ag = w.ag;
+			pa.ac = ac;
+			pa.prev_err_bits = result_error_bits;
+			pa.error_limit = error_limit;
+			pa.goal = goal;
+			double wf = tuning_.window_factor * double(goal / 2) + 4096.0;
+			pa.first_window = unsigned(std::min<double>(double(C), wf));
+			pa.round_base = round_base;
+			pa.res = res;
+			pa.res_next = res_next;
+			pa.tris = unsigned(T);
+			pa.blk = w.blk;
+			pa.sc = w.sc;
 			MO_CUDA_CHECK(cudaMemsetAsync(w.sc->bar, 0, sizeof(unsigned int) * 3, stream));
-			unsigned int blocks = std::max(1u, std::min(coop_blocks_, gridFor(std::max(C, V), kThreads)));
-			void* params[] = {&ra};
-			cudaEvent_t e0 = probeBegin("kRounds", stream);
-			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kRounds, dim3(blocks), dim3(kThreads), params, 0, stream));
+			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->cut, 0xFF, 8, stream));
+			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->done, 0, 12, stream));
+			MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->result_error_bits, &result_error_bits, 4, cudaMemcpyHostToDevice, stream));
+			unsigned int want = gridFor(std::max(std::max(C, V), T), kThreads);
+			unsigned int blocks = std::max(1u, std::min(perform_blocks_, want));
+			void* params[] = {&pa};
+			cudaEvent_t e0 = probeBegin("kPerform", stream);
+			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, stream));
 			probeEnd(e0, stream);
 		}
-		// stop rules
-		const size_t goal = (result_count - m.target_index_count) / 3;
-		const unsigned int nblk = unsigned((C + kStopTile - 1) / kStopTile);
-		MO_LAUNCH(kStopReduce, nblk, 256, 0, stream, C, w.status, w.skind, w.serr, w.blk);
-		MO_LAUNCH(kStopScanBlocks, 1, 1024, 0, stream, w.blk, nblk);
-		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->cut, 0xFF, 8, stream));
-		MO_LAUNCH(kStopFind, nblk, 256, 0, stream, C, w.status, w.skind, w.serr, w.blk, result_error_bits, error_limit, goal, &w.sc->cut);
+		if (timed)
+			MO_CUDA_CHECK(cudaEventRecord(ev[7], stream));
 		readScalars();
 		if (hs->grid_error)
 			throw std::runtime_error(hs->grid_error & 2 ? "collapse decision round made no progress" : "grid barrier wait limit reached");
-		const unsigned int round = hs->rounds;
-		const unsigned long long active_sum = hs->active_sum;
 		const unsigned long long cutv = hs->cut;
 		const size_t cut = cutv == ~0ull ? C : size_t(cutv >> 2);
 		const unsigned int reason = cutv == ~0ull ? 0 : unsigned(cutv & 3);
-		if (timed)
-			MO_CUDA_CHECK(cudaEventRecord(ev[7], stream));
-
-		// apply commits before the cut
-		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->done, 0, 12, stream));
-		MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->result_error_bits, &result_error_bits, 4, cudaMemcpyHostToDevice, stream));
-		if (cut)
-			MO_LAUNCH(kApply, gridFor(cut, kThreads), kThreads, 0, stream, cut, w.srec, w.skind, w.status, w.serr, w.remap, w.wedge, w.loop, w.loopback, w.cr, w.vq,
-			    w.pos, w.aq, w.ag, ac, w.sc);
-		readScalars();
+		round_base += hs->rounds;
 		if (passes < kMaxPassStats)
 		{
 			PassStats& ps = rr.pass[passes];
@@ -1886,26 +1904,14 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			ps.skipped = hs->skipped;
 			ps.invalid = hs->invalid;
 			ps.stop = reason;
-			ps.rounds = round;
-			ps.active = unsigned(active_sum);
+			ps.rounds = hs->rounds;
+			ps.active = unsigned(hs->active_sum);
+			ps.windows = hs->windows;
 		}
 		passes++;
-		const unsigned int done = hs->done;
 		result_error_bits = hs->result_error_bits;
-		if (done == 0)
-		{
-			if (timed)
-				MO_CUDA_CHECK(cudaEventRecord(ev[8], stream));
+		if (hs->done == 0)
 			break;
-		}
-
-		MO_LAUNCH(kRemapLoops, gV, kThreads, 0, stream, V, w.cr, w.loop, w.loopback);
-		MO_LAUNCH(kCompactCount, gT, kThreads, 0, stream, res, T, w.cr, w.remap, w.blkcnt);
-		scanExclusive(w.blkcnt, w.blkcnt, gT, &w.sc->tri_total, w.scratch, stream);
-		MO_LAUNCH(kCompactEmit, gT, kThreads, 0, stream, res, T, w.cr, w.remap, w.blkcnt, res_next);
-		if (timed)
-			MO_CUDA_CHECK(cudaEventRecord(ev[8], stream));
-		readScalars();
 		result_count = size_t(hs->tri_total) * 3;
 		std::swap(res, res_next);
 		if (timed)
@@ -1915,7 +1921,6 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			acc_rank += elapsed(4, 5);
 			acc_sort += elapsed(5, 6);
 			acc_perf += elapsed(6, 7);
-			acc_apply += elapsed(7, 8);
 		}
 	}
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "mo_prims.cuh"
@@ -47,6 +48,7 @@ struct PassStats
 	unsigned int stop;
 	unsigned int rounds;
 	unsigned int active; // candidates processed by the decision kernels, summed over rounds
+	unsigned int windows; // sorted-order windows decided before the stop cut was found
 };
 
 struct RunResult
@@ -92,6 +94,15 @@ private:
 	size_t cap_ = 0;
 };
 
+// Launch-shape parameters (picked by the autotuner, or set with environment variables
+// MESHOPTGPU_PERFORM_BLOCKS_PER_SM and MESHOPTGPU_WINDOW_FACTOR).
+struct Tuning
+{
+	int perform_blocks_per_sm = 2;  // resident blocks per SM of the cooperative pass kernel
+	double window_factor = 2.0;     // first decision window = factor * (triangle goal / 2) + 4096
+	static Tuning fromEnvironment();
+};
+
 class Simplifier
 {
 public:
@@ -115,7 +126,18 @@ private:
 	int device_;
 	DeviceArena arena_;
 	unsigned int* pinned_ = nullptr; // small pinned readback buffer
-	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative rounds kernel
+	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative pass kernel (occupancy)
+	unsigned int perform_blocks_ = 1;
+	int sms_ = 1;
+	Tuning tuning_;
+
+public:
+	void setTuning(const Tuning& t)
+	{
+		tuning_ = t;
+		perform_blocks_ = std::min(coop_blocks_, unsigned(std::max(1, sms_ * t.perform_blocks_per_sm)));
+	}
+	const Tuning& tuning() const { return tuning_; }
 };
 
 } // namespace mogpu
