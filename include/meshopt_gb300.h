@@ -87,11 +87,14 @@ typedef struct meshoptgpu_PassStats
 /* Copies up to max_passes entries; returns the number of passes of the last call. */
 MESHOPTGPU_API int meshoptgpu_getLastPassStats(meshoptgpu_PassStats* out, int max_passes);
 
-/* Device time (ms, CUDA events) of the phases of the calling thread's last call, when
- * timing was enabled with meshoptgpu_setTiming(1): setup, adjacency, pick, rank, sort,
- * perform, apply, total. Returns the number of values written (8). */
+/* Device time (ms) of the phases of the calling thread's last call. The first 8 values are
+ * CUDA-event times, filled when timing was enabled with meshoptgpu_setTiming(1): setup,
+ * adjacency, pick, rank, sort, perform, apply, total. The next 8 split the cooperative pass
+ * kernel by phase, summed over passes (SM clock of one block): init, window marks, decision
+ * rounds, stop rules, apply, loop remap + counts, count scan, compaction emit.
+ * Returns the number of values written (16). */
 MESHOPTGPU_API void meshoptgpu_setTiming(int enabled);
-MESHOPTGPU_API int meshoptgpu_getLastPhaseTimes(float* out8);
+MESHOPTGPU_API int meshoptgpu_getLastPhaseTimes(float* out16);
 
 /* Device-resident form of meshopt_simplifyWithAttributes: every array pointer is a DEVICE
  * pointer on the current device, except attribute_weights (host, at most 32 floats).

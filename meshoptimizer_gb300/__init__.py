@@ -194,9 +194,10 @@ def set_timing(enabled: bool):
 
 
 def last_phase_times():
-    out = (C.c_float * 8)()
+    out = (C.c_float * 16)()
     load().meshoptgpu_getLastPhaseTimes(C.cast(out, C.c_void_p))
-    keys = ["setup", "adjacency", "pick", "rank", "sort", "perform", "apply", "total"]
+    keys = ["setup", "adjacency", "pick", "rank", "sort", "perform", "apply", "total",
+            "k_init", "k_marks", "k_rounds", "k_stop", "k_apply", "k_loops", "k_scan", "k_emit"]
     return dict(zip(keys, [float(x) for x in out]))
 
 

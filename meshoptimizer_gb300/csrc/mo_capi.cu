@@ -299,12 +299,13 @@ void meshoptgpu_setTiming(int enabled)
 	state().timing = enabled != 0;
 }
 
-int meshoptgpu_getLastPhaseTimes(float* out8)
+int meshoptgpu_getLastPhaseTimes(float* out16)
 {
 	const PhaseTimes& t = state().times;
 	float v[8] = {t.setup, t.adjacency, t.pick, t.rank, t.sort, t.perform, t.apply, t.total};
-	memcpy(out8, v, sizeof(v));
-	return 8;
+	memcpy(out16, v, sizeof(v));
+	memcpy(out16 + 8, state().last.perform_phase_ms, sizeof(v));
+	return 16;
 }
 
 size_t meshoptgpu_simplifyDevice(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions,

@@ -64,6 +64,7 @@ struct Scalars
 	unsigned long long active_sum; // candidates processed by the rounds of the last pass
 	unsigned int carry[3];        // stop-rule prefix (triangles, flips, max error) after a window
 	unsigned int windows;         // sorted-order windows the last pass needed
+	unsigned long long phase_cycles[8]; // kPerform phases, SM cycles of block 0, summed over the run
 };
 
 __device__ __forceinline__ size_t gtid()
@@ -1093,8 +1094,43 @@ __device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& 
 	}
 }
 
+// kPerform phases timed by block 0 between grid barriers (SM clock cycles)
+enum
+{
+	kPhInit = 0,
+	kPhMarks = 1,
+	kPhRounds = 2,
+	kPhStop = 3,
+	kPhApply = 4,
+	kPhLoops = 5,
+	kPhScan = 6,
+	kPhEmit = 7,
+};
+
+struct PhaseClock
+{
+	long long last;
+	long long acc[8];
+	__device__ void start()
+	{
+		last = clock64();
+		for (int i = 0; i < 8; ++i)
+			acc[i] = 0;
+	}
+	__device__ void lap(int phase)
+	{
+		long long t = clock64();
+		acc[phase] += t - last;
+		last = t;
+	}
+};
+
 __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 {
+	PhaseClock pc;
+	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+	if (timer)
+		pc.start();
 	__shared__ unsigned int sm[3][33];
 	Scalars* sc = a.sc;
 	const unsigned int G = gridDim.x;
@@ -1124,6 +1160,8 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 		if (gtid() == 0)
 			sc->act_count[(round + 2) % 3] = 0; // appended to by the window's first round
 		gridBarrier(sc->bar, &sc->grid_error);
+		if (timer)
+			pc.lap(windows == 1 ? kPhInit : kPhMarks);
 
 		unsigned int n = K1 - K0;
 		bool first = true;
@@ -1166,6 +1204,8 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 				}
 			}
 			gridBarrier(sc->bar, &sc->grid_error);
+			if (timer)
+				pc.lap(kPhRounds);
 			unsigned int nn = __ldcg(next_count);
 			if (nn >= n)
 			{
@@ -1247,6 +1287,8 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 			}
 		}
 		gridBarrier(sc->bar, &sc->grid_error);
+		if (timer)
+			pc.lap(kPhStop);
 		if (__ldcg(&sc->cut) != ~0ull || K1 == a.count || __ldcg(&sc->grid_error))
 			break;
 		carryT = __ldcg(&sc->carry[0]);
@@ -1293,8 +1335,13 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 		}
 	}
 	gridBarrier(sc->bar, &sc->grid_error);
+	if (timer)
+		pc.lap(kPhApply);
 	if (__ldcg(&sc->done) == 0 || __ldcg(&sc->grid_error))
 	{
+		if (timer)
+			for (int i = 0; i < 8; ++i)
+				atomicAdd(&sc->phase_cycles[i], (unsigned long long)pc.acc[i]);
 		if (gtid() == 0)
 		{
 			sc->rounds = round - a.round_base;
@@ -1339,6 +1386,8 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 	if (threadIdx.x == 0)
 		a.blk[blockIdx.x] = make_uint4(ktot.x, 0, 0, 0);
 	gridBarrier(sc->bar, &sc->grid_error);
+	if (timer)
+		pc.lap(kPhLoops);
 	if (blockIdx.x == 0)
 	{
 		unsigned int run = 0;
@@ -1360,6 +1409,8 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 		}
 	}
 	gridBarrier(sc->bar, &sc->grid_error);
+	if (timer)
+		pc.lap(kPhScan);
 	{
 		unsigned int w = __ldcg(&a.blk[blockIdx.x].y) + ek;
 		for (unsigned int t = tt0; t < tt1; ++t)
@@ -1373,6 +1424,12 @@ __global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
 				w++;
 			}
 		}
+	}
+	if (timer)
+	{
+		pc.lap(kPhEmit);
+		for (int i = 0; i < 8; ++i)
+			atomicAdd(&sc->phase_cycles[i], (unsigned long long)pc.acc[i]);
 	}
 }
 
@@ -1934,6 +1991,13 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 
 	float rerr;
 	memcpy(&rerr, &result_error_bits, 4);
+	{
+		int khz = 0;
+		cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device_);
+		readScalars();
+		for (int i = 0; i < 8; ++i)
+			rr.perform_phase_ms[i] = khz ? float(double(hs->phase_cycles[i]) / khz) : 0.f;
+	}
 	rr.index_count = result_count;
 	rr.result_error_sq = rerr;
 	rr.result_error = sqrtf(rerr) * error_scale;

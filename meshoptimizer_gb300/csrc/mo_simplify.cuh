@@ -59,6 +59,9 @@ struct RunResult
 	float scale = 0.f;
 	int passes = 0;
 	PassStats pass[kMaxPassStats];
+	// time inside the cooperative pass kernel by phase (block 0's SM clock): init, window marks,
+	// decision rounds, stop rules, apply, loop remap + counts, count scan, compaction emit
+	float perform_phase_ms[8] = {};
 };
 
 // Device timings of the phases of one run (milliseconds, from CUDA events).
