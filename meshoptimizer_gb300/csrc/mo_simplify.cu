@@ -808,17 +808,21 @@ __global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int
 	ckey[c] = sortKey(bits);
 }
 
-// sorted record: {i0, i1, r0, r1} plus error bits and source kind
+// sorted record: {r0, r1, begin and end of r0's adjacency} for the decision rounds, the raw
+// endpoints {i0, i1} for commits, plus error bits and source kind
 __global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ order, const unsigned int* __restrict__ cv0, const unsigned int* __restrict__ cv1,
-    const unsigned int* __restrict__ cerr, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind, uint4* __restrict__ srec,
-    unsigned int* __restrict__ serr, unsigned char* __restrict__ skind, unsigned char* __restrict__ status)
+    const unsigned int* __restrict__ cerr, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
+    const unsigned int* __restrict__ adj_off, uint4* __restrict__ srec, uint2* __restrict__ sidx, unsigned int* __restrict__ serr,
+    unsigned char* __restrict__ skind, unsigned char* __restrict__ status)
 {
 	size_t k = gtid();
 	if (k >= count)
 		return;
 	unsigned int c = order[k];
 	unsigned int i0 = cv0[c], i1 = cv1[c];
-	srec[k] = make_uint4(i0, i1, remap[i0], remap[i1]);
+	unsigned int r0 = remap[i0];
+	srec[k] = make_uint4(r0, remap[i1], adj_off[r0], adj_off[r0 + 1]);
+	sidx[k] = make_uint2(i0, i1);
 	serr[k] = cerr[c];
 	skind[k] = kind[i0];
 	status[k] = kUndecided;
@@ -848,7 +852,8 @@ struct PerformArgs
 {
 	// sorted candidates
 	unsigned int count;
-	const uint4* srec;
+	const uint4* srec; // {r0, r1, adjacency begin of r0, adjacency end of r0}
+	const uint2* sidx; // {i0, i1}
 	const unsigned char* skind;
 	const unsigned int* serr;
 	unsigned char* status;
@@ -898,40 +903,72 @@ struct PerformArgs
 __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, unsigned int round)
 {
 	uint4 rec = __ldg(a.srec + k);
-	unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
+	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
 	const unsigned long long tag = roundTag(round);
 	const unsigned long long mine = tag | k;
 	const unsigned long long* minT = a.minT[round & 1];
 	const unsigned long long* minS = a.minS[round & 1];
-	if (__ldcg(a.touched + r0) | __ldcg(a.touched + r1))
+	// independent loads first: lock flags and endpoint marks
+	unsigned char t0 = __ldcg(a.touched + r0), t1 = __ldcg(a.touched + r1);
+	unsigned long long m0 = __ldcg(minT + r0), m1 = __ldcg(minT + r1);
+	if (t0 | t1)
 	{
 		a.status[k] = kSkipLocked;
 		return false;
 	}
-	if (__ldcg(minT + r0) != mine || __ldcg(minT + r1) != mine)
+	if (m0 != mine || m1 != mine)
 		return true;
-	unsigned int b = __ldg(a.adj_off + r0), e = __ldg(a.adj_off + r0 + 1);
-	for (unsigned int j = b; j < e; ++j)
+	// one-ring sources: four half-edges per step so the loads overlap
+	for (unsigned int j = b; j < e; j += 4)
 	{
-		uint2 ed = __ldg(a.adj + j);
-		if (earlierThan(__ldcg(minS + ed.x), tag, k) || earlierThan(__ldcg(minS + ed.y), tag, k))
+		uint2 ed[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
+			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
+		unsigned long long sx[4], sy[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
+		{
+			sx[q] = __ldcg(minS + ed[q].x);
+			sy[q] = __ldcg(minS + ed[q].y);
+		}
+		bool wait = false;
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
+			wait |= earlierThan(sx[q], tag, k) | earlierThan(sy[q], tag, k);
+		if (wait)
 			return true;
 	}
 	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
-	for (unsigned int j = b; j < e; ++j)
+	for (unsigned int j = b; j < e; j += 4)
 	{
-		uint2 ed = __ldg(a.adj + j);
-		unsigned int mx = __ldcg(a.moved_by + ed.x), my = __ldcg(a.moved_by + ed.y);
-		unsigned int va = mx < k ? __ldcg(a.moved_to + ed.x) : ed.x;
-		unsigned int vb = my < k ? __ldcg(a.moved_to + ed.y) : ed.y;
-		if (va == r1 || vb == r1 || va == vb)
-			continue;
-		if (triFlip(ldpos(a.pos, va), ldpos(a.pos, vb), v0, v1))
+		uint2 ed[4];
+		unsigned int mx[4], my[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
+			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r1, r1);
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
 		{
-			a.status[k] = kSkipFlip;
-			return false;
+			mx[q] = __ldcg(a.moved_by + ed[q].x);
+			my[q] = __ldcg(a.moved_by + ed[q].y);
+		}
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
+		{
+			unsigned int va = mx[q] < k ? __ldcg(a.moved_to + ed[q].x) : ed[q].x;
+			unsigned int vb = my[q] < k ? __ldcg(a.moved_to + ed[q].y) : ed[q].y;
+			if (va == r1 || vb == r1 || va == vb)
+				continue;
+			if (triFlip(ldpos(a.pos, va), ldpos(a.pos, vb), v0, v1))
+			{
+				a.status[k] = kSkipFlip;
+				return false;
+			}
 		}
 	}
+	uint2 ii = __ldg(a.sidx + k);
+	const unsigned int i0 = ii.x, i1 = ii.y;
 	unsigned char kd = __ldg(a.skind + k);
 	unsigned int target;
 	if (kd == kComplex)
@@ -957,9 +994,9 @@ __device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int
 {
 	uint4 rec = __ldg(a.srec + k);
 	unsigned long long key = roundTag(round) | k;
-	atomicMin(&a.minT[round & 1][rec.z], key);
-	atomicMin(&a.minT[round & 1][rec.w], key);
-	atomicMin(&a.minS[round & 1][rec.z], key);
+	atomicMin(&a.minT[round & 1][rec.x], key);
+	atomicMin(&a.minT[round & 1][rec.y], key);
+	atomicMin(&a.minS[round & 1][rec.x], key);
 }
 
 // per sorted candidate: triangles removed if committed, flip rejection, committed error
@@ -1015,23 +1052,39 @@ __device__ __forceinline__ bool keepTriangle(const unsigned int* __restrict__ re
 	return r0 != r1 && r0 != r2 && r1 != r2;
 }
 
-// the collapse_remap writes and quadric merges of one committed candidate
+__device__ __forceinline__ void mergeAttributes(const PerformArgs& a, unsigned int v, unsigned int t)
+{
+	Quadric A = ldquadric(a.aq, t);
+	qadd(A, ldquadric(a.aq, v));
+	stquadric(a.aq, t, A);
+	const int ac = a.ac;
+	for (int q = 0; q < ac; ++q)
+	{
+		float4 g = a.ag[(size_t)t * ac + q], h = a.ag[(size_t)v * ac + q];
+		g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
+		a.ag[(size_t)t * ac + q] = g;
+	}
+}
+
+// the collapse_remap writes and quadric merges of one committed candidate; attribute sources
+// of one commit merge in increasing vertex order, as updateQuadrics' vertex loop does
 __device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& errbits, unsigned int& derrbits)
 {
 	uint4 rec = __ldg(a.srec + k);
-	unsigned int i0 = rec.x, i1 = rec.y, r0 = rec.z, r1 = rec.w;
+	uint2 ii = __ldg(a.sidx + k);
+	const unsigned int r0 = rec.x, r1 = rec.y, i0 = ii.x, i1 = ii.y;
 	unsigned char kd = __ldg(a.skind + k);
+	Quadric Q1 = ldquadric(a.vq, r1);
+	Quadric Q0 = ldquadric(a.vq, r0);
+	float e = __uint_as_float(__ldg(a.serr + k));
 
-	unsigned int moved[kMaxAttributes];
-	int nm = 0;
+	unsigned int mv0 = i0, mv1 = ~0u; // moved vertices of a non-complex commit, at most two
 	if (kd == kComplex)
 	{
 		unsigned int v = i0;
 		do
 		{
 			a.cr[v] = complexTarget(v, i1, a.remap, a.loop, a.loopback);
-			if (nm < kMaxAttributes)
-				moved[nm++] = v;
 			v = a.wedge[v];
 		} while (v != i0);
 	}
@@ -1042,52 +1095,44 @@ __device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& 
 		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
 		a.cr[i0] = i1;
 		a.cr[s0] = s1;
-		moved[nm++] = i0;
 		if (s0 != i0)
-			moved[nm++] = s0;
+			mv0 = min(i0, s0), mv1 = max(i0, s0);
 	}
 	else
-	{
 		a.cr[i0] = i1;
-		moved[nm++] = i0;
-	}
 
-	Quadric Q1 = ldquadric(a.vq, r1);
-	Quadric Q0 = ldquadric(a.vq, r0);
 	qadd(Q1, Q0);
 	stquadric(a.vq, r1, Q1);
-
-	float e = __uint_as_float(__ldg(a.serr + k));
 	errbits = e == e ? __float_as_uint(e) : 0u;
 
 	if (a.ac)
 	{
-		// attribute sources of one commit merge in increasing vertex order (:1642-1671)
-		for (int x = 1; x < nm; ++x)
+		if (kd == kComplex)
 		{
-			unsigned int v = moved[x];
-			int y = x - 1;
-			while (y >= 0 && moved[y] > v)
+			// all wedges of the source, in increasing vertex order (selection by repeated minimum)
+			unsigned int last = 0;
+			bool first = true;
+			for (;;)
 			{
-				moved[y + 1] = moved[y];
-				--y;
+				unsigned int best = ~0u, v = i0;
+				do
+				{
+					if ((first || v > last) && v < best)
+						best = v;
+					v = a.wedge[v];
+				} while (v != i0);
+				if (best == ~0u)
+					break;
+				mergeAttributes(a, best, a.cr[best]);
+				last = best;
+				first = false;
 			}
-			moved[y + 1] = v;
 		}
-		const int ac = a.ac;
-		for (int m = 0; m < nm; ++m)
+		else
 		{
-			unsigned int v = moved[m];
-			unsigned int t = a.cr[v];
-			Quadric A = ldquadric(a.aq, t);
-			qadd(A, ldquadric(a.aq, v));
-			stquadric(a.aq, t, A);
-			for (int q = 0; q < ac; ++q)
-			{
-				float4 g = a.ag[(size_t)t * ac + q], h = a.ag[(size_t)v * ac + q];
-				g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
-				a.ag[(size_t)t * ac + q] = g;
-			}
+			mergeAttributes(a, mv0, a.cr[mv0]);
+			if (mv1 != ~0u)
+				mergeAttributes(a, mv1, a.cr[mv1]);
 		}
 		float d = qerror(Q0, ldpos(a.pos, a.remap[a.cr[r0]]));
 		derrbits = d == d ? __float_as_uint(d) : 0u;
@@ -1125,7 +1170,7 @@ struct PhaseClock
 	}
 };
 
-__global__ void __launch_bounds__(kThreads) kPerform(PerformArgs a)
+__global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 {
 	PhaseClock pc;
 	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
@@ -1468,6 +1513,7 @@ struct Work
 	uint2* adj;
 	unsigned int *cv0, *cv1, *cerr, *ckey;
 	uint4* srec;
+	uint2* sidx;
 	unsigned int* serr;
 	unsigned char *skind, *status;
 	unsigned int *act0, *act1;
@@ -1533,6 +1579,7 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 	w.cerr = c.take<unsigned int>(cap);
 	w.ckey = c.take<unsigned int>(big);
 	w.srec = c.take<uint4>(cap);
+	w.sidx = c.take<uint2>(cap);
 	w.serr = c.take<unsigned int>(cap);
 	w.skind = c.take<unsigned char>(cap);
 	w.status = c.take<unsigned char>(cap);
@@ -1885,7 +1932,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
 		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream);
-		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.srec, w.serr, w.skind, w.status);
+		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr, w.skind,
+		    w.status);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
@@ -1895,6 +1943,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			PerformArgs pa;
 			pa.count = unsigned(C);
 			pa.srec = w.srec;
+			pa.sidx = w.sidx;
 			pa.skind = w.skind;
 			pa.serr = w.serr;
 			pa.status = w.status;

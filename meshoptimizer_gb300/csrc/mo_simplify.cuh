@@ -101,7 +101,7 @@ private:
 // MESHOPTGPU_PERFORM_BLOCKS_PER_SM and MESHOPTGPU_WINDOW_FACTOR).
 struct Tuning
 {
-	int perform_blocks_per_sm = 2;  // resident blocks per SM of the cooperative pass kernel
+	int perform_blocks_per_sm = 4;  // resident blocks per SM of the cooperative pass kernel
 	double window_factor = 2.0;     // first decision window = factor * (triangle goal / 2) + 4096
 	static Tuning fromEnvironment();
 };
