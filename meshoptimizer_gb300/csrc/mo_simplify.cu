@@ -35,6 +35,7 @@ namespace
 
 constexpr int kThreads = 256;
 constexpr int kStopTile = 1024; // sorted candidates per block in the stop-rule scan
+constexpr unsigned int kApplyTile = 4096; // sorted positions compacted per block step in the apply phase
 
 struct Scalars
 {
@@ -1345,19 +1346,47 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 	if (__ldcg(&sc->grid_error))
 		return;
 
-	// ---- apply the committed prefix
+	// ---- apply the committed prefix: each block compacts the commits of its chunk of [0, cut)
+	// in shared memory, 4096 sorted positions at a time, so every lane applies a commit
 	const unsigned long long cutv = __ldcg(&sc->cut);
 	const unsigned int cut = cutv == ~0ull ? a.count : (unsigned int)(cutv >> 2);
 	unsigned int nd = 0, ns = 0, ni = 0, em = 0, dm = 0;
-	for (size_t k = gtid(); k < cut; k += gthreads)
 	{
-		unsigned char st = __ldcg(a.status + k);
-		nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
-		if (st == kCommit)
+		__shared__ unsigned int clist[kApplyTile];
+		const unsigned int per_block = (cut + G - 1) / G;
+		const unsigned int c0 = min(cut, blockIdx.x * per_block), c1 = min(cut, c0 + per_block);
+		for (unsigned int base = c0; base < c1; base += kApplyTile)
 		{
-			unsigned int eb = 0, db = 0;
-			applyCommit(a, (unsigned int)k, eb, db);
-			em = max(em, eb), dm = max(dm, db);
+			const unsigned int lim = min(c1, base + kApplyTile);
+			const unsigned int per = kApplyTile / kThreads; // 16 consecutive positions per thread
+			const unsigned int p0 = base + threadIdx.x * per;
+			unsigned int mine = 0;
+			for (unsigned int q = 0; q < per; ++q)
+			{
+				unsigned int k = p0 + q;
+				if (k < lim)
+				{
+					unsigned char st = __ldcg(a.status + k);
+					nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
+					mine += st == kCommit;
+				}
+			}
+			unsigned int off = mine, d1 = 0, d2 = 0;
+			uint3 tot = blockScan3(off, d1, d2, sm);
+			for (unsigned int q = 0; q < per; ++q)
+			{
+				unsigned int k = p0 + q;
+				if (k < lim && __ldcg(a.status + k) == kCommit)
+					clist[off++] = k;
+			}
+			__syncthreads();
+			for (unsigned int x = threadIdx.x; x < tot.x; x += blockDim.x)
+			{
+				unsigned int eb = 0, db = 0;
+				applyCommit(a, clist[x], eb, db);
+				em = max(em, eb), dm = max(dm, db);
+			}
+			__syncthreads();
 		}
 	}
 	{
