@@ -53,12 +53,132 @@ def kperform_bytes(p, vertices, next_triangles):
 
 
 WORKLOADS = {
+    "groups_4096": None,  # cluster groups: handled by bench_groups()
     "sphere_attr_2m": lambda: W.config_sphere_attr(9),
     "sphere_attr_524k": lambda: W.config_sphere_attr(8),
     "heightfield_256": W.config_heightfield_256,
     "fractal_3163": lambda: W.config_fractal_3163(3163),
     "fractal_1024": lambda: W.config_fractal_3163(1024),
 }
+
+
+def load_groups(count=4096, seed=3):
+    """4096 connected patches of a displaced icosphere, 200-512 triangles each, LockBorder, 50%, 2e-2."""
+    meshes = []
+    for idx, pos in W.sphere_patches(count, seed=seed):
+        meshes.append(dict(indices=idx, positions=pos, target=W.target_count(len(idx), 0.5), error=2e-2, options=1))
+    return meshes
+
+
+def cpu_groups(meshes, threads):
+    """Oracle port over independent groups on `threads` host threads (static work split)."""
+    import concurrent.futures as cf
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    if not oracle.available("port"):
+        oracle.build(with_reference=False)
+    oracle.load("port")
+
+    def work(chunk):
+        return [oracle.simplify("port", m["indices"], m["positions"], m["target"], m["error"], m["options"]) for m in chunk]
+
+    chunks = [meshes[i::threads] for i in range(threads)]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        parts = list(ex.map(work, chunks))
+    dt = time.perf_counter() - t0
+    out = [None] * len(meshes)
+    for i, part in enumerate(parts):
+        for j, r in enumerate(part):
+            out[i + j * threads] = r
+    return dt, out
+
+
+def bench_groups(args, mg, torch):
+    """Cluster groups: batched (one persistent launch) vs plain (one drop-in call per group)."""
+    meshes = load_groups()
+    tris = sum(len(m["indices"]) // 3 for m in meshes)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    d_in, descs = [], []
+    for m in meshes:
+        di = torch.from_numpy(m["indices"].view(np.int32)).to(dev)
+        dp = torch.from_numpy(m["positions"]).to(dev)
+        do = torch.empty(max(len(m["indices"]), 1), dtype=torch.int32, device=dev)
+        d_in.append((di, dp, do))
+        descs.append(dict(d_indices=di.data_ptr(), index_count=len(m["indices"]), d_positions=dp.data_ptr(), vertex_count=len(m["positions"]),
+                          target=m["target"], error=m["error"], options=m["options"], d_destination=do.data_ptr()))
+    for _ in range(max(args.warmup, 1)):
+        mg.simplify_batch_device(descs, stream=stream.cuda_stream)   # the first call autotunes the block size
+    launches0 = mg.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            counts, errs = mg.simplify_batch_device(descs, stream=stream.cuda_stream)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    launches = mg.launch_count() - launches0
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    value = tris * args.steps / (total_ms / 1e3) / 1e6
+    out_tris = int(sum(int(c) for c in counts)) // 3
+    batched_out = [d_in[i][2][:int(counts[i])].cpu().numpy().view(np.uint32) for i in range(len(meshes))]
+
+    # e2e: host arrays through meshoptgpu_simplifyBatchHost (one packed copy each way)
+    for _ in range(max(args.warmup, 1)):
+        mg.simplify_batch(meshes)
+    tt = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_res = mg.simplify_batch(meshes)
+        tt += time.perf_counter() - t0
+    h2d = sum(m["indices"].nbytes + m["positions"].nbytes for m in meshes)
+    d2h = sum(len(r[0]) * 4 for r in host_res)
+
+    # plain: one drop-in call per group (host pointers), and one device-resident call per group
+    for m in meshes[:64]:
+        mg.simplify(m["indices"], m["positions"], m["target"], m["error"], m["options"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain = [mg.simplify(m["indices"], m["positions"], m["target"], m["error"], m["options"]) for m in meshes]
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for m, dsc in zip(meshes, descs):
+        mg.simplify_device(dsc["d_destination"], dsc["d_indices"], dsc["index_count"], dsc["d_positions"], dsc["vertex_count"], 12,
+                           m["target"], m["error"], m["options"], stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    t_plain_dev = time.perf_counter() - t0
+
+    exact = all(np.array_equal(a, b[0]) for a, b in zip(batched_out, plain)) and all(np.array_equal(a[0], b[0]) for a, b in zip(host_res, plain))
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dt, ref = cpu_groups(meshes, threads)
+        exact = exact and all(np.array_equal(a, r[0]) for a, r in zip(batched_out, ref))
+        cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
+               "sample": f"all {len(meshes)} groups once, independent groups split statically over {threads} threads"}
+    line = {
+        "metric": "input Mtris/s simplified (bit-exact)", "value": round(value, 4), "unit": "Mtris/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cluster_groups_4096", "groups": len(meshes), "input_tris": tris, "output_tris": out_tris,
+                   "tris_per_group": "200-512", "options": "LockBorder", "target": "50%", "target_error": 2e-2,
+                   "batch_threads_per_cta": mg.batch_threads(), "l2": "flushed between steps (512 MiB write, outside the timed events)"},
+        "e2e": {"value": round(tris * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": round(1e3 * tt / args.steps, 3)},
+        "plain_gpu": {"dropin_host_mtris_s": round(tris / t_plain / 1e6, 4), "dropin_host_ms": round(1e3 * t_plain, 1),
+                      "device_resident_mtris_s": round(tris / t_plain_dev / 1e6, 4), "device_resident_ms": round(1e3 * t_plain_dev, 1),
+                      "calls": len(meshes)},
+        "cpu_baseline": cpu, "bit_exact_vs_plain_and_oracle": bool(exact), "clocks": clocks.summary(), "gpu_launches": int(launches),
+    }
+    print(json.dumps(line))
 
 
 def load_workload(name):
@@ -216,6 +336,9 @@ def main():
 
     mgbuild.build()
     mg.load()
+    if args.workload == "groups_4096":
+        bench_groups(args, mg, torch)
+        return
     c = load_workload(args.workload)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)

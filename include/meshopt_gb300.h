@@ -106,6 +106,41 @@ MESHOPTGPU_API size_t meshoptgpu_simplifyDevice(unsigned int* destination, const
     size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
     size_t target_index_count, float target_error, unsigned int options, float* result_error, void* stream);
 
+/* ---- batched simplification: many meshes in one persistent launch ---- */
+
+/* One mesh of a batch: meshopt_simplify's arguments (positions only) plus its output buffer,
+ * which must hold index_count indices. */
+typedef struct meshoptgpu_BatchMesh
+{
+	const unsigned int* indices;
+	size_t index_count;
+	const float* vertex_positions;
+	size_t vertex_count;
+	size_t vertex_positions_stride;
+	size_t target_index_count;
+	float target_error;
+	unsigned int options; /* LockBorder, ErrorAbsolute, Regularize, RegularizeLight */
+	unsigned int* destination;
+} meshoptgpu_BatchMesh;
+
+/* Simplifies every mesh of the batch in one launch of a persistent kernel: each CTA takes
+ * meshes from a device work queue and runs the whole simplifier for one mesh at a time, in
+ * shared memory when the mesh fits. Results are the same as mesh_count separate
+ * meshopt_simplify calls. All pointers inside meshes[] are DEVICE pointers; the meshes[]
+ * array itself and the result arrays are host memory. Returns a meshoptgpu_Status* value. */
+MESHOPTGPU_API int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, size_t mesh_count, size_t* result_index_counts, float* result_errors,
+    void* stream);
+
+/* The same with HOST pointers inside meshes[]: inputs are packed into one device buffer and
+ * copied once, results copied back once. */
+MESHOPTGPU_API int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh_count, size_t* result_index_counts, float* result_errors);
+
+/* Batch launch shape: threads per CTA (128, 256 or 512; 0 = autotune, the default) and the
+ * shared-memory budget per CTA in bytes (0 = default). The autotuner times each thread count
+ * on the first batch of a size class and keeps the fastest for that class. */
+MESHOPTGPU_API void meshoptgpu_setBatchConfig(int threads, unsigned int smem_bytes);
+MESHOPTGPU_API int meshoptgpu_getBatchThreads(void);
+
 /* Kernel launch accounting for the calling thread: the number of kernels this library has
  * launched, and optional CUDA-event timing of every launch of one kernel (selected by its
  * name prefix, e.g. "kDecide"; NULL disables). The events are recorded on the launching

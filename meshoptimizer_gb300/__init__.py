@@ -45,11 +45,18 @@ EXPORTS = [
     "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
     "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
     "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc",
+    "meshoptgpu_simplifyBatch", "meshoptgpu_simplifyBatchHost", "meshoptgpu_setBatchConfig", "meshoptgpu_getBatchThreads",
 ]
 
 
 class PassStats(C.Structure):
     _fields_ = [(n, C.c_uint) for n in ("triangles", "candidates", "evaluated", "done", "skipped", "invalid", "stop", "rounds", "active", "windows")]
+
+
+class BatchMesh(C.Structure):
+    _fields_ = [("indices", C.c_void_p), ("index_count", C.c_size_t), ("vertex_positions", C.c_void_p),
+                ("vertex_count", C.c_size_t), ("vertex_positions_stride", C.c_size_t), ("target_index_count", C.c_size_t),
+                ("target_error", C.c_float), ("options", C.c_uint), ("destination", C.c_void_p)]
 
 
 class SimplifyError(RuntimeError):
@@ -90,6 +97,12 @@ def load():
     lib.meshoptgpu_getLaunchCount.restype = C.c_ulonglong
     lib.meshoptgpu_setKernelProfile.argtypes = [C.c_char_p]
     lib.meshoptgpu_getKernelProfile.argtypes = [vp, vp]
+    lib.meshoptgpu_simplifyBatch.restype = C.c_int
+    lib.meshoptgpu_simplifyBatch.argtypes = [vp, sz, vp, vp, vp]
+    lib.meshoptgpu_simplifyBatchHost.restype = C.c_int
+    lib.meshoptgpu_simplifyBatchHost.argtypes = [vp, sz, vp, vp]
+    lib.meshoptgpu_setBatchConfig.argtypes = [C.c_int, C.c_uint]
+    lib.meshoptgpu_getBatchThreads.restype = C.c_int
     lib.meshoptgpu_simplifyScaleNoAlloc.restype = C.c_int
     lib.meshoptgpu_simplifyScaleNoAlloc.argtypes = [vp, vp, sz, sz, vp]
     _lib = lib
@@ -233,3 +246,57 @@ def simplify_scale_noalloc(d_extent, d_positions, vertex_count, positions_stride
     """
     return int(load().meshoptgpu_simplifyScaleNoAlloc(C.c_void_p(d_extent), C.c_void_p(d_positions or None), vertex_count,
                                                       positions_stride, C.c_void_p(stream or None)))
+
+
+def simplify_batch(meshes, check=True):
+    """meshoptgpu_simplifyBatchHost on host arrays.
+
+    meshes: list of dicts with indices (uint32), positions (float32 [V, k>=3]), target (index count),
+    error, options. Returns a list of (indices, result_error), identical to per-mesh meshopt_simplify.
+    """
+    lib = load()
+    n = len(meshes)
+    arr = (BatchMesh * max(n, 1))()
+    keep = []
+    outs = []
+    for i, m in enumerate(meshes):
+        idx = np.ascontiguousarray(m["indices"], dtype=np.uint32)
+        pos = np.ascontiguousarray(m["positions"], dtype=np.float32)
+        out = np.empty(max(len(idx), 1), np.uint32)
+        keep += [idx, pos]
+        outs.append(out)
+        arr[i] = BatchMesh(idx.ctypes.data, len(idx), pos.ctypes.data, pos.shape[0], pos.shape[1] * 4, int(m["target"]),
+                           float(m["error"]), int(m.get("options", 0)), out.ctypes.data)
+    counts = np.zeros(max(n, 1), np.uint64)
+    errs = np.zeros(max(n, 1), np.float32)
+    st = lib.meshoptgpu_simplifyBatchHost(C.cast(arr, C.c_void_p), n, counts.ctypes.data, errs.ctypes.data)
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, last_status()[1])
+    return [(outs[i][:int(counts[i])].copy(), float(errs[i])) for i in range(n)]
+
+
+def simplify_batch_device(descs, stream=0, check=True):
+    """meshoptgpu_simplifyBatch with device pointers: descs is a list of dicts with keys
+    d_indices, index_count, d_positions, vertex_count, stride, target, error, options, d_destination.
+    Returns (counts uint64 array, errors float32 array)."""
+    lib = load()
+    n = len(descs)
+    arr = (BatchMesh * max(n, 1))()
+    for i, m in enumerate(descs):
+        arr[i] = BatchMesh(m["d_indices"], m["index_count"], m["d_positions"], m["vertex_count"], m.get("stride", 12), int(m["target"]),
+                           float(m["error"]), int(m.get("options", 0)), m["d_destination"])
+    counts = np.zeros(max(n, 1), np.uint64)
+    errs = np.zeros(max(n, 1), np.float32)
+    st = lib.meshoptgpu_simplifyBatch(C.cast(arr, C.c_void_p), n, counts.ctypes.data, errs.ctypes.data, C.c_void_p(stream or None))
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, last_status()[1])
+    return counts[:n], errs[:n]
+
+
+def set_batch_config(threads=0, smem_bytes=0):
+    """Threads per CTA of the batch kernel (128/256/512, 0 = autotune) and shared-memory budget."""
+    load().meshoptgpu_setBatchConfig(int(threads), int(smem_bytes))
+
+
+def batch_threads():
+    return int(load().meshoptgpu_getBatchThreads())

@@ -1,0 +1,845 @@
+// mo_batch.cu - many small meshes simplified in one persistent launch.
+//
+// Each CTA takes meshes from a device work queue (an atomic ticket) and runs the whole
+// edge-collapse simplification of one mesh (meshopt_simplifyEdge, src/simplifier.cpp:2344-2626,
+// positions only) with block-level phases. The scratch of a mesh lives in shared memory when
+// it fits the launch's dynamic shared memory, otherwise in a per-CTA slab of global memory;
+// every phase addresses it through generic pointers, so one code path serves both.
+//
+// Inside a CTA the greedy collapse loop (performEdgeCollapses :1498-1636) runs exactly as the
+// reference writes it, on one warp: lane 0 walks the sorted candidates and evaluates the stop
+// rules, locks and commits, and the 32 lanes split the one-ring of the flip test
+// (hasTriangleFlips :1201-1232). All other phases use the whole block.
+#include "mo_common.cuh"
+#include "mo_prims.cuh"
+#include "mo_probe.cuh"
+#include "mo_batch.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace mogpu
+{
+
+namespace
+{
+
+constexpr unsigned int kSortBinsC = 2560;
+
+struct CtaWork
+{
+	unsigned int* idx;      // I: current result indices (compacted in place)
+	float4* pos;            // V: rescaled positions
+	unsigned int* remap;    // V
+	unsigned int* wedge;    // V
+	unsigned int* loop;     // V
+	unsigned int* loopback; // V
+	unsigned char* kind;    // V
+	unsigned char* locked;  // V
+	Quadric* vq;            // V
+	unsigned int* adj_off;  // V + 1
+	uint2* adj;             // I
+	unsigned int* fill;     // V
+	unsigned int* cr;       // V
+	unsigned int* table;    // H
+	unsigned int* cv0;      // cap
+	unsigned int* cv1;      // cap
+	unsigned int* cerr;     // cap
+	unsigned int* order;    // cap
+	unsigned int* hist;     // 2560
+	unsigned int* red;      // 64 words of block-reduction scratch
+};
+
+__host__ __device__ inline size_t alignUp(size_t v, size_t a)
+{
+	return (v + a - 1) & ~(a - 1);
+}
+
+__host__ __device__ inline size_t hashBucketsFor(size_t count)
+{
+	size_t b = 1;
+	while (b < count + count / 4)
+		b *= 2;
+	return b;
+}
+
+// Carves the workspace of a mesh with I indices and V vertices from `base` (nullptr: size only).
+__host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t V)
+{
+	size_t off = 0;
+	size_t H = hashBucketsFor(V ? V : 1);
+	size_t cap = I + 4;
+	auto take = [&](size_t bytes) {
+		char* p = base ? base + off : nullptr;
+		off = alignUp(off + bytes, 16);
+		return p;
+	};
+	w.idx = reinterpret_cast<unsigned int*>(take(I * 4));
+	w.pos = reinterpret_cast<float4*>(take(V * 16));
+	w.remap = reinterpret_cast<unsigned int*>(take(V * 4));
+	w.wedge = reinterpret_cast<unsigned int*>(take(V * 4));
+	w.loop = reinterpret_cast<unsigned int*>(take(V * 4));
+	w.loopback = reinterpret_cast<unsigned int*>(take(V * 4));
+	w.kind = reinterpret_cast<unsigned char*>(take(V));
+	w.locked = reinterpret_cast<unsigned char*>(take(V));
+	w.vq = reinterpret_cast<Quadric*>(take(V * sizeof(Quadric)));
+	w.adj_off = reinterpret_cast<unsigned int*>(take((V + 1) * 4));
+	w.adj = reinterpret_cast<uint2*>(take(I * 8));
+	w.fill = reinterpret_cast<unsigned int*>(take(V * 4));
+	w.cr = reinterpret_cast<unsigned int*>(take(V * 4));
+	// the hash table is only live during setup; the candidate arrays only during passes
+	size_t shared_at = off;
+	w.table = reinterpret_cast<unsigned int*>(take(H * 4));
+	size_t after_table = off;
+	off = shared_at;
+	w.cv0 = reinterpret_cast<unsigned int*>(take(cap * 4));
+	w.cv1 = reinterpret_cast<unsigned int*>(take(cap * 4));
+	w.cerr = reinterpret_cast<unsigned int*>(take(cap * 4));
+	w.order = reinterpret_cast<unsigned int*>(take(cap * 4));
+	w.hist = reinterpret_cast<unsigned int*>(take(kSortBinsC * 4));
+	w.red = reinterpret_cast<unsigned int*>(take(64 * 4));
+	return off > after_table ? off : after_table;
+}
+
+// ---------------------------------------------------------------- block helpers
+
+// exclusive scan of data[0..n) in place over the block; returns the total
+template <int NT>
+__device__ unsigned int blockScanArray(unsigned int* data, unsigned int n, unsigned int* red)
+{
+	unsigned int carry = 0;
+	for (unsigned int base = 0; base < n; base += NT)
+	{
+		unsigned int i = base + threadIdx.x;
+		unsigned int v = i < n ? data[i] : 0u;
+		unsigned int tot;
+		unsigned int ex = blockExclusiveScan<NT>(v, red, &tot);
+		if (i < n)
+			data[i] = carry + ex;
+		carry += tot;
+		__syncthreads();
+	}
+	return carry;
+}
+
+template <int NT>
+__device__ unsigned int blockSum(unsigned int v, unsigned int* red)
+{
+	unsigned int tot;
+	blockExclusiveScan<NT>(v, red, &tot);
+	__syncthreads();
+	return tot;
+}
+
+__device__ __forceinline__ unsigned int mix32b(unsigned int h)
+{
+	h ^= h >> 16;
+	h *= 0x7feb352du;
+	h ^= h >> 15;
+	h *= 0x846ca68bu;
+	h ^= h >> 16;
+	return h;
+}
+
+__device__ __forceinline__ unsigned int posBitsB(float f)
+{
+	unsigned int u = __float_as_uint(f);
+	return u == 0x80000000u ? 0u : u;
+}
+
+// ordered min/max folds, see rescalePositions :551-567 (leftmost of equal values, NaN skipped)
+__device__ __forceinline__ float fmin_l(float l, float r)
+{
+	return l > r ? r : l;
+}
+
+__device__ __forceinline__ float fmax_l(float l, float r)
+{
+	return l < r ? r : l;
+}
+
+// ---------------------------------------------------------------- one mesh
+
+template <int NT>
+__device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
+{
+	const unsigned int tid = threadIdx.x;
+	const unsigned int I = d.index_count, V = d.vertex_count;
+	const float* P = d.positions;
+	const unsigned int sf = d.stride_f;
+	__shared__ unsigned int s_flag;
+	__shared__ float s_mm[NT / 32][6];
+	__shared__ float s_minv[3], s_scale, s_extent;
+	__shared__ unsigned int s_cap, s_count, s_trunc, s_done, s_errbits;
+
+	if (tid == 0)
+		s_flag = 0;
+	__syncthreads();
+	for (unsigned int i = tid; i < I; i += NT)
+	{
+		unsigned int v = d.indices[i];
+		w.idx[i] = v;
+		if (v >= V)
+			s_flag = 1;
+	}
+	__syncthreads();
+	if (s_flag)
+	{
+		if (tid == 0)
+			*out = BatchResult{I, 0.f, 0, 2};
+		for (unsigned int i = tid; i < I; i += NT)
+			d.out[i] = d.indices[i];
+		return;
+	}
+
+	// ---- position remap (buildPositionRemap :195-214) in a block-local hash table
+	const unsigned int H = (unsigned int)hashBucketsFor(V ? V : 1), mask = H - 1;
+	for (unsigned int i = tid; i < H; i += NT)
+		w.table[i] = ~0u;
+	__syncthreads();
+	for (unsigned int i = tid; i < V; i += NT)
+	{
+		const float* p = P + (size_t)i * sf;
+		float x = p[0], y = p[1], z = p[2];
+		unsigned int h = mix32b(posBitsB(x) * 0x9e3779b1u ^ mix32b(posBitsB(y) + 0x85ebca6bu) ^ mix32b(posBitsB(z) * 0xc2b2ae35u + 1u));
+		unsigned int b = h & mask, slot = ~0u;
+		for (unsigned int probe = 0; probe <= mask; ++probe)
+		{
+			unsigned int cur = w.table[b];
+			if (cur == ~0u)
+			{
+				unsigned int prev = atomicCAS(&w.table[b], ~0u, i);
+				if (prev == ~0u)
+				{
+					slot = b;
+					break;
+				}
+				cur = prev;
+			}
+			const float* q = P + (size_t)cur * sf;
+			if (q[0] == x && q[1] == y && q[2] == z)
+			{
+				atomicMin(&w.table[b], i);
+				slot = b;
+				break;
+			}
+			b = (b + probe + 1) & mask;
+		}
+		w.remap[i] = slot; // slot for now
+	}
+	__syncthreads();
+	for (unsigned int i = tid; i < V; i += NT)
+	{
+		unsigned int s = w.remap[i];
+		w.remap[i] = s == ~0u ? i : w.table[s];
+	}
+	__syncthreads();
+	// wedge cycle (:229-239): dup i -> previous member of its class (or the primary); the
+	// primary -> largest duplicate
+	for (unsigned int i = tid; i < V; i += NT)
+	{
+		w.wedge[i] = i;
+		w.fill[i] = 0;
+	}
+	__syncthreads();
+	for (unsigned int i = tid; i < V; i += NT)
+	{
+		unsigned int r = w.remap[i];
+		if (r == i)
+			continue;
+		unsigned int pred = r;
+		for (unsigned int j = r + 1; j < i; ++j)
+			if (w.remap[j] == r)
+				pred = j;
+		w.wedge[i] = pred;
+		atomicMax(&w.fill[r], i);
+	}
+	__syncthreads();
+	for (unsigned int i = tid; i < V; i += NT)
+		if (w.remap[i] == i && w.fill[i])
+			w.wedge[i] = w.fill[i];
+	__syncthreads();
+
+	// ---- rescale (rescalePositions :544-603): ordered folds over contiguous thread chunks
+	{
+		float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+		unsigned int per = (V + NT - 1) / NT, b0 = min(V, tid * per), b1 = min(V, b0 + per);
+		for (unsigned int i = b0; i < b1; ++i)
+		{
+			const float* p = P + (size_t)i * sf;
+			for (int j = 0; j < 3; ++j)
+			{
+				mn[j] = mn[j] > p[j] ? p[j] : mn[j];
+				mx[j] = mx[j] < p[j] ? p[j] : mx[j];
+			}
+		}
+		for (int o = 1; o < 32; o <<= 1)
+			for (int j = 0; j < 3; ++j)
+			{
+				float a = __shfl_down_sync(0xffffffffu, mn[j], o), c = __shfl_down_sync(0xffffffffu, mx[j], o);
+				if ((tid & 31) + o < 32 && ((tid & (2 * o - 1)) == 0))
+					mn[j] = fmin_l(mn[j], a), mx[j] = fmax_l(mx[j], c);
+			}
+		if ((tid & 31) == 0)
+			for (int j = 0; j < 3; ++j)
+				s_mm[tid >> 5][j] = mn[j], s_mm[tid >> 5][3 + j] = mx[j];
+		__syncthreads();
+		if (tid == 0)
+		{
+			for (int q = 1; q < NT / 32; ++q)
+				for (int j = 0; j < 3; ++j)
+					s_mm[0][j] = fmin_l(s_mm[0][j], s_mm[q][j]), s_mm[0][3 + j] = fmax_l(s_mm[0][3 + j], s_mm[q][3 + j]);
+			float extent = 0.f;
+			extent = (s_mm[0][3] - s_mm[0][0]) < extent ? extent : (s_mm[0][3] - s_mm[0][0]);
+			extent = (s_mm[0][4] - s_mm[0][1]) < extent ? extent : (s_mm[0][4] - s_mm[0][1]);
+			extent = (s_mm[0][5] - s_mm[0][2]) < extent ? extent : (s_mm[0][5] - s_mm[0][2]);
+			s_extent = extent;
+			s_scale = extent == 0 ? 0.f : 1.f / extent;
+			for (int j = 0; j < 3; ++j)
+				s_minv[j] = s_mm[0][j];
+		}
+		__syncthreads();
+		for (unsigned int i = tid; i < V; i += NT)
+		{
+			const float* p = P + (size_t)i * sf;
+			w.pos[i] = make_float4((p[0] - s_minv[0]) * s_scale, (p[1] - s_minv[1]) * s_scale, (p[2] - s_minv[2]) * s_scale, 0.f);
+		}
+	}
+
+	// ---- raw adjacency (updateEdgeAdjacency :52-109, no remap): corner lists, unordered
+	for (unsigned int i = tid; i <= V; i += NT)
+		w.adj_off[i] = 0;
+	__syncthreads();
+	for (unsigned int p = tid; p < I; p += NT)
+		atomicAdd(&w.adj_off[w.idx[p]], 1u);
+	__syncthreads();
+	blockScanArray<NT>(w.adj_off, V + 1, w.red);
+	for (unsigned int i = tid; i < V; i += NT)
+		w.fill[i] = 0;
+	__syncthreads();
+	for (unsigned int p = tid; p < I; p += NT)
+	{
+		unsigned int v = w.idx[p];
+		unsigned int s = w.adj_off[v] + atomicAdd(&w.fill[v], 1u);
+		unsigned int f = p / 3, c = p - f * 3;
+		w.adj[s] = make_uint2(w.idx[f * 3 + (c == 2 ? 0 : c + 1)], w.idx[f * 3 + (c == 0 ? 2 : c - 1)]);
+	}
+	__syncthreads();
+
+	// ---- classification (classifyVertices :364-542, open edges from each vertex's own list)
+	for (unsigned int v = tid; v < V; v += NT)
+	{
+		unsigned int b = w.adj_off[v], e = w.adj_off[v + 1];
+		bool degen = false;
+		for (unsigned int j = b; j < e; ++j)
+			degen |= w.adj[j].x == v;
+		unsigned int outc = 0, outt = ~0u, inc = 0, ins = ~0u;
+		if (!degen)
+			for (unsigned int j = b; j < e; ++j)
+			{
+				uint2 ej = w.adj[j];
+				bool back = false, fwd = false;
+				for (unsigned int q = b; q < e; ++q)
+				{
+					uint2 eq = w.adj[q];
+					back |= eq.y == ej.x;
+					fwd |= eq.x == ej.y;
+				}
+				if (!back)
+					outc++, outt = ej.x;
+				if (!fwd)
+					inc++, ins = ej.y;
+			}
+		w.loop[v] = degen ? v : (outc == 0 ? ~0u : (outc == 1 ? outt : v));
+		w.loopback[v] = degen ? v : (inc == 0 ? ~0u : (inc == 1 ? ins : v));
+	}
+	__syncthreads();
+	for (unsigned int i = tid; i < V; i += NT)
+	{
+		unsigned int r = w.remap[i], wi = w.wedge[r];
+		unsigned char k;
+		if (wi == r)
+		{
+			unsigned int openi = w.loopback[r], openo = w.loop[r];
+			if (openi == ~0u && openo == ~0u)
+				k = kManifold;
+			else if (openi != ~0u && openo != ~0u && w.remap[openi] == w.remap[openo] && openi != r)
+				k = kSeam;
+			else if (openi != r && openo != r)
+				k = kBorder;
+			else
+				k = kLocked;
+		}
+		else if (w.wedge[wi] == r)
+		{
+			unsigned int openiv = w.loopback[r], openov = w.loop[r], openiw = w.loopback[wi], openow = w.loop[wi];
+			if (openiv != ~0u && openiv != r && openov != ~0u && openov != r && openiw != ~0u && openiw != wi && openow != ~0u && openow != wi)
+				k = (w.remap[openiv] == w.remap[openow] && w.remap[openov] == w.remap[openiw] && w.remap[openiv] != w.remap[openov]) ? kSeam : kLocked;
+			else
+				k = kLocked;
+		}
+		else
+			k = kLocked;
+		if ((d.options & kOptLockBorder) && k == kBorder)
+			k = kLocked;
+		w.kind[i] = k;
+	}
+	__syncthreads();
+
+	// ---- capacity (boundEdgeCollapses :1292-1308) from the raw degrees
+	{
+		unsigned int dual = 0;
+		for (unsigned int i = tid; i < V; i += NT)
+		{
+			unsigned char k = w.kind[i];
+			dual += (k == kManifold || k == kSeam) ? (w.adj_off[i + 1] - w.adj_off[i]) : 0;
+		}
+		unsigned int tot = blockSum<NT>(dual, w.red);
+		if (tid == 0)
+			s_cap = I - tot / 2 + 3;
+	}
+
+	// ---- remapped corner lists in corner order, then the quadric folds (:1057-1157)
+	for (unsigned int i = tid; i <= V; i += NT)
+		w.adj_off[i] = 0;
+	__syncthreads();
+	for (unsigned int p = tid; p < I; p += NT)
+		atomicAdd(&w.adj_off[w.remap[w.idx[p]]], 1u);
+	__syncthreads();
+	blockScanArray<NT>(w.adj_off, V + 1, w.red);
+	for (unsigned int i = tid; i < V; i += NT)
+		w.fill[i] = 0;
+	__syncthreads();
+	for (unsigned int p = tid; p < I; p += NT)
+	{
+		unsigned int v = w.remap[w.idx[p]];
+		w.adj[w.adj_off[v] + atomicAdd(&w.fill[v], 1u)].x = p;
+	}
+	__syncthreads();
+	for (unsigned int v = tid; v < V; v += NT)
+	{
+		// insertion sort of the vertex's corners (few per vertex)
+		unsigned int b = w.adj_off[v], e = w.adj_off[v + 1];
+		for (unsigned int j = b + 1; j < e; ++j)
+		{
+			unsigned int x = w.adj[j].x;
+			unsigned int q = j;
+			while (q > b && w.adj[q - 1].x > x)
+			{
+				w.adj[q].x = w.adj[q - 1].x;
+				--q;
+			}
+			w.adj[q].x = x;
+		}
+	}
+	__syncthreads();
+	{
+		const float factor = (d.options & kOptRegularizeLight) ? 1e-2f : ((d.options & kOptRegularize) ? 1e-1f : 1e-7f);
+		for (unsigned int r = tid; r < V; r += NT)
+		{
+			if (w.remap[r] != r)
+			{
+				stquadric(w.vq, r, qzero());
+				continue;
+			}
+			unsigned int b = w.adj_off[r], e = w.adj_off[r + 1];
+			Quadric Q = qzero();
+			for (unsigned int j = b; j < e; ++j)
+			{
+				unsigned int f = w.adj[j].x / 3;
+				unsigned int i0 = w.idx[f * 3 + 0], i1 = w.idx[f * 3 + 1], i2 = w.idx[f * 3 + 2];
+				float4 a0 = w.pos[i0], a1 = w.pos[i1], a2 = w.pos[i2];
+				Quadric F = qtriangle(V3{a0.x, a0.y, a0.z}, V3{a1.x, a1.y, a1.z}, V3{a2.x, a2.y, a2.z}, 1.f);
+				qadd(Q, F);
+			}
+			float wt = Q.w * factor;
+			float4 pr = w.pos[r];
+			Quadric Pq = qpoint(pr.x, pr.y, pr.z, wt);
+			qadd(Q, Pq);
+			unsigned int lastf = ~0u;
+			for (unsigned int j = b; j < e; ++j)
+			{
+				unsigned int f = w.adj[j].x / 3;
+				if (f == lastf)
+					continue;
+				lastf = f;
+				for (int ed = 0; ed < 3; ++ed)
+				{
+					unsigned int i0 = w.idx[f * 3 + ed], i1 = w.idx[f * 3 + (ed == 2 ? 0 : ed + 1)];
+					unsigned char k0 = w.kind[i0], k1 = w.kind[i1];
+					bool b0 = k0 == kBorder || k0 == kSeam, b1 = k1 == kBorder || k1 == kSeam;
+					if (!b0 && !b1)
+						continue;
+					if (b0 && w.loop[i0] != i1)
+						continue;
+					if (b1 && w.loopback[i1] != i0)
+						continue;
+					bool to0 = w.remap[i0] == r, to1 = w.remap[i1] == r;
+					if (!to0 && !to1)
+						continue;
+					unsigned int i2 = w.idx[f * 3 + (ed == 0 ? 2 : ed - 1)];
+					float weight = (k0 == kBorder || k1 == kBorder) ? 10.f : 0.5f;
+					float4 a0 = w.pos[i0], a1 = w.pos[i1], a2 = w.pos[i2];
+					V3 p0{a0.x, a0.y, a0.z}, p1{a1.x, a1.y, a1.z}, p2{a2.x, a2.y, a2.z};
+					Quadric E = qedge(p0, p1, p2, weight);
+					Quadric Tq = qtriangle(p0, p1, p2, weight);
+					Tq.w = 0;
+					qadd(E, Tq);
+					if (to0)
+						qadd(Q, E);
+					if (to1)
+						qadd(Q, E);
+				}
+			}
+			stquadric(w.vq, r, Q);
+		}
+	}
+	__syncthreads();
+
+	// ---- pass loop (:2493-2541)
+	const float error_scale = (d.options & kOptErrorAbsolute) ? s_extent : 1.f;
+	const float error_limit = (d.target_error * d.target_error) / (error_scale * error_scale);
+	unsigned int result_count = I;
+	float result_error = 0.f;
+	unsigned int passes = 0;
+
+	while (result_count > d.target_index_count)
+	{
+		const unsigned int T = result_count / 3;
+
+		// adjacency of the current result, welded by remap (unordered lists)
+		for (unsigned int i = tid; i <= V; i += NT)
+			w.adj_off[i] = 0;
+		__syncthreads();
+		for (unsigned int p = tid; p < result_count; p += NT)
+			atomicAdd(&w.adj_off[w.remap[w.idx[p]]], 1u);
+		__syncthreads();
+		blockScanArray<NT>(w.adj_off, V + 1, w.red);
+		for (unsigned int i = tid; i < V; i += NT)
+			w.fill[i] = 0;
+		__syncthreads();
+		for (unsigned int t = tid; t < T; t += NT)
+		{
+			unsigned int a = w.remap[w.idx[t * 3 + 0]], b = w.remap[w.idx[t * 3 + 1]], c = w.remap[w.idx[t * 3 + 2]];
+			w.adj[w.adj_off[a] + atomicAdd(&w.fill[a], 1u)] = make_uint2(b, c);
+			w.adj[w.adj_off[b] + atomicAdd(&w.fill[b], 1u)] = make_uint2(c, a);
+			w.adj[w.adj_off[c] + atomicAdd(&w.fill[c], 1u)] = make_uint2(a, b);
+		}
+		__syncthreads();
+
+		// pick (pickEdgeCollapses :1310-1372), chunked block scan over triangles
+		if (tid == 0)
+			s_count = 0, s_trunc = ~0u;
+		__syncthreads();
+		for (unsigned int base = 0; base < T; base += NT)
+		{
+			unsigned int t = base + tid;
+			unsigned int v0[3], v1[3], bd[3], n = 0;
+			if (t < T)
+			{
+				unsigned int a[3] = {w.idx[t * 3], w.idx[t * 3 + 1], w.idx[t * 3 + 2]};
+				for (int e = 0; e < 3; ++e)
+				{
+					unsigned int i0 = a[e], i1 = a[e == 2 ? 0 : e + 1];
+					unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
+					if (r0 == r1)
+						continue;
+					unsigned int k0 = w.kind[i0], k1 = w.kind[i1];
+					bool c01 = canCollapse(k0, k1), c10 = canCollapse(k1, k0);
+					if (!(c01 | c10))
+						continue;
+					if (hasOpposite(k0, k1) && r1 > r0)
+						continue;
+					if ((k0 == kBorder || k0 == kSeam) && k1 != kManifold && w.loop[i0] != i1)
+						continue;
+					if ((k1 == kBorder || k1 == kSeam) && k0 != kManifold && w.loopback[i1] != i0)
+						continue;
+					if (c01 & c10)
+						v0[n] = i0, v1[n] = i1, bd[n] = 1;
+					else
+						v0[n] = c01 ? i0 : i1, v1[n] = c01 ? i1 : i0, bd[n] = 0;
+					n++;
+				}
+			}
+			unsigned int tot;
+			unsigned int ex = blockExclusiveScan<NT>(n, w.red, &tot);
+			unsigned int o = s_count + ex;
+			if (t < T)
+			{
+				if (o + 3 > s_cap)
+					atomicMin(&s_trunc, o);
+				else
+					for (unsigned int q = 0; q < n; ++q)
+						w.cv0[o + q] = v0[q], w.cv1[o + q] = v1[q], w.cerr[o + q] = bd[q];
+			}
+			__syncthreads();
+			if (tid == 0)
+				s_count += tot;
+			__syncthreads();
+		}
+		const unsigned int C = min(s_count, s_trunc);
+		if (C == 0)
+			break;
+
+		// rank (rankEdgeCollapses :1374-1450, positions only)
+		for (unsigned int c = tid; c < C; c += NT)
+		{
+			unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+			bool bidi = w.cerr[c] != 0;
+			float4 a0 = w.pos[i0], a1 = w.pos[i1];
+			V3 p0{a0.x, a0.y, a0.z}, p1{a1.x, a1.y, a1.z};
+			float ei = qerror(ldquadric(w.vq, w.remap[i0]), p1);
+			float ej = bidi ? qerror(ldquadric(w.vq, w.remap[i1]), p0) : FLT_MAX;
+			bool rev = bidi & (ej < ei);
+			w.cv0[c] = rev ? i1 : i0;
+			w.cv1[c] = rev ? i0 : i1;
+			w.cerr[c] = __float_as_uint(ej < ei ? ej : ei);
+		}
+		// sort (sortEdgeCollapses :1452-1496): histogram, scan, stable scatter by warp 0
+		for (unsigned int i = tid; i < kSortBinsC; i += NT)
+			w.hist[i] = 0;
+		__syncthreads();
+		for (unsigned int c = tid; c < C; c += NT)
+			atomicAdd(&w.hist[sortKey(w.cerr[c])], 1u);
+		__syncthreads();
+		blockScanArray<NT>(w.hist, kSortBinsC, w.red);
+		if (tid < 32)
+		{
+			const unsigned int lane = tid;
+			for (unsigned int base = 0; base < C; base += 32)
+			{
+				unsigned int c = base + lane;
+				unsigned int key = c < C ? sortKey(w.cerr[c]) : 0x10000u + lane;
+				unsigned int peers = __match_any_sync(0xffffffffu, key);
+				unsigned int rank = __popc(peers & ((1u << lane) - 1u));
+				unsigned int leader = __ffs(peers) - 1;
+				unsigned int basepos = 0;
+				if (c < C && lane == leader)
+				{
+					basepos = w.hist[key];
+					w.hist[key] = basepos + __popc(peers);
+				}
+				basepos = __shfl_sync(0xffffffffu, basepos, leader);
+				if (c < C)
+					w.order[basepos + rank] = c;
+				__syncwarp();
+			}
+		}
+		for (unsigned int i = tid; i < V; i += NT)
+			w.cr[i] = i, w.locked[i] = 0;
+		__syncthreads();
+
+		// perform (performEdgeCollapses :1498-1636) on warp 0, serial order, lanes split the flip test
+		const unsigned int goal = (result_count - d.target_index_count) / 3;
+		if (tid < 32)
+		{
+			const unsigned int lane = tid;
+			unsigned int edge_collapses = 0, triangle_collapses = 0, edge_goal = goal / 2;
+			for (unsigned int i = 0; i < C; ++i)
+			{
+				unsigned int c = w.order[i];
+				float err = __uint_as_float(w.cerr[c]);
+				if (err > error_limit)
+					break;
+				if (triangle_collapses >= goal)
+					break;
+				float error_goal = edge_goal < C ? 1.5f * __uint_as_float(w.cerr[w.order[edge_goal]]) : FLT_MAX;
+				if (err > error_goal && err > result_error && triangle_collapses > goal / 6)
+					break;
+				unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+				unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
+				unsigned char kd = w.kind[i0];
+				if (w.locked[r0] | w.locked[r1])
+					continue;
+				// flip test, lanes over r0's one-ring
+				unsigned int b = w.adj_off[r0], e = w.adj_off[r0 + 1];
+				float4 a0 = w.pos[r0], a1 = w.pos[r1];
+				V3 v0{a0.x, a0.y, a0.z}, v1{a1.x, a1.y, a1.z};
+				bool flip = false;
+				for (unsigned int j = b + lane; j < e; j += 32)
+				{
+					uint2 ed = w.adj[j];
+					unsigned int va = w.cr[ed.x], vb = w.cr[ed.y];
+					if (va == r1 || vb == r1 || va == vb)
+						continue;
+					float4 pa = w.pos[va], pb = w.pos[vb];
+					flip |= triFlip(V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, v0, v1);
+				}
+				if (__any_sync(0xffffffffu, flip))
+				{
+					edge_goal++;
+					continue;
+				}
+				if (lane == 0)
+				{
+					if (kd == kSeam)
+					{
+						unsigned int s0 = w.wedge[i0];
+						unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+						s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+						w.cr[i0] = i1;
+						w.cr[s0] = s1;
+					}
+					else
+						w.cr[i0] = i1;
+					w.locked[r0] = 1;
+					w.locked[r1] = 1;
+				}
+				__syncwarp();
+				triangle_collapses += (kd == kBorder) ? 1 : 2;
+				edge_collapses++;
+				result_error = result_error < err ? err : result_error;
+			}
+			if (lane == 0)
+			{
+				s_done = edge_collapses;
+				s_errbits = __float_as_uint(result_error);
+			}
+		}
+		__syncthreads();
+		result_error = __uint_as_float(s_errbits);
+		passes++;
+		if (s_done == 0)
+			break;
+
+		// updateQuadrics (:1638-1673): every target receives at most one source per pass
+		for (unsigned int i = tid; i < V; i += NT)
+		{
+			unsigned int t = w.cr[i];
+			if (t != i && w.remap[i] == i)
+			{
+				unsigned int r1 = w.remap[t];
+				Quadric Q = ldquadric(w.vq, r1);
+				qadd(Q, ldquadric(w.vq, i));
+				stquadric(w.vq, r1, Q);
+			}
+		}
+		// remapEdgeLoops (:1845-1864), in place
+		for (unsigned int i = tid; i < V; i += NT)
+		{
+			unsigned int* arrs[2] = {w.loop, w.loopback};
+			for (int q = 0; q < 2; ++q)
+			{
+				unsigned int* L = arrs[q];
+				unsigned int l = L[i];
+				if (l == ~0u)
+					continue;
+				unsigned int r = w.cr[l];
+				if (i == r)
+				{
+					unsigned int ll = L[l];
+					L[i] = ll != ~0u ? w.cr[ll] : ~0u;
+				}
+				else
+					L[i] = r;
+			}
+		}
+		__syncthreads();
+		// remapIndexBuffer (:1811-1843): in-place order-preserving compaction by chunks
+		unsigned int written = 0;
+		for (unsigned int base = 0; base < T; base += NT)
+		{
+			unsigned int t = base + tid;
+			unsigned int v0 = 0, v1 = 0, v2 = 0;
+			bool keep = false;
+			if (t < T)
+			{
+				v0 = w.cr[w.idx[t * 3]], v1 = w.cr[w.idx[t * 3 + 1]], v2 = w.cr[w.idx[t * 3 + 2]];
+				unsigned int r0 = w.remap[v0], r1 = w.remap[v1], r2 = w.remap[v2];
+				keep = r0 != r1 && r0 != r2 && r1 != r2;
+			}
+			unsigned int tot;
+			unsigned int ex = blockExclusiveScan<NT>(keep ? 1u : 0u, w.red, &tot);
+			if (keep)
+			{
+				unsigned int o = (written + ex) * 3;
+				w.idx[o] = v0, w.idx[o + 1] = v1, w.idx[o + 2] = v2;
+			}
+			written += tot;
+			__syncthreads();
+		}
+		result_count = written * 3;
+	}
+
+	for (unsigned int i = tid; i < result_count; i += NT)
+		d.out[i] = w.idx[i];
+	if (tid == 0)
+		*out = BatchResult{result_count, sqrtf(result_error) * error_scale, passes, 0};
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) kBatch(const BatchDesc* __restrict__ descs, unsigned int count, unsigned int* ticket, BatchResult* results,
+    char* slabs, size_t slab_bytes, unsigned int smem_bytes)
+{
+	extern __shared__ __align__(16) char smem[];
+	__shared__ unsigned int s_job;
+	for (;;)
+	{
+		if (threadIdx.x == 0)
+			s_job = atomicAdd(ticket, 1u);
+		__syncthreads();
+		unsigned int job = s_job;
+		if (job >= count)
+			break;
+		BatchDesc d = descs[job];
+		CtaWork w;
+		size_t need = carve(w, nullptr, d.index_count, d.vertex_count);
+		char* base = need <= smem_bytes ? smem : slabs + (size_t)blockIdx.x * slab_bytes;
+		carve(w, base, d.index_count, d.vertex_count);
+		simplifyMesh<NT>(d, w, &results[job]);
+		__syncthreads();
+	}
+}
+
+} // namespace
+
+size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count)
+{
+	CtaWork w;
+	return carve(w, nullptr, index_count, vertex_count);
+}
+
+void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
+    unsigned int smem_bytes, unsigned int blocks, int threads, cudaStream_t stream)
+{
+	MO_CUDA_CHECK(cudaMemsetAsync(d_ticket, 0, sizeof(unsigned int), stream));
+	switch (threads)
+	{
+	case 128:
+		MO_CUDA_CHECK(cudaFuncSetAttribute(kBatch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes)));
+		MO_LAUNCH(kBatch<128>, blocks, 128, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
+		break;
+	case 512:
+		MO_CUDA_CHECK(cudaFuncSetAttribute(kBatch<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes)));
+		MO_LAUNCH(kBatch<512>, blocks, 512, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
+		break;
+	default:
+		MO_CUDA_CHECK(cudaFuncSetAttribute(kBatch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes)));
+		MO_LAUNCH(kBatch<256>, blocks, 256, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
+		break;
+	}
+	MO_CUDA_CHECK(cudaGetLastError());
+}
+
+int batchBlocksPerSM(int threads, unsigned int smem_bytes)
+{
+	int n = 0;
+	switch (threads)
+	{
+	case 128:
+		cudaFuncSetAttribute(kBatch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<128>, 128, smem_bytes);
+		break;
+	case 512:
+		cudaFuncSetAttribute(kBatch<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<512>, 512, smem_bytes);
+		break;
+	default:
+		cudaFuncSetAttribute(kBatch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<256>, 256, smem_bytes);
+		break;
+	}
+	return n;
+}
+
+} // namespace mogpu

@@ -1,0 +1,41 @@
+// mo_batch.cuh - persistent multi-mesh simplification (one CTA per mesh, device work queue).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace mogpu
+{
+
+// one mesh of a batch; device pointers
+struct BatchDesc
+{
+	const unsigned int* indices;
+	const float* positions;
+	unsigned int* out;
+	unsigned int index_count;
+	unsigned int vertex_count;
+	unsigned int stride_f; // position stride in floats
+	unsigned int target_index_count;
+	float target_error;
+	unsigned int options;
+};
+
+struct BatchResult
+{
+	unsigned int index_count;
+	float result_error;
+	unsigned int passes;
+	unsigned int status; // 0 ok, 2 invalid index
+};
+
+// scratch bytes one mesh needs (shared memory when it fits, else a global slab)
+size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count);
+
+// resident CTAs per SM for a thread count and dynamic shared memory size
+int batchBlocksPerSM(int threads, unsigned int smem_bytes);
+
+void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
+    unsigned int smem_bytes, unsigned int blocks, int threads, cudaStream_t stream);
+
+} // namespace mogpu

@@ -9,10 +9,15 @@
 #include "mo_common.cuh"
 #include "mo_probe.cuh"
 #include "mo_simplify.cuh"
+#include "mo_batch.cuh"
 
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <numeric>
+#include <vector>
 #include <new>
 #include <string>
 
@@ -29,6 +34,19 @@ struct HostStaging
 	{
 		if (ptr)
 			cudaFreeHost(ptr);
+	}
+	void* ensure(size_t bytes)
+	{
+		if (bytes <= cap)
+			return ptr;
+		if (ptr)
+			cudaFreeHost(ptr);
+		ptr = nullptr;
+		cap = 0;
+		size_t want = bytes + bytes / 4 + 4096;
+		MO_CUDA_CHECK(cudaMallocHost(&ptr, want));
+		cap = want;
+		return ptr;
 	}
 };
 
@@ -67,6 +85,11 @@ struct ThreadState
 	RunResult last;
 	PhaseTimes times;
 	bool timing = false;
+	// batched path
+	DeviceBuffer batch_meta, batch_slabs, batch_io;
+	HostStaging batch_host;
+	int batch_threads = 0;          // 0: autotune
+	unsigned int batch_smem = 0;    // 0: default budget
 
 	~ThreadState()
 	{
@@ -227,6 +250,267 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		return failHost(destination, indices, index_count, result_error, statusOf(e), e.what());
 	}
 }
+
+// ---------------------------------------------------------------- batched path
+
+const size_t kBatchSmemDefault = 96 * 1024;     // shared-memory budget per CTA
+const size_t kBatchSlabTotal = size_t(4) << 30; // global slabs for meshes beyond the budget
+
+struct BatchTuner
+{
+	std::mutex lock;
+	std::map<int, int> threads; // size class -> fastest threads per CTA
+} g_tuner;
+
+int sizeClass(size_t max_index_count)
+{
+	int c = 0;
+	while ((size_t(1) << c) < max_index_count)
+		++c;
+	return c;
+}
+
+// Runs descs (device pointers) through the persistent kernel; results in the same order.
+void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, std::vector<BatchResult>& results, cudaStream_t st)
+{
+	const size_t n = descs.size();
+	results.assign(n, BatchResult{0, 0.f, 0, 0});
+	if (n == 0)
+		return;
+	// largest meshes first so the queue's tail is short; results are mapped back below
+	std::vector<unsigned int> perm(n);
+	std::iota(perm.begin(), perm.end(), 0u);
+	std::stable_sort(perm.begin(), perm.end(), [&](unsigned int a, unsigned int b) { return descs[a].index_count > descs[b].index_count; });
+	std::vector<BatchDesc> ordered(n);
+	size_t budget = s.batch_smem ? s.batch_smem : kBatchSmemDefault;
+	size_t maxfit = 0, maxslab = 0, maxidx = 0;
+	for (size_t i = 0; i < n; ++i)
+	{
+		ordered[i] = descs[perm[i]];
+		size_t ws = batchWorkspaceBytes(ordered[i].index_count, ordered[i].vertex_count);
+		(ws <= budget ? maxfit : maxslab) = std::max(ws <= budget ? maxfit : maxslab, ws);
+		maxidx = std::max<size_t>(maxidx, ordered[i].index_count);
+	}
+	unsigned int smem = unsigned((maxfit + 15) & ~size_t(15));
+	int sms = 0;
+	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
+
+	size_t meta = align256(n * sizeof(BatchDesc)) + align256(n * sizeof(BatchResult)) + 256;
+	char* mbase = static_cast<char*>(s.batch_meta.ensure(meta));
+	BatchDesc* d_descs = reinterpret_cast<BatchDesc*>(mbase);
+	BatchResult* d_res = reinterpret_cast<BatchResult*>(mbase + align256(n * sizeof(BatchDesc)));
+	unsigned int* d_ticket = reinterpret_cast<unsigned int*>(mbase + align256(n * sizeof(BatchDesc)) + align256(n * sizeof(BatchResult)));
+	MO_CUDA_CHECK(cudaMemcpyAsync(d_descs, ordered.data(), n * sizeof(BatchDesc), cudaMemcpyHostToDevice, st));
+
+	auto launch = [&](int threads) {
+		int per_sm = std::max(1, batchBlocksPerSM(threads, smem));
+		unsigned int blocks = unsigned(std::min<size_t>(size_t(per_sm) * sms, n));
+		if (maxslab)
+			blocks = unsigned(std::max<size_t>(1, std::min<size_t>(blocks, kBatchSlabTotal / maxslab)));
+		char* slabs = maxslab ? static_cast<char*>(s.batch_slabs.ensure(size_t(blocks) * maxslab)) : nullptr;
+		launchBatch(d_descs, unsigned(n), d_ticket, d_res, slabs, maxslab, smem, blocks, threads, st);
+	};
+
+	int threads = s.batch_threads;
+	if (threads == 0)
+	{
+		int cls = sizeClass(maxidx);
+		{
+			std::lock_guard<std::mutex> g(g_tuner.lock);
+			auto it = g_tuner.threads.find(cls);
+			if (it != g_tuner.threads.end())
+				threads = it->second;
+		}
+		if (threads == 0)
+		{
+			// autotune: time each block size on this batch (identical results), keep the fastest
+			cudaEvent_t e0, e1;
+			MO_CUDA_CHECK(cudaEventCreate(&e0));
+			MO_CUDA_CHECK(cudaEventCreate(&e1));
+			float best = 1e30f;
+			for (int t : {128, 256, 512})
+			{
+				MO_CUDA_CHECK(cudaEventRecord(e0, st));
+				launch(t);
+				MO_CUDA_CHECK(cudaEventRecord(e1, st));
+				MO_CUDA_CHECK(cudaEventSynchronize(e1));
+				float ms = 0;
+				MO_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+				if (ms < best)
+					best = ms, threads = t;
+			}
+			cudaEventDestroy(e0);
+			cudaEventDestroy(e1);
+			std::lock_guard<std::mutex> g(g_tuner.lock);
+			g_tuner.threads[cls] = threads;
+		}
+	}
+	launch(threads);
+	std::vector<BatchResult> tmp(n);
+	MO_CUDA_CHECK(cudaMemcpyAsync(tmp.data(), d_res, n * sizeof(BatchResult), cudaMemcpyDeviceToHost, st));
+	MO_CUDA_CHECK(cudaStreamSynchronize(st));
+	probe().collect();
+	for (size_t i = 0; i < n; ++i)
+		results[perm[i]] = tmp[i];
+}
+
+std::string checkBatchMesh(const meshoptgpu_BatchMesh& m)
+{
+	if (m.index_count % 3 != 0)
+		return "index_count must be a multiple of 3";
+	if (m.vertex_positions_stride < 12 || m.vertex_positions_stride > 256 || m.vertex_positions_stride % 4 != 0)
+		return "vertex_positions_stride must be in [12, 256] and a multiple of 4";
+	if (m.target_index_count > m.index_count)
+		return "target_index_count must not exceed index_count";
+	if (!(m.target_error >= 0))
+		return "target_error must be >= 0";
+	if (m.options & ~kSupportedOptions)
+		return "batched meshes support LockBorder, ErrorAbsolute, Regularize and RegularizeLight only";
+	if (m.index_count >= (size_t(1) << 32) || m.vertex_count >= (size_t(1) << 32))
+		return "batched meshes must have fewer than 2^32 indices and vertices";
+	return std::string();
+}
+
+int finishBatch(const std::vector<BatchResult>& res, size_t* counts, float* errors)
+{
+	int status = meshoptgpu_StatusOk;
+	for (size_t i = 0; i < res.size(); ++i)
+	{
+		if (counts)
+			counts[i] = res[i].index_count;
+		if (errors)
+			errors[i] = res[i].result_error;
+		if (res[i].status)
+			status = meshoptgpu_StatusInvalidArgument;
+	}
+	if (status != meshoptgpu_StatusOk)
+		setStatus(status, "a batched mesh has an index out of range of its vertex_count");
+	else
+		setStatus(meshoptgpu_StatusOk, "");
+	return status;
+}
+
+} // namespace
+
+extern "C" {
+
+int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, size_t mesh_count, size_t* result_index_counts, float* result_errors, void* stream)
+{
+	for (size_t i = 0; i < mesh_count; ++i)
+	{
+		std::string bad = checkBatchMesh(meshes[i]);
+		if (!bad.empty())
+		{
+			int st = (meshes[i].options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+			setStatus(st, "mesh " + std::to_string(i) + ": " + bad);
+			return st;
+		}
+	}
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		std::vector<BatchDesc> descs(mesh_count);
+		for (size_t i = 0; i < mesh_count; ++i)
+		{
+			const meshoptgpu_BatchMesh& m = meshes[i];
+			descs[i] = BatchDesc{m.indices, m.vertex_positions, m.destination, unsigned(m.index_count), unsigned(m.vertex_count),
+			    unsigned(m.vertex_positions_stride / 4), unsigned(m.target_index_count), m.target_error, m.options};
+		}
+		std::vector<BatchResult> res;
+		runBatch(s, descs, res, static_cast<cudaStream_t>(stream));
+		return finishBatch(res, result_index_counts, result_errors);
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
+int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh_count, size_t* result_index_counts, float* result_errors)
+{
+	for (size_t i = 0; i < mesh_count; ++i)
+	{
+		std::string bad = checkBatchMesh(meshes[i]);
+		if (!bad.empty())
+		{
+			int st = (meshes[i].options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+			setStatus(st, "mesh " + std::to_string(i) + ": " + bad);
+			return st;
+		}
+	}
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		// pack inputs: per mesh indices then positions (16-byte aligned), outputs after all inputs
+		std::vector<size_t> off_idx(mesh_count), off_pos(mesh_count), off_out(mesh_count);
+		size_t in_bytes = 0, out_words = 0;
+		for (size_t i = 0; i < mesh_count; ++i)
+		{
+			off_idx[i] = in_bytes;
+			in_bytes = (in_bytes + meshes[i].index_count * 4 + 15) & ~size_t(15);
+			off_pos[i] = in_bytes;
+			in_bytes = (in_bytes + meshes[i].vertex_count * meshes[i].vertex_positions_stride + 15) & ~size_t(15);
+			off_out[i] = out_words;
+			out_words += meshes[i].index_count;
+		}
+		char* h = static_cast<char*>(s.batch_host.ensure(in_bytes + 16));
+		for (size_t i = 0; i < mesh_count; ++i)
+		{
+			memcpy(h + off_idx[i], meshes[i].indices, meshes[i].index_count * 4);
+			memcpy(h + off_pos[i], meshes[i].vertex_positions, meshes[i].vertex_count * meshes[i].vertex_positions_stride);
+		}
+		char* d = static_cast<char*>(s.batch_io.ensure(align256(in_bytes) + out_words * 4 + 256));
+		unsigned int* d_out = reinterpret_cast<unsigned int*>(d + align256(in_bytes));
+		cudaStream_t st = s.stream;
+		MO_CUDA_CHECK(cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, st));
+		std::vector<BatchDesc> descs(mesh_count);
+		for (size_t i = 0; i < mesh_count; ++i)
+		{
+			const meshoptgpu_BatchMesh& m = meshes[i];
+			descs[i] = BatchDesc{reinterpret_cast<const unsigned int*>(d + off_idx[i]), reinterpret_cast<const float*>(d + off_pos[i]), d_out + off_out[i],
+			    unsigned(m.index_count), unsigned(m.vertex_count), unsigned(m.vertex_positions_stride / 4), unsigned(m.target_index_count), m.target_error,
+			    m.options};
+		}
+		std::vector<BatchResult> res;
+		runBatch(s, descs, res, st);
+		// results back in one copy (the packed outputs), then scattered to the callers' buffers
+		unsigned int* hout = static_cast<unsigned int*>(s.batch_host.ensure(std::max(in_bytes + 16, out_words * 4 + 16)));
+		MO_CUDA_CHECK(cudaMemcpyAsync(hout, d_out, out_words * 4, cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		for (size_t i = 0; i < mesh_count; ++i)
+			memcpy(meshes[i].destination, hout + off_out[i], size_t(res[i].index_count) * 4);
+		return finishBatch(res, result_index_counts, result_errors);
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
+void meshoptgpu_setBatchConfig(int threads, unsigned int smem_bytes)
+{
+	ThreadState& s = state();
+	s.batch_threads = (threads == 128 || threads == 256 || threads == 512) ? threads : 0;
+	s.batch_smem = smem_bytes;
+}
+
+int meshoptgpu_getBatchThreads(void)
+{
+	ThreadState& s = state();
+	if (s.batch_threads)
+		return s.batch_threads;
+	std::lock_guard<std::mutex> g(g_tuner.lock);
+	return g_tuner.threads.empty() ? 0 : g_tuner.threads.rbegin()->second;
+}
+
+} // extern "C"
+
+namespace
+{
 
 } // namespace
 
