@@ -54,6 +54,7 @@ def kperform_bytes(p, vertices, next_triangles):
 
 WORKLOADS = {
     "groups_4096": None,  # cluster groups: handled by bench_groups()
+    "serving": None,      # request loop: handled by bench_serving()
     "sphere_attr_2m": lambda: W.config_sphere_attr(9),
     "sphere_attr_524k": lambda: W.config_sphere_attr(8),
     "heightfield_256": W.config_heightfield_256,
@@ -177,6 +178,81 @@ def bench_groups(args, mg, torch):
                       "device_resident_mtris_s": round(tris / t_plain_dev / 1e6, 4), "device_resident_ms": round(1e3 * t_plain_dev, 1),
                       "calls": len(meshes)},
         "cpu_baseline": cpu, "bit_exact_vs_plain_and_oracle": bool(exact), "clocks": clocks.summary(), "gpu_launches": int(launches),
+    }
+    print(json.dumps(line))
+
+
+def bench_serving(args, mg, torch):
+    """Open-loop Poisson arrivals of simplify requests against the continuous-batching server and
+    against the plain path (one request at a time); p50/p99 latency and Mtris/s per rate.
+
+    Requests: seeded heightfield meshes whose triangle counts are lognormal (median 20k, sigma 1,
+    clipped to [1k, 1M]), kept resident on the device as a pool of distinct meshes; each request
+    picks a pool mesh, a target ratio uniform in [0.1, 0.5] and target_error 1e-2."""
+    import random
+
+    pool_size = 96
+    sizes = W.lognormal_sizes(pool_size, seed=4, median=20000.0, sigma=1.0)
+    dev = torch.device("cuda", 0)
+    pool = []
+    for i, t in enumerate(sizes):
+        n = int(round((t / 2) ** 0.5)) + 1
+        idx, pos = W.heightfield(n, seed=1000 + i, amp=0.05)
+        pool.append((torch.from_numpy(idx.view(np.int32)).to(dev), torch.from_numpy(pos).to(dev), len(idx), len(pos)))
+    n_req = args.requests
+    rng = random.Random(7)
+    reqs = []
+    for r in range(n_req):
+        m = rng.randrange(pool_size)
+        ratio = rng.uniform(0.1, 0.5)
+        reqs.append((m, W.target_count(pool[m][2], ratio)))
+    out_off = np.cumsum([0] + [pool[m][2] for m, _ in reqs])
+    out = torch.empty(int(out_off[-1]) + 1, dtype=torch.int32, device=dev)
+    total_tris = sum(pool[m][2] // 3 for m, _ in reqs)
+
+    def run(rate, plain):
+        gaps = np.random.default_rng(int(rate) * 7 + (1 if plain else 0)).exponential(1.0 / rate, size=n_req)
+        arrivals = np.cumsum(gaps)
+        with mg.Server(memory_budget=40 << 30, plain=plain) as srv:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tickets = []
+            for i, (m, target) in enumerate(reqs):
+                now = time.perf_counter() - t0
+                if arrivals[i] > now:
+                    time.sleep(arrivals[i] - now)
+                di, dp, ni, nv = pool[m]
+                tickets.append(srv.submit(di.data_ptr(), ni, dp.data_ptr(), nv, target, 1e-2, 0, out.data_ptr() + 4 * int(out_off[i])))
+            res = [srv.wait(t) for t in tickets]
+            t_end = time.perf_counter() - t0
+            stats = srv.stats()
+        lat = np.array([r[3] for r in res])
+        ok = all(r[0] == mg.STATUS_OK for r in res)
+        return {"rate_per_s": rate, "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                "mean_ms": round(float(lat.mean()), 3), "mtris_s": round(total_tris / t_end / 1e6, 3), "wall_s": round(t_end, 3),
+                "all_ok": ok, "batches": stats["batches"], "single_mesh_runs": stats["singles"],
+                "peak_reserved_gb": round(stats["peak_reserved"] / 2 ** 30, 3), "peak_in_flight": stats["peak_inflight"]}, res
+
+    rates = [float(x) for x in args.rates.split(",")]
+    served, plain = [], []
+    served_res = None
+    for rate in rates:
+        line, res = run(rate, False)
+        served.append(line)
+        served_res = served_res or res
+    plain_res = None
+    for rate in rates[: args.plain_rates]:
+        line, res = run(rate, True)
+        plain.append(line)
+        plain_res = plain_res or res
+    # the served results equal the plain (single-mesh path, alone) results request by request
+    same = plain_res is not None and all(a[1] == b[1] and a[2] == b[2] for a, b in zip(served_res, plain_res))
+    line = {
+        "metric": "input Mtris/s simplified (bit-exact); p50/p99 request latency", "value": served[0]["mtris_s"], "unit": "Mtris/s", "n_gpus": 1,
+        "steps": n_req, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serving_poisson", "requests_per_rate": n_req, "pool_meshes": pool_size, "tris": "lognormal median 20k sigma 1 [1k,1M]",
+                   "ratio": "U[0.1,0.5]", "target_error": 1e-2, "memory_budget_gb": 40, "request_input_tris": total_tris},
+        "served": served, "plain": plain, "served_equals_plain": bool(same),
     }
     print(json.dumps(line))
 
@@ -313,6 +389,9 @@ def main():
     ap.add_argument("--kernel", default="kPerform", help="kernel whose CUDA-event time gives the roofline line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--requests", type=int, default=10000, help="serving: requests per arrival rate")
+    ap.add_argument("--rates", default="250,500,1000,2000", help="serving: Poisson arrival rates (requests/s)")
+    ap.add_argument("--plain-rates", type=int, default=2, help="serving: how many of the rates also run the plain path")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -338,6 +417,9 @@ def main():
     mg.load()
     if args.workload == "groups_4096":
         bench_groups(args, mg, torch)
+        return
+    if args.workload == "serving":
+        bench_serving(args, mg, torch)
         return
     c = load_workload(args.workload)
     dev = torch.device("cuda", local)

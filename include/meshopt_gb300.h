@@ -141,6 +141,44 @@ MESHOPTGPU_API int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* mesh
 MESHOPTGPU_API void meshoptgpu_setBatchConfig(int threads, unsigned int smem_bytes);
 MESHOPTGPU_API int meshoptgpu_getBatchThreads(void);
 
+/* ---- serving: continuous batching of simplify requests ---- */
+
+typedef struct meshoptgpu_Server meshoptgpu_Server;
+
+typedef struct meshoptgpu_ServerConfig
+{
+	size_t memory_budget;     /* device bytes the server may hold for admitted requests (0: 40 GB) */
+	int batch_workers;        /* concurrent batch launches, one stream each (0: 4) */
+	int large_workers;        /* concurrent single-mesh simplifications for large requests (0: 2) */
+	size_t large_index_count; /* requests with more indices take the single-mesh path (0: 600000) */
+	int max_batch;            /* requests per batch launch at most (0: 2048) */
+	int batch_threads;        /* threads per CTA of the batch kernel (0: 256) */
+	int plain;                /* 1: no batching, one request at a time on the single-mesh path */
+} meshoptgpu_ServerConfig;
+
+/* Creates a server on the current device. Requests are admitted while their device scratch
+ * fits the memory budget; when a worker frees up it takes every request that has arrived in
+ * the meantime (up to max_batch) as one launch, so work that arrives while other requests are
+ * on the GPU overlaps with them. Returns NULL on failure (see meshoptgpu_getLastStatus). */
+MESHOPTGPU_API meshoptgpu_Server* meshoptgpu_serverCreate(const meshoptgpu_ServerConfig* config);
+
+/* Waits for all admitted requests, stops the workers and frees the server. */
+MESHOPTGPU_API void meshoptgpu_serverDestroy(meshoptgpu_Server* server);
+
+/* Submits one request without blocking. Pointers in mesh are DEVICE pointers that must stay
+ * valid until the request completes; options as in meshoptgpu_BatchMesh. Returns a ticket
+ * (>= 0) or a negative meshoptgpu_Status* value. */
+MESHOPTGPU_API long long meshoptgpu_serverSubmit(meshoptgpu_Server* server, const meshoptgpu_BatchMesh* mesh);
+
+/* Blocks until the request completes; fills the result index count and error, and the
+ * request's latency from submission to completion in milliseconds. Returns its status. */
+MESHOPTGPU_API int meshoptgpu_serverWait(meshoptgpu_Server* server, long long ticket, size_t* result_index_count, float* result_error,
+    double* latency_ms);
+
+/* Server counters: requests completed, batch launches, single-mesh launches, peak device
+ * bytes reserved, peak requests in flight. */
+MESHOPTGPU_API void meshoptgpu_serverStats(meshoptgpu_Server* server, unsigned long long* out5);
+
 /* Kernel launch accounting for the calling thread: the number of kernels this library has
  * launched, and optional CUDA-event timing of every launch of one kernel (selected by its
  * name prefix, e.g. "kDecide"; NULL disables). The events are recorded on the launching

@@ -46,6 +46,7 @@ EXPORTS = [
     "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
     "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc",
     "meshoptgpu_simplifyBatch", "meshoptgpu_simplifyBatchHost", "meshoptgpu_setBatchConfig", "meshoptgpu_getBatchThreads",
+    "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
 ]
 
 
@@ -57,6 +58,11 @@ class BatchMesh(C.Structure):
     _fields_ = [("indices", C.c_void_p), ("index_count", C.c_size_t), ("vertex_positions", C.c_void_p),
                 ("vertex_count", C.c_size_t), ("vertex_positions_stride", C.c_size_t), ("target_index_count", C.c_size_t),
                 ("target_error", C.c_float), ("options", C.c_uint), ("destination", C.c_void_p)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget", C.c_size_t), ("batch_workers", C.c_int), ("large_workers", C.c_int),
+                ("large_index_count", C.c_size_t), ("max_batch", C.c_int), ("batch_threads", C.c_int), ("plain", C.c_int)]
 
 
 class SimplifyError(RuntimeError):
@@ -103,6 +109,14 @@ def load():
     lib.meshoptgpu_simplifyBatchHost.argtypes = [vp, sz, vp, vp]
     lib.meshoptgpu_setBatchConfig.argtypes = [C.c_int, C.c_uint]
     lib.meshoptgpu_getBatchThreads.restype = C.c_int
+    lib.meshoptgpu_serverCreate.restype = C.c_void_p
+    lib.meshoptgpu_serverCreate.argtypes = [vp]
+    lib.meshoptgpu_serverDestroy.argtypes = [vp]
+    lib.meshoptgpu_serverSubmit.restype = C.c_longlong
+    lib.meshoptgpu_serverSubmit.argtypes = [vp, vp]
+    lib.meshoptgpu_serverWait.restype = C.c_int
+    lib.meshoptgpu_serverWait.argtypes = [vp, C.c_longlong, vp, vp, vp]
+    lib.meshoptgpu_serverStats.argtypes = [vp, vp]
     lib.meshoptgpu_simplifyScaleNoAlloc.restype = C.c_int
     lib.meshoptgpu_simplifyScaleNoAlloc.argtypes = [vp, vp, sz, sz, vp]
     _lib = lib
@@ -300,3 +314,46 @@ def set_batch_config(threads=0, smem_bytes=0):
 
 def batch_threads():
     return int(load().meshoptgpu_getBatchThreads())
+
+
+class Server:
+    """Continuous-batching request server (meshoptgpu_server*): submit device-resident meshes
+    without blocking, wait for tickets; latencies are measured natively from submission to
+    completion."""
+
+    def __init__(self, memory_budget=0, batch_workers=0, large_workers=0, large_index_count=0, max_batch=0, batch_threads=0, plain=False):
+        self.lib = load()
+        cfg = ServerConfig(memory_budget, batch_workers, large_workers, large_index_count, max_batch, batch_threads, 1 if plain else 0)
+        self.h = self.lib.meshoptgpu_serverCreate(C.byref(cfg))
+        if not self.h:
+            raise SimplifyError(*last_status())
+
+    def submit(self, d_indices, index_count, d_positions, vertex_count, target, error, options, d_destination, stride=12):
+        m = BatchMesh(d_indices, index_count, d_positions, vertex_count, stride, int(target), float(error), int(options), d_destination)
+        t = self.lib.meshoptgpu_serverSubmit(C.c_void_p(self.h), C.byref(m))
+        if t < 0:
+            raise SimplifyError(-t, last_status()[1])
+        return t
+
+    def wait(self, ticket):
+        n = C.c_size_t(0)
+        e = C.c_float(0)
+        lat = C.c_double(0)
+        st = self.lib.meshoptgpu_serverWait(C.c_void_p(self.h), ticket, C.byref(n), C.byref(e), C.byref(lat))
+        return st, int(n.value), float(e.value), float(lat.value)
+
+    def stats(self):
+        out = (C.c_ulonglong * 5)()
+        self.lib.meshoptgpu_serverStats(C.c_void_p(self.h), C.cast(out, C.c_void_p))
+        return dict(zip(["completed", "batches", "singles", "peak_reserved", "peak_inflight"], [int(x) for x in out]))
+
+    def close(self):
+        if self.h:
+            self.lib.meshoptgpu_serverDestroy(C.c_void_p(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

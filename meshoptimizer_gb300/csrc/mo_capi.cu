@@ -11,9 +11,13 @@
 #include "mo_simplify.cuh"
 #include "mo_batch.cuh"
 
+#include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <thread>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -114,12 +118,13 @@ struct ThreadState
 	}
 };
 
-thread_local ThreadState* tls = nullptr;
+// per-thread state, freed when the thread exits (server workers) or on request
+thread_local std::unique_ptr<ThreadState> tls;
 
 ThreadState& state()
 {
 	if (!tls)
-		tls = new ThreadState();
+		tls.reset(new ThreadState());
 	return *tls;
 }
 
@@ -390,6 +395,178 @@ int finishBatch(const std::vector<BatchResult>& res, size_t* counts, float* erro
 	return status;
 }
 
+// ---------------------------------------------------------------- serving
+
+struct ServerRequest
+{
+	BatchDesc desc;
+	size_t index_count = 0, vertex_count = 0;
+	size_t reserve = 0;
+	std::chrono::steady_clock::time_point submitted, completed;
+	bool done = false;
+	int status = meshoptgpu_StatusOk;
+	size_t result_count = 0;
+	float result_error = 0.f;
+};
+
+struct ServerImpl
+{
+	meshoptgpu_ServerConfig cfg;
+	int device = 0;
+	int sms = 1;
+	std::mutex m;
+	std::condition_variable cv_work, cv_done;
+	std::deque<ServerRequest*> small_q, large_q;
+	std::vector<std::unique_ptr<ServerRequest>> reqs; // index = ticket
+	size_t reserved = 0, peak_reserved = 0;
+	unsigned long long completed = 0, batches = 0, singles = 0, inflight = 0, peak_inflight = 0;
+	bool stop = false;
+	std::vector<std::thread> threads;
+};
+
+const size_t kServerBudgetDefault = size_t(40) << 30;
+
+// device bytes a request holds while it runs on the batch path (its global slab; meshes that
+// fit shared memory hold none) or on the single-mesh path (its arena)
+size_t batchReserve(const ServerRequest& r)
+{
+	size_t ws = batchWorkspaceBytes(r.index_count, r.vertex_count);
+	return ws <= kBatchSmemDefault ? 4096 : ws;
+}
+
+void publish(ServerImpl& S, std::vector<ServerRequest*>& done_reqs, size_t release)
+{
+	std::lock_guard<std::mutex> g(S.m);
+	auto now = std::chrono::steady_clock::now();
+	for (ServerRequest* r : done_reqs)
+	{
+		r->done = true;
+		r->completed = now;
+	}
+	S.completed += done_reqs.size();
+	S.inflight -= done_reqs.size();
+	S.reserved -= release;
+	S.cv_done.notify_all();
+	S.cv_work.notify_all();
+}
+
+void batchWorker(ServerImpl* S)
+{
+	cudaSetDevice(S->device);
+	ThreadState& ts = state();
+	ts.batch_threads = S->cfg.batch_threads;
+	for (;;)
+	{
+		std::vector<ServerRequest*> take;
+		size_t reserve = 0;
+		{
+			std::unique_lock<std::mutex> lk(S->m);
+			S->cv_work.wait(lk, [&] {
+				if (S->stop)
+					return true;
+				return !S->small_q.empty() && S->reserved + batchReserve(*S->small_q.front()) <= S->cfg.memory_budget;
+			});
+			if (S->stop && S->small_q.empty())
+				return;
+			// continuous batching: everything that arrived since this worker last launched, in
+			// arrival order, while the memory budget and the batch limit allow
+			size_t maxslab = 0;
+			while (!S->small_q.empty() && take.size() < size_t(S->cfg.max_batch))
+			{
+				ServerRequest* r = S->small_q.front();
+				size_t slab = batchReserve(*r) > 4096 ? batchReserve(*r) : 0;
+				size_t nm = std::max(maxslab, slab);
+				size_t blocks = std::min<size_t>(take.size() + 1, size_t(S->sms) * 4);
+				size_t need = blocks * nm + 4096 * (take.size() + 1);
+				if (S->reserved + need > S->cfg.memory_budget && !take.empty())
+					break;
+				maxslab = nm;
+				reserve = need;
+				take.push_back(r);
+				S->small_q.pop_front();
+			}
+			S->reserved += reserve;
+			S->peak_reserved = std::max(S->peak_reserved, S->reserved);
+			S->inflight += take.size();
+			S->peak_inflight = std::max(S->peak_inflight, S->inflight);
+			S->batches++;
+		}
+		std::vector<BatchDesc> descs(take.size());
+		for (size_t i = 0; i < take.size(); ++i)
+			descs[i] = take[i]->desc;
+		std::vector<BatchResult> res;
+		try
+		{
+			ts.ensure();
+			runBatch(ts, descs, res, ts.stream);
+			for (size_t i = 0; i < take.size(); ++i)
+			{
+				take[i]->result_count = res[i].index_count;
+				take[i]->result_error = res[i].result_error;
+				take[i]->status = res[i].status ? meshoptgpu_StatusInvalidArgument : meshoptgpu_StatusOk;
+			}
+		}
+		catch (const std::exception& e)
+		{
+			for (ServerRequest* r : take)
+				r->status = statusOf(e);
+			fprintf(stderr, "meshopt_gb300: server batch failed: %s\n", e.what());
+		}
+		publish(*S, take, reserve);
+	}
+}
+
+void largeWorker(ServerImpl* S)
+{
+	cudaSetDevice(S->device);
+	ThreadState& ts = state();
+	for (;;)
+	{
+		ServerRequest* r = nullptr;
+		{
+			std::unique_lock<std::mutex> lk(S->m);
+			S->cv_work.wait(lk, [&] {
+				if (S->stop)
+					return true;
+				return !S->large_q.empty() && S->reserved + S->large_q.front()->reserve <= S->cfg.memory_budget;
+			});
+			if (S->stop && S->large_q.empty())
+				return;
+			r = S->large_q.front();
+			S->large_q.pop_front();
+			S->reserved += r->reserve;
+			S->peak_reserved = std::max(S->peak_reserved, S->reserved);
+			S->inflight++;
+			S->peak_inflight = std::max(S->peak_inflight, S->inflight);
+			S->singles++;
+		}
+		try
+		{
+			ts.ensure();
+			MeshDesc m;
+			m.indices = r->desc.indices;
+			m.index_count = r->index_count;
+			m.positions = r->desc.positions;
+			m.vertex_count = r->vertex_count;
+			m.positions_stride = size_t(r->desc.stride_f) * 4;
+			m.target_index_count = r->desc.target_index_count;
+			m.target_error = r->desc.target_error;
+			m.options = r->desc.options;
+			RunResult rr = ts.simplifier->run(m, r->desc.out, ts.stream);
+			r->result_count = rr.index_count;
+			r->result_error = rr.result_error;
+			r->status = meshoptgpu_StatusOk;
+		}
+		catch (const std::exception& e)
+		{
+			r->status = statusOf(e);
+			fprintf(stderr, "meshopt_gb300: server request failed: %s\n", e.what());
+		}
+		std::vector<ServerRequest*> one{r};
+		publish(*S, one, r->reserve);
+	}
+}
+
 } // namespace
 
 extern "C" {
@@ -489,6 +666,116 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		setStatus(statusOf(e), e.what());
 		return statusOf(e);
 	}
+}
+
+meshoptgpu_Server* meshoptgpu_serverCreate(const meshoptgpu_ServerConfig* config)
+{
+	try
+	{
+		std::unique_ptr<ServerImpl> S(new ServerImpl());
+		meshoptgpu_ServerConfig c = config ? *config : meshoptgpu_ServerConfig{};
+		c.memory_budget = c.memory_budget ? c.memory_budget : kServerBudgetDefault;
+		c.batch_workers = c.batch_workers > 0 ? c.batch_workers : 4;
+		c.large_workers = c.large_workers > 0 ? c.large_workers : 2;
+		c.large_index_count = c.large_index_count ? c.large_index_count : 600000;
+		c.max_batch = c.max_batch > 0 ? c.max_batch : 2048;
+		c.batch_threads = (c.batch_threads == 128 || c.batch_threads == 256 || c.batch_threads == 512) ? c.batch_threads : 256;
+		S->cfg = c;
+		MO_CUDA_CHECK(cudaGetDevice(&S->device));
+		MO_CUDA_CHECK(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->device));
+		ServerImpl* raw = S.get();
+		if (!c.plain)
+			for (int i = 0; i < c.batch_workers; ++i)
+				S->threads.emplace_back(batchWorker, raw);
+		for (int i = 0; i < (c.plain ? 1 : c.large_workers); ++i)
+			S->threads.emplace_back(largeWorker, raw);
+		setStatus(meshoptgpu_StatusOk, "");
+		return reinterpret_cast<meshoptgpu_Server*>(S.release());
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return nullptr;
+	}
+}
+
+void meshoptgpu_serverDestroy(meshoptgpu_Server* server)
+{
+	if (!server)
+		return;
+	ServerImpl* S = reinterpret_cast<ServerImpl*>(server);
+	{
+		std::unique_lock<std::mutex> lk(S->m);
+		S->cv_done.wait(lk, [&] { return S->small_q.empty() && S->large_q.empty() && S->inflight == 0; });
+		S->stop = true;
+		S->cv_work.notify_all();
+	}
+	for (std::thread& t : S->threads)
+		t.join();
+	delete S;
+}
+
+long long meshoptgpu_serverSubmit(meshoptgpu_Server* server, const meshoptgpu_BatchMesh* mesh)
+{
+	if (!server || !mesh)
+		return -meshoptgpu_StatusInvalidArgument;
+	ServerImpl* S = reinterpret_cast<ServerImpl*>(server);
+	std::string bad = checkBatchMesh(*mesh);
+	if (!bad.empty())
+	{
+		int st = (mesh->options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+		setStatus(st, bad);
+		return -st;
+	}
+	std::unique_ptr<ServerRequest> r(new ServerRequest());
+	r->desc = BatchDesc{mesh->indices, mesh->vertex_positions, mesh->destination, unsigned(mesh->index_count), unsigned(mesh->vertex_count),
+	    unsigned(mesh->vertex_positions_stride / 4), unsigned(mesh->target_index_count), mesh->target_error, mesh->options};
+	r->index_count = mesh->index_count;
+	r->vertex_count = mesh->vertex_count;
+	bool large = S->cfg.plain || mesh->index_count > S->cfg.large_index_count;
+	r->reserve = large ? Simplifier::workspaceBytes(mesh->index_count, mesh->vertex_count, 0) : batchReserve(*r);
+	if (r->reserve > S->cfg.memory_budget)
+	{
+		setStatus(meshoptgpu_StatusOutOfMemory, "request needs more device scratch than the server's memory budget");
+		return -meshoptgpu_StatusOutOfMemory;
+	}
+	r->submitted = std::chrono::steady_clock::now();
+	std::lock_guard<std::mutex> g(S->m);
+	long long ticket = (long long)S->reqs.size();
+	(large ? S->large_q : S->small_q).push_back(r.get());
+	S->reqs.push_back(std::move(r));
+	S->cv_work.notify_all();
+	return ticket;
+}
+
+int meshoptgpu_serverWait(meshoptgpu_Server* server, long long ticket, size_t* result_index_count, float* result_error, double* latency_ms)
+{
+	if (!server)
+		return meshoptgpu_StatusInvalidArgument;
+	ServerImpl* S = reinterpret_cast<ServerImpl*>(server);
+	std::unique_lock<std::mutex> lk(S->m);
+	if (ticket < 0 || ticket >= (long long)S->reqs.size())
+		return meshoptgpu_StatusInvalidArgument;
+	ServerRequest* r = S->reqs[size_t(ticket)].get();
+	S->cv_done.wait(lk, [&] { return r->done; });
+	if (result_index_count)
+		*result_index_count = r->result_count;
+	if (result_error)
+		*result_error = r->result_error;
+	if (latency_ms)
+		*latency_ms = std::chrono::duration<double, std::milli>(r->completed - r->submitted).count();
+	return r->status;
+}
+
+void meshoptgpu_serverStats(meshoptgpu_Server* server, unsigned long long* out5)
+{
+	ServerImpl* S = reinterpret_cast<ServerImpl*>(server);
+	std::lock_guard<std::mutex> g(S->m);
+	out5[0] = S->completed;
+	out5[1] = S->batches;
+	out5[2] = S->singles;
+	out5[3] = S->peak_reserved;
+	out5[4] = S->peak_inflight;
 }
 
 void meshoptgpu_setBatchConfig(int threads, unsigned int smem_bytes)
@@ -669,8 +956,7 @@ size_t meshoptgpu_workspaceBytes(size_t index_count, size_t vertex_count, size_t
 
 void meshoptgpu_releaseThreadResources(void)
 {
-	delete tls;
-	tls = nullptr;
+	tls.reset();
 }
 
 } // extern "C"
