@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 namespace mogpu
 {
@@ -799,22 +800,37 @@ size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count)
 	return carve(w, nullptr, index_count, vertex_count);
 }
 
+// the dynamic shared-memory limit of every batch kernel instance is raised once, to the
+// device's opt-in maximum: setting it per launch would race between threads launching batches
+// with different sizes
+void raiseSmemLimits()
+{
+	static std::once_flag once;
+	std::call_once(once, [] {
+		int dev = 0, optin = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+		int limit = optin - 4096; // room for the kernel's static shared memory
+		cudaFuncSetAttribute(kBatch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+	});
+}
+
 void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
     unsigned int smem_bytes, unsigned int blocks, int threads, cudaStream_t stream)
 {
+	raiseSmemLimits();
 	MO_CUDA_CHECK(cudaMemsetAsync(d_ticket, 0, sizeof(unsigned int), stream));
 	switch (threads)
 	{
 	case 128:
-		MO_CUDA_CHECK(cudaFuncSetAttribute(kBatch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes)));
 		MO_LAUNCH(kBatch<128>, blocks, 128, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
 		break;
 	case 512:
-		MO_CUDA_CHECK(cudaFuncSetAttribute(kBatch<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes)));
 		MO_LAUNCH(kBatch<512>, blocks, 512, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
 		break;
 	default:
-		MO_CUDA_CHECK(cudaFuncSetAttribute(kBatch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes)));
 		MO_LAUNCH(kBatch<256>, blocks, 256, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
 		break;
 	}
@@ -823,19 +839,17 @@ void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_t
 
 int batchBlocksPerSM(int threads, unsigned int smem_bytes)
 {
+	raiseSmemLimits();
 	int n = 0;
 	switch (threads)
 	{
 	case 128:
-		cudaFuncSetAttribute(kBatch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<128>, 128, smem_bytes);
 		break;
 	case 512:
-		cudaFuncSetAttribute(kBatch<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<512>, 512, smem_bytes);
 		break;
 	default:
-		cudaFuncSetAttribute(kBatch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<256>, 256, smem_bytes);
 		break;
 	}
