@@ -58,6 +58,8 @@ WORKLOADS = {
     "sphere_attr_2m": lambda: W.config_sphere_attr(9),
     "sphere_attr_524k": lambda: W.config_sphere_attr(8),
     "heightfield_256": W.config_heightfield_256,
+    "heightfield_20k": lambda: dict(name="heightfield_101", indices=W.heightfield(101, seed=9)[0], positions=W.heightfield(101, seed=9)[1],
+                                    target=W.target_count(3 * 2 * 100 * 100, 0.3), error=1e-2, options=0),
     "fractal_3163": lambda: W.config_fractal_3163(3163),
     "fractal_1024": lambda: W.config_fractal_3163(1024),
 }
