@@ -215,7 +215,7 @@ def bench_serving(args, mg, torch):
     def run(rate, plain):
         gaps = np.random.default_rng(int(rate) * 7 + (1 if plain else 0)).exponential(1.0 / rate, size=n_req)
         arrivals = np.cumsum(gaps)
-        with mg.Server(memory_budget=40 << 30, plain=plain, large_workers=args.serve_workers) as srv:
+        with mg.Server(memory_budget=40 << 30, plain=plain, large_workers=args.serve_workers, perform_blocks=args.serve_blocks) as srv:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             tickets = []
@@ -254,7 +254,7 @@ def bench_serving(args, mg, torch):
         "steps": n_req, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "serving_poisson", "requests_per_rate": n_req, "pool_meshes": pool_size, "tris": "lognormal median 20k sigma 1 [1k,1M]",
                    "ratio": "U[0.1,0.5]", "target_error": 1e-2, "memory_budget_gb": 40, "request_input_tris": total_tris,
-                   "single_mesh_workers": args.serve_workers},
+                   "single_mesh_workers": args.serve_workers, "pass_kernel_grid_cap": args.serve_blocks or 64},
         "served": served, "plain": plain, "served_equals_plain": bool(same),
     }
     print(json.dumps(line))
@@ -396,6 +396,7 @@ def main():
     ap.add_argument("--rates", default="250,500,1000,2000", help="serving: Poisson arrival rates (requests/s)")
     ap.add_argument("--plain-rates", type=int, default=2, help="serving: how many of the rates also run the plain path")
     ap.add_argument("--serve-workers", type=int, default=16, help="serving: concurrent single-mesh workers")
+    ap.add_argument("--serve-blocks", type=int, default=0, help="serving: pass-kernel grid cap per request (0: server default)")
     args = ap.parse_args()
 
     if args.impl == "reference":

@@ -155,6 +155,8 @@ typedef struct meshoptgpu_ServerConfig
 	int max_batch;            /* requests per batch launch at most (0: 2048) */
 	int batch_threads;        /* threads per CTA of the batch kernel (0: 256) */
 	int plain;                /* 1: no batching, one request at a time on the single-mesh path */
+	int perform_blocks;       /* cap on the cooperative pass kernel's grid per single-mesh request, so
+	                             that concurrent requests share the GPU (0: 64; plain mode: no cap) */
 } meshoptgpu_ServerConfig;
 
 /* Creates a server on the current device. Requests are admitted while their device scratch

@@ -62,7 +62,8 @@ class BatchMesh(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget", C.c_size_t), ("batch_workers", C.c_int), ("large_workers", C.c_int),
-                ("large_index_count", C.c_size_t), ("max_batch", C.c_int), ("batch_threads", C.c_int), ("plain", C.c_int)]
+                ("large_index_count", C.c_size_t), ("max_batch", C.c_int), ("batch_threads", C.c_int), ("plain", C.c_int),
+                ("perform_blocks", C.c_int)]
 
 
 class SimplifyError(RuntimeError):
@@ -321,9 +322,11 @@ class Server:
     without blocking, wait for tickets; latencies are measured natively from submission to
     completion."""
 
-    def __init__(self, memory_budget=0, batch_workers=0, large_workers=0, large_index_count=0, max_batch=0, batch_threads=0, plain=False):
+    def __init__(self, memory_budget=0, batch_workers=0, large_workers=0, large_index_count=0, max_batch=0, batch_threads=0, plain=False,
+                 perform_blocks=0):
         self.lib = load()
-        cfg = ServerConfig(memory_budget, batch_workers, large_workers, large_index_count, max_batch, batch_threads, 1 if plain else 0)
+        cfg = ServerConfig(memory_budget, batch_workers, large_workers, large_index_count, max_batch, batch_threads, 1 if plain else 0,
+                           perform_blocks)
         self.h = self.lib.meshoptgpu_serverCreate(C.byref(cfg))
         if not self.h:
             raise SimplifyError(*last_status())

@@ -520,6 +520,17 @@ void largeWorker(ServerImpl* S)
 {
 	cudaSetDevice(S->device);
 	ThreadState& ts = state();
+	try
+	{
+		ts.ensure();
+		Tuning t = ts.simplifier->tuning();
+		t.perform_grid_cap = S->cfg.perform_blocks;
+		ts.simplifier->setTuning(t);
+	}
+	catch (const std::exception& e)
+	{
+		fprintf(stderr, "meshopt_gb300: server worker setup failed: %s\n", e.what());
+	}
 	for (;;)
 	{
 		ServerRequest* r = nullptr;
@@ -680,6 +691,7 @@ meshoptgpu_Server* meshoptgpu_serverCreate(const meshoptgpu_ServerConfig* config
 		c.large_index_count = c.large_index_count ? c.large_index_count : 600000;
 		c.max_batch = c.max_batch > 0 ? c.max_batch : 2048;
 		c.batch_threads = (c.batch_threads == 128 || c.batch_threads == 256 || c.batch_threads == 512) ? c.batch_threads : 256;
+		c.perform_blocks = c.plain ? 0 : (c.perform_blocks > 0 ? c.perform_blocks : 64);
 		S->cfg = c;
 		MO_CUDA_CHECK(cudaGetDevice(&S->device));
 		MO_CUDA_CHECK(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->device));

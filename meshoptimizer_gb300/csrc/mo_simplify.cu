@@ -863,8 +863,7 @@ struct PerformArgs
 	unsigned long long* minT[2];
 	unsigned long long* minS[2];
 	unsigned char* touched;
-	unsigned int* moved_by;
-	unsigned int* moved_to;
+	unsigned long long* moved; // (sorted index of the commit that moved the vertex << 32) | target; ~0: not moved
 	unsigned int* cr;
 	unsigned int* list[2];
 	// mesh
@@ -899,19 +898,22 @@ struct PerformArgs
 //    commit seen on an endpoint has a smaller sorted index);
 //  * otherwise it waits until it is the earliest undecided candidate on both endpoints (minT)
 //    and no undecided earlier candidate moves a vertex of its one-ring (minS); then the flip
-//    test runs against the one-ring as moved by earlier commits only (moved_by < k).
+//    test runs against the one-ring as moved by earlier commits only (moving commit < k).
 // Returns true if k stays undecided.
-__device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, unsigned int round)
+__device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
 {
-	uint4 rec = __ldg(a.srec + k);
 	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
 	const unsigned long long tag = roundTag(round);
 	const unsigned long long mine = tag | k;
 	const unsigned long long* minT = a.minT[round & 1];
 	const unsigned long long* minS = a.minS[round & 1];
-	// independent loads first: lock flags and endpoint marks
+	// issued together: lock flags, endpoint marks and the first four half-edges of the one-ring
 	unsigned char t0 = __ldcg(a.touched + r0), t1 = __ldcg(a.touched + r1);
 	unsigned long long m0 = __ldcg(minT + r0), m1 = __ldcg(minT + r1);
+	uint2 ed[4];
+#pragma unroll
+	for (int q = 0; q < 4; ++q)
+		ed[q] = b + q < e ? __ldg(a.adj + b + q) : make_uint2(r0, r0);
 	if (t0 | t1)
 	{
 		a.status[k] = kSkipLocked;
@@ -919,13 +921,9 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 	}
 	if (m0 != mine || m1 != mine)
 		return true;
-	// one-ring sources: four half-edges per step so the loads overlap
-	for (unsigned int j = b; j < e; j += 4)
+	// no undecided earlier candidate may move a vertex of the one-ring (its sources)
+	for (unsigned int j = b;;)
 	{
-		uint2 ed[4];
-#pragma unroll
-		for (int q = 0; q < 4; ++q)
-			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
 		unsigned long long sx[4], sy[4];
 #pragma unroll
 		for (int q = 0; q < 4; ++q)
@@ -939,26 +937,30 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 			wait |= earlierThan(sx[q], tag, k) | earlierThan(sy[q], tag, k);
 		if (wait)
 			return true;
+		j += 4;
+		if (j >= e)
+			break;
+#pragma unroll
+		for (int q = 0; q < 4; ++q)
+			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
 	}
+	// flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232)
 	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
 	for (unsigned int j = b; j < e; j += 4)
 	{
-		uint2 ed[4];
-		unsigned int mx[4], my[4];
-#pragma unroll
-		for (int q = 0; q < 4; ++q)
-			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r1, r1);
+		unsigned long long mx[4], my[4];
 #pragma unroll
 		for (int q = 0; q < 4; ++q)
 		{
-			mx[q] = __ldcg(a.moved_by + ed[q].x);
-			my[q] = __ldcg(a.moved_by + ed[q].y);
+			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r1, r1);
+			mx[q] = __ldcg(a.moved + ed[q].x);
+			my[q] = __ldcg(a.moved + ed[q].y);
 		}
 #pragma unroll
 		for (int q = 0; q < 4; ++q)
 		{
-			unsigned int va = mx[q] < k ? __ldcg(a.moved_to + ed[q].x) : ed[q].x;
-			unsigned int vb = my[q] < k ? __ldcg(a.moved_to + ed[q].y) : ed[q].y;
+			unsigned int va = (unsigned int)(mx[q] >> 32) < k ? (unsigned int)mx[q] : ed[q].x;
+			unsigned int vb = (unsigned int)(my[q] >> 32) < k ? (unsigned int)my[q] : ed[q].y;
 			if (va == r1 || vb == r1 || va == vb)
 				continue;
 			if (triFlip(ldpos(a.pos, va), ldpos(a.pos, vb), v0, v1))
@@ -983,17 +985,15 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 	}
 	else
 		target = i1;
-	a.moved_to[r0] = target;
-	a.moved_by[r0] = k;
+	a.moved[r0] = ((unsigned long long)k << 32) | target;
 	a.touched[r0] = 1;
 	a.touched[r1] = 1;
 	a.status[k] = kCommit;
 	return false;
 }
 
-__device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int k, unsigned int round)
+__device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
 {
-	uint4 rec = __ldg(a.srec + k);
 	unsigned long long key = roundTag(round) | k;
 	atomicMin(&a.minT[round & 1][rec.x], key);
 	atomicMin(&a.minT[round & 1][rec.y], key);
@@ -1173,6 +1173,7 @@ struct PhaseClock
 
 __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 {
+	__shared__ unsigned int s_app[33];
 	PhaseClock pc;
 	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
 	if (timer)
@@ -1182,12 +1183,11 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 	const unsigned int G = gridDim.x;
 	const size_t gthreads = (size_t)G * blockDim.x;
 	const unsigned int lane = threadIdx.x & 31;
-	const size_t wbase = (size_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
 
 	for (size_t i = gtid(); i < a.vcount; i += gthreads)
 	{
 		a.touched[i] = 0;
-		a.moved_by[i] = ~0u;
+		a.moved[i] = ~0ull;
 		a.cr[i] = (unsigned int)i;
 	}
 
@@ -1202,7 +1202,10 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		// ---- decision rounds over the window [K0, K1)
 		++windows;
 		for (size_t x = gtid(); x < K1 - K0; x += gthreads)
-			markCandidate(a, K0 + (unsigned int)x, round + 1);
+		{
+			unsigned int k = K0 + (unsigned int)x;
+			markCandidate(a, k, __ldg(a.srec + k), round + 1);
+		}
 		if (gtid() == 0)
 			sc->act_count[(round + 2) % 3] = 0; // appended to by the window's first round
 		gridBarrier(sc->bar, &sc->grid_error);
@@ -1225,29 +1228,40 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 			// barrier that ended round-1
 			if (gtid() == 0)
 				sc->act_count[(round + 2) % 3] = 0;
-			for (size_t base = wbase; base < n; base += gthreads)
+			for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += gthreads)
 			{
-				size_t x = base + lane;
+				size_t x = base + threadIdx.x;
 				bool keep = false;
 				unsigned int k = 0;
 				if (x < n)
 				{
 					k = list ? __ldcg(list + x) : K0 + (unsigned int)x;
-					keep = decideOne(a, k, round);
+					uint4 rec = __ldg(a.srec + k);
+					keep = decideOne(a, k, rec, round);
 					if (keep)
-						markCandidate(a, k, round + 1);
+						markCandidate(a, k, rec, round + 1);
 				}
+				// block-aggregated append: one global atomic per block and iteration
 				unsigned int m = __ballot_sync(0xffffffffu, keep);
-				if (m)
+				unsigned int w = threadIdx.x >> 5;
+				if (lane == 0)
+					s_app[w] = __popc(m);
+				__syncthreads();
+				if (threadIdx.x == 0)
 				{
-					unsigned int leader = __ffs(m) - 1;
-					unsigned int o = 0;
-					if (lane == leader)
-						o = atomicAdd(next_count, __popc(m));
-					o = __shfl_sync(0xffffffffu, o, leader);
-					if (keep)
-						next[o + __popc(m & ((1u << lane) - 1u))] = k;
+					unsigned int run = 0;
+					for (unsigned int q = 0; q < blockDim.x / 32; ++q)
+					{
+						unsigned int c = s_app[q];
+						s_app[q] = run;
+						run += c;
+					}
+					s_app[32] = run ? atomicAdd(next_count, run) : 0u;
 				}
+				__syncthreads();
+				if (keep)
+					next[s_app[32] + s_app[w] + __popc(m & ((1u << lane) - 1u))] = k;
+				__syncthreads();
 			}
 			gridBarrier(sc->bar, &sc->grid_error);
 			if (timer)
@@ -1548,7 +1562,8 @@ struct Work
 	unsigned int *act0, *act1;
 	unsigned long long *minT, *minS;
 	unsigned char* touched;
-	unsigned int *moved_by, *moved_to, *cr;
+	unsigned long long* moved;
+	unsigned int* cr;
 	uint4* blk;
 	unsigned int* blkcnt;
 	unsigned int* scratch;
@@ -1617,8 +1632,7 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 	w.minT = c.take<unsigned long long>(2 * Vp);
 	w.minS = c.take<unsigned long long>(2 * Vp);
 	w.touched = c.take<unsigned char>(Vp);
-	w.moved_by = c.take<unsigned int>(Vp);
-	w.moved_to = c.take<unsigned int>(Vp);
+	w.moved = c.take<unsigned long long>(Vp);
 	w.cr = c.take<unsigned int>(Vp);
 	w.blk = c.take<uint4>(std::max<size_t>(cap / kStopTile + 2, 8192)); // >= blocks of any cooperative launch
 	w.blkcnt = c.take<unsigned int>(T / kThreads + 2);
@@ -1982,8 +1996,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.minS[0] = w.minS;
 			pa.minS[1] = w.minS + (V + 1);
 			pa.touched = w.touched;
-			pa.moved_by = w.moved_by;
-			pa.moved_to = w.moved_to;
+			pa.moved = w.moved;
 			pa.cr = w.cr;
 			pa.list[0] = w.act0;
 			pa.list[1] = w.act1;
@@ -2015,6 +2028,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->result_error_bits, &result_error_bits, 4, cudaMemcpyHostToDevice, stream));
 			unsigned int want = gridFor(std::max(std::max(C, V), T), kThreads);
 			unsigned int blocks = std::max(1u, std::min(perform_blocks_, want));
+			if (tuning_.perform_grid_cap > 0)
+				blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
 			void* params[] = {&pa};
 			cudaEvent_t e0 = probeBegin("kPerform", stream);
 			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, stream));

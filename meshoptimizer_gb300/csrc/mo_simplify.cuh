@@ -103,6 +103,8 @@ struct Tuning
 {
 	int perform_blocks_per_sm = 4;  // resident blocks per SM of the cooperative pass kernel
 	double window_factor = 2.0;     // first decision window = factor * (triangle goal / 2) + 4096
+	int perform_grid_cap = 0;       // at most this many blocks for the pass kernel (0: no cap); lets
+	                                // concurrent simplifications share the GPU
 	static Tuning fromEnvironment();
 };
 
