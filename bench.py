@@ -99,9 +99,10 @@ def cpu_groups(meshes, threads):
     return dt, out
 
 
-def bench_groups(args, mg, torch):
-    """Cluster groups: batched (one persistent launch) vs plain (one drop-in call per group)."""
-    meshes = load_groups()
+def bench_groups(args, mg, torch, seed_offset=0):
+    """Cluster groups: batched (one persistent launch) vs plain (one drop-in call per group).
+    Each rank simplifies its own 4096 groups (seed + rank): replicas, weak scaling."""
+    meshes = load_groups(seed=3 + seed_offset)
     tris = sum(len(m["indices"]) // 3 for m in meshes)
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
@@ -181,7 +182,7 @@ def bench_groups(args, mg, torch):
                       "calls": len(meshes)},
         "cpu_baseline": cpu, "bit_exact_vs_plain_and_oracle": bool(exact), "clocks": clocks.summary(), "gpu_launches": int(launches),
     }
-    print(json.dumps(line))
+    return line
 
 
 def bench_serving(args, mg, torch):
@@ -257,7 +258,7 @@ def bench_serving(args, mg, torch):
                    "single_mesh_workers": args.serve_workers, "pass_kernel_grid_cap": args.serve_blocks or 64},
         "served": served, "plain": plain, "served_equals_plain": bool(same),
     }
-    print(json.dumps(line))
+    return line
 
 
 def load_workload(name):
@@ -392,6 +393,7 @@ def main():
     ap.add_argument("--kernel", default="kPerform", help="kernel whose CUDA-event time gives the roofline line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched-groups and serving summaries of the default line")
     ap.add_argument("--requests", type=int, default=10000, help="serving: requests per arrival rate")
     ap.add_argument("--rates", default="250,500,1000,2000", help="serving: Poisson arrival rates (requests/s)")
     ap.add_argument("--plain-rates", type=int, default=2, help="serving: how many of the rates also run the plain path")
@@ -421,10 +423,10 @@ def main():
     mgbuild.build()
     mg.load()
     if args.workload == "groups_4096":
-        bench_groups(args, mg, torch)
+        print(json.dumps(bench_groups(args, mg, torch, seed_offset=rank)))
         return
     if args.workload == "serving":
-        bench_serving(args, mg, torch)
+        print(json.dumps(bench_serving(args, mg, torch)))
         return
     c = load_workload(args.workload)
     dev = torch.device("cuda", local)
@@ -465,11 +467,11 @@ def main():
     k_launches, k_ms = mg.kernel_profile()
     mg.set_kernel_profile(None)
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * c["tris"] * args.steps / (total_ms / 1e3) / 1e6
+    from meshoptimizer_gb300 import replicas
+
+    rate, secs, _ = replicas.aggregate(total_ms / 1e3, float(c["tris"] * args.steps), dist=dist, device=dev)
+    total_ms = secs * 1e3
+    value = rate / 1e6
     gpu_out = out[:n_out].cpu().numpy().view(np.uint32)
 
     # per-pass and per-phase view of one more run (not timed for the value)
@@ -555,6 +557,13 @@ def main():
         "phases_ms": {k: round(v, 3) for k, v in phases.items()},
         "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active", "windows")} for p in passes],
     }
+    if not args.no_extras and world == 1:
+        g = bench_groups(argparse.Namespace(steps=3, warmup=3, no_cpu_baseline=args.no_cpu_baseline), mg, torch)
+        line["batched_groups"] = {k: g[k] for k in ("value", "unit", "ms_per_step", "e2e", "plain_gpu", "cpu_baseline",
+                                                   "bit_exact_vs_plain_and_oracle")}
+        line["batched_groups"]["config"] = g["config"]
+        sv = bench_serving(argparse.Namespace(requests=2000, rates="500,1000", plain_rates=1, serve_workers=16, serve_blocks=0), mg, torch)
+        line["serving"] = {k: sv[k] for k in ("served", "plain", "served_equals_plain", "config")}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
