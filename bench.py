@@ -539,9 +539,17 @@ def main():
 
     cpu = None
     bit_exact = None
+    fp64 = None
     if not args.no_cpu_baseline:
         mt, runs, secs, ref_out, ref_err = cpu_baseline(c)
         bit_exact = bool(np.array_equal(ref_out, gpu_out)) and abs(ref_err - err) <= 1e-6 * max(abs(ref_err), 1e-30)
+        import oracle
+
+        # the FP32 path's result error stated against the FP64 oracle (same driver in double)
+        out64, err64, _ = oracle.simplify("port", c["indices"], c["positions"], c["target"], c["error"], c["options"],
+                                          attributes=c.get("attributes"), weights=c.get("weights"), fp64=True)
+        fp64 = {"fp32_result_error": err, "fp64_result_error": err64, "relative_difference": abs(err - err64) / err64 if err64 else 0.0,
+                "fp64_output_tris": len(out64) // 3}
         cpu = {"value": round(mt, 4), "unit": "Mtris/s", "cores": 1, "kind": "port",
                "sample": f"{runs} full simplification(s) of {c['name']} in {secs:.1f} s, single thread (the simplifier has no threading)"}
 
@@ -552,7 +560,7 @@ def main():
         "config": {"workload": c["name"], "input_tris": c["tris"], "output_tris": int(n_out) // 3, "target_index_count": c["target"],
                    "target_error": c["error"], "options": c["options"], "attributes": ac, "result_error": err,
                    "l2": "flushed between steps (512 MiB write, outside the timed events)", "parallelism": f"replicas{world}"},
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact,
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact, "error_vs_fp64_oracle": fp64,
         "clocks": clocks.summary(), "gpu_launches": int(launches),
         "phases_ms": {k: round(v, 3) for k, v in phases.items()},
         "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active", "windows")} for p in passes],
