@@ -137,7 +137,9 @@ void setStatus(int status, const std::string& msg)
 		fprintf(stderr, "meshopt_gb300: %s\n", msg.c_str());
 }
 
-const unsigned int kSupportedOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight;
+const unsigned int kSupportedOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight | kOptSparse | kOptPermissive;
+// the one-CTA-per-mesh batch kernel implements the positions-only subset
+const unsigned int kBatchOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight;
 
 // argument checks of meshopt_simplifyEdge (:2348-2357); returns an error message or empty
 std::string checkArgs(size_t index_count, size_t vertex_positions_stride, size_t target_index_count, float target_error,
@@ -369,7 +371,7 @@ std::string checkBatchMesh(const meshoptgpu_BatchMesh& m)
 		return "target_index_count must not exceed index_count";
 	if (!(m.target_error >= 0))
 		return "target_error must be >= 0";
-	if (m.options & ~kSupportedOptions)
+	if (m.options & ~kBatchOptions)
 		return "batched meshes support LockBorder, ErrorAbsolute, Regularize and RegularizeLight only";
 	if (m.index_count >= (size_t(1) << 32) || m.vertex_count >= (size_t(1) << 32))
 		return "batched meshes must have fewer than 2^32 indices and vertices";
@@ -589,7 +591,7 @@ int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, size_t mesh_cou
 		std::string bad = checkBatchMesh(meshes[i]);
 		if (!bad.empty())
 		{
-			int st = (meshes[i].options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+			int st = (meshes[i].options & ~kBatchOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
 			setStatus(st, "mesh " + std::to_string(i) + ": " + bad);
 			return st;
 		}
@@ -623,7 +625,7 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		std::string bad = checkBatchMesh(meshes[i]);
 		if (!bad.empty())
 		{
-			int st = (meshes[i].options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+			int st = (meshes[i].options & ~kBatchOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
 			setStatus(st, "mesh " + std::to_string(i) + ": " + bad);
 			return st;
 		}
@@ -735,7 +737,7 @@ long long meshoptgpu_serverSubmit(meshoptgpu_Server* server, const meshoptgpu_Ba
 	std::string bad = checkBatchMesh(*mesh);
 	if (!bad.empty())
 	{
-		int st = (mesh->options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+		int st = (mesh->options & ~kBatchOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
 		setStatus(st, bad);
 		return -st;
 	}

@@ -448,6 +448,126 @@ __global__ void kLockBorder(size_t n, unsigned char* kind)
 		kind[i] = kLocked;
 }
 
+// Permissive mode (classifyVertices :481-515): a seam or locked primary becomes Complex unless
+// one of its wedges is protected by vertex_lock or has a half-edge without an opposite edge in
+// position space (hasEdge with remap/wedge, :345-362). `off/csr` is the raw corner list.
+__device__ bool hasEdgeWedged(unsigned int a, unsigned int b, const unsigned int* __restrict__ idx, const unsigned int* __restrict__ off,
+    const unsigned int* __restrict__ csr, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge)
+{
+	unsigned int rb = remap[b];
+	unsigned int v = a;
+	do
+	{
+		for (unsigned int j = off[v]; j < off[v + 1]; ++j)
+		{
+			unsigned int nx, pv;
+			cornerNeighbours(idx, csr[j], nx, pv);
+			if (remap[nx] == rb)
+				return true;
+		}
+		v = wedge[v];
+	} while (v != a);
+	return false;
+}
+
+__global__ void kPermissivePrimary(size_t n, const unsigned int* __restrict__ idx, const unsigned int* __restrict__ off, const unsigned int* __restrict__ csr,
+    const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge, const unsigned char* __restrict__ lock, const unsigned char* __restrict__ kind,
+    unsigned char* __restrict__ newkind)
+{
+	size_t vi = gtid();
+	if (vi >= n)
+		return;
+	unsigned int i = (unsigned int)vi;
+	unsigned char k = kind[i];
+	newkind[i] = k;
+	if (remap[i] != i || (k != kSeam && k != kLocked))
+		return;
+	bool protect = false;
+	unsigned int v = i;
+	do
+	{
+		protect |= lock && (lock[v] & kVertexProtect) != 0;
+		v = wedge[v];
+	} while (v != i);
+	do
+	{
+		for (unsigned int j = off[v]; j < off[v + 1] && !protect; ++j)
+		{
+			unsigned int nx, pv;
+			cornerNeighbours(idx, csr[j], nx, pv);
+			protect |= !hasEdgeWedged(nx, v, idx, off, csr, remap, wedge);
+		}
+		v = wedge[v];
+	} while (v != i);
+	newkind[i] = protect ? k : (unsigned char)kComplex;
+}
+
+__global__ void kPermissiveWedges(size_t n, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ newkind, unsigned char* kind)
+{
+	size_t i = gtid();
+	if (i >= n)
+		return;
+	unsigned char k = kind[i];
+	kind[i] = (k == kSeam || k == kLocked) ? newkind[remap[i]] : k;
+}
+
+// ---------------------------------------------------------------- setup: sparse subset (buildSparseRemap :242-294)
+
+__global__ void kFirstUse(const unsigned int* __restrict__ idx, size_t n, unsigned int* first)
+{
+	size_t p = gtid();
+	if (p < n)
+		atomicMin(&first[idx[p]], (unsigned int)p);
+}
+
+__global__ void kFirstFlags(const unsigned int* __restrict__ idx, size_t n, const unsigned int* __restrict__ first, unsigned int* __restrict__ flags)
+{
+	size_t p = gtid();
+	if (p < n)
+		flags[p] = first[idx[p]] == (unsigned int)p;
+}
+
+// dense id of a vertex = rank of its first use among all first uses (order of first appearance)
+__global__ void kSparseIds(const unsigned int* __restrict__ idx, size_t n, const unsigned int* __restrict__ first, const unsigned int* __restrict__ rank,
+    unsigned int* __restrict__ dense_idx, unsigned int* __restrict__ sparse_remap)
+{
+	size_t p = gtid();
+	if (p >= n)
+		return;
+	unsigned int v = idx[p];
+	unsigned int f = first[v];
+	unsigned int d = rank[f];
+	dense_idx[p] = d;
+	if (f == (unsigned int)p)
+		sparse_remap[d] = v;
+}
+
+__global__ void kSparseGather(const unsigned int* __restrict__ sparse_remap, size_t u, const float* __restrict__ pos, size_t pstride_f,
+    const float* __restrict__ attr, size_t astride_f, size_t acount, const unsigned char* __restrict__ lock, float* __restrict__ pos_out,
+    float* __restrict__ attr_out, unsigned char* __restrict__ lock_out)
+{
+	size_t d = gtid();
+	if (d >= u)
+		return;
+	unsigned int v = sparse_remap[d];
+	const float* p = pos + (size_t)v * pstride_f;
+	pos_out[d * 3 + 0] = p[0];
+	pos_out[d * 3 + 1] = p[1];
+	pos_out[d * 3 + 2] = p[2];
+	if (attr)
+		for (size_t k = 0; k < acount; ++k)
+			attr_out[d * acount + k] = attr[(size_t)v * astride_f + k];
+	if (lock)
+		lock_out[d] = lock[v];
+}
+
+__global__ void kSparseOut(const unsigned int* __restrict__ in, size_t n, const unsigned int* __restrict__ sparse_remap, unsigned int* __restrict__ out)
+{
+	size_t p = gtid();
+	if (p < n)
+		out[p] = sparse_remap[in[p]];
+}
+
 // ---------------------------------------------------------------- setup: quadrics
 
 // Per primary vertex r, in the order the reference accumulates into vertex_quadrics[r]:
@@ -1715,6 +1835,76 @@ size_t Simplifier::workspaceBytes(size_t index_count, size_t vertex_count, size_
 	return layout(w, nullptr, index_count, vertex_count, attribute_count);
 }
 
+// Sparse subset (meshopt_SimplifySparse): the indices are rewritten to dense ids in order of
+// first appearance, the used vertices are gathered into a compact mesh, the compact mesh is
+// simplified, and the result is mapped back to the original vertex ids (:2367-2369, :2616-2619).
+RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStream_t stream, PhaseTimes* times, SetupDump* dump)
+{
+	const size_t I = m.index_count, V = m.vertex_count;
+	const size_t ac = m.attribute_count; // every attribute column is gathered; zero weights are dropped later
+	// layout of the compact mesh in its own arena (the inner run uses the main one)
+	auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+	size_t b_first = al((V + 1) * 4), b_flags = al((I + 1) * 4), b_rank = al((I + 1) * 4), b_dense = al((I + 1) * 4), b_map = al((I + 1) * 4);
+	size_t b_pos = al((I + 1) * 12), b_attr = al((I + 1) * 4 * (ac ? ac : 1)), b_lock = al(I + 1), b_res = al((I + 1) * 4), b_scan = al(scanScratchWords(I + 2) * 4);
+	size_t b_sc = 256;
+	sparse_arena_.reserve(b_first + b_flags + b_rank + b_dense + b_map + b_pos + b_attr + b_lock + b_res + b_scan + b_sc);
+	char* base = sparse_arena_.base();
+	unsigned int* first = reinterpret_cast<unsigned int*>(base);
+	unsigned int* flags = reinterpret_cast<unsigned int*>(base += b_first);
+	unsigned int* rank = reinterpret_cast<unsigned int*>(base += b_flags);
+	unsigned int* dense = reinterpret_cast<unsigned int*>(base += b_rank);
+	unsigned int* smap = reinterpret_cast<unsigned int*>(base += b_dense);
+	float* cpos = reinterpret_cast<float*>(base += b_map);
+	float* cattr = reinterpret_cast<float*>(base += b_pos);
+	unsigned char* clock = reinterpret_cast<unsigned char*>(base += b_attr);
+	unsigned int* cres = reinterpret_cast<unsigned int*>(base += b_lock);
+	unsigned int* scratch = reinterpret_cast<unsigned int*>(base += b_res);
+	unsigned int* total = reinterpret_cast<unsigned int*>(base += b_scan);
+
+	MO_CUDA_CHECK(cudaMemsetAsync(total, 0, 8, stream));
+	if (I)
+		MO_LAUNCH(kValidateIndices, gridFor(I, kThreads), kThreads, 0, stream, m.indices, I, V, total + 1);
+	unsigned int hv[2] = {0, 0};
+	MO_CUDA_CHECK(cudaMemcpyAsync(pinned_, total, 8, cudaMemcpyDeviceToHost, stream));
+	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
+	memcpy(hv, pinned_, 8);
+	if (hv[1])
+		throw std::invalid_argument("index out of range of vertex_count");
+
+	MO_CUDA_CHECK(cudaMemsetAsync(first, 0xFF, (V + 1) * 4, stream));
+	if (I)
+	{
+		const unsigned int gI = gridFor(I, kThreads);
+		MO_LAUNCH(kFirstUse, gI, kThreads, 0, stream, m.indices, I, first);
+		MO_LAUNCH(kFirstFlags, gI, kThreads, 0, stream, m.indices, I, first, flags);
+		scanExclusive(flags, rank, I, total, scratch, stream);
+		MO_LAUNCH(kSparseIds, gI, kThreads, 0, stream, m.indices, I, first, rank, dense, smap);
+	}
+	else
+		MO_CUDA_CHECK(cudaMemsetAsync(total, 0, 4, stream));
+	MO_CUDA_CHECK(cudaMemcpyAsync(pinned_, total, 4, cudaMemcpyDeviceToHost, stream));
+	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
+	const size_t U = pinned_[0];
+	if (U)
+		MO_LAUNCH(kSparseGather, gridFor(U, kThreads), kThreads, 0, stream, smap, U, m.positions, m.positions_stride / 4, ac ? m.attributes : nullptr,
+		    m.attributes_stride / 4, ac, m.lock, cpos, cattr, m.lock ? clock : nullptr);
+
+	MeshDesc cm = m;
+	cm.indices = dense;
+	cm.vertex_count = U;
+	cm.positions = cpos;
+	cm.positions_stride = 12;
+	cm.attributes = ac ? cattr : nullptr;
+	cm.attributes_stride = ac * 4;
+	cm.lock = m.lock ? clock : nullptr;
+	cm.options = m.options & ~kOptSparse;
+	RunResult rr = run(cm, cres, stream, times, dump);
+	if (rr.index_count)
+		MO_LAUNCH(kSparseOut, gridFor(rr.index_count, kThreads), kThreads, 0, stream, cres, rr.index_count, smap, d_out);
+	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
+	return rr;
+}
+
 float Simplifier::scale(const float* d_positions, size_t vertex_count, size_t stride, cudaStream_t stream)
 {
 	MO_CUDA_CHECK(cudaSetDevice(device_));
@@ -1740,6 +1930,8 @@ float Simplifier::scale(const float* d_positions, size_t vertex_count, size_t st
 RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t stream, PhaseTimes* times, SetupDump* dump)
 {
 	MO_CUDA_CHECK(cudaSetDevice(device_));
+	if (m.options & kOptSparse)
+		return runSparse(m, d_out, stream, times, dump);
 	RunResult rr;
 	const size_t I = m.index_count, V = m.vertex_count;
 
@@ -1843,6 +2035,11 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	{
 		MO_LAUNCH(kOpenEdges, gV, kThreads, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.loop, w.loopback);
 		MO_LAUNCH(kClassify, gV, kThreads, 0, stream, V, w.remap, w.wedge, w.loop, w.loopback, w.kind);
+		if (m.options & kOptPermissive)
+		{
+			MO_LAUNCH(kPermissivePrimary, gV, kThreads, 0, stream, V, w.res0, w.off_raw, w.csr_raw, w.remap, w.wedge, m.lock, w.kind, w.touched);
+			MO_LAUNCH(kPermissiveWedges, gV, kThreads, 0, stream, V, w.remap, w.touched, w.kind);
+		}
 		if (m.lock)
 		{
 			MO_LAUNCH(kLockMark, gV, kThreads, 0, stream, V, m.lock, w.remap, w.kind);

@@ -128,8 +128,11 @@ public:
 	static size_t workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count);
 
 private:
+	RunResult runSparse(const MeshDesc& mesh, unsigned int* d_out, cudaStream_t stream, PhaseTimes* times, SetupDump* dump);
+
 	int device_;
 	DeviceArena arena_;
+	DeviceArena sparse_arena_; // compact copy of a sparse subset
 	unsigned int* pinned_ = nullptr; // small pinned readback buffer
 	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative pass kernel (occupancy)
 	unsigned int perform_blocks_ = 1;

@@ -15,7 +15,8 @@ from meshoptimizer_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 REL_TOL = 1e-6
-GPU_OPTIONS = mg.SimplifyLockBorder | mg.SimplifyErrorAbsolute | mg.SimplifyRegularize | mg.SimplifyRegularizeLight
+GPU_OPTIONS = (mg.SimplifyLockBorder | mg.SimplifyErrorAbsolute | mg.SimplifyRegularize | mg.SimplifyRegularizeLight | mg.SimplifySparse
+               | mg.SimplifyPermissive)
 
 
 def close(a, b):
@@ -175,8 +176,38 @@ def test_scale():
     assert mg.simplify_scale(vb) == 3.0
 
 
+@pytest.mark.parametrize("seed", range(16))
+def test_permissive_and_sparse(port, seed):
+    """Permissive (complex collapses across attribute seams, Protect flags) and Sparse subsets."""
+    rng = np.random.default_rng(100 + seed)
+    if seed % 2:
+        idx, pos, attr, w = W.octa_sphere(3, seed=seed)
+        V = len(pos)
+        opt = mg.SimplifyPermissive | (mg.SimplifySparse if seed % 4 == 1 else 0)
+        lock = rng.choice([0, 0, 0, 2, 1, 4], size=V).astype(np.uint8) if seed % 3 == 0 else None
+        if opt & mg.SimplifySparse:
+            tri = idx.reshape(-1, 3)
+            idx = tri[rng.random(len(tri)) < 0.5].reshape(-1).astype(np.uint32)
+        _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.2), 5e-2, opt, attributes=attr, weights=w, lock=lock)
+    else:
+        pos = rng.integers(0, 10, size=(120, 3)).astype(np.float32)
+        idx = rng.integers(0, 100, size=3 * int(rng.integers(5, 150))).astype(np.uint32)
+        opt = [mg.SimplifySparse, mg.SimplifyPermissive, mg.SimplifySparse | mg.SimplifyLockBorder,
+               mg.SimplifyPermissive | mg.SimplifyErrorAbsolute][(seed // 2) % 4]
+        attrs = rng.random((120, 2)).astype(np.float32) if seed % 4 == 0 else None
+        weights = np.array([1.0, 0.5], np.float32) if attrs is not None else None
+        _compare_with_oracle(port, idx, pos, 0, float(np.finfo(np.float32).max), opt, attributes=attrs, weights=weights)
+
+
+def test_sparse_subset_of_large_buffer(port):
+    """A cluster-sized subset of a big vertex buffer: work and error relative to the subset."""
+    idx, pos = W.heightfield(200, seed=12, amp=0.05)
+    tri = idx.reshape(-1, 3)[5000:5600].reshape(-1).astype(np.uint32)
+    _compare_with_oracle(port, tri, pos, W.target_count(len(tri), 0.5), 1e-2, mg.SimplifySparse | mg.SimplifyLockBorder)
+
+
 def test_unsupported_option_reports_status():
     idx, pos = W.heightfield(8, seed=1)
-    out, err = mg.simplify(idx, pos, 0, 1e-2, mg.SimplifyPermissive, check=False)
+    out, err = mg.simplify(idx, pos, 0, 1e-2, mg.SimplifyPrune, check=False)
     st, msg = mg.last_status()
     assert st == mg.STATUS_UNSUPPORTED and np.array_equal(out, idx)
