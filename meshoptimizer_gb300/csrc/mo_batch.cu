@@ -49,6 +49,12 @@ struct CtaWork
 	unsigned int* order;    // cap
 	unsigned int* hist;     // 2560
 	unsigned int* red;      // 64 words of block-reduction scratch
+	unsigned long long* minT;  // V: round-tagged earliest undecided candidate touching the vertex
+	unsigned long long* minS;  // V: ... whose source is the vertex
+	unsigned long long* moved; // V: (sorted index of the moving commit << 32) | target, ~0: not moved
+	unsigned char* status;     // cap: decision per sorted position
+	unsigned int* list0;       // cap: undecided candidates of the round
+	unsigned int* list1;       // cap
 };
 
 __host__ __device__ inline size_t alignUp(size_t v, size_t a)
@@ -99,6 +105,12 @@ __host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t
 	w.order = reinterpret_cast<unsigned int*>(take(cap * 4));
 	w.hist = reinterpret_cast<unsigned int*>(take(kSortBinsC * 4));
 	w.red = reinterpret_cast<unsigned int*>(take(64 * 4));
+	w.minT = reinterpret_cast<unsigned long long*>(take(V * 8));
+	w.minS = reinterpret_cast<unsigned long long*>(take(V * 8));
+	w.moved = reinterpret_cast<unsigned long long*>(take(V * 8));
+	w.status = reinterpret_cast<unsigned char*>(take(cap));
+	w.list0 = reinterpret_cast<unsigned int*>(take(cap * 4));
+	w.list1 = reinterpret_cast<unsigned int*>(take(cap * 4));
 	return off > after_table ? off : after_table;
 }
 
@@ -171,10 +183,13 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
 	__shared__ unsigned int s_flag;
 	__shared__ float s_mm[NT / 32][6];
 	__shared__ float s_minv[3], s_scale, s_extent;
-	__shared__ unsigned int s_cap, s_count, s_trunc, s_done, s_errbits;
+	__shared__ unsigned int s_cap, s_count, s_trunc, s_done, s_errbits, s_next, s_stall;
+	__shared__ unsigned long long s_cut;
+	__shared__ unsigned int s_carry[3];
+	__shared__ unsigned int s_maxes[NT];
 
 	if (tid == 0)
-		s_flag = 0;
+		s_flag = 0, s_stall = 0;
 	__syncthreads();
 	for (unsigned int i = tid; i < I; i += NT)
 	{
@@ -503,6 +518,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
 	unsigned int result_count = I;
 	float result_error = 0.f;
 	unsigned int passes = 0;
+	unsigned int round = 0; // decision rounds are numbered across passes, so mark tags never repeat
 
 	while (result_count > d.target_index_count)
 	{
@@ -630,77 +646,255 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
 			w.cr[i] = i, w.locked[i] = 0;
 		__syncthreads();
 
-		// perform (performEdgeCollapses :1498-1636) on warp 0, serial order, lanes split the flip test
+		// perform (performEdgeCollapses :1498-1636) in block-level decision rounds: a candidate is
+		// decided once nothing earlier in sorted order can change its outcome (the rule of the
+		// multi-CTA path's kPerform), over a window of sorted order that grows until the stop
+		// rules fire; the stop rules are a prefix scan of the decisions
 		const unsigned int goal = (result_count - d.target_index_count) / 3;
-		if (tid < 32)
+		for (unsigned int i = tid; i < V; i += NT)
+			w.locked[i] = 0, w.moved[i] = ~0ull, w.minT[i] = ~0ull, w.minS[i] = ~0ull;
+		for (unsigned int k = tid; k < C; k += NT)
+			w.status[k] = kUndecided;
+		if (tid == 0)
+			s_cut = ~0ull, s_carry[0] = 0, s_carry[1] = 0, s_carry[2] = __float_as_uint(result_error);
+		__syncthreads();
 		{
-			const unsigned int lane = tid;
-			unsigned int edge_collapses = 0, triangle_collapses = 0, edge_goal = goal / 2;
-			for (unsigned int i = 0; i < C; ++i)
+			unsigned int K0 = 0, K1 = (unsigned int)min((unsigned long long)C, 2ull * (goal / 2) + 64ull);
+			for (;;)
 			{
-				unsigned int c = w.order[i];
-				float err = __uint_as_float(w.cerr[c]);
-				if (err > error_limit)
-					break;
-				if (triangle_collapses >= goal)
-					break;
-				float error_goal = edge_goal < C ? 1.5f * __uint_as_float(w.cerr[w.order[edge_goal]]) : FLT_MAX;
-				if (err > error_goal && err > result_error && triangle_collapses > goal / 6)
-					break;
-				unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
-				unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
-				unsigned char kd = w.kind[i0];
-				if (w.locked[r0] | w.locked[r1])
-					continue;
-				// flip test, lanes over r0's one-ring
-				unsigned int b = w.adj_off[r0], e = w.adj_off[r0 + 1];
-				float4 a0 = w.pos[r0], a1 = w.pos[r1];
-				V3 v0{a0.x, a0.y, a0.z}, v1{a1.x, a1.y, a1.z};
-				bool flip = false;
-				for (unsigned int j = b + lane; j < e; j += 32)
+				// rounds over [K0, K1)
+				unsigned int n = K1 - K0;
+				bool first = true;
+				unsigned int* cur = w.list0;
+				unsigned int* nxt = w.list1;
+				while (n)
 				{
-					uint2 ed = w.adj[j];
-					unsigned int va = w.cr[ed.x], vb = w.cr[ed.y];
-					if (va == r1 || vb == r1 || va == vb)
-						continue;
-					float4 pa = w.pos[va], pb = w.pos[vb];
-					flip |= triFlip(V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, v0, v1);
-				}
-				if (__any_sync(0xffffffffu, flip))
-				{
-					edge_goal++;
-					continue;
-				}
-				if (lane == 0)
-				{
-					if (kd == kSeam)
+					++round;
+					const unsigned long long tag = (unsigned long long)(0xFFFFFFFFu - round) << 32;
+					for (unsigned int x = tid; x < n; x += NT)
 					{
-						unsigned int s0 = w.wedge[i0];
-						unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
-						s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
-						w.cr[i0] = i1;
-						w.cr[s0] = s1;
+						unsigned int k = first ? K0 + x : cur[x];
+						unsigned int c = w.order[k];
+						unsigned int r0 = w.remap[w.cv0[c]], r1 = w.remap[w.cv1[c]];
+						atomicMin(&w.minT[r0], tag | k);
+						atomicMin(&w.minT[r1], tag | k);
+						atomicMin(&w.minS[r0], tag | k);
 					}
-					else
-						w.cr[i0] = i1;
-					w.locked[r0] = 1;
-					w.locked[r1] = 1;
+					if (tid == 0)
+						s_next = 0;
+					__syncthreads();
+					for (unsigned int base = 0; base < n; base += NT)
+					{
+						unsigned int x = base + tid;
+						bool keep = false;
+						unsigned int k = 0;
+						if (x < n)
+						{
+							k = first ? K0 + x : cur[x];
+							unsigned int c = w.order[k];
+							unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+							unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
+							const unsigned long long mine = tag | k;
+							if (w.locked[r0] | w.locked[r1])
+								w.status[k] = kSkipLocked;
+							else if (w.minT[r0] != mine || w.minT[r1] != mine)
+								keep = true;
+							else
+							{
+								unsigned int b = w.adj_off[r0], e = w.adj_off[r0 + 1];
+								for (unsigned int j = b; j < e && !keep; ++j)
+								{
+									uint2 ed = w.adj[j];
+									unsigned long long sx = w.minS[ed.x], sy = w.minS[ed.y];
+									keep = ((sx >> 32) == (tag >> 32) && (unsigned int)sx < k) || ((sy >> 32) == (tag >> 32) && (unsigned int)sy < k);
+								}
+								if (!keep)
+								{
+									float4 a0 = w.pos[r0], a1 = w.pos[r1];
+									V3 v0{a0.x, a0.y, a0.z}, v1{a1.x, a1.y, a1.z};
+									bool flip = false;
+									for (unsigned int j = b; j < e && !flip; ++j)
+									{
+										uint2 ed = w.adj[j];
+										unsigned long long mx = w.moved[ed.x], my = w.moved[ed.y];
+										unsigned int va = (unsigned int)(mx >> 32) < k ? (unsigned int)mx : ed.x;
+										unsigned int vb = (unsigned int)(my >> 32) < k ? (unsigned int)my : ed.y;
+										if (va == r1 || vb == r1 || va == vb)
+											continue;
+										float4 pa = w.pos[va], pb = w.pos[vb];
+										flip = triFlip(V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, v0, v1);
+									}
+									if (flip)
+										w.status[k] = kSkipFlip;
+									else
+									{
+										unsigned int target = i1;
+										if (w.kind[i0] == kSeam)
+										{
+											unsigned int s0 = w.wedge[i0];
+											unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+											s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+											target = (s0 == r0) ? s1 : i1;
+										}
+										w.moved[r0] = ((unsigned long long)k << 32) | target;
+										w.locked[r0] = 1;
+										w.locked[r1] = 1;
+										w.status[k] = kCommit;
+									}
+								}
+							}
+						}
+						unsigned int m = __ballot_sync(0xffffffffu, keep);
+						if (keep)
+						{
+							unsigned int lane = tid & 31;
+							unsigned int leader = __ffs(m) - 1;
+							unsigned int o = 0;
+							if (lane == leader)
+								o = atomicAdd(&s_next, __popc(m));
+							o = __shfl_sync(m, o, leader);
+							nxt[o + __popc(m & ((1u << lane) - 1u))] = k;
+						}
+					}
+					__syncthreads();
+					unsigned int nn = s_next;
+					__syncthreads();
+					if (nn >= n)
+					{
+						if (tid == 0)
+							s_stall = 1;
+						break;
+					}
+					n = nn;
+					first = false;
+					unsigned int* t = cur;
+					cur = nxt;
+					nxt = t;
 				}
-				__syncwarp();
-				triangle_collapses += (kd == kBorder) ? 1 : 2;
-				edge_collapses++;
-				result_error = result_error < err ? err : result_error;
+				// stop rules over [K0, K1): contiguous thread chunks, block scan, carried prefix
+				const unsigned int len = K1 - K0, per = (len + NT - 1) / NT;
+				const unsigned int t0 = min(K1, K0 + tid * per), t1 = min(K1, t0 + per);
+				unsigned int sT = 0, sF = 0, sM = 0;
+				for (unsigned int k = t0; k < t1; ++k)
+				{
+					unsigned char st = w.status[k];
+					unsigned int c = w.order[k];
+					float e = __uint_as_float(w.cerr[c]);
+					if (st == kCommit)
+					{
+						sT += w.kind[w.cv0[c]] == kBorder ? 1u : 2u;
+						if (e == e)
+							sM = max(sM, w.cerr[c]);
+					}
+					sF += st == kSkipFlip;
+				}
+				unsigned int eT, eF;
+				{
+					unsigned int tot;
+					eT = blockExclusiveScan<NT>(sT, w.red, &tot);
+					__syncthreads();
+					eF = blockExclusiveScan<NT>(sF, w.red, &tot);
+					__syncthreads();
+				}
+				// exclusive max over the threads before this one (in thread order)
+				s_maxes[tid] = sM;
+				__syncthreads();
+				unsigned int eM = 0;
+				for (unsigned int q = 0; q < tid; ++q)
+					eM = max(eM, s_maxes[q]);
+				unsigned long long T = (unsigned long long)s_carry[0] + eT, F = (unsigned long long)s_carry[1] + eF;
+				unsigned int M = max(s_carry[2], eM);
+				for (unsigned int k = t0; k < t1; ++k)
+				{
+					unsigned int c = w.order[k];
+					float e = __uint_as_float(w.cerr[c]);
+					unsigned int reason = 0;
+					if (e > error_limit)
+						reason = 1;
+					else if (T >= goal)
+						reason = 2;
+					else
+					{
+						unsigned long long eg = goal / 2 + F;
+						float error_goal = eg < C ? 1.5f * __uint_as_float(w.cerr[w.order[eg]]) : FLT_MAX;
+						if (e > error_goal && e > __uint_as_float(M) && T > goal / 6)
+							reason = 3;
+					}
+					if (reason)
+					{
+						atomicMin(&s_cut, ((unsigned long long)k << 2) | reason);
+						break;
+					}
+					unsigned char st = w.status[k];
+					if (st == kCommit)
+					{
+						T += w.kind[w.cv0[c]] == kBorder ? 1u : 2u;
+						if (e == e)
+							M = max(M, w.cerr[c]);
+					}
+					F += st == kSkipFlip;
+				}
+				__syncthreads();
+				if (s_cut != ~0ull || K1 == C || s_stall)
+					break;
+				// carry the prefix over the window into the next one
+				if (tid == NT - 1)
+				{
+					s_carry[0] = (unsigned int)T;
+					s_carry[1] = (unsigned int)F;
+					s_carry[2] = M;
+				}
+				__syncthreads();
+				K0 = K1;
+				K1 = (unsigned int)min((unsigned long long)C, 2ull * K1);
 			}
-			if (lane == 0)
+		}
+		// apply the committed prefix: collapse_remap writes, done count, result error
+		{
+			const unsigned int cut = s_cut == ~0ull ? C : (unsigned int)(s_cut >> 2);
+			for (unsigned int i = tid; i < V; i += NT)
+				w.cr[i] = i;
+			__syncthreads();
+			unsigned int done = 0, em = 0;
+			for (unsigned int k = tid; k < cut; k += NT)
 			{
-				s_done = edge_collapses;
-				s_errbits = __float_as_uint(result_error);
+				if (w.status[k] != kCommit)
+					continue;
+				unsigned int c = w.order[k];
+				unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+				if (w.kind[i0] == kSeam)
+				{
+					unsigned int s0 = w.wedge[i0];
+					unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+					s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+					w.cr[i0] = i1;
+					w.cr[s0] = s1;
+				}
+				else
+					w.cr[i0] = i1;
+				done++;
+				float e = __uint_as_float(w.cerr[c]);
+				if (e == e)
+					em = max(em, w.cerr[c]);
+			}
+			unsigned int tot;
+			blockExclusiveScan<NT>(done, w.red, &tot);
+			__syncthreads();
+			s_maxes[tid] = em;
+			__syncthreads();
+			if (tid == 0)
+			{
+				unsigned int mm = __float_as_uint(result_error);
+				for (unsigned int q = 0; q < NT; ++q)
+					mm = max(mm, s_maxes[q]);
+				s_done = tot;
+				s_errbits = mm;
 			}
 		}
 		__syncthreads();
 		result_error = __uint_as_float(s_errbits);
 		passes++;
-		if (s_done == 0)
+		if (s_done == 0 || s_stall)
 			break;
 
 		// updateQuadrics (:1638-1673): every target receives at most one source per pass
@@ -765,7 +959,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
 	for (unsigned int i = tid; i < result_count; i += NT)
 		d.out[i] = w.idx[i];
 	if (tid == 0)
-		*out = BatchResult{result_count, sqrtf(result_error) * error_scale, passes, 0};
+		*out = BatchResult{result_count, sqrtf(result_error) * error_scale, passes, s_stall ? 3u : 0u};
 }
 
 template <int NT>

@@ -26,7 +26,7 @@ struct BatchResult
 	unsigned int index_count;
 	float result_error;
 	unsigned int passes;
-	unsigned int status; // 0 ok, 2 invalid index
+	unsigned int status; // 0 ok, 2 invalid index, 3 a decision round made no progress
 };
 
 // scratch bytes one mesh needs (shared memory when it fits, else a global slab)

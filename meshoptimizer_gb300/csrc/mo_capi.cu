@@ -260,8 +260,8 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 
 // ---------------------------------------------------------------- batched path
 
-const size_t kBatchSmemDefault = 96 * 1024;     // shared-memory budget per CTA
-const size_t kBatchSlabTotal = size_t(4) << 30; // global slabs for meshes beyond the budget
+const size_t kBatchSmemDefault = 104 * 1024;    // shared-memory budget per CTA (two CTAs per SM)
+const size_t kBatchSlabTotal = size_t(16) << 30; // global slabs for meshes beyond the budget
 
 struct BatchTuner
 {
@@ -388,10 +388,12 @@ int finishBatch(const std::vector<BatchResult>& res, size_t* counts, float* erro
 		if (errors)
 			errors[i] = res[i].result_error;
 		if (res[i].status)
-			status = meshoptgpu_StatusInvalidArgument;
+			status = res[i].status == 3 ? meshoptgpu_StatusCudaError : meshoptgpu_StatusInvalidArgument;
 	}
-	if (status != meshoptgpu_StatusOk)
+	if (status == meshoptgpu_StatusInvalidArgument)
 		setStatus(status, "a batched mesh has an index out of range of its vertex_count");
+	else if (status != meshoptgpu_StatusOk)
+		setStatus(status, "a batched mesh's decision round made no progress");
 	else
 		setStatus(meshoptgpu_StatusOk, "");
 	return status;
