@@ -216,7 +216,8 @@ def bench_serving(args, mg, torch):
     def run(rate, plain):
         gaps = np.random.default_rng(int(rate) * 7 + (1 if plain else 0)).exponential(1.0 / rate, size=n_req)
         arrivals = np.cumsum(gaps)
-        with mg.Server(memory_budget=40 << 30, plain=plain, large_workers=args.serve_workers, perform_blocks=args.serve_blocks) as srv:
+        with mg.Server(memory_budget=40 << 30, plain=plain, large_workers=args.serve_workers, perform_blocks=args.serve_blocks,
+                       large_index_count=args.serve_large, batch_workers=args.serve_batch_workers) as srv:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             tickets = []
@@ -255,7 +256,8 @@ def bench_serving(args, mg, torch):
         "steps": n_req, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "serving_poisson", "requests_per_rate": n_req, "pool_meshes": pool_size, "tris": "lognormal median 20k sigma 1 [1k,1M]",
                    "ratio": "U[0.1,0.5]", "target_error": 1e-2, "memory_budget_gb": 40, "request_input_tris": total_tris,
-                   "single_mesh_workers": args.serve_workers, "pass_kernel_grid_cap": args.serve_blocks or 64},
+                   "single_mesh_workers": args.serve_workers, "pass_kernel_grid_cap": args.serve_blocks or 64,
+                   "batch_kernel_max_index_count": args.serve_large or 300000},
         "served": served, "plain": plain, "served_equals_plain": bool(same),
     }
     return line
@@ -399,6 +401,8 @@ def main():
     ap.add_argument("--plain-rates", type=int, default=2, help="serving: how many of the rates also run the plain path")
     ap.add_argument("--serve-workers", type=int, default=16, help="serving: concurrent single-mesh workers")
     ap.add_argument("--serve-blocks", type=int, default=0, help="serving: pass-kernel grid cap per request (0: server default)")
+    ap.add_argument("--serve-large", type=int, default=0, help="serving: index count above which requests skip the batch kernel (0: default)")
+    ap.add_argument("--serve-batch-workers", type=int, default=0, help="serving: concurrent batch launches (0: default)")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -570,7 +574,8 @@ def main():
         line["batched_groups"] = {k: g[k] for k in ("value", "unit", "ms_per_step", "e2e", "plain_gpu", "cpu_baseline",
                                                    "bit_exact_vs_plain_and_oracle")}
         line["batched_groups"]["config"] = g["config"]
-        sv = bench_serving(argparse.Namespace(requests=2000, rates="500,1000", plain_rates=1, serve_workers=16, serve_blocks=0), mg, torch)
+        sv = bench_serving(argparse.Namespace(requests=2000, rates="500,1000", plain_rates=1, serve_workers=16, serve_blocks=0, serve_large=0,
+                                              serve_batch_workers=0), mg, torch)
         line["serving"] = {k: sv[k] for k in ("served", "plain", "served_equals_plain", "config")}
     print(json.dumps(line))
     if dist:

@@ -6,10 +6,13 @@
 // it fits the launch's dynamic shared memory, otherwise in a per-CTA slab of global memory;
 // every phase addresses it through generic pointers, so one code path serves both.
 //
-// Inside a CTA the greedy collapse loop (performEdgeCollapses :1498-1636) runs exactly as the
-// reference writes it, on one warp: lane 0 walks the sorted candidates and evaluates the stop
-// rules, locks and commits, and the 32 lanes split the one-ring of the flip test
-// (hasTriangleFlips :1201-1232). All other phases use the whole block.
+// Inside a CTA the greedy collapse loop (performEdgeCollapses :1498-1636) runs in one of two
+// exact forms. For a mesh in shared memory it runs as the reference writes it, on one warp:
+// lane 0 walks the sorted candidates and evaluates the stop rules, locks and commits, and the
+// 32 lanes split the one-ring of the flip test (hasTriangleFlips :1201-1232). For a mesh in a
+// global slab it runs as block-level decision rounds (the rule of the multi-CTA kPerform),
+// which hide the global-memory latency a serial walk would pay per candidate. All other phases
+// use the whole block.
 #include "mo_common.cuh"
 #include "mo_prims.cuh"
 #include "mo_probe.cuh"
@@ -174,7 +177,7 @@ __device__ __forceinline__ float fmax_l(float l, float r)
 // ---------------------------------------------------------------- one mesh
 
 template <int NT>
-__device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
+__device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, bool serial)
 {
 	const unsigned int tid = threadIdx.x;
 	const unsigned int I = d.index_count, V = d.vertex_count;
@@ -646,249 +649,326 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out)
 			w.cr[i] = i, w.locked[i] = 0;
 		__syncthreads();
 
-		// perform (performEdgeCollapses :1498-1636) in block-level decision rounds: a candidate is
-		// decided once nothing earlier in sorted order can change its outcome (the rule of the
-		// multi-CTA path's kPerform), over a window of sorted order that grows until the stop
-		// rules fire; the stop rules are a prefix scan of the decisions
 		const unsigned int goal = (result_count - d.target_index_count) / 3;
-		for (unsigned int i = tid; i < V; i += NT)
-			w.locked[i] = 0, w.moved[i] = ~0ull, w.minT[i] = ~0ull, w.minS[i] = ~0ull;
-		for (unsigned int k = tid; k < C; k += NT)
-			w.status[k] = kUndecided;
-		if (tid == 0)
-			s_cut = ~0ull, s_carry[0] = 0, s_carry[1] = 0, s_carry[2] = __float_as_uint(result_error);
-		__syncthreads();
+		if (serial)
 		{
-			unsigned int K0 = 0, K1 = (unsigned int)min((unsigned long long)C, 2ull * (goal / 2) + 64ull);
-			for (;;)
+			// meshes in shared memory: the reference's serial loop on one warp is cheaper than rounds
+			for (unsigned int i = tid; i < V; i += NT)
+				w.cr[i] = i, w.locked[i] = 0;
+			__syncthreads();
+
+			// perform (performEdgeCollapses :1498-1636) on warp 0, serial order, lanes split the flip test
+			if (tid < 32)
 			{
-				// rounds over [K0, K1)
-				unsigned int n = K1 - K0;
-				bool first = true;
-				unsigned int* cur = w.list0;
-				unsigned int* nxt = w.list1;
-				while (n)
+				const unsigned int lane = tid;
+				unsigned int edge_collapses = 0, triangle_collapses = 0, edge_goal = goal / 2;
+				for (unsigned int i = 0; i < C; ++i)
 				{
-					++round;
-					const unsigned long long tag = (unsigned long long)(0xFFFFFFFFu - round) << 32;
-					for (unsigned int x = tid; x < n; x += NT)
+					unsigned int c = w.order[i];
+					float err = __uint_as_float(w.cerr[c]);
+					if (err > error_limit)
+						break;
+					if (triangle_collapses >= goal)
+						break;
+					float error_goal = edge_goal < C ? 1.5f * __uint_as_float(w.cerr[w.order[edge_goal]]) : FLT_MAX;
+					if (err > error_goal && err > result_error && triangle_collapses > goal / 6)
+						break;
+					unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+					unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
+					unsigned char kd = w.kind[i0];
+					if (w.locked[r0] | w.locked[r1])
+						continue;
+					// flip test, lanes over r0's one-ring
+					unsigned int b = w.adj_off[r0], e = w.adj_off[r0 + 1];
+					float4 a0 = w.pos[r0], a1 = w.pos[r1];
+					V3 v0{a0.x, a0.y, a0.z}, v1{a1.x, a1.y, a1.z};
+					bool flip = false;
+					for (unsigned int j = b + lane; j < e; j += 32)
 					{
-						unsigned int k = first ? K0 + x : cur[x];
-						unsigned int c = w.order[k];
-						unsigned int r0 = w.remap[w.cv0[c]], r1 = w.remap[w.cv1[c]];
-						atomicMin(&w.minT[r0], tag | k);
-						atomicMin(&w.minT[r1], tag | k);
-						atomicMin(&w.minS[r0], tag | k);
+						uint2 ed = w.adj[j];
+						unsigned int va = w.cr[ed.x], vb = w.cr[ed.y];
+						if (va == r1 || vb == r1 || va == vb)
+							continue;
+						float4 pa = w.pos[va], pb = w.pos[vb];
+						flip |= triFlip(V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, v0, v1);
 					}
-					if (tid == 0)
-						s_next = 0;
-					__syncthreads();
-					for (unsigned int base = 0; base < n; base += NT)
+					if (__any_sync(0xffffffffu, flip))
 					{
-						unsigned int x = base + tid;
-						bool keep = false;
-						unsigned int k = 0;
-						if (x < n)
+						edge_goal++;
+						continue;
+					}
+					if (lane == 0)
+					{
+						if (kd == kSeam)
 						{
-							k = first ? K0 + x : cur[x];
+							unsigned int s0 = w.wedge[i0];
+							unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+							s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+							w.cr[i0] = i1;
+							w.cr[s0] = s1;
+						}
+						else
+							w.cr[i0] = i1;
+						w.locked[r0] = 1;
+						w.locked[r1] = 1;
+					}
+					__syncwarp();
+					triangle_collapses += (kd == kBorder) ? 1 : 2;
+					edge_collapses++;
+					result_error = result_error < err ? err : result_error;
+				}
+				if (lane == 0)
+				{
+					s_done = edge_collapses;
+					s_errbits = __float_as_uint(result_error);
+				}
+			}
+		}
+		else
+		{
+			// perform (performEdgeCollapses :1498-1636) in block-level decision rounds: a candidate is
+			// decided once nothing earlier in sorted order can change its outcome (the rule of the
+			// multi-CTA path's kPerform), over a window of sorted order that grows until the stop
+			// rules fire; the stop rules are a prefix scan of the decisions
+			for (unsigned int i = tid; i < V; i += NT)
+				w.locked[i] = 0, w.moved[i] = ~0ull, w.minT[i] = ~0ull, w.minS[i] = ~0ull;
+			for (unsigned int k = tid; k < C; k += NT)
+				w.status[k] = kUndecided;
+			if (tid == 0)
+				s_cut = ~0ull, s_carry[0] = 0, s_carry[1] = 0, s_carry[2] = __float_as_uint(result_error);
+			__syncthreads();
+			{
+				unsigned int K0 = 0, K1 = (unsigned int)min((unsigned long long)C, 2ull * (goal / 2) + 64ull);
+				for (;;)
+				{
+					// rounds over [K0, K1)
+					unsigned int n = K1 - K0;
+					bool first = true;
+					unsigned int* cur = w.list0;
+					unsigned int* nxt = w.list1;
+					while (n)
+					{
+						++round;
+						const unsigned long long tag = (unsigned long long)(0xFFFFFFFFu - round) << 32;
+						for (unsigned int x = tid; x < n; x += NT)
+						{
+							unsigned int k = first ? K0 + x : cur[x];
 							unsigned int c = w.order[k];
-							unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
-							unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
-							const unsigned long long mine = tag | k;
-							if (w.locked[r0] | w.locked[r1])
-								w.status[k] = kSkipLocked;
-							else if (w.minT[r0] != mine || w.minT[r1] != mine)
-								keep = true;
-							else
+							unsigned int r0 = w.remap[w.cv0[c]], r1 = w.remap[w.cv1[c]];
+							atomicMin(&w.minT[r0], tag | k);
+							atomicMin(&w.minT[r1], tag | k);
+							atomicMin(&w.minS[r0], tag | k);
+						}
+						if (tid == 0)
+							s_next = 0;
+						__syncthreads();
+						for (unsigned int base = 0; base < n; base += NT)
+						{
+							unsigned int x = base + tid;
+							bool keep = false;
+							unsigned int k = 0;
+							if (x < n)
 							{
-								unsigned int b = w.adj_off[r0], e = w.adj_off[r0 + 1];
-								for (unsigned int j = b; j < e && !keep; ++j)
+								k = first ? K0 + x : cur[x];
+								unsigned int c = w.order[k];
+								unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+								unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
+								const unsigned long long mine = tag | k;
+								if (w.locked[r0] | w.locked[r1])
+									w.status[k] = kSkipLocked;
+								else if (w.minT[r0] != mine || w.minT[r1] != mine)
+									keep = true;
+								else
 								{
-									uint2 ed = w.adj[j];
-									unsigned long long sx = w.minS[ed.x], sy = w.minS[ed.y];
-									keep = ((sx >> 32) == (tag >> 32) && (unsigned int)sx < k) || ((sy >> 32) == (tag >> 32) && (unsigned int)sy < k);
-								}
-								if (!keep)
-								{
-									float4 a0 = w.pos[r0], a1 = w.pos[r1];
-									V3 v0{a0.x, a0.y, a0.z}, v1{a1.x, a1.y, a1.z};
-									bool flip = false;
-									for (unsigned int j = b; j < e && !flip; ++j)
+									unsigned int b = w.adj_off[r0], e = w.adj_off[r0 + 1];
+									for (unsigned int j = b; j < e && !keep; ++j)
 									{
 										uint2 ed = w.adj[j];
-										unsigned long long mx = w.moved[ed.x], my = w.moved[ed.y];
-										unsigned int va = (unsigned int)(mx >> 32) < k ? (unsigned int)mx : ed.x;
-										unsigned int vb = (unsigned int)(my >> 32) < k ? (unsigned int)my : ed.y;
-										if (va == r1 || vb == r1 || va == vb)
-											continue;
-										float4 pa = w.pos[va], pb = w.pos[vb];
-										flip = triFlip(V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, v0, v1);
+										unsigned long long sx = w.minS[ed.x], sy = w.minS[ed.y];
+										keep = ((sx >> 32) == (tag >> 32) && (unsigned int)sx < k) || ((sy >> 32) == (tag >> 32) && (unsigned int)sy < k);
 									}
-									if (flip)
-										w.status[k] = kSkipFlip;
-									else
+									if (!keep)
 									{
-										unsigned int target = i1;
-										if (w.kind[i0] == kSeam)
+										float4 a0 = w.pos[r0], a1 = w.pos[r1];
+										V3 v0{a0.x, a0.y, a0.z}, v1{a1.x, a1.y, a1.z};
+										bool flip = false;
+										for (unsigned int j = b; j < e && !flip; ++j)
 										{
-											unsigned int s0 = w.wedge[i0];
-											unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
-											s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
-											target = (s0 == r0) ? s1 : i1;
+											uint2 ed = w.adj[j];
+											unsigned long long mx = w.moved[ed.x], my = w.moved[ed.y];
+											unsigned int va = (unsigned int)(mx >> 32) < k ? (unsigned int)mx : ed.x;
+											unsigned int vb = (unsigned int)(my >> 32) < k ? (unsigned int)my : ed.y;
+											if (va == r1 || vb == r1 || va == vb)
+												continue;
+											float4 pa = w.pos[va], pb = w.pos[vb];
+											flip = triFlip(V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, v0, v1);
 										}
-										w.moved[r0] = ((unsigned long long)k << 32) | target;
-										w.locked[r0] = 1;
-										w.locked[r1] = 1;
-										w.status[k] = kCommit;
+										if (flip)
+											w.status[k] = kSkipFlip;
+										else
+										{
+											unsigned int target = i1;
+											if (w.kind[i0] == kSeam)
+											{
+												unsigned int s0 = w.wedge[i0];
+												unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+												s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+												target = (s0 == r0) ? s1 : i1;
+											}
+											w.moved[r0] = ((unsigned long long)k << 32) | target;
+											w.locked[r0] = 1;
+											w.locked[r1] = 1;
+											w.status[k] = kCommit;
+										}
 									}
 								}
 							}
+							unsigned int m = __ballot_sync(0xffffffffu, keep);
+							if (keep)
+							{
+								unsigned int lane = tid & 31;
+								unsigned int leader = __ffs(m) - 1;
+								unsigned int o = 0;
+								if (lane == leader)
+									o = atomicAdd(&s_next, __popc(m));
+								o = __shfl_sync(m, o, leader);
+								nxt[o + __popc(m & ((1u << lane) - 1u))] = k;
+							}
 						}
-						unsigned int m = __ballot_sync(0xffffffffu, keep);
-						if (keep)
+						__syncthreads();
+						unsigned int nn = s_next;
+						__syncthreads();
+						if (nn >= n)
 						{
-							unsigned int lane = tid & 31;
-							unsigned int leader = __ffs(m) - 1;
-							unsigned int o = 0;
-							if (lane == leader)
-								o = atomicAdd(&s_next, __popc(m));
-							o = __shfl_sync(m, o, leader);
-							nxt[o + __popc(m & ((1u << lane) - 1u))] = k;
+							if (tid == 0)
+								s_stall = 1;
+							break;
 						}
+						n = nn;
+						first = false;
+						unsigned int* t = cur;
+						cur = nxt;
+						nxt = t;
+					}
+					// stop rules over [K0, K1): contiguous thread chunks, block scan, carried prefix
+					const unsigned int len = K1 - K0, per = (len + NT - 1) / NT;
+					const unsigned int t0 = min(K1, K0 + tid * per), t1 = min(K1, t0 + per);
+					unsigned int sT = 0, sF = 0, sM = 0;
+					for (unsigned int k = t0; k < t1; ++k)
+					{
+						unsigned char st = w.status[k];
+						unsigned int c = w.order[k];
+						float e = __uint_as_float(w.cerr[c]);
+						if (st == kCommit)
+						{
+							sT += w.kind[w.cv0[c]] == kBorder ? 1u : 2u;
+							if (e == e)
+								sM = max(sM, w.cerr[c]);
+						}
+						sF += st == kSkipFlip;
+					}
+					unsigned int eT, eF;
+					{
+						unsigned int tot;
+						eT = blockExclusiveScan<NT>(sT, w.red, &tot);
+						__syncthreads();
+						eF = blockExclusiveScan<NT>(sF, w.red, &tot);
+						__syncthreads();
+					}
+					// exclusive max over the threads before this one (in thread order)
+					s_maxes[tid] = sM;
+					__syncthreads();
+					unsigned int eM = 0;
+					for (unsigned int q = 0; q < tid; ++q)
+						eM = max(eM, s_maxes[q]);
+					unsigned long long T = (unsigned long long)s_carry[0] + eT, F = (unsigned long long)s_carry[1] + eF;
+					unsigned int M = max(s_carry[2], eM);
+					for (unsigned int k = t0; k < t1; ++k)
+					{
+						unsigned int c = w.order[k];
+						float e = __uint_as_float(w.cerr[c]);
+						unsigned int reason = 0;
+						if (e > error_limit)
+							reason = 1;
+						else if (T >= goal)
+							reason = 2;
+						else
+						{
+							unsigned long long eg = goal / 2 + F;
+							float error_goal = eg < C ? 1.5f * __uint_as_float(w.cerr[w.order[eg]]) : FLT_MAX;
+							if (e > error_goal && e > __uint_as_float(M) && T > goal / 6)
+								reason = 3;
+						}
+						if (reason)
+						{
+							atomicMin(&s_cut, ((unsigned long long)k << 2) | reason);
+							break;
+						}
+						unsigned char st = w.status[k];
+						if (st == kCommit)
+						{
+							T += w.kind[w.cv0[c]] == kBorder ? 1u : 2u;
+							if (e == e)
+								M = max(M, w.cerr[c]);
+						}
+						F += st == kSkipFlip;
 					}
 					__syncthreads();
-					unsigned int nn = s_next;
-					__syncthreads();
-					if (nn >= n)
-					{
-						if (tid == 0)
-							s_stall = 1;
+					if (s_cut != ~0ull || K1 == C || s_stall)
 						break;
-					}
-					n = nn;
-					first = false;
-					unsigned int* t = cur;
-					cur = nxt;
-					nxt = t;
-				}
-				// stop rules over [K0, K1): contiguous thread chunks, block scan, carried prefix
-				const unsigned int len = K1 - K0, per = (len + NT - 1) / NT;
-				const unsigned int t0 = min(K1, K0 + tid * per), t1 = min(K1, t0 + per);
-				unsigned int sT = 0, sF = 0, sM = 0;
-				for (unsigned int k = t0; k < t1; ++k)
-				{
-					unsigned char st = w.status[k];
-					unsigned int c = w.order[k];
-					float e = __uint_as_float(w.cerr[c]);
-					if (st == kCommit)
+					// carry the prefix over the window into the next one
+					if (tid == NT - 1)
 					{
-						sT += w.kind[w.cv0[c]] == kBorder ? 1u : 2u;
-						if (e == e)
-							sM = max(sM, w.cerr[c]);
+						s_carry[0] = (unsigned int)T;
+						s_carry[1] = (unsigned int)F;
+						s_carry[2] = M;
 					}
-					sF += st == kSkipFlip;
-				}
-				unsigned int eT, eF;
-				{
-					unsigned int tot;
-					eT = blockExclusiveScan<NT>(sT, w.red, &tot);
 					__syncthreads();
-					eF = blockExclusiveScan<NT>(sF, w.red, &tot);
-					__syncthreads();
+					K0 = K1;
+					K1 = (unsigned int)min((unsigned long long)C, 2ull * K1);
 				}
-				// exclusive max over the threads before this one (in thread order)
-				s_maxes[tid] = sM;
+			}
+			// apply the committed prefix: collapse_remap writes, done count, result error
+			{
+				const unsigned int cut = s_cut == ~0ull ? C : (unsigned int)(s_cut >> 2);
+				for (unsigned int i = tid; i < V; i += NT)
+					w.cr[i] = i;
 				__syncthreads();
-				unsigned int eM = 0;
-				for (unsigned int q = 0; q < tid; ++q)
-					eM = max(eM, s_maxes[q]);
-				unsigned long long T = (unsigned long long)s_carry[0] + eT, F = (unsigned long long)s_carry[1] + eF;
-				unsigned int M = max(s_carry[2], eM);
-				for (unsigned int k = t0; k < t1; ++k)
+				unsigned int done = 0, em = 0;
+				for (unsigned int k = tid; k < cut; k += NT)
 				{
+					if (w.status[k] != kCommit)
+						continue;
 					unsigned int c = w.order[k];
-					float e = __uint_as_float(w.cerr[c]);
-					unsigned int reason = 0;
-					if (e > error_limit)
-						reason = 1;
-					else if (T >= goal)
-						reason = 2;
+					unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
+					if (w.kind[i0] == kSeam)
+					{
+						unsigned int s0 = w.wedge[i0];
+						unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+						s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+						w.cr[i0] = i1;
+						w.cr[s0] = s1;
+					}
 					else
-					{
-						unsigned long long eg = goal / 2 + F;
-						float error_goal = eg < C ? 1.5f * __uint_as_float(w.cerr[w.order[eg]]) : FLT_MAX;
-						if (e > error_goal && e > __uint_as_float(M) && T > goal / 6)
-							reason = 3;
-					}
-					if (reason)
-					{
-						atomicMin(&s_cut, ((unsigned long long)k << 2) | reason);
-						break;
-					}
-					unsigned char st = w.status[k];
-					if (st == kCommit)
-					{
-						T += w.kind[w.cv0[c]] == kBorder ? 1u : 2u;
-						if (e == e)
-							M = max(M, w.cerr[c]);
-					}
-					F += st == kSkipFlip;
+						w.cr[i0] = i1;
+					done++;
+					float e = __uint_as_float(w.cerr[c]);
+					if (e == e)
+						em = max(em, w.cerr[c]);
 				}
+				unsigned int tot;
+				blockExclusiveScan<NT>(done, w.red, &tot);
 				__syncthreads();
-				if (s_cut != ~0ull || K1 == C || s_stall)
-					break;
-				// carry the prefix over the window into the next one
-				if (tid == NT - 1)
-				{
-					s_carry[0] = (unsigned int)T;
-					s_carry[1] = (unsigned int)F;
-					s_carry[2] = M;
-				}
+				s_maxes[tid] = em;
 				__syncthreads();
-				K0 = K1;
-				K1 = (unsigned int)min((unsigned long long)C, 2ull * K1);
-			}
-		}
-		// apply the committed prefix: collapse_remap writes, done count, result error
-		{
-			const unsigned int cut = s_cut == ~0ull ? C : (unsigned int)(s_cut >> 2);
-			for (unsigned int i = tid; i < V; i += NT)
-				w.cr[i] = i;
-			__syncthreads();
-			unsigned int done = 0, em = 0;
-			for (unsigned int k = tid; k < cut; k += NT)
-			{
-				if (w.status[k] != kCommit)
-					continue;
-				unsigned int c = w.order[k];
-				unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
-				if (w.kind[i0] == kSeam)
+				if (tid == 0)
 				{
-					unsigned int s0 = w.wedge[i0];
-					unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
-					s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
-					w.cr[i0] = i1;
-					w.cr[s0] = s1;
+					unsigned int mm = __float_as_uint(result_error);
+					for (unsigned int q = 0; q < NT; ++q)
+						mm = max(mm, s_maxes[q]);
+					s_done = tot;
+					s_errbits = mm;
 				}
-				else
-					w.cr[i0] = i1;
-				done++;
-				float e = __uint_as_float(w.cerr[c]);
-				if (e == e)
-					em = max(em, w.cerr[c]);
-			}
-			unsigned int tot;
-			blockExclusiveScan<NT>(done, w.red, &tot);
-			__syncthreads();
-			s_maxes[tid] = em;
-			__syncthreads();
-			if (tid == 0)
-			{
-				unsigned int mm = __float_as_uint(result_error);
-				for (unsigned int q = 0; q < NT; ++q)
-					mm = max(mm, s_maxes[q]);
-				s_done = tot;
-				s_errbits = mm;
 			}
 		}
 		__syncthreads();
@@ -981,7 +1061,7 @@ __global__ void __launch_bounds__(NT) kBatch(const BatchDesc* __restrict__ descs
 		size_t need = carve(w, nullptr, d.index_count, d.vertex_count);
 		char* base = need <= smem_bytes ? smem : slabs + (size_t)blockIdx.x * slab_bytes;
 		carve(w, base, d.index_count, d.vertex_count);
-		simplifyMesh<NT>(d, w, &results[job]);
+		simplifyMesh<NT>(d, w, &results[job], base == smem);
 		__syncthreads();
 	}
 }

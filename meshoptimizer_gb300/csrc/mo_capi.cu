@@ -692,7 +692,7 @@ meshoptgpu_Server* meshoptgpu_serverCreate(const meshoptgpu_ServerConfig* config
 		c.memory_budget = c.memory_budget ? c.memory_budget : kServerBudgetDefault;
 		c.batch_workers = c.batch_workers > 0 ? c.batch_workers : 4;
 		c.large_workers = c.large_workers > 0 ? c.large_workers : 8;
-		c.large_index_count = c.large_index_count ? c.large_index_count : 600000;
+		c.large_index_count = c.large_index_count ? c.large_index_count : 300000;
 		c.max_batch = c.max_batch > 0 ? c.max_batch : 2048;
 		c.batch_threads = (c.batch_threads == 128 || c.batch_threads == 256 || c.batch_threads == 512) ? c.batch_threads : 256;
 		c.perform_blocks = c.plain ? 0 : (c.perform_blocks > 0 ? c.perform_blocks : 64);
@@ -748,10 +748,9 @@ long long meshoptgpu_serverSubmit(meshoptgpu_Server* server, const meshoptgpu_Ba
 	    unsigned(mesh->vertex_positions_stride / 4), unsigned(mesh->target_index_count), mesh->target_error, mesh->options};
 	r->index_count = mesh->index_count;
 	r->vertex_count = mesh->vertex_count;
-	// meshes whose whole simplification fits one CTA's shared memory go to the batch kernel;
-	// the rest take the multi-CTA single-mesh path on one of the concurrent workers
-	bool large = S->cfg.plain || mesh->index_count > S->cfg.large_index_count ||
-	    batchWorkspaceBytes(mesh->index_count, mesh->vertex_count) > kBatchSmemDefault;
+	// meshes up to large_index_count indices go to the batch kernel (one CTA per mesh, shared
+	// memory or a global slab); larger ones take the multi-CTA single-mesh path
+	bool large = S->cfg.plain || mesh->index_count > S->cfg.large_index_count;
 	r->reserve = large ? Simplifier::workspaceBytes(mesh->index_count, mesh->vertex_count, 0) : batchReserve(*r);
 	if (r->reserve > S->cfg.memory_budget)
 	{
