@@ -257,7 +257,7 @@ def bench_serving(args, mg, torch):
         "config": {"workload": "serving_poisson", "requests_per_rate": n_req, "pool_meshes": pool_size, "tris": "lognormal median 20k sigma 1 [1k,1M]",
                    "ratio": "U[0.1,0.5]", "target_error": 1e-2, "memory_budget_gb": 40, "request_input_tris": total_tris,
                    "single_mesh_workers": args.serve_workers, "pass_kernel_grid_cap": args.serve_blocks or 64,
-                   "batch_kernel_max_index_count": args.serve_large or 300000},
+                   "batch_kernel_max_index_count": args.serve_large or 30000},
         "served": served, "plain": plain, "served_equals_plain": bool(same),
     }
     return line

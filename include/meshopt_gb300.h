@@ -148,10 +148,11 @@ typedef struct meshoptgpu_Server meshoptgpu_Server;
 typedef struct meshoptgpu_ServerConfig
 {
 	size_t memory_budget;     /* device bytes the server may hold for admitted requests (0: 40 GB) */
-	int batch_workers;        /* concurrent batch launches, one stream each (0: 4) */
+	int batch_workers;        /* concurrent batch launches, one stream each (0: 8) */
 	int large_workers;        /* concurrent single-mesh simplifications, one stream each (0: 8) */
 	size_t large_index_count; /* requests with more indices take the multi-CTA single-mesh path, the
-	                             others the batch kernel (0: 300000, i.e. 100k triangles) */
+	                             others the batch kernel (0: 30000, i.e. 10k triangles; measured best
+	                             p99 under Poisson load: larger meshes on one CTA take too long) */
 	int max_batch;            /* requests per batch launch at most (0: 2048) */
 	int batch_threads;        /* threads per CTA of the batch kernel (0: 256) */
 	int plain;                /* 1: no batching, one request at a time on the single-mesh path */

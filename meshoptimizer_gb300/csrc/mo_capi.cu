@@ -690,9 +690,9 @@ meshoptgpu_Server* meshoptgpu_serverCreate(const meshoptgpu_ServerConfig* config
 		std::unique_ptr<ServerImpl> S(new ServerImpl());
 		meshoptgpu_ServerConfig c = config ? *config : meshoptgpu_ServerConfig{};
 		c.memory_budget = c.memory_budget ? c.memory_budget : kServerBudgetDefault;
-		c.batch_workers = c.batch_workers > 0 ? c.batch_workers : 4;
+		c.batch_workers = c.batch_workers > 0 ? c.batch_workers : 8;
 		c.large_workers = c.large_workers > 0 ? c.large_workers : 8;
-		c.large_index_count = c.large_index_count ? c.large_index_count : 300000;
+		c.large_index_count = c.large_index_count ? c.large_index_count : 30000;
 		c.max_batch = c.max_batch > 0 ? c.max_batch : 2048;
 		c.batch_threads = (c.batch_threads == 128 || c.batch_threads == 256 || c.batch_threads == 512) ? c.batch_threads : 256;
 		c.perform_blocks = c.plain ? 0 : (c.perform_blocks > 0 ? c.perform_blocks : 64);
