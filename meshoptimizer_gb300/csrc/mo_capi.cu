@@ -137,7 +137,8 @@ void setStatus(int status, const std::string& msg)
 		fprintf(stderr, "meshopt_gb300: %s\n", msg.c_str());
 }
 
-const unsigned int kSupportedOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight | kOptSparse | kOptPermissive;
+const unsigned int kSupportedOptions =
+    kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight | kOptSparse | kOptPermissive | kOptPrune | kOptInternalDebug;
 // the one-CTA-per-mesh batch kernel implements the positions-only subset
 const unsigned int kBatchOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight;
 

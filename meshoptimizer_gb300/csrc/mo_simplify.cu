@@ -330,6 +330,13 @@ __global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned 
 	atomicAdd(&cnt[v], 1u);
 }
 
+__global__ void kIota(unsigned int* __restrict__ out, size_t n)
+{
+	size_t i = gtid();
+	if (i < n)
+		out[i] = (unsigned int)i;
+}
+
 __global__ void kRemapKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ keys)
 {
 	size_t i = gtid();
@@ -1641,6 +1648,164 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 	}
 }
 
+// ---------------------------------------------------------------- prune (buildComponents / measureComponents / pruneComponents, :1866-2024)
+
+__device__ __forceinline__ unsigned int ufFind(unsigned int* parent, unsigned int x)
+{
+	unsigned int p = __ldcg(parent + x);
+	while (p != x)
+	{
+		unsigned int gp = __ldcg(parent + p);
+		if (gp != p)
+			atomicCAS(parent + x, p, gp); // path halving
+		x = p;
+		p = __ldcg(parent + x);
+	}
+	return x;
+}
+
+// lock-free union-find over the welded edges: the larger root is linked under the smaller, so
+// a component's root is its smallest primary vertex, as the reference's union-find leaves it
+__global__ void kUnionEdges(const unsigned int* __restrict__ idx, size_t tris, const unsigned int* __restrict__ remap, unsigned int* parent)
+{
+	size_t t = gtid();
+	if (t >= tris)
+		return;
+	for (int e = 0; e < 3; ++e)
+	{
+		unsigned int a = remap[idx[t * 3 + e]], b = remap[idx[t * 3 + (e == 2 ? 0 : e + 1)]];
+		for (int guard = 0; guard < 1 << 20; ++guard)
+		{
+			unsigned int ra = ufFind(parent, a), rb = ufFind(parent, b);
+			if (ra == rb)
+				break;
+			unsigned int hi = max(ra, rb), lo = min(ra, rb);
+			if (atomicCAS(parent + hi, hi, lo) == hi)
+				break;
+		}
+	}
+}
+
+__global__ void kComponentRoots(size_t n, const unsigned int* __restrict__ remap, unsigned int* parent, unsigned int* __restrict__ rootflag)
+{
+	size_t i = gtid();
+	if (i >= n)
+		return;
+	unsigned int r = remap[i] == i ? ufFind(parent, (unsigned int)i) : ~0u;
+	rootflag[i] = r == (unsigned int)i;
+}
+
+// component ids in order of their roots (next_component++ over primaries in vertex order)
+__global__ void kComponentIds(size_t n, const unsigned int* __restrict__ remap, unsigned int* parent, const unsigned int* __restrict__ rootrank,
+    unsigned int* __restrict__ comp)
+{
+	size_t i = gtid();
+	if (i >= n)
+		return;
+	unsigned int r = ufFind(parent, remap[(unsigned int)i]);
+	comp[i] = rootrank[r];
+}
+
+// center = average position (sums in vertex order, as measureComponents), radius^2 = max
+// squared distance; one thread per component over its vertices sorted by (component, index)
+__global__ void kMeasureComponents(size_t ncomp, const unsigned int* __restrict__ off, const unsigned int* __restrict__ verts,
+    const float4* __restrict__ pos, float* __restrict__ err)
+{
+	size_t c = gtid();
+	if (c >= ncomp)
+		return;
+	unsigned int b = off[c], e = off[c + 1];
+	float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+	for (unsigned int j = b; j < e; ++j)
+	{
+		float4 p = pos[verts[j]];
+		sx += p.x;
+		sy += p.y;
+		sz += p.z;
+		sw += 1;
+	}
+	float iw = sw == 0.f ? 0.f : 1.f / sw;
+	sx *= iw;
+	sy *= iw;
+	sz *= iw;
+	float r2 = 0.f;
+	for (unsigned int j = b; j < e; ++j)
+	{
+		float4 p = pos[verts[j]];
+		float dx = p.x - sx, dy = p.y - sy, dz = p.z - sz;
+		float r = dx * dx + dy * dy + dz * dz;
+		r2 = r2 < r ? r : r2;
+	}
+	err[c] = r2;
+}
+
+__global__ void kMinFloat(const float* __restrict__ v, size_t n, unsigned int* out)
+{
+	size_t i = gtid();
+	if (i < n)
+		atomicMin(out, __float_as_uint(v[i])); // non-negative errors: bits order as floats
+}
+
+// largest component error not above the cutoff (cleanup loop, :2557-2560)
+__global__ void kMaxBelow(const float* __restrict__ v, size_t n, float cutoff, unsigned int* out)
+{
+	size_t i = gtid();
+	if (i < n && v[i] <= cutoff && v[i] > 0.f)
+		atomicMax(out, __float_as_uint(v[i]));
+}
+
+__device__ __forceinline__ bool pruneKeep(const unsigned int* __restrict__ res, size_t t, const unsigned int* __restrict__ comp,
+    const float* __restrict__ err, float cutoff, uint3& tri, float& e)
+{
+	tri = make_uint3(res[t * 3], res[t * 3 + 1], res[t * 3 + 2]);
+	e = err[comp[tri.x]];
+	return e > cutoff;
+}
+
+__global__ void __launch_bounds__(kThreads) kPruneCount(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ comp,
+    const float* __restrict__ err, float cutoff, unsigned int* __restrict__ blkcnt, unsigned int* minerr)
+{
+	size_t t = gtid();
+	uint3 tri;
+	float e = 0.f;
+	bool keep = t < tris && pruneKeep(res, t, comp, err, cutoff, tri, e);
+	if (keep)
+		atomicMin(minerr, __float_as_uint(e));
+	unsigned int c = __syncthreads_count(keep);
+	if (threadIdx.x == 0)
+		blkcnt[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(kThreads) kPruneEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ comp,
+    const float* __restrict__ err, float cutoff, const unsigned int* __restrict__ blkoff, unsigned int* __restrict__ out)
+{
+	__shared__ unsigned int smem[kThreads / 32 + 1];
+	size_t t = gtid();
+	uint3 tri = make_uint3(0, 0, 0);
+	float e = 0.f;
+	bool keep = t < tris && pruneKeep(res, t, comp, err, cutoff, tri, e);
+	unsigned int total;
+	unsigned int pre = blockExclusiveScan<kThreads>(keep ? 1u : 0u, smem, &total);
+	if (keep)
+	{
+		size_t w = (size_t)(blkoff[blockIdx.x] + pre) * 3;
+		out[w] = tri.x, out[w + 1] = tri.y, out[w + 2] = tri.z;
+	}
+}
+
+// meshopt_SimplifyInternalDebug (:2601-2614): vertex kind in bits 28-30, loop bit 31
+__global__ void kDebugBits(unsigned int* res, size_t tris, const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop,
+    const unsigned int* __restrict__ loopback)
+{
+	size_t t = gtid();
+	if (t >= tris)
+		return;
+	unsigned int a = res[t * 3], b = res[t * 3 + 1], c = res[t * 3 + 2];
+	res[t * 3 + 0] = a | ((unsigned int)kind[a] << 28) | ((unsigned int)(loop[a] == b || loopback[b] == a) << 31);
+	res[t * 3 + 1] = b | ((unsigned int)kind[b] << 28) | ((unsigned int)(loop[b] == c || loopback[c] == b) << 31);
+	res[t * 3 + 2] = c | ((unsigned int)kind[c] << 28) | ((unsigned int)(loop[c] == a || loopback[a] == c) << 31);
+}
+
 // ---------------------------------------------------------------- workspace
 
 struct Carver
@@ -1684,11 +1849,20 @@ struct Work
 	unsigned char* touched;
 	unsigned long long* moved;
 	unsigned int* cr;
+	unsigned int *comp, *parent;
+	float* comp_err;
 	uint4* blk;
 	unsigned int* blkcnt;
 	unsigned int* scratch;
 	unsigned int hash_mask;
 };
+
+inline float __uint_as_float_host(unsigned int u)
+{
+	float f;
+	memcpy(&f, &u, 4);
+	return f;
+}
 
 size_t hashBuckets(size_t count)
 {
@@ -1753,6 +1927,9 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 	w.minS = c.take<unsigned long long>(2 * Vp);
 	w.touched = c.take<unsigned char>(Vp);
 	w.moved = c.take<unsigned long long>(Vp);
+	w.comp = c.take<unsigned int>(Vp);
+	w.parent = c.take<unsigned int>(Vp + 1);
+	w.comp_err = c.take<float>(Vp + 1);
 	w.cr = c.take<unsigned int>(Vp);
 	w.blk = c.take<uint4>(std::max<size_t>(cap / kStopTile + 2, 8192)); // >= blocks of any cooperative launch
 	w.blkcnt = c.take<unsigned int>(T / kThreads + 2);
@@ -1897,7 +2074,7 @@ RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStre
 	cm.attributes = ac ? cattr : nullptr;
 	cm.attributes_stride = ac * 4;
 	cm.lock = m.lock ? clock : nullptr;
-	cm.options = m.options & ~kOptSparse;
+	cm.options = m.options & ~(kOptSparse | kOptInternalDebug); // debug bits are not produced for sparse subsets (:2602)
 	RunResult rr = run(cm, cres, stream, times, dump);
 	if (rr.index_count)
 		MO_LAUNCH(kSparseOut, gridFor(rr.index_count, kThreads), kThreads, 0, stream, cres, rr.index_count, smap, d_out);
@@ -2075,6 +2252,24 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		else
 			MO_LAUNCH(kFillAttributeQuadrics<32>, gridFor(V, 64), 64, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.pos, w.attr, ac, w.aq, w.ag);
 	}
+	size_t comp_count = 0;
+	if ((m.options & kOptPrune) && V)
+	{
+		// components of the welded mesh, numbered in root order, then their radii
+		MO_LAUNCH(kIota, gV, kThreads, 0, stream, w.parent, V);
+		if (I)
+			MO_LAUNCH(kUnionEdges, gridFor(I / 3, kThreads), kThreads, 0, stream, w.res0, I / 3, w.remap, w.parent);
+		MO_LAUNCH(kComponentRoots, gV, kThreads, 0, stream, V, w.remap, w.parent, w.flags);
+		scanExclusive(w.flags, w.fill, V, &w.sc->dup_count, w.scratch, stream);
+		MO_LAUNCH(kComponentIds, gV, kThreads, 0, stream, V, w.remap, w.parent, w.fill, w.comp);
+		readScalars();
+		comp_count = hs->dup_count;
+		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (comp_count + 1) * 4, stream));
+		MO_LAUNCH(kCountKeys, gV, kThreads, 0, stream, w.comp, nullptr, V, w.cnt);
+		scanExclusive(w.cnt, w.off_rm, comp_count + 1, nullptr, w.scratch, stream);
+		radixSortPairs(w.comp, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, V, bitsFor(comp_count ? comp_count - 1 : 0), w.scratch, stream);
+		MO_LAUNCH(kMeasureComponents, gridFor(comp_count, kThreads), kThreads, 0, stream, comp_count, w.off_rm, w.vals_a, w.pos, w.comp_err);
+	}
 	if (V)
 		MO_LAUNCH(kDualCount, gV, kThreads, 0, stream, w.off_raw, w.kind, V, &w.sc->dual);
 	MO_LAUNCH(kCapacity, 1, 32, 0, stream, I, w.sc);
@@ -2132,6 +2327,37 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	unsigned int* res = w.res0;
 	unsigned int* res_next = w.res1;
 	unsigned int result_error_bits = 0;
+	float vertex_error = 0.f;
+	float comp_next = 0.f;
+	// pruneComponents (:1996-2024): keep triangles of components above the cutoff, in order;
+	// comp_next becomes the smallest error among the components left
+	auto prune = [&](float cutoff) {
+		const size_t T = result_count / 3;
+		const unsigned int gT = gridFor(T, kThreads);
+		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->done, 0xFF, 4, stream)); // min error of kept components
+		if (T)
+		{
+			MO_LAUNCH(kPruneCount, gT, kThreads, 0, stream, res, T, w.comp, w.comp_err, cutoff, w.blkcnt, &w.sc->done);
+			scanExclusive(w.blkcnt, w.blkcnt, gT, &w.sc->tri_total, w.scratch, stream);
+			MO_LAUNCH(kPruneEmit, gT, kThreads, 0, stream, res, T, w.comp, w.comp_err, cutoff, w.blkcnt, res_next);
+		}
+		else
+			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->tri_total, 0, 4, stream));
+		readScalars();
+		unsigned int mb = hs->done;
+		comp_next = mb == ~0u ? FLT_MAX : __uint_as_float_host(mb);
+		result_count = size_t(hs->tri_total) * 3;
+		std::swap(res, res_next);
+	};
+	if (comp_count)
+	{
+		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->done, 0xFF, 4, stream));
+		MO_LAUNCH(kMinFloat, gridFor(comp_count, kThreads), kThreads, 0, stream, w.comp_err, comp_count, &w.sc->done);
+		readScalars();
+		comp_next = __uint_as_float_host(hs->done);
+	}
+	else if (m.options & kOptPrune)
+		comp_next = FLT_MAX;
 	int passes = 0;
 	unsigned int round_base = 0; // decision rounds are numbered across the run (mark tags never repeat)
 	MO_CUDA_CHECK(cudaMemsetAsync(w.minT, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
@@ -2259,8 +2485,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		result_error_bits = hs->result_error_bits;
 		if (hs->done == 0)
 			break;
+		const float derr_pass = __uint_as_float_host(hs->vertex_error_bits);
 		result_count = size_t(hs->tri_total) * 3;
 		std::swap(res, res_next);
+		vertex_error = ac == 0 ? __uint_as_float_host(result_error_bits) : derr_pass;
+		if ((m.options & kOptPrune) && result_count > m.target_index_count && comp_next <= vertex_error)
+			prune(vertex_error);
 		if (timed)
 		{
 			acc_adj += elapsed(2, 3);
@@ -2270,6 +2500,30 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			acc_perf += elapsed(6, 7);
 		}
 	}
+
+	// prune cleanup (:2543-2569): remove small components towards the error limit
+	bool comp_stale = true;
+	while ((m.options & kOptPrune) && result_count > m.target_index_count && comp_next <= error_limit)
+	{
+		float cutoff = comp_next * 1.5f < error_limit ? comp_next * 1.5f : error_limit;
+		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->skipped, 0, 4, stream));
+		if (comp_count)
+			MO_LAUNCH(kMaxBelow, gridFor(comp_count, kThreads), kThreads, 0, stream, w.comp_err, comp_count, cutoff, &w.sc->skipped);
+		readScalars();
+		const float maxerr = __uint_as_float_host(hs->skipped);
+		const size_t before = result_count;
+		prune(cutoff);
+		if (result_count == before && !comp_stale)
+			break;
+		comp_stale = false;
+		float re = __uint_as_float_host(result_error_bits);
+		re = re < maxerr ? maxerr : re;
+		memcpy(&result_error_bits, &re, 4);
+		vertex_error = vertex_error < maxerr ? maxerr : vertex_error;
+	}
+
+	if ((m.options & kOptInternalDebug) && result_count)
+		MO_LAUNCH(kDebugBits, gridFor(result_count / 3, kThreads), kThreads, 0, stream, res, result_count / 3, w.kind, w.loop, w.loopback);
 
 	if (result_count)
 		MO_CUDA_CHECK(cudaMemcpyAsync(d_out, res, result_count * 4, cudaMemcpyDeviceToDevice, stream));

@@ -163,6 +163,17 @@ def known_answer_cases():
     add("simplifySeamAttr", "seam_attr_lockborder", _np(a, "ib"), vb, 16, 12, 2.0, options=1, attrs=vb[3:].copy(), astride=16,
         weights=np.array([1.0], np.float32), expect=_np(a, "expected"), expect_count=18, expect_error_near=(0.35, 0.01))
 
+    a = _arrays(_function_body(src, "simplifyPrune"))
+    add("simplifyPrune", "prune", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-2, options=8, expect=_np(a, "expected"), expect_count=3,
+        expect_error_lt=1e-4)
+    add("simplifyPrune", "prune_subset", _np(a, "expected"), _np(a, "vb"), 12, 3, 1e-2, options=8, expect_count=3)
+    add("simplifyPrune", "prune_subset_sparse", _np(a, "expected"), _np(a, "vb"), 12, 3, 1e-2, options=8 | 2, expect=_np(a, "expected"),
+        expect_count=3)
+
+    a = _arrays(_function_body(src, "simplifyPruneCleanup"))
+    add("simplifyPruneCleanup", "prune_cleanup", _np(a, "ib"), _np(a, "vb"), 12, 3, 1.0, options=1 | 8, expect=_np(a, "expected"),
+        expect_count=3, expect_error_near=(0.37, 0.01))
+
     a = _arrays(_function_body(src, "simplifyDebug"))
     add("simplifyDebug", "debug_kinds", _np(a, "ib"), _np(a, "vb"), 12, 3, 1e-2, options=1 << 30,
         expect=_np(a, "expected"), expect_count=3, expect_error_lt=1e-4)

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 REL_TOL = 1e-6
 GPU_OPTIONS = (mg.SimplifyLockBorder | mg.SimplifyErrorAbsolute | mg.SimplifyRegularize | mg.SimplifyRegularizeLight | mg.SimplifySparse
-               | mg.SimplifyPermissive)
+               | mg.SimplifyPermissive | mg.SimplifyPrune | (1 << 30))
 
 
 def close(a, b):
@@ -206,8 +206,32 @@ def test_sparse_subset_of_large_buffer(port):
     _compare_with_oracle(port, tri, pos, W.target_count(len(tri), 0.5), 1e-2, mg.SimplifySparse | mg.SimplifyLockBorder)
 
 
+@pytest.mark.parametrize("seed", range(10))
+def test_prune(port, seed):
+    """Prune: disconnected pieces of different sizes removed in the pass loop and the cleanup loop."""
+    rng = np.random.default_rng(300 + seed)
+    parts_idx, parts_pos, base = [], [], 0
+    for p in range(int(rng.integers(2, 7))):
+        n = int(rng.integers(3, 14))
+        idx, pos = W.heightfield(n, seed=seed * 10 + p, amp=0.05)
+        pos = pos * np.float32(rng.uniform(0.05, 1.0)) + rng.uniform(-2, 2, size=3).astype(np.float32)
+        parts_idx.append(idx + base)
+        parts_pos.append(pos)
+        base += len(pos)
+    idx = np.concatenate(parts_idx).astype(np.uint32)
+    pos = np.concatenate(parts_pos).astype(np.float32)
+    opt = mg.SimplifyPrune | [0, mg.SimplifyLockBorder, mg.SimplifySparse, mg.SimplifyErrorAbsolute][seed % 4]
+    err = [1e-2, 5e-2, 0.2][seed % 3] * (4.0 if opt & mg.SimplifyErrorAbsolute else 1.0)
+    _compare_with_oracle(port, idx, pos, W.target_count(len(idx), float(rng.uniform(0.05, 0.5))), err, opt)
+
+
+def test_internal_debug_bits(port):
+    idx, pos = W.heightfield(12, seed=4, amp=0.05)
+    _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.3), 1e-2, 1 << 30, stats=False)
+
+
 def test_unsupported_option_reports_status():
     idx, pos = W.heightfield(8, seed=1)
-    out, err = mg.simplify(idx, pos, 0, 1e-2, mg.SimplifyPrune, check=False)
+    out, err = mg.simplify(idx, pos, 0, 1e-2, 1 << 29, check=False)  # the internal solve bit (simplifyWithUpdate)
     st, msg = mg.last_status()
     assert st == mg.STATUS_UNSUPPORTED and np.array_equal(out, idx)
