@@ -483,6 +483,7 @@ def main():
     step()
     phases = mg.last_phase_times()
     passes = mg.last_pass_stats()
+    trace = mg.last_round_trace()
     mg.set_timing(False)
 
     # end to end through the drop-in C ABI with pinned host buffers
@@ -568,6 +569,7 @@ def main():
         "clocks": clocks.summary(), "gpu_launches": int(launches),
         "phases_ms": {k: round(v, 3) for k, v in phases.items()},
         "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active", "windows")} for p in passes],
+        "round_trace_us": [[n, round(t, 1)] for n, t in trace[:64]],
     }
     if not args.no_extras and world == 1:
         g = bench_groups(argparse.Namespace(steps=3, warmup=3, no_cpu_baseline=args.no_cpu_baseline), mg, torch)

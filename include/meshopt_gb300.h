@@ -94,6 +94,11 @@ MESHOPTGPU_API int meshoptgpu_getLastPassStats(meshoptgpu_PassStats* out, int ma
  * rounds, stop rules, apply, loop remap + counts, count scan, compaction emit.
  * Returns the number of values written (16). */
 MESHOPTGPU_API void meshoptgpu_setTiming(int enabled);
+
+/* Decision rounds of the calling thread's last call on the single-mesh path, in order (at most
+ * 512): candidates processed by the round and its duration in microseconds (SM clock of one
+ * block). Returns the number of rounds recorded. */
+MESHOPTGPU_API int meshoptgpu_getLastRoundTrace(unsigned int* active, float* micros, int max_rounds);
 MESHOPTGPU_API int meshoptgpu_getLastPhaseTimes(float* out16);
 
 /* Device-resident form of meshopt_simplifyWithAttributes: every array pointer is a DEVICE

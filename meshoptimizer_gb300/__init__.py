@@ -47,6 +47,7 @@ EXPORTS = [
     "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc",
     "meshoptgpu_simplifyBatch", "meshoptgpu_simplifyBatchHost", "meshoptgpu_setBatchConfig", "meshoptgpu_getBatchThreads",
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
+    "meshoptgpu_getLastRoundTrace",
 ]
 
 
@@ -110,6 +111,8 @@ def load():
     lib.meshoptgpu_simplifyBatchHost.argtypes = [vp, sz, vp, vp]
     lib.meshoptgpu_setBatchConfig.argtypes = [C.c_int, C.c_uint]
     lib.meshoptgpu_getBatchThreads.restype = C.c_int
+    lib.meshoptgpu_getLastRoundTrace.restype = C.c_int
+    lib.meshoptgpu_getLastRoundTrace.argtypes = [vp, vp, C.c_int]
     lib.meshoptgpu_serverCreate.restype = C.c_void_p
     lib.meshoptgpu_serverCreate.argtypes = [vp]
     lib.meshoptgpu_serverDestroy.argtypes = [vp]
@@ -360,3 +363,11 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def last_round_trace():
+    """[(active candidates, microseconds)] per decision round of the last single-mesh call."""
+    n_ = (C.c_uint * 512)()
+    t_ = (C.c_float * 512)()
+    n = load().meshoptgpu_getLastRoundTrace(C.cast(n_, C.c_void_p), C.cast(t_, C.c_void_p), 512)
+    return [(int(n_[i]), float(t_[i])) for i in range(min(n, 512))]

@@ -884,6 +884,18 @@ int meshoptgpu_getLastPassStats(meshoptgpu_PassStats* out, int max_passes)
 	return s.last.passes;
 }
 
+int meshoptgpu_getLastRoundTrace(unsigned int* active, float* micros, int max_rounds)
+{
+	const RunResult& r = state().last;
+	int n = int(r.round_trace.size());
+	for (int i = 0; i < n && i < max_rounds; ++i)
+	{
+		active[i] = r.round_trace[i].first;
+		micros[i] = r.round_trace[i].second;
+	}
+	return n;
+}
+
 void meshoptgpu_setTiming(int enabled)
 {
 	state().timing = enabled != 0;

@@ -66,6 +66,8 @@ struct Scalars
 	unsigned int carry[3];        // stop-rule prefix (triangles, flips, max error) after a window
 	unsigned int windows;         // sorted-order windows the last pass needed
 	unsigned long long phase_cycles[8]; // kPerform phases, SM cycles of block 0, summed over the run
+	unsigned int trace_count;           // decision rounds traced so far in the run
+	unsigned int trace[2 * 512];        // per round: active candidates, SM cycles / 16
 };
 
 __device__ __forceinline__ size_t gtid()
@@ -1392,7 +1394,17 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 			}
 			gridBarrier(sc->bar, &sc->grid_error);
 			if (timer)
+			{
+				long long before = pc.last;
 				pc.lap(kPhRounds);
+				unsigned int tc = sc->trace_count;
+				if (tc < 512)
+				{
+					sc->trace[2 * tc] = n;
+					sc->trace[2 * tc + 1] = (unsigned int)((pc.last - before) >> 4);
+					sc->trace_count = tc + 1;
+				}
+			}
 			unsigned int nn = __ldcg(next_count);
 			if (nn >= n)
 			{
@@ -2541,6 +2553,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		readScalars();
 		for (int i = 0; i < 8; ++i)
 			rr.perform_phase_ms[i] = khz ? float(double(hs->phase_cycles[i]) / khz) : 0.f;
+		rr.round_trace.clear();
+		for (unsigned int i = 0; i < hs->trace_count && i < 512; ++i)
+			rr.round_trace.push_back({hs->trace[2 * i], khz ? float(double(hs->trace[2 * i + 1]) * 16.0 / khz * 1e3) : 0.f});
 	}
 	rr.index_count = result_count;
 	rr.result_error_sq = rerr;

@@ -62,6 +62,8 @@ struct RunResult
 	// time inside the cooperative pass kernel by phase (block 0's SM clock): init, window marks,
 	// decision rounds, stop rules, apply, loop remap + counts, count scan, compaction emit
 	float perform_phase_ms[8] = {};
+	// decision rounds of the run in order: active candidates and duration (microseconds)
+	std::vector<std::pair<unsigned int, float>> round_trace;
 };
 
 // Device timings of the phases of one run (milliseconds, from CUDA events).
