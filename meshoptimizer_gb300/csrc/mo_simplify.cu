@@ -35,6 +35,7 @@ namespace
 
 constexpr int kThreads = 256;
 constexpr int kStopTile = 1024; // sorted candidates per block in the stop-rule scan
+constexpr size_t kPinnedBytes = 16384; // host readback buffer of the scalars block
 constexpr unsigned int kApplyTile = 4096; // sorted positions compacted per block step in the apply phase
 
 struct Scalars
@@ -69,6 +70,8 @@ struct Scalars
 	unsigned int trace_count;           // decision rounds traced so far in the run
 	unsigned int trace[2 * 512];        // per round: active candidates, SM cycles / 16
 };
+
+static_assert(sizeof(Scalars) <= kPinnedBytes, "the scalars block must fit the pinned readback buffer");
 
 __device__ __forceinline__ size_t gtid()
 {
@@ -2002,7 +2005,7 @@ void DeviceArena::reserve(size_t bytes)
 Simplifier::Simplifier(int device) : device_(device)
 {
 	MO_CUDA_CHECK(cudaSetDevice(device));
-	MO_CUDA_CHECK(cudaMallocHost(&pinned_, 4096));
+	MO_CUDA_CHECK(cudaMallocHost(&pinned_, kPinnedBytes));
 	int sms = 0, per_sm = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
