@@ -1076,26 +1076,38 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 		for (int q = 0; q < 4; ++q)
 			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
 	}
-	// flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232)
+	#ifndef MO_FLIP_BATCH
+#define MO_FLIP_BATCH 2
+#endif
+	// flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232);
+	// the neighbours' own positions are loaded with their moved records (a moved neighbour's
+	// target position is loaded after)
 	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
-	for (unsigned int j = b; j < e; j += 4)
+	constexpr int FB = MO_FLIP_BATCH;
+	for (unsigned int j = b; j < e; j += FB)
 	{
-		unsigned long long mx[4], my[4];
+		unsigned long long mx[FB], my[FB];
+		float4 px[FB], py[FB];
 #pragma unroll
-		for (int q = 0; q < 4; ++q)
+		for (int q = 0; q < FB; ++q)
 		{
 			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r1, r1);
 			mx[q] = __ldcg(a.moved + ed[q].x);
 			my[q] = __ldcg(a.moved + ed[q].y);
+			px[q] = __ldg(a.pos + ed[q].x);
+			py[q] = __ldg(a.pos + ed[q].y);
 		}
 #pragma unroll
-		for (int q = 0; q < 4; ++q)
+		for (int q = 0; q < FB; ++q)
 		{
-			unsigned int va = (unsigned int)(mx[q] >> 32) < k ? (unsigned int)mx[q] : ed[q].x;
-			unsigned int vb = (unsigned int)(my[q] >> 32) < k ? (unsigned int)my[q] : ed[q].y;
+			bool mvx = (unsigned int)(mx[q] >> 32) < k, mvy = (unsigned int)(my[q] >> 32) < k;
+			unsigned int va = mvx ? (unsigned int)mx[q] : ed[q].x;
+			unsigned int vb = mvy ? (unsigned int)my[q] : ed[q].y;
 			if (va == r1 || vb == r1 || va == vb)
 				continue;
-			if (triFlip(ldpos(a.pos, va), ldpos(a.pos, vb), v0, v1))
+			V3 pa = mvx ? ldpos(a.pos, va) : V3{px[q].x, px[q].y, px[q].z};
+			V3 pb = mvy ? ldpos(a.pos, vb) : V3{py[q].x, py[q].y, py[q].z};
+			if (triFlip(pa, pb, v0, v1))
 			{
 				a.status[k] = kSkipFlip;
 				return false;
@@ -1344,7 +1356,17 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		if (timer)
 			pc.lap(windows == 1 ? kPhInit : kPhMarks);
 
-		unsigned int n = K1 - K0;
+		// the first round walks the window grid-stride (block b takes every G-th tile of blockDim
+		// candidates), so the earliest candidates, which most others wait on, are decided first;
+		// every block keeps the candidates it left undecided in its own region of the lists,
+		// compacted with shared-memory atomics, and walks that region in the later rounds; only
+		// the per-round total crosses blocks (one global add per block, read after the barrier)
+		const unsigned int wlen = K1 - K0;
+		const unsigned int stride = G * blockDim.x;
+		const unsigned int tiles = (wlen + stride - 1) / stride;
+		const size_t region = (size_t)blockIdx.x * tiles * blockDim.x;
+		unsigned int nb = tiles * blockDim.x; // this block's undecided candidates (slots in the first round)
+		unsigned int n = wlen;                // all blocks'
 		bool first = true;
 		unsigned int guard = 0;
 		while (n)
@@ -1353,48 +1375,45 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 			if (++guard > a.count + 1 || __ldcg(&sc->grid_error))
 				break;
 			active_sum += n;
-			const unsigned int* list = first ? nullptr : a.list[round & 1];
-			unsigned int* next = a.list[(round + 1) & 1];
-			unsigned int* next_count = &sc->act_count[(round + 1) % 3];
-			// the count round+1 appends to; every thread read it (as round-2's result) before the
+			const unsigned int* cur = a.list[round & 1] + region;
+			unsigned int* next = a.list[(round + 1) & 1] + region;
+			unsigned int* next_total = &sc->act_count[(round + 1) % 3];
+			// the total round+1 adds to; every thread read it (as round-2's result) before the
 			// barrier that ended round-1
 			if (gtid() == 0)
 				sc->act_count[(round + 2) % 3] = 0;
-			for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += gthreads)
+			if (threadIdx.x == 0)
+				s_app[0] = 0;
+			__syncthreads();
+			for (unsigned int base = 0; base < nb; base += blockDim.x)
 			{
-				size_t x = base + threadIdx.x;
+				unsigned int x = base + threadIdx.x;
+				unsigned int g = first ? base * G + blockIdx.x * blockDim.x + threadIdx.x : x;
 				bool keep = false;
 				unsigned int k = 0;
-				if (x < n)
+				if (first ? g < wlen : x < nb)
 				{
-					k = list ? __ldcg(list + x) : K0 + (unsigned int)x;
+					k = first ? K0 + g : __ldcg(cur + x);
 					uint4 rec = __ldg(a.srec + k);
 					keep = decideOne(a, k, rec, round);
 					if (keep)
 						markCandidate(a, k, rec, round + 1);
 				}
-				// block-aggregated append: one global atomic per block and iteration
 				unsigned int m = __ballot_sync(0xffffffffu, keep);
-				unsigned int w = threadIdx.x >> 5;
-				if (lane == 0)
-					s_app[w] = __popc(m);
-				__syncthreads();
-				if (threadIdx.x == 0)
+				if (m)
 				{
-					unsigned int run = 0;
-					for (unsigned int q = 0; q < blockDim.x / 32; ++q)
-					{
-						unsigned int c = s_app[q];
-						s_app[q] = run;
-						run += c;
-					}
-					s_app[32] = run ? atomicAdd(next_count, run) : 0u;
+					unsigned int leader = __ffs(m) - 1, o = 0;
+					if (lane == leader)
+						o = atomicAdd(&s_app[0], __popc(m));
+					o = __shfl_sync(0xffffffffu, o, leader);
+					if (keep)
+						next[o + __popc(m & ((1u << lane) - 1u))] = k;
 				}
-				__syncthreads();
-				if (keep)
-					next[s_app[32] + s_app[w] + __popc(m & ((1u << lane) - 1u))] = k;
-				__syncthreads();
 			}
+			__syncthreads();
+			nb = s_app[0];
+			if (threadIdx.x == 0 && nb)
+				atomicAdd(next_total, nb);
 			gridBarrier(sc->bar, &sc->grid_error);
 			if (timer)
 			{
@@ -1408,7 +1427,7 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 					sc->trace_count = tc + 1;
 				}
 			}
-			unsigned int nn = __ldcg(next_count);
+			unsigned int nn = __ldcg(next_total);
 			if (nn >= n)
 			{
 				if (gtid() == 0)
@@ -1887,6 +1906,10 @@ size_t hashBuckets(size_t count)
 	return b;
 }
 
+// the undecided-candidate lists hold one region of whole blockDim tiles per kPerform block:
+// at most the window plus one tile per block
+constexpr size_t kListSlack = size_t(1) << 19;
+
 size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 {
 	Carver c{base};
@@ -1936,8 +1959,8 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 	w.serr = c.take<unsigned int>(cap);
 	w.skind = c.take<unsigned char>(cap);
 	w.status = c.take<unsigned char>(cap);
-	w.act0 = c.take<unsigned int>(cap);
-	w.act1 = c.take<unsigned int>(cap);
+	w.act0 = c.take<unsigned int>(cap + kListSlack); // per-block regions of whole tiles
+	w.act1 = c.take<unsigned int>(cap + kListSlack);
 	w.minT = c.take<unsigned long long>(2 * Vp);
 	w.minS = c.take<unsigned long long>(2 * Vp);
 	w.touched = c.take<unsigned char>(Vp);
@@ -2468,6 +2491,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			unsigned int blocks = std::max(1u, std::min(perform_blocks_, want));
 			if (tuning_.perform_grid_cap > 0)
 				blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
+			if (size_t(blocks) * kThreads > kListSlack)
+				throw std::runtime_error("kPerform grid exceeds the candidate list slack");
 			void* params[] = {&pa};
 			cudaEvent_t e0 = probeBegin("kPerform", stream);
 			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, stream));
