@@ -113,8 +113,12 @@ MESHOPTGPU_API size_t meshoptgpu_simplifyDevice(unsigned int* destination, const
 
 /* ---- batched simplification: many meshes in one persistent launch ---- */
 
-/* One mesh of a batch: meshopt_simplify's arguments (positions only) plus its output buffer,
- * which must hold index_count indices. */
+/* One mesh of a batch: meshopt_simplifyWithAttributes' arguments plus its output buffer,
+ * which must hold index_count indices. The fields after `destination` are optional (zero /
+ * NULL: positions only, no vertex_lock), so a zero-initialised struct with the first nine
+ * fields set is a meshopt_simplify call. With meshopt_SimplifySparse, any number of meshes
+ * may share one vertex buffer (and attribute and lock arrays) and index subsets of it, as a
+ * cluster-LOD builder's groups do; each is simplified as a separate sparse call would. */
 typedef struct meshoptgpu_BatchMesh
 {
 	const unsigned int* indices;
@@ -124,8 +128,14 @@ typedef struct meshoptgpu_BatchMesh
 	size_t vertex_positions_stride;
 	size_t target_index_count;
 	float target_error;
-	unsigned int options; /* LockBorder, ErrorAbsolute, Regularize, RegularizeLight */
+	unsigned int options; /* every meshopt_Simplify* option except Prune and InternalDebug
+	                         (the server accepts those too and runs them on the single-mesh path) */
 	unsigned int* destination;
+	const float* vertex_attributes;
+	size_t vertex_attributes_stride;
+	const float* attribute_weights; /* HOST memory, attribute_count floats (read during the call) */
+	size_t attribute_count;
+	const unsigned char* vertex_lock;
 } meshoptgpu_BatchMesh;
 
 /* Simplifies every mesh of the batch in one launch of a persistent kernel: each CTA takes
@@ -175,8 +185,9 @@ MESHOPTGPU_API meshoptgpu_Server* meshoptgpu_serverCreate(const meshoptgpu_Serve
 MESHOPTGPU_API void meshoptgpu_serverDestroy(meshoptgpu_Server* server);
 
 /* Submits one request without blocking. Pointers in mesh are DEVICE pointers that must stay
- * valid until the request completes; options as in meshoptgpu_BatchMesh. Returns a ticket
- * (>= 0) or a negative meshoptgpu_Status* value. */
+ * valid until the request completes, except attribute_weights (host memory, copied before
+ * the call returns); every option meshopt_simplifyWithAttributes takes is accepted. Returns a
+ * ticket (>= 0) or a negative meshoptgpu_Status* value. */
 MESHOPTGPU_API long long meshoptgpu_serverSubmit(meshoptgpu_Server* server, const meshoptgpu_BatchMesh* mesh);
 
 /* Blocks until the request completes; fills the result index count and error, and the

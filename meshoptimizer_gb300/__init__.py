@@ -58,7 +58,9 @@ class PassStats(C.Structure):
 class BatchMesh(C.Structure):
     _fields_ = [("indices", C.c_void_p), ("index_count", C.c_size_t), ("vertex_positions", C.c_void_p),
                 ("vertex_count", C.c_size_t), ("vertex_positions_stride", C.c_size_t), ("target_index_count", C.c_size_t),
-                ("target_error", C.c_float), ("options", C.c_uint), ("destination", C.c_void_p)]
+                ("target_error", C.c_float), ("options", C.c_uint), ("destination", C.c_void_p),
+                ("vertex_attributes", C.c_void_p), ("vertex_attributes_stride", C.c_size_t), ("attribute_weights", C.c_void_p),
+                ("attribute_count", C.c_size_t), ("vertex_lock", C.c_void_p)]
 
 
 class ServerConfig(C.Structure):
@@ -266,25 +268,51 @@ def simplify_scale_noalloc(d_extent, d_positions, vertex_count, positions_stride
                                                       positions_stride, C.c_void_p(stream or None)))
 
 
+def _weights(m, keep):
+    w = m.get("weights")
+    if w is None:
+        return None, 0
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    keep.append(w)
+    return w.ctypes.data, len(w)
+
+
 def simplify_batch(meshes, check=True):
     """meshoptgpu_simplifyBatchHost on host arrays.
 
     meshes: list of dicts with indices (uint32), positions (float32 [V, k>=3]), target (index count),
-    error, options. Returns a list of (indices, result_error), identical to per-mesh meshopt_simplify.
+    error, options, and optionally attributes (float32 [V, k>=a]), weights (a floats) and lock
+    (uint8 [V]). Meshes of a sparse group may pass the same positions/attributes/lock arrays: they
+    are uploaded once. Returns a list of (indices, result_error), identical to per-mesh
+    meshopt_simplifyWithAttributes calls.
     """
     lib = load()
     n = len(meshes)
     arr = (BatchMesh * max(n, 1))()
     keep = []
     outs = []
+    arrays = {}
+
+    def shared(a, dtype):
+        # the same array object for several meshes gives the same pointer (deduplicated natively)
+        key = id(a)
+        if key not in arrays:
+            arrays[key] = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+        return arrays[key]
+
     for i, m in enumerate(meshes):
         idx = np.ascontiguousarray(m["indices"], dtype=np.uint32)
-        pos = np.ascontiguousarray(m["positions"], dtype=np.float32)
+        pos = shared(m["positions"], np.float32)
         out = np.empty(max(len(idx), 1), np.uint32)
-        keep += [idx, pos]
+        keep.append(idx)
         outs.append(out)
-        arr[i] = BatchMesh(idx.ctypes.data, len(idx), pos.ctypes.data, pos.shape[0], pos.shape[1] * 4, int(m["target"]),
-                           float(m["error"]), int(m.get("options", 0)), out.ctypes.data)
+        wp, wc = _weights(m, keep)
+        attr = shared(m["attributes"], np.float32) if wc else None
+        lock = shared(m["lock"], np.uint8) if m.get("lock") is not None else None
+        arr[i] = BatchMesh(idx.ctypes.data, len(idx), pos.ctypes.data, pos.shape[0], pos.shape[1] * 4, int(m["target"]), float(m["error"]),
+                           int(m.get("options", 0)), out.ctypes.data, attr.ctypes.data if wc else None, attr.shape[1] * 4 if wc else 0, wp, wc,
+                           lock.ctypes.data if lock is not None else None)
     counts = np.zeros(max(n, 1), np.uint64)
     errs = np.zeros(max(n, 1), np.float32)
     st = lib.meshoptgpu_simplifyBatchHost(C.cast(arr, C.c_void_p), n, counts.ctypes.data, errs.ctypes.data)
@@ -293,16 +321,24 @@ def simplify_batch(meshes, check=True):
     return [(outs[i][:int(counts[i])].copy(), float(errs[i])) for i in range(n)]
 
 
+def _device_mesh(m, keep):
+    wp, wc = _weights(m, keep)
+    return BatchMesh(m["d_indices"], m["index_count"], m["d_positions"], m["vertex_count"], m.get("stride", 12), int(m["target"]),
+                     float(m["error"]), int(m.get("options", 0)), m["d_destination"], m.get("d_attributes") if wc else None,
+                     m.get("attr_stride", 0) if wc else 0, wp, wc, m.get("d_lock"))
+
+
 def simplify_batch_device(descs, stream=0, check=True):
     """meshoptgpu_simplifyBatch with device pointers: descs is a list of dicts with keys
-    d_indices, index_count, d_positions, vertex_count, stride, target, error, options, d_destination.
+    d_indices, index_count, d_positions, vertex_count, stride, target, error, options, d_destination,
+    and optionally d_attributes, attr_stride (bytes), weights (host floats), d_lock.
     Returns (counts uint64 array, errors float32 array)."""
     lib = load()
     n = len(descs)
     arr = (BatchMesh * max(n, 1))()
+    keep = []
     for i, m in enumerate(descs):
-        arr[i] = BatchMesh(m["d_indices"], m["index_count"], m["d_positions"], m["vertex_count"], m.get("stride", 12), int(m["target"]),
-                           float(m["error"]), int(m.get("options", 0)), m["d_destination"])
+        arr[i] = _device_mesh(m, keep)
     counts = np.zeros(max(n, 1), np.uint64)
     errs = np.zeros(max(n, 1), np.float32)
     st = lib.meshoptgpu_simplifyBatch(C.cast(arr, C.c_void_p), n, counts.ctypes.data, errs.ctypes.data, C.c_void_p(stream or None))
@@ -334,8 +370,12 @@ class Server:
         if not self.h:
             raise SimplifyError(*last_status())
 
-    def submit(self, d_indices, index_count, d_positions, vertex_count, target, error, options, d_destination, stride=12):
-        m = BatchMesh(d_indices, index_count, d_positions, vertex_count, stride, int(target), float(error), int(options), d_destination)
+    def submit(self, d_indices, index_count, d_positions, vertex_count, target, error, options, d_destination, stride=12, d_attributes=None,
+               attr_stride=0, weights=None, d_lock=None):
+        keep = []
+        m = _device_mesh(dict(d_indices=d_indices, index_count=index_count, d_positions=d_positions, vertex_count=vertex_count, stride=stride,
+                              target=target, error=error, options=options, d_destination=d_destination, d_attributes=d_attributes,
+                              attr_stride=attr_stride, weights=weights, d_lock=d_lock), keep)
         t = self.lib.meshoptgpu_serverSubmit(C.c_void_p(self.h), C.byref(m))
         if t < 0:
             raise SimplifyError(-t, last_status()[1])

@@ -58,6 +58,10 @@ struct CtaWork
 	unsigned char* status;     // cap: decision per sorted position
 	unsigned int* list0;       // cap: undecided candidates of the round
 	unsigned int* list1;       // cap
+	unsigned int* back;        // V: sparse meshes, local vertex -> vertex of the shared buffer
+	float* attr;               // V * ac: rescaled attributes
+	Quadric* aq;               // V: attribute quadrics (per wedge)
+	float4* ag;                // V * ac: attribute gradients
 };
 
 __host__ __device__ inline size_t alignUp(size_t v, size_t a)
@@ -73,8 +77,15 @@ __host__ __device__ inline size_t hashBucketsFor(size_t count)
 	return b;
 }
 
-// Carves the workspace of a mesh with I indices and V vertices from `base` (nullptr: size only).
-__host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t V)
+// vertices a mesh's workspace is carved for: its own, or for a sparse mesh at most one per index
+__host__ __device__ inline size_t localVertexBound(size_t I, size_t vertex_count, bool sparse)
+{
+	return sparse ? (I < vertex_count ? I : vertex_count) : vertex_count;
+}
+
+// Carves the workspace of a mesh with I indices, V (local) vertices and ac attributes from
+// `base` (nullptr: size only).
+__host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t V, size_t ac, bool sparse)
 {
 	size_t off = 0;
 	size_t H = hashBucketsFor(V ? V : 1);
@@ -97,9 +108,14 @@ __host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t
 	w.adj = reinterpret_cast<uint2*>(take(I * 8));
 	w.fill = reinterpret_cast<unsigned int*>(take(V * 4));
 	w.cr = reinterpret_cast<unsigned int*>(take(V * 4));
-	// the hash table is only live during setup; the candidate arrays only during passes
+	w.back = sparse ? reinterpret_cast<unsigned int*>(take(V * 4)) : nullptr;
+	w.attr = ac ? reinterpret_cast<float*>(take(V * ac * 4)) : nullptr;
+	w.aq = ac ? reinterpret_cast<Quadric*>(take(V * sizeof(Quadric))) : nullptr;
+	w.ag = ac ? reinterpret_cast<float4*>(take(V * ac * 16)) : nullptr;
+	// the hash table (64-bit entries for a sparse mesh's first-use table) is only live during
+	// setup; the candidate arrays only during passes
 	size_t shared_at = off;
-	w.table = reinterpret_cast<unsigned int*>(take(H * 4));
+	w.table = reinterpret_cast<unsigned int*>(take(H * (sparse ? 8 : 4)));
 	size_t after_table = off;
 	off = shared_at;
 	w.cv0 = reinterpret_cast<unsigned int*>(take(cap * 4));
@@ -180,10 +196,12 @@ template <int NT>
 __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, bool serial)
 {
 	const unsigned int tid = threadIdx.x;
-	const unsigned int I = d.index_count, V = d.vertex_count;
+	const unsigned int I = d.index_count;
 	const float* P = d.positions;
 	const unsigned int sf = d.stride_f;
-	__shared__ unsigned int s_flag;
+	const unsigned int ac = d.ac;
+	unsigned int* const back = w.back; // sparse: local vertex -> vertex of the shared buffer
+	__shared__ unsigned int s_flag, s_unique;
 	__shared__ float s_mm[NT / 32][6];
 	__shared__ float s_minv[3], s_scale, s_extent;
 	__shared__ unsigned int s_cap, s_count, s_trunc, s_done, s_errbits, s_next, s_stall;
@@ -198,7 +216,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 	{
 		unsigned int v = d.indices[i];
 		w.idx[i] = v;
-		if (v >= V)
+		if (v >= d.vertex_count)
 			s_flag = 1;
 	}
 	__syncthreads();
@@ -211,6 +229,68 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		return;
 	}
 
+	// ---- sparse subset (buildSparseRemap :242-294): local ids in order of first use. A
+	// 64-bit table keyed by the shared-buffer vertex keeps its first index position (atomicMin);
+	// the positions that are first uses, ranked by a block scan, give the local ids.
+	unsigned int V = d.vertex_count;
+	if (back)
+	{
+		unsigned long long* t64 = reinterpret_cast<unsigned long long*>(w.table);
+		const unsigned int HS = (unsigned int)hashBucketsFor(localVertexBound(I, d.vertex_count, true) ? localVertexBound(I, d.vertex_count, true) : 1);
+		const unsigned int smask = HS - 1;
+		for (unsigned int i = tid; i < HS; i += NT)
+			t64[i] = ~0ull;
+		__syncthreads();
+		for (unsigned int p = tid; p < I; p += NT)
+		{
+			unsigned int v = w.idx[p];
+			unsigned long long key = ((unsigned long long)v << 32) | p;
+			unsigned int b = mix32b(v) & smask, slot = 0;
+			for (unsigned int probe = 0; probe <= smask; ++probe)
+			{
+				unsigned long long cur = t64[b];
+				if (cur == ~0ull)
+				{
+					unsigned long long prev = atomicCAS(&t64[b], ~0ull, key);
+					if (prev == ~0ull)
+					{
+						slot = b;
+						break;
+					}
+					cur = prev;
+				}
+				if ((unsigned int)(cur >> 32) == v)
+				{
+					atomicMin(&t64[b], key);
+					slot = b;
+					break;
+				}
+				b = (b + probe + 1) & smask;
+			}
+			w.adj[p].x = slot;
+		}
+		__syncthreads();
+		for (unsigned int p = tid; p < I; p += NT)
+			w.adj[p].y = (unsigned int)t64[w.adj[p].x]; // first position of this vertex
+		__syncthreads();
+		// the table is dead from here: its region holds the candidate arrays later
+		for (unsigned int p = tid; p < I; p += NT)
+			w.cv0[p] = w.adj[p].y == p;
+		__syncthreads();
+		unsigned int unique = blockScanArray<NT>(w.cv0, I, w.red);
+		for (unsigned int p = tid; p < I; p += NT)
+			if (w.adj[p].y == p)
+				back[w.cv0[p]] = w.idx[p];
+		__syncthreads();
+		for (unsigned int p = tid; p < I; p += NT)
+			w.idx[p] = w.cv0[w.adj[p].y];
+		if (tid == 0)
+			s_unique = unique;
+		__syncthreads();
+		V = s_unique;
+	}
+	auto src = [&](unsigned int i) { return back ? back[i] : i; };
+
 	// ---- position remap (buildPositionRemap :195-214) in a block-local hash table
 	const unsigned int H = (unsigned int)hashBucketsFor(V ? V : 1), mask = H - 1;
 	for (unsigned int i = tid; i < H; i += NT)
@@ -218,7 +298,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 	__syncthreads();
 	for (unsigned int i = tid; i < V; i += NT)
 	{
-		const float* p = P + (size_t)i * sf;
+		const float* p = P + (size_t)src(i) * sf;
 		float x = p[0], y = p[1], z = p[2];
 		unsigned int h = mix32b(posBitsB(x) * 0x9e3779b1u ^ mix32b(posBitsB(y) + 0x85ebca6bu) ^ mix32b(posBitsB(z) * 0xc2b2ae35u + 1u));
 		unsigned int b = h & mask, slot = ~0u;
@@ -235,7 +315,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 				}
 				cur = prev;
 			}
-			const float* q = P + (size_t)cur * sf;
+			const float* q = P + (size_t)src(cur) * sf;
 			if (q[0] == x && q[1] == y && q[2] == z)
 			{
 				atomicMin(&w.table[b], i);
@@ -285,7 +365,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		unsigned int per = (V + NT - 1) / NT, b0 = min(V, tid * per), b1 = min(V, b0 + per);
 		for (unsigned int i = b0; i < b1; ++i)
 		{
-			const float* p = P + (size_t)i * sf;
+			const float* p = P + (size_t)src(i) * sf;
 			for (int j = 0; j < 3; ++j)
 			{
 				mn[j] = mn[j] > p[j] ? p[j] : mn[j];
@@ -320,9 +400,16 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		__syncthreads();
 		for (unsigned int i = tid; i < V; i += NT)
 		{
-			const float* p = P + (size_t)i * sf;
+			const float* p = P + (size_t)src(i) * sf;
 			w.pos[i] = make_float4((p[0] - s_minv[0]) * s_scale, (p[1] - s_minv[1]) * s_scale, (p[2] - s_minv[2]) * s_scale, 0.f);
 		}
+		// rescaleAttributes (:605-621): weighted copies of the used attributes
+		if (ac)
+			for (unsigned int x = tid; x < V * ac; x += NT)
+			{
+				unsigned int i = x / ac, k = x - i * ac;
+				w.attr[x] = d.attributes[(size_t)src(i) * d.attr_stride_f + d.amap->src[k]] * d.amap->weight[k];
+			}
 	}
 
 	// ---- raw adjacency (updateEdgeAdjacency :52-109, no remap): corner lists, unordered
@@ -357,14 +444,14 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 			for (unsigned int j = b; j < e; ++j)
 			{
 				uint2 ej = w.adj[j];
-				bool back = false, fwd = false;
+				bool bk = false, fwd = false;
 				for (unsigned int q = b; q < e; ++q)
 				{
 					uint2 eq = w.adj[q];
-					back |= eq.y == ej.x;
+					bk |= eq.y == ej.x;
 					fwd |= eq.x == ej.y;
 				}
-				if (!back)
+				if (!bk)
 					outc++, outt = ej.x;
 				if (!fwd)
 					inc++, ins = ej.y;
@@ -399,11 +486,76 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		}
 		else
 			k = kLocked;
-		if ((d.options & kOptLockBorder) && k == kBorder)
-			k = kLocked;
 		w.kind[i] = k;
 	}
 	__syncthreads();
+	if (d.options & kOptPermissive)
+	{
+		// Permissive (:481-515): a seam or locked primary becomes Complex unless a wedge is
+		// protected or has a half-edge with no opposite in position space (hasEdge :345-362);
+		// the new kinds are staged in `locked` (unused until the passes), then copied to wedges
+		for (unsigned int i = tid; i < V; i += NT)
+		{
+			unsigned char k = w.kind[i];
+			unsigned char nk = k;
+			if (w.remap[i] == i && (k == kSeam || k == kLocked))
+			{
+				bool protect = false;
+				unsigned int v = i;
+				do
+				{
+					protect |= d.lock && (d.lock[src(v)] & kVertexProtect) != 0;
+					v = w.wedge[v];
+				} while (v != i);
+				do
+				{
+					for (unsigned int j = w.adj_off[v]; j < w.adj_off[v + 1] && !protect; ++j)
+					{
+						// hasEdge(nx -> v) over the wedges of nx
+						unsigned int a = w.adj[j].x, rb = w.remap[v], u = a;
+						bool found = false;
+						do
+						{
+							for (unsigned int q = w.adj_off[u]; q < w.adj_off[u + 1] && !found; ++q)
+								found = w.remap[w.adj[q].x] == rb;
+							u = w.wedge[u];
+						} while (u != a && !found);
+						protect |= !found;
+					}
+					v = w.wedge[v];
+				} while (v != i);
+				nk = protect ? k : (unsigned char)kComplex;
+			}
+			w.locked[i] = nk;
+		}
+		__syncthreads();
+		for (unsigned int i = tid; i < V; i += NT)
+		{
+			unsigned char k = w.kind[i];
+			if (k == kSeam || k == kLocked)
+				w.kind[i] = w.locked[w.remap[i]];
+		}
+		__syncthreads();
+	}
+	if (d.lock)
+	{
+		// vertex_lock (:517-531): a locked wedge locks its whole position
+		for (unsigned int i = tid; i < V; i += NT)
+			if (d.lock[src(i)] & kVertexLock)
+				w.kind[w.remap[i]] = kLocked;
+		__syncthreads();
+		for (unsigned int i = tid; i < V; i += NT)
+			if (w.kind[w.remap[i]] == kLocked)
+				w.kind[i] = kLocked;
+		__syncthreads();
+	}
+	if (d.options & kOptLockBorder)
+	{
+		for (unsigned int i = tid; i < V; i += NT)
+			if (w.kind[i] == kBorder)
+				w.kind[i] = kLocked;
+		__syncthreads();
+	}
 
 	// ---- capacity (boundEdgeCollapses :1292-1308) from the raw degrees
 	{
@@ -418,40 +570,44 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 			s_cap = I - tot / 2 + 3;
 	}
 
-	// ---- remapped corner lists in corner order, then the quadric folds (:1057-1157)
-	for (unsigned int i = tid; i <= V; i += NT)
-		w.adj_off[i] = 0;
-	__syncthreads();
-	for (unsigned int p = tid; p < I; p += NT)
-		atomicAdd(&w.adj_off[w.remap[w.idx[p]]], 1u);
-	__syncthreads();
-	blockScanArray<NT>(w.adj_off, V + 1, w.red);
-	for (unsigned int i = tid; i < V; i += NT)
-		w.fill[i] = 0;
-	__syncthreads();
-	for (unsigned int p = tid; p < I; p += NT)
-	{
-		unsigned int v = w.remap[w.idx[p]];
-		w.adj[w.adj_off[v] + atomicAdd(&w.fill[v], 1u)].x = p;
-	}
-	__syncthreads();
-	for (unsigned int v = tid; v < V; v += NT)
-	{
-		// insertion sort of the vertex's corners (few per vertex)
-		unsigned int b = w.adj_off[v], e = w.adj_off[v + 1];
-		for (unsigned int j = b + 1; j < e; ++j)
+	// ---- corner lists in corner order (remapped for the position quadrics, raw for the
+	// attribute quadrics), then the quadric folds (:1057-1179)
+	auto cornerLists = [&](bool remapped) {
+		for (unsigned int i = tid; i <= V; i += NT)
+			w.adj_off[i] = 0;
+		__syncthreads();
+		for (unsigned int p = tid; p < I; p += NT)
+			atomicAdd(&w.adj_off[remapped ? w.remap[w.idx[p]] : w.idx[p]], 1u);
+		__syncthreads();
+		blockScanArray<NT>(w.adj_off, V + 1, w.red);
+		for (unsigned int i = tid; i < V; i += NT)
+			w.fill[i] = 0;
+		__syncthreads();
+		for (unsigned int p = tid; p < I; p += NT)
 		{
-			unsigned int x = w.adj[j].x;
-			unsigned int q = j;
-			while (q > b && w.adj[q - 1].x > x)
-			{
-				w.adj[q].x = w.adj[q - 1].x;
-				--q;
-			}
-			w.adj[q].x = x;
+			unsigned int v = remapped ? w.remap[w.idx[p]] : w.idx[p];
+			w.adj[w.adj_off[v] + atomicAdd(&w.fill[v], 1u)].x = p;
 		}
-	}
-	__syncthreads();
+		__syncthreads();
+		for (unsigned int v = tid; v < V; v += NT)
+		{
+			// insertion sort of the vertex's corners (few per vertex)
+			unsigned int b = w.adj_off[v], e = w.adj_off[v + 1];
+			for (unsigned int j = b + 1; j < e; ++j)
+			{
+				unsigned int x = w.adj[j].x;
+				unsigned int q = j;
+				while (q > b && w.adj[q - 1].x > x)
+				{
+					w.adj[q].x = w.adj[q - 1].x;
+					--q;
+				}
+				w.adj[q].x = x;
+			}
+		}
+		__syncthreads();
+	};
+	cornerLists(true);
 	{
 		const float factor = (d.options & kOptRegularizeLight) ? 1e-2f : ((d.options & kOptRegularize) ? 1e-1f : 1e-7f);
 		for (unsigned int r = tid; r < V; r += NT)
@@ -471,7 +627,8 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 				Quadric F = qtriangle(V3{a0.x, a0.y, a0.z}, V3{a1.x, a1.y, a1.z}, V3{a2.x, a2.y, a2.z}, 1.f);
 				qadd(Q, F);
 			}
-			float wt = Q.w * factor;
+			bool priority = d.lock && (d.lock[src(r)] & kVertexPriority) != 0;
+			float wt = Q.w * (priority ? 1.0f : factor);
 			float4 pr = w.pos[r];
 			Quadric Pq = qpoint(pr.x, pr.y, pr.z, wt);
 			qadd(Q, Pq);
@@ -514,6 +671,29 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		}
 	}
 	__syncthreads();
+	if (ac)
+	{
+		// fillAttributeQuadrics (:1159-1179): per wedge over its faces in face order; the
+		// gradients accumulate in place (each vertex is owned by one thread)
+		cornerLists(false);
+		for (unsigned int v = tid; v < V; v += NT)
+		{
+			float4* G = w.ag + (size_t)v * ac;
+			for (unsigned int k = 0; k < ac; ++k)
+				G[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+			Quadric Q = qzero();
+			for (unsigned int j = w.adj_off[v]; j < w.adj_off[v + 1]; ++j)
+			{
+				unsigned int f = w.adj[j].x / 3;
+				unsigned int i0 = w.idx[f * 3 + 0], i1 = w.idx[f * 3 + 1], i2 = w.idx[f * 3 + 2];
+				float4 a0 = w.pos[i0], a1 = w.pos[i1], a2 = w.pos[i2];
+				addAttributeQuadric<32>(Q, G, (int)ac, V3{a0.x, a0.y, a0.z}, V3{a1.x, a1.y, a1.z}, V3{a2.x, a2.y, a2.z}, w.attr + (size_t)i0 * ac,
+				    w.attr + (size_t)i1 * ac, w.attr + (size_t)i2 * ac);
+			}
+			stquadric(w.aq, v, Q);
+		}
+		__syncthreads();
+	}
 
 	// ---- pass loop (:2493-2541)
 	const float error_scale = (d.options & kOptErrorAbsolute) ? s_extent : 1.f;
@@ -601,7 +781,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		if (C == 0)
 			break;
 
-		// rank (rankEdgeCollapses :1374-1450, positions only)
+		// rank (rankEdgeCollapses :1374-1450)
 		for (unsigned int c = tid; c < C; c += NT)
 		{
 			unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
@@ -610,6 +790,32 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 			V3 p0{a0.x, a0.y, a0.z}, p1{a1.x, a1.y, a1.z};
 			float ei = qerror(ldquadric(w.vq, w.remap[i0]), p1);
 			float ej = bidi ? qerror(ldquadric(w.vq, w.remap[i1]), p0) : FLT_MAX;
+			if (ac)
+			{
+				auto term = [&](unsigned int v, unsigned int t) {
+					float4 pt = w.pos[t];
+					return qerrorAttr(ldquadric(w.aq, v), w.ag + (size_t)v * ac, (int)ac, V3{pt.x, pt.y, pt.z}, w.attr + (size_t)t * ac);
+				};
+				ei += term(i0, i1);
+				ej += bidi ? term(i1, i0) : 0;
+				if (w.kind[i0] == kSeam)
+				{
+					unsigned int s0 = w.wedge[i0];
+					unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
+					s1 = (s1 != ~0u) ? s1 : w.wedge[i1];
+					ei += term(s0, s1);
+					ej += bidi ? term(s1, s0) : 0;
+				}
+				else
+				{
+					if (w.kind[i0] == kComplex)
+						for (unsigned int v = w.wedge[i0]; v != i0; v = w.wedge[v])
+							ei += term(v, complexTarget(v, i1, w.remap, w.loop, w.loopback));
+					if (w.kind[i1] == kComplex && bidi)
+						for (unsigned int v = w.wedge[i1]; v != i1; v = w.wedge[v])
+							ej += term(v, complexTarget(v, i0, w.remap, w.loop, w.loopback));
+				}
+			}
 			bool rev = bidi & (ej < ei);
 			w.cv0[c] = rev ? i1 : i0;
 			w.cv1[c] = rev ? i0 : i1;
@@ -699,7 +905,16 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 					}
 					if (lane == 0)
 					{
-						if (kd == kSeam)
+						if (kd == kComplex)
+						{
+							unsigned int v = i0;
+							do
+							{
+								w.cr[v] = complexTarget(v, i1, w.remap, w.loop, w.loopback);
+								v = w.wedge[v];
+							} while (v != i0);
+						}
+						else if (kd == kSeam)
 						{
 							unsigned int s0 = w.wedge[i0];
 							unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
@@ -808,7 +1023,9 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 										else
 										{
 											unsigned int target = i1;
-											if (w.kind[i0] == kSeam)
+											if (w.kind[i0] == kComplex)
+												target = complexTarget(r0, i1, w.remap, w.loop, w.loopback);
+											else if (w.kind[i0] == kSeam)
 											{
 												unsigned int s0 = w.wedge[i0];
 												unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
@@ -941,7 +1158,16 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 						continue;
 					unsigned int c = w.order[k];
 					unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
-					if (w.kind[i0] == kSeam)
+					if (w.kind[i0] == kComplex)
+					{
+						unsigned int v = i0;
+						do
+						{
+							w.cr[v] = complexTarget(v, i1, w.remap, w.loop, w.loopback);
+							v = w.wedge[v];
+						} while (v != i0);
+					}
+					else if (w.kind[i0] == kSeam)
 					{
 						unsigned int s0 = w.wedge[i0];
 						unsigned int s1 = w.loop[i0] == i1 ? w.loopback[s0] : w.loop[s0];
@@ -977,16 +1203,51 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		if (s_done == 0 || s_stall)
 			break;
 
-		// updateQuadrics (:1638-1673): every target receives at most one source per pass
+		// updateQuadrics (:1638-1673): every target receives at most one source per pass. The
+		// moved wedges of one commit all belong to its source position (whose primary always
+		// moves), and no other commit targets their targets, so each moved primary merges the
+		// attribute quadrics of its wedges in increasing vertex order, as the reference's vertex
+		// loop does
 		for (unsigned int i = tid; i < V; i += NT)
 		{
 			unsigned int t = w.cr[i];
-			if (t != i && w.remap[i] == i)
+			if (t == i || w.remap[i] != i)
+				continue;
+			unsigned int r1 = w.remap[t];
+			Quadric Q = ldquadric(w.vq, r1);
+			qadd(Q, ldquadric(w.vq, i));
+			stquadric(w.vq, r1, Q);
+			if (ac)
 			{
-				unsigned int r1 = w.remap[t];
-				Quadric Q = ldquadric(w.vq, r1);
-				qadd(Q, ldquadric(w.vq, i));
-				stquadric(w.vq, r1, Q);
+				unsigned int last = 0;
+				bool firstw = true;
+				for (;;)
+				{
+					unsigned int best = ~0u, v = i;
+					do
+					{
+						if ((firstw || v > last) && v < best)
+							best = v;
+						v = w.wedge[v];
+					} while (v != i);
+					if (best == ~0u)
+						break;
+					unsigned int tb = w.cr[best];
+					if (tb != best)
+					{
+						Quadric A = ldquadric(w.aq, tb);
+						qadd(A, ldquadric(w.aq, best));
+						stquadric(w.aq, tb, A);
+						for (unsigned int q = 0; q < ac; ++q)
+						{
+							float4 g = w.ag[(size_t)tb * ac + q], h = w.ag[(size_t)best * ac + q];
+							g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
+							w.ag[(size_t)tb * ac + q] = g;
+						}
+					}
+					last = best;
+					firstw = false;
+				}
 			}
 		}
 		// remapEdgeLoops (:1845-1864), in place
@@ -1037,7 +1298,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 	}
 
 	for (unsigned int i = tid; i < result_count; i += NT)
-		d.out[i] = w.idx[i];
+		d.out[i] = src(w.idx[i]);
 	if (tid == 0)
 		*out = BatchResult{result_count, sqrtf(result_error) * error_scale, passes, s_stall ? 3u : 0u};
 }
@@ -1058,9 +1319,11 @@ __global__ void __launch_bounds__(NT) kBatch(const BatchDesc* __restrict__ descs
 			break;
 		BatchDesc d = descs[job];
 		CtaWork w;
-		size_t need = carve(w, nullptr, d.index_count, d.vertex_count);
+		const bool sparse = (d.options & kOptSparse) != 0;
+		const size_t vb = localVertexBound(d.index_count, d.vertex_count, sparse);
+		size_t need = carve(w, nullptr, d.index_count, vb, d.ac, sparse);
 		char* base = need <= smem_bytes ? smem : slabs + (size_t)blockIdx.x * slab_bytes;
-		carve(w, base, d.index_count, d.vertex_count);
+		carve(w, base, d.index_count, vb, d.ac, sparse);
 		simplifyMesh<NT>(d, w, &results[job], base == smem);
 		__syncthreads();
 	}
@@ -1068,10 +1331,10 @@ __global__ void __launch_bounds__(NT) kBatch(const BatchDesc* __restrict__ descs
 
 } // namespace
 
-size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count)
+size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count, size_t ac, bool sparse)
 {
 	CtaWork w;
-	return carve(w, nullptr, index_count, vertex_count);
+	return carve(w, nullptr, index_count, localVertexBound(index_count, vertex_count, sparse), ac, sparse);
 }
 
 // the dynamic shared-memory limit of every batch kernel instance is raised once, to the

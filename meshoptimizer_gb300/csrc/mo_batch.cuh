@@ -7,6 +7,14 @@
 namespace mogpu
 {
 
+// attributes with weight > 0 of a batched mesh (rescaleAttributes :605-621, :2410-2421): source
+// column and weight of each used attribute
+struct BatchAttr
+{
+	unsigned int src[32];
+	float weight[32];
+};
+
 // one mesh of a batch; device pointers
 struct BatchDesc
 {
@@ -14,11 +22,16 @@ struct BatchDesc
 	const float* positions;
 	unsigned int* out;
 	unsigned int index_count;
-	unsigned int vertex_count;
-	unsigned int stride_f; // position stride in floats
+	unsigned int vertex_count; // of the vertex buffer the indices address
+	unsigned int stride_f;     // position stride in floats
 	unsigned int target_index_count;
 	float target_error;
 	unsigned int options;
+	const float* attributes;   // nullptr: positions only
+	const unsigned char* lock; // vertex_lock, nullptr: none
+	const BatchAttr* amap;     // used attributes (ac of them)
+	unsigned int attr_stride_f;
+	unsigned int ac;
 };
 
 struct BatchResult
@@ -29,8 +42,9 @@ struct BatchResult
 	unsigned int status; // 0 ok, 2 invalid index, 3 a decision round made no progress
 };
 
-// scratch bytes one mesh needs (shared memory when it fits, else a global slab)
-size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count);
+// scratch bytes one mesh needs (shared memory when it fits, else a global slab); a sparse mesh
+// has at most min(index_count, vertex_count) vertices of its own
+size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count, size_t ac, bool sparse);
 
 // resident CTAs per SM for a thread count and dynamic shared memory size
 int batchBlocksPerSM(int threads, unsigned int smem_bytes);

@@ -91,7 +91,7 @@ struct ThreadState
 	bool timing = false;
 	// batched path
 	DeviceBuffer batch_meta, batch_slabs, batch_io;
-	HostStaging batch_host;
+	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
 	unsigned int batch_smem = 0;    // 0: default budget
 
@@ -139,8 +139,9 @@ void setStatus(int status, const std::string& msg)
 
 const unsigned int kSupportedOptions =
     kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight | kOptSparse | kOptPermissive | kOptPrune | kOptInternalDebug;
-// the one-CTA-per-mesh batch kernel implements the positions-only subset
-const unsigned int kBatchOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight;
+// the one-CTA-per-mesh batch kernel implements every option but the component pruning and the
+// debug output
+const unsigned int kBatchOptions = kOptLockBorder | kOptErrorAbsolute | kOptRegularize | kOptRegularizeLight | kOptSparse | kOptPermissive;
 
 // argument checks of meshopt_simplifyEdge (:2348-2357); returns an error message or empty
 std::string checkArgs(size_t index_count, size_t vertex_positions_stride, size_t target_index_count, float target_error,
@@ -278,8 +279,71 @@ int sizeClass(size_t max_index_count)
 	return c;
 }
 
+// The used attributes (weight > 0, :2410-2421) of a batched mesh, deduplicated across the
+// batch: meshes with the same weights share one map in device memory.
+struct AttrMaps
+{
+	std::vector<BatchAttr> maps;
+	std::map<std::string, int> index;
+
+	// returns the map's index (or -1 when no attribute has a positive weight); ac = used count
+	int add(const float* weights, size_t count, unsigned int& ac)
+	{
+		BatchAttr a;
+		memset(&a, 0, sizeof(a));
+		ac = 0;
+		for (size_t k = 0; k < count; ++k)
+			if (weights[k] > 0)
+			{
+				a.src[ac] = unsigned(k);
+				a.weight[ac] = weights[k];
+				ac++;
+			}
+		if (ac == 0)
+			return -1;
+		std::string key(reinterpret_cast<const char*>(&a), sizeof(a));
+		auto it = index.find(key);
+		if (it != index.end())
+			return it->second;
+		maps.push_back(a);
+		index.emplace(key, int(maps.size()) - 1);
+		return int(maps.size()) - 1;
+	}
+};
+
+// The kernel descriptor of one batched mesh (device pointers); amap is patched by runBatch.
+BatchDesc makeDesc(const meshoptgpu_BatchMesh& m, const unsigned int* indices, const float* positions, const float* attributes,
+    const unsigned char* lock, unsigned int* out, AttrMaps& maps, int& attr_index)
+{
+	BatchDesc d{};
+	d.indices = indices;
+	d.positions = positions;
+	d.out = out;
+	d.index_count = unsigned(m.index_count);
+	d.vertex_count = unsigned(m.vertex_count);
+	d.stride_f = unsigned(m.vertex_positions_stride / 4);
+	d.target_index_count = unsigned(m.target_index_count);
+	d.target_error = m.target_error;
+	d.options = m.options;
+	d.lock = lock;
+	unsigned int ac = 0;
+	attr_index = m.attribute_count ? maps.add(m.attribute_weights, m.attribute_count, ac) : -1;
+	d.attributes = ac ? attributes : nullptr;
+	d.attr_stride_f = ac ? unsigned(m.vertex_attributes_stride / 4) : 0;
+	d.ac = ac;
+	d.amap = nullptr;
+	return d;
+}
+
+size_t descWorkspace(const BatchDesc& d)
+{
+	return batchWorkspaceBytes(d.index_count, d.vertex_count, d.ac, (d.options & kOptSparse) != 0);
+}
+
 // Runs descs (device pointers) through the persistent kernel; results in the same order.
-void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, std::vector<BatchResult>& results, cudaStream_t st)
+// attr_of[i] indexes maps.maps for descs[i] (-1: none).
+void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& maps, const std::vector<int>& attr_of, std::vector<BatchResult>& results,
+    cudaStream_t st)
 {
 	const size_t n = descs.size();
 	results.assign(n, BatchResult{0, 0.f, 0, 0});
@@ -295,7 +359,7 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, std::vector<BatchRe
 	for (size_t i = 0; i < n; ++i)
 	{
 		ordered[i] = descs[perm[i]];
-		size_t ws = batchWorkspaceBytes(ordered[i].index_count, ordered[i].vertex_count);
+		size_t ws = descWorkspace(ordered[i]);
 		(ws <= budget ? maxfit : maxslab) = std::max(ws <= budget ? maxfit : maxslab, ws);
 		maxidx = std::max<size_t>(maxidx, ordered[i].index_count);
 	}
@@ -303,12 +367,26 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, std::vector<BatchRe
 	int sms = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
 
-	size_t meta = align256(n * sizeof(BatchDesc)) + align256(n * sizeof(BatchResult)) + 256;
+	// device metadata: descriptors, results, the ticket, the attribute maps; descriptors and
+	// maps go up in one copy from pinned staging
+	const size_t nm = maps.maps.size();
+	const size_t off_res = align256(n * sizeof(BatchDesc)), off_ticket = off_res + align256(n * sizeof(BatchResult));
+	const size_t off_maps = off_ticket + 256;
+	size_t meta = off_maps + align256(nm * sizeof(BatchAttr));
 	char* mbase = static_cast<char*>(s.batch_meta.ensure(meta));
 	BatchDesc* d_descs = reinterpret_cast<BatchDesc*>(mbase);
-	BatchResult* d_res = reinterpret_cast<BatchResult*>(mbase + align256(n * sizeof(BatchDesc)));
-	unsigned int* d_ticket = reinterpret_cast<unsigned int*>(mbase + align256(n * sizeof(BatchDesc)) + align256(n * sizeof(BatchResult)));
-	MO_CUDA_CHECK(cudaMemcpyAsync(d_descs, ordered.data(), n * sizeof(BatchDesc), cudaMemcpyHostToDevice, st));
+	BatchResult* d_res = reinterpret_cast<BatchResult*>(mbase + off_res);
+	unsigned int* d_ticket = reinterpret_cast<unsigned int*>(mbase + off_ticket);
+	BatchAttr* d_maps = reinterpret_cast<BatchAttr*>(mbase + off_maps);
+	for (size_t i = 0; i < n; ++i)
+		ordered[i].amap = attr_of[perm[i]] >= 0 ? d_maps + attr_of[perm[i]] : nullptr;
+	char* hmeta = static_cast<char*>(s.batch_meta_host.ensure(meta));
+	memcpy(hmeta, ordered.data(), n * sizeof(BatchDesc));
+	if (nm)
+		memcpy(hmeta + off_maps, maps.maps.data(), nm * sizeof(BatchAttr));
+	MO_CUDA_CHECK(cudaMemcpyAsync(d_descs, hmeta, n * sizeof(BatchDesc), cudaMemcpyHostToDevice, st));
+	if (nm)
+		MO_CUDA_CHECK(cudaMemcpyAsync(d_maps, hmeta + off_maps, nm * sizeof(BatchAttr), cudaMemcpyHostToDevice, st));
 
 	auto launch = [&](int threads) {
 		int per_sm = std::max(1, batchBlocksPerSM(threads, smem));
@@ -362,21 +440,26 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, std::vector<BatchRe
 		results[perm[i]] = tmp[i];
 }
 
-std::string checkBatchMesh(const meshoptgpu_BatchMesh& m)
+// argument checks of a batched mesh: those of meshopt_simplifyEdge (:2348-2357), then the
+// batch kernel's option set unless the mesh may take the single-mesh path
+std::string checkBatchMesh(const meshoptgpu_BatchMesh& m, bool any_option = false)
 {
-	if (m.index_count % 3 != 0)
-		return "index_count must be a multiple of 3";
-	if (m.vertex_positions_stride < 12 || m.vertex_positions_stride > 256 || m.vertex_positions_stride % 4 != 0)
-		return "vertex_positions_stride must be in [12, 256] and a multiple of 4";
-	if (m.target_index_count > m.index_count)
-		return "target_index_count must not exceed index_count";
-	if (!(m.target_error >= 0))
-		return "target_error must be >= 0";
-	if (m.options & ~kBatchOptions)
-		return "batched meshes support LockBorder, ErrorAbsolute, Regularize and RegularizeLight only";
+	if (m.attribute_count && (!m.vertex_attributes || !m.attribute_weights))
+		return "vertex_attributes and attribute_weights are required when attribute_count > 0";
+	std::string bad = checkArgs(m.index_count, m.vertex_positions_stride, m.target_index_count, m.target_error, m.vertex_attributes_stride,
+	    m.attribute_weights, m.attribute_count, m.options);
+	if (!bad.empty())
+		return bad;
+	if (!any_option && (m.options & ~kBatchOptions))
+		return "batched meshes support every option but Prune and InternalDebug";
 	if (m.index_count >= (size_t(1) << 32) || m.vertex_count >= (size_t(1) << 32))
 		return "batched meshes must have fewer than 2^32 indices and vertices";
 	return std::string();
+}
+
+int batchCheckStatus(const meshoptgpu_BatchMesh& m, bool any_option = false)
+{
+	return (m.options & ~(any_option ? kSupportedOptions : kBatchOptions)) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
 }
 
 int finishBatch(const std::vector<BatchResult>& res, size_t* counts, float* errors)
@@ -405,6 +488,7 @@ int finishBatch(const std::vector<BatchResult>& res, size_t* counts, float* erro
 struct ServerRequest
 {
 	BatchDesc desc;
+	std::vector<float> weights; // attribute weights, copied at submission
 	size_t index_count = 0, vertex_count = 0;
 	size_t reserve = 0;
 	std::chrono::steady_clock::time_point submitted, completed;
@@ -435,7 +519,7 @@ const size_t kServerBudgetDefault = size_t(40) << 30;
 // fit shared memory hold none) or on the single-mesh path (its arena)
 size_t batchReserve(const ServerRequest& r)
 {
-	size_t ws = batchWorkspaceBytes(r.index_count, r.vertex_count);
+	size_t ws = descWorkspace(r.desc);
 	return ws <= kBatchSmemDefault ? 4096 : ws;
 }
 
@@ -497,13 +581,20 @@ void batchWorker(ServerImpl* S)
 			S->batches++;
 		}
 		std::vector<BatchDesc> descs(take.size());
+		std::vector<int> attr_of(take.size(), -1);
+		AttrMaps maps;
 		for (size_t i = 0; i < take.size(); ++i)
+		{
 			descs[i] = take[i]->desc;
+			unsigned int ac = 0;
+			if (!take[i]->weights.empty())
+				attr_of[i] = maps.add(take[i]->weights.data(), take[i]->weights.size(), ac);
+		}
 		std::vector<BatchResult> res;
 		try
 		{
 			ts.ensure();
-			runBatch(ts, descs, res, ts.stream);
+			runBatch(ts, descs, maps, attr_of, res, ts.stream);
 			for (size_t i = 0; i < take.size(); ++i)
 			{
 				take[i]->result_count = res[i].index_count;
@@ -568,6 +659,14 @@ void largeWorker(ServerImpl* S)
 			m.target_index_count = r->desc.target_index_count;
 			m.target_error = r->desc.target_error;
 			m.options = r->desc.options;
+			m.lock = r->desc.lock;
+			if (!r->weights.empty())
+			{
+				m.attributes = r->desc.attributes;
+				m.attributes_stride = size_t(r->desc.attr_stride_f) * 4;
+				m.weights = r->weights.data();
+				m.attribute_count = r->weights.size();
+			}
 			RunResult rr = ts.simplifier->run(m, r->desc.out, ts.stream);
 			r->result_count = rr.index_count;
 			r->result_error = rr.result_error;
@@ -594,7 +693,7 @@ int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, size_t mesh_cou
 		std::string bad = checkBatchMesh(meshes[i]);
 		if (!bad.empty())
 		{
-			int st = (meshes[i].options & ~kBatchOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+			int st = batchCheckStatus(meshes[i]);
 			setStatus(st, "mesh " + std::to_string(i) + ": " + bad);
 			return st;
 		}
@@ -604,14 +703,15 @@ int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, size_t mesh_cou
 		ThreadState& s = state();
 		s.ensure();
 		std::vector<BatchDesc> descs(mesh_count);
+		std::vector<int> attr_of(mesh_count);
+		AttrMaps maps;
 		for (size_t i = 0; i < mesh_count; ++i)
 		{
 			const meshoptgpu_BatchMesh& m = meshes[i];
-			descs[i] = BatchDesc{m.indices, m.vertex_positions, m.destination, unsigned(m.index_count), unsigned(m.vertex_count),
-			    unsigned(m.vertex_positions_stride / 4), unsigned(m.target_index_count), m.target_error, m.options};
+			descs[i] = makeDesc(m, m.indices, m.vertex_positions, m.vertex_attributes, m.vertex_lock, m.destination, maps, attr_of[i]);
 		}
 		std::vector<BatchResult> res;
-		runBatch(s, descs, res, static_cast<cudaStream_t>(stream));
+		runBatch(s, descs, maps, attr_of, res, static_cast<cudaStream_t>(stream));
 		return finishBatch(res, result_index_counts, result_errors);
 	}
 	catch (const std::exception& e)
@@ -628,7 +728,7 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		std::string bad = checkBatchMesh(meshes[i]);
 		if (!bad.empty())
 		{
-			int st = (meshes[i].options & ~kBatchOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+			int st = batchCheckStatus(meshes[i]);
 			setStatus(st, "mesh " + std::to_string(i) + ": " + bad);
 			return st;
 		}
@@ -637,38 +737,62 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 	{
 		ThreadState& s = state();
 		s.ensure();
-		// pack inputs: per mesh indices then positions (16-byte aligned), outputs after all inputs
-		std::vector<size_t> off_idx(mesh_count), off_pos(mesh_count), off_out(mesh_count);
+		// pack inputs into one pinned buffer (16-byte aligned pieces): per mesh its indices, and
+		// every distinct vertex, attribute and lock array once (meshes of a sparse group share
+		// them); outputs follow all inputs on the device
 		size_t in_bytes = 0, out_words = 0;
+		std::map<std::pair<const void*, size_t>, size_t> shared;
+		std::vector<std::pair<const void*, size_t>> pieces; // (source, bytes) in pack order
+		auto place = [&](const void* p, size_t bytes, bool dedupe) -> size_t {
+			if (!p || !bytes)
+				return ~size_t(0);
+			if (dedupe)
+			{
+				auto it = shared.find({p, bytes});
+				if (it != shared.end())
+					return it->second;
+			}
+			size_t at = in_bytes;
+			in_bytes = (in_bytes + bytes + 15) & ~size_t(15);
+			pieces.push_back({p, bytes});
+			if (dedupe)
+				shared.emplace(std::make_pair(p, bytes), at);
+			return at;
+		};
+		std::vector<size_t> off_idx(mesh_count), off_pos(mesh_count), off_attr(mesh_count), off_lock(mesh_count), off_out(mesh_count);
 		for (size_t i = 0; i < mesh_count; ++i)
 		{
-			off_idx[i] = in_bytes;
-			in_bytes = (in_bytes + meshes[i].index_count * 4 + 15) & ~size_t(15);
-			off_pos[i] = in_bytes;
-			in_bytes = (in_bytes + meshes[i].vertex_count * meshes[i].vertex_positions_stride + 15) & ~size_t(15);
+			const meshoptgpu_BatchMesh& m = meshes[i];
+			off_idx[i] = place(m.indices, m.index_count * 4, false);
+			off_pos[i] = place(m.vertex_positions, m.vertex_count * m.vertex_positions_stride, true);
+			off_attr[i] = m.attribute_count ? place(m.vertex_attributes, m.vertex_count * m.vertex_attributes_stride, true) : ~size_t(0);
+			off_lock[i] = place(m.vertex_lock, m.vertex_count, true);
 			off_out[i] = out_words;
-			out_words += meshes[i].index_count;
+			out_words += m.index_count;
 		}
 		char* h = static_cast<char*>(s.batch_host.ensure(in_bytes + 16));
-		for (size_t i = 0; i < mesh_count; ++i)
 		{
-			memcpy(h + off_idx[i], meshes[i].indices, meshes[i].index_count * 4);
-			memcpy(h + off_pos[i], meshes[i].vertex_positions, meshes[i].vertex_count * meshes[i].vertex_positions_stride);
+			size_t at = 0;
+			for (auto& pc : pieces)
+			{
+				memcpy(h + at, pc.first, pc.second);
+				at = (at + pc.second + 15) & ~size_t(15);
+			}
 		}
 		char* d = static_cast<char*>(s.batch_io.ensure(align256(in_bytes) + out_words * 4 + 256));
 		unsigned int* d_out = reinterpret_cast<unsigned int*>(d + align256(in_bytes));
 		cudaStream_t st = s.stream;
 		MO_CUDA_CHECK(cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, st));
 		std::vector<BatchDesc> descs(mesh_count);
+		std::vector<int> attr_of(mesh_count);
+		AttrMaps maps;
+		auto at = [&](size_t off) { return off == ~size_t(0) ? nullptr : d + off; };
 		for (size_t i = 0; i < mesh_count; ++i)
-		{
-			const meshoptgpu_BatchMesh& m = meshes[i];
-			descs[i] = BatchDesc{reinterpret_cast<const unsigned int*>(d + off_idx[i]), reinterpret_cast<const float*>(d + off_pos[i]), d_out + off_out[i],
-			    unsigned(m.index_count), unsigned(m.vertex_count), unsigned(m.vertex_positions_stride / 4), unsigned(m.target_index_count), m.target_error,
-			    m.options};
-		}
+			descs[i] = makeDesc(meshes[i], reinterpret_cast<const unsigned int*>(at(off_idx[i])), reinterpret_cast<const float*>(at(off_pos[i])),
+			    reinterpret_cast<const float*>(at(off_attr[i])), reinterpret_cast<const unsigned char*>(at(off_lock[i])), d_out + off_out[i], maps,
+			    attr_of[i]);
 		std::vector<BatchResult> res;
-		runBatch(s, descs, res, st);
+		runBatch(s, descs, maps, attr_of, res, st);
 		// results back in one copy (the packed outputs), then scattered to the callers' buffers
 		unsigned int* hout = static_cast<unsigned int*>(s.batch_host.ensure(std::max(in_bytes + 16, out_words * 4 + 16)));
 		MO_CUDA_CHECK(cudaMemcpyAsync(hout, d_out, out_words * 4, cudaMemcpyDeviceToHost, st));
@@ -737,22 +861,26 @@ long long meshoptgpu_serverSubmit(meshoptgpu_Server* server, const meshoptgpu_Ba
 	if (!server || !mesh)
 		return -meshoptgpu_StatusInvalidArgument;
 	ServerImpl* S = reinterpret_cast<ServerImpl*>(server);
-	std::string bad = checkBatchMesh(*mesh);
+	std::string bad = checkBatchMesh(*mesh, true);
 	if (!bad.empty())
 	{
-		int st = (mesh->options & ~kBatchOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument;
+		int st = batchCheckStatus(*mesh, true);
 		setStatus(st, bad);
 		return -st;
 	}
 	std::unique_ptr<ServerRequest> r(new ServerRequest());
-	r->desc = BatchDesc{mesh->indices, mesh->vertex_positions, mesh->destination, unsigned(mesh->index_count), unsigned(mesh->vertex_count),
-	    unsigned(mesh->vertex_positions_stride / 4), unsigned(mesh->target_index_count), mesh->target_error, mesh->options};
+	AttrMaps unused;
+	int attr_index = -1;
+	r->desc = makeDesc(*mesh, mesh->indices, mesh->vertex_positions, mesh->vertex_attributes, mesh->vertex_lock, mesh->destination, unused, attr_index);
+	if (r->desc.ac)
+		r->weights.assign(mesh->attribute_weights, mesh->attribute_weights + mesh->attribute_count);
 	r->index_count = mesh->index_count;
 	r->vertex_count = mesh->vertex_count;
 	// meshes up to large_index_count indices go to the batch kernel (one CTA per mesh, shared
-	// memory or a global slab); larger ones take the multi-CTA single-mesh path
-	bool large = S->cfg.plain || mesh->index_count > S->cfg.large_index_count;
-	r->reserve = large ? Simplifier::workspaceBytes(mesh->index_count, mesh->vertex_count, 0) : batchReserve(*r);
+	// memory or a global slab); larger ones, and the options the batch kernel does not have,
+	// take the multi-CTA single-mesh path
+	bool large = S->cfg.plain || mesh->index_count > S->cfg.large_index_count || (mesh->options & ~kBatchOptions);
+	r->reserve = large ? Simplifier::workspaceBytes(mesh->index_count, mesh->vertex_count, r->desc.ac) : batchReserve(*r);
 	if (r->reserve > S->cfg.memory_budget)
 	{
 		setStatus(meshoptgpu_StatusOutOfMemory, "request needs more device scratch than the server's memory budget");

@@ -670,60 +670,6 @@ __global__ void kRescaleAttributes(const float* __restrict__ data, size_t stride
 		out[i * am.count + k] = data[i * stride_f + am.src[k]] * am.weight[k];
 }
 
-// quadricFromAttributes :870-950 for one face, accumulated into Q/G of one vertex
-template <int MAXA>
-__device__ __forceinline__ void addAttributeQuadric(Quadric& Qacc, float4* Gacc, int count, const V3& p0, const V3& p1, const V3& p2,
-    const float* __restrict__ va0, const float* __restrict__ va1, const float* __restrict__ va2)
-{
-	V3 p10 = {p1.x - p0.x, p1.y - p0.y, p1.z - p0.z};
-	V3 p20 = {p2.x - p0.x, p2.y - p0.y, p2.z - p0.z};
-	V3 nn = {p10.y * p20.z - p10.z * p20.y, p10.z * p20.x - p10.x * p20.z, p10.x * p20.y - p10.y * p20.x};
-	float area = sqrtf(nn.x * nn.x + nn.y * nn.y + nn.z * nn.z) * 0.5f;
-	float w = area;
-	const V3& v0 = p10;
-	const V3& v1 = p20;
-	float d00 = v0.x * v0.x + v0.y * v0.y + v0.z * v0.z;
-	float d01 = v0.x * v1.x + v0.y * v1.y + v0.z * v1.z;
-	float d11 = v1.x * v1.x + v1.y * v1.y + v1.z * v1.z;
-	float denom = d00 * d11 - d01 * d01;
-	float denomr = denom == 0 ? 0.f : 1.f / denom;
-	float gx1 = (d11 * v0.x - d01 * v1.x) * denomr;
-	float gx2 = (d00 * v1.x - d01 * v0.x) * denomr;
-	float gy1 = (d11 * v0.y - d01 * v1.y) * denomr;
-	float gy2 = (d00 * v1.y - d01 * v0.y) * denomr;
-	float gz1 = (d11 * v0.z - d01 * v1.z) * denomr;
-	float gz2 = (d00 * v1.z - d01 * v0.z) * denomr;
-
-	Quadric Q = qzero();
-	Q.w = w;
-#pragma unroll
-	for (int k = 0; k < MAXA; ++k)
-	{
-		if (k >= count)
-			break;
-		float a0 = va0[k], a1 = va1[k], a2 = va2[k];
-		float gx = gx1 * (a1 - a0) + gx2 * (a2 - a0);
-		float gy = gy1 * (a1 - a0) + gy2 * (a2 - a0);
-		float gz = gz1 * (a1 - a0) + gz2 * (a2 - a0);
-		float gw = a0 - p0.x * gx - p0.y * gy - p0.z * gz;
-		Q.a00 += w * (gx * gx);
-		Q.a11 += w * (gy * gy);
-		Q.a22 += w * (gz * gz);
-		Q.a10 += w * (gy * gx);
-		Q.a20 += w * (gz * gx);
-		Q.a21 += w * (gz * gy);
-		Q.b0 += w * (gx * gw);
-		Q.b1 += w * (gy * gw);
-		Q.b2 += w * (gz * gw);
-		Q.c += w * (gw * gw);
-		Gacc[k].x += w * gx;
-		Gacc[k].y += w * gy;
-		Gacc[k].z += w * gz;
-		Gacc[k].w += w * gw;
-	}
-	qadd(Qacc, Q);
-}
-
 // fillAttributeQuadrics :1159-1179 per raw vertex v over its faces in face order
 template <int MAXA>
 __global__ void kFillAttributeQuadrics(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ off, const unsigned int* __restrict__ csr,
@@ -871,19 +817,6 @@ __global__ void kPickEmit(const unsigned int* __restrict__ res, size_t tris, con
 }
 
 // ---------------------------------------------------------------- pass: rank
-
-__device__ __forceinline__ float qerrorAttr(const Quadric& Q, const float4* __restrict__ G, int count, const V3& v, const float* __restrict__ va)
-{
-	float r = qeval(Q, v);
-	for (int k = 0; k < count; ++k)
-	{
-		float a = va[k];
-		float4 g4 = G[k];
-		float g = v.x * g4.x + v.y * g4.y + v.z * g4.z + g4.w;
-		r += a * (a * Q.w - 2 * g);
-	}
-	return fabsf(r);
-}
 
 // rankEdgeCollapses :1374-1450, one candidate per thread; also writes the 12-bit sort key
 __global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr,

@@ -214,6 +214,37 @@ def sphere_patches(count: int = 4096, seed: int = 3, tmin: int = 200, tmax: int 
     return out
 
 
+def cluster_groups(levels: int = 7, group_tris: int = 1024, seed: int = 2, protect_seams: bool = True):
+    """Cluster-LOD style groups over one shared vertex buffer: the octahedron sphere (normals +
+    UV, seam split) cut into groups of ``group_tris`` triangles in latitude/longitude order.
+
+    As a cluster-LOD builder prepares one level (demo/clusterlod.h lockBoundary), every
+    position that two groups share is locked (bit 0 of vertex_lock) and, with protect_seams,
+    vertices whose position has a duplicate with different attributes are protected (bit 1).
+    Returns (groups: list of uint32 index arrays into the shared buffer, positions float32 [V,3],
+    attributes float32 [V,5], weights float32 [5], lock uint8 [V])."""
+    idx, pos, attr, w = octa_sphere(levels, seed=seed)
+    tri = idx.reshape(-1, 3).astype(np.int64)
+    c = pos[tri].mean(axis=1).astype(np.float64)
+    theta = np.arccos(np.clip(c[:, 2] / np.linalg.norm(c, axis=1), -1.0, 1.0))
+    phi = np.arctan2(c[:, 1], c[:, 0])
+    bands = max(1, int(round(math.sqrt(len(tri) / group_tris))))
+    band = np.minimum((theta / math.pi * bands).astype(np.int64), bands - 1)
+    order = np.lexsort((phi, band))
+    groups = [np.ascontiguousarray(tri[order[g:g + group_tris]].reshape(-1), dtype=np.uint32) for g in range(0, len(order), group_tris)]
+    # position remap: the smallest vertex with the same position
+    _, first, inv = np.unique(pos, axis=0, return_index=True, return_inverse=True)
+    inv = inv.reshape(-1)
+    remap = first[inv]
+    count = np.zeros(len(pos), np.int64)
+    for g in groups:
+        count[np.unique(remap[g])] += 1
+    lock = (count[remap] > 1).astype(np.uint8)
+    if protect_seams:
+        lock |= np.where(np.any(attr != attr[remap], axis=1), 2, 0).astype(np.uint8)
+    return groups, pos, attr, w, lock
+
+
 def lognormal_sizes(count: int, seed: int = 4, median: float = 20000.0, sigma: float = 1.0, lo: int = 1000, hi: int = 1000000):
     """Request triangle counts: lognormal(median, sigma) clipped to [lo, hi]."""
     z = normal(seed, count)
