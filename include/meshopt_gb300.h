@@ -210,6 +210,24 @@ MESHOPTGPU_API void meshoptgpu_getKernelProfile(unsigned long long* launches, do
 /* Bytes of device scratch one call on a mesh of this shape needs (for admission control). */
 MESHOPTGPU_API size_t meshoptgpu_workspaceBytes(size_t index_count, size_t vertex_count, size_t attribute_count);
 
+/* ---- compaction after simplification, on device data ---- */
+
+/* Device forms of meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch
+ * (meshoptimizer.h; src/vfetchoptimizer.cpp:7-71) and meshopt_generatePositionRemap
+ * (src/indexgenerator.cpp:555-578), for callers that keep the simplified mesh in HBM: every
+ * buffer is a DEVICE pointer, the work is queued on `stream` (a cudaStream_t or NULL) and the
+ * call returns once the result is known. Results equal the reference's. The fetch functions
+ * return the number of used vertices; on invalid input (an index >= vertex_count, a
+ * vertex_size outside 1..256) or a CUDA error they return 0 and set the status read by
+ * meshoptgpu_getLastStatus. optimizeVertexFetch allows destination == vertices (other
+ * overlaps are not supported) and rewrites indices in place. */
+MESHOPTGPU_API size_t meshoptgpu_optimizeVertexFetchRemapDevice(unsigned int* destination, const unsigned int* indices, size_t index_count,
+    size_t vertex_count, void* stream);
+MESHOPTGPU_API size_t meshoptgpu_optimizeVertexFetchDevice(void* destination, unsigned int* indices, size_t index_count, const void* vertices,
+    size_t vertex_count, size_t vertex_size, void* stream);
+MESHOPTGPU_API int meshoptgpu_generatePositionRemapDevice(unsigned int* destination, const float* vertex_positions, size_t vertex_count,
+    size_t vertex_positions_stride, void* stream);
+
 /* Allocation-free mesh extent. No counterpart in the reference: it is the device-pointer
  * form of meshopt_simplifyScale for callers that must not allocate device memory while they
  * run (work recorded into a CUDA graph, a frame loop with a fixed memory budget, a plugin

@@ -48,6 +48,7 @@ EXPORTS = [
     "meshoptgpu_simplifyBatch", "meshoptgpu_simplifyBatchHost", "meshoptgpu_setBatchConfig", "meshoptgpu_getBatchThreads",
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
+    "meshoptgpu_optimizeVertexFetchRemapDevice", "meshoptgpu_optimizeVertexFetchDevice", "meshoptgpu_generatePositionRemapDevice",
 ]
 
 
@@ -125,6 +126,12 @@ def load():
     lib.meshoptgpu_serverStats.argtypes = [vp, vp]
     lib.meshoptgpu_simplifyScaleNoAlloc.restype = C.c_int
     lib.meshoptgpu_simplifyScaleNoAlloc.argtypes = [vp, vp, sz, sz, vp]
+    lib.meshoptgpu_optimizeVertexFetchRemapDevice.restype = sz
+    lib.meshoptgpu_optimizeVertexFetchRemapDevice.argtypes = [vp, vp, sz, sz, vp]
+    lib.meshoptgpu_optimizeVertexFetchDevice.restype = sz
+    lib.meshoptgpu_optimizeVertexFetchDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp]
+    lib.meshoptgpu_generatePositionRemapDevice.restype = C.c_int
+    lib.meshoptgpu_generatePositionRemapDevice.argtypes = [vp, vp, sz, sz, vp]
     _lib = lib
     return lib
 
@@ -345,6 +352,35 @@ def simplify_batch_device(descs, stream=0, check=True):
     if check and st != STATUS_OK:
         raise SimplifyError(st, last_status()[1])
     return counts[:n], errs[:n]
+
+
+def optimize_vertex_fetch_remap_device(d_destination, d_indices, index_count, vertex_count, stream=0, check=True):
+    """meshoptgpu_optimizeVertexFetchRemapDevice: new index per vertex in order of first use
+    (~0u unused) written to d_destination; returns the used vertex count."""
+    n = load().meshoptgpu_optimizeVertexFetchRemapDevice(d_destination, d_indices, index_count, vertex_count, C.c_void_p(stream or None))
+    st, msg = last_status()
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, msg)
+    return int(n)
+
+
+def optimize_vertex_fetch_device(d_destination, d_indices, index_count, d_vertices, vertex_count, vertex_size, stream=0, check=True):
+    """meshoptgpu_optimizeVertexFetchDevice: vertices in order of first use to d_destination (may be
+    d_vertices), indices rewritten in place; returns the used vertex count."""
+    n = load().meshoptgpu_optimizeVertexFetchDevice(d_destination, d_indices, index_count, d_vertices, vertex_count, vertex_size,
+                                                   C.c_void_p(stream or None))
+    st, msg = last_status()
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, msg)
+    return int(n)
+
+
+def generate_position_remap_device(d_destination, d_positions, vertex_count, positions_stride=12, stream=0, check=True):
+    """meshoptgpu_generatePositionRemapDevice: smallest vertex with an equal position, per vertex."""
+    st = load().meshoptgpu_generatePositionRemapDevice(d_destination, d_positions, vertex_count, positions_stride, C.c_void_p(stream or None))
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, last_status()[1])
+    return int(st)
 
 
 def set_batch_config(threads=0, smem_bytes=0):

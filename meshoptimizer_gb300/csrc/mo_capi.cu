@@ -10,6 +10,7 @@
 #include "mo_probe.cuh"
 #include "mo_simplify.cuh"
 #include "mo_batch.cuh"
+#include "mo_vfetch.cuh"
 
 #include <chrono>
 #include <condition_variable>
@@ -90,7 +91,7 @@ struct ThreadState
 	PhaseTimes times;
 	bool timing = false;
 	// batched path
-	DeviceBuffer batch_meta, batch_slabs, batch_io;
+	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch;
 	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
 	unsigned int batch_smem = 0;    // 0: default budget
@@ -800,6 +801,116 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		for (size_t i = 0; i < mesh_count; ++i)
 			memcpy(meshes[i].destination, hout + off_out[i], size_t(res[i].index_count) * 4);
 		return finishBatch(res, result_index_counts, result_errors);
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
+size_t meshoptgpu_optimizeVertexFetchRemapDevice(unsigned int* destination, const unsigned int* indices, size_t index_count, size_t vertex_count,
+    void* stream)
+{
+	try
+	{
+		if (vertex_count && !destination)
+			throw std::invalid_argument("destination is required");
+		if (vertex_count >= (size_t(1) << 32) || index_count >= (size_t(1) << 32))
+			throw std::invalid_argument("counts must be below 2^32");
+		ThreadState& s = state();
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		unsigned int* scratch = static_cast<unsigned int*>(s.compact_scratch.ensure((vertexOrderScratchWords(index_count, vertex_count) + 64) * 4));
+		unsigned int* counters = scratch + vertexOrderScratchWords(index_count, vertex_count);
+		vertexOrder(destination, indices, index_count, vertex_count, scratch, counters, st);
+		unsigned int h[2];
+		MO_CUDA_CHECK(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		probe().collect();
+		if (h[1])
+			throw std::invalid_argument("an index is out of range of vertex_count");
+		setStatus(meshoptgpu_StatusOk, "");
+		return h[0];
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return 0;
+	}
+}
+
+size_t meshoptgpu_optimizeVertexFetchDevice(void* destination, unsigned int* indices, size_t index_count, const void* vertices, size_t vertex_count,
+    size_t vertex_size, void* stream)
+{
+	try
+	{
+		if (vertex_size == 0 || vertex_size > 256)
+			throw std::invalid_argument("vertex_size must be in [1, 256]");
+		if (vertex_count >= (size_t(1) << 32) || index_count >= (size_t(1) << 32))
+			throw std::invalid_argument("counts must be below 2^32");
+		ThreadState& s = state();
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		// scratch: the order table, the vertex-order scratch, counters, and for an in-place call
+		// a copy of the vertices
+		const size_t ow = (vertex_count + 63) & ~size_t(63), sw = vertexOrderScratchWords(index_count, vertex_count);
+		const size_t copy_bytes = destination == vertices ? vertex_count * vertex_size : 0;
+		char* base = static_cast<char*>(s.compact_scratch.ensure((ow + sw + 64) * 4 + copy_bytes + 256));
+		unsigned int* order = reinterpret_cast<unsigned int*>(base);
+		unsigned int* scratch = order + ow;
+		unsigned int* counters = scratch + sw;
+		const void* src = vertices;
+		if (copy_bytes)
+		{
+			void* copy = base + (ow + sw + 64) * 4;
+			MO_CUDA_CHECK(cudaMemcpyAsync(copy, vertices, copy_bytes, cudaMemcpyDeviceToDevice, st));
+			src = copy;
+		}
+		vertexOrder(order, indices, index_count, vertex_count, scratch, counters, st);
+		unsigned int h[2];
+		MO_CUDA_CHECK(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		if (h[1])
+		{
+			probe().collect();
+			throw std::invalid_argument("an index is out of range of vertex_count");
+		}
+		moveVertices(destination, src, vertex_count, vertex_size, order, st);
+		rewriteIndices(indices, index_count, order, st);
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		probe().collect();
+		setStatus(meshoptgpu_StatusOk, "");
+		return h[0];
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return 0;
+	}
+}
+
+int meshoptgpu_generatePositionRemapDevice(unsigned int* destination, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
+    void* stream)
+{
+	try
+	{
+		if (vertex_positions_stride < 12 || vertex_positions_stride > 256 || vertex_positions_stride % 4 != 0)
+			throw std::invalid_argument("vertex_positions_stride must be in [12, 256] and a multiple of 4");
+		if (vertex_count >= (size_t(1) << 32))
+			throw std::invalid_argument("vertex_count must be below 2^32");
+		ThreadState& s = state();
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		const size_t sw = positionRemapScratchWords(vertex_count);
+		unsigned int* scratch = static_cast<unsigned int*>(s.compact_scratch.ensure((sw + 64) * 4));
+		unsigned int* counters = scratch + sw;
+		positionRemap(destination, vertex_positions, vertex_count, vertex_positions_stride / 4, scratch, counters, st);
+		unsigned int h[2];
+		MO_CUDA_CHECK(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		probe().collect();
+		if (h[1])
+			throw std::runtime_error("position table overflow");
+		setStatus(meshoptgpu_StatusOk, "");
+		return meshoptgpu_StatusOk;
 	}
 	catch (const std::exception& e)
 	{

@@ -80,3 +80,53 @@ float mo_simplifyScale(const float* vertex_positions, size_t vertex_count, size_
 {
 	return rescale_positions_f32(NULL, vertex_positions, vertex_count, vertex_positions_stride / sizeof(float), NULL);
 }
+
+/* ---- the step after the simplifier in its callers (compaction of the vertex buffer) ---- */
+
+/* meshopt_optimizeVertexFetchRemap (src/vfetchoptimizer.cpp:7-26): each vertex's new index in
+ * order of first use by the index buffer, ~0u for unused vertices; returns the used count */
+size_t mo_optimizeVertexFetchRemap(unsigned int* destination, const unsigned int* indices, size_t index_count, size_t vertex_count)
+{
+	unsigned int used = 0;
+	memset(destination, 0xff, vertex_count * sizeof(unsigned int));
+	for (size_t i = 0; i < index_count; ++i)
+	{
+		unsigned int* slot = &destination[indices[i]];
+		if (*slot == ~0u)
+			*slot = used++;
+	}
+	return used;
+}
+
+/* meshopt_optimizeVertexFetch (src/vfetchoptimizer.cpp:28-71): vertices copied in order of first
+ * use, indices rewritten in place; destination may be vertices */
+size_t mo_optimizeVertexFetch(void* destination, unsigned int* indices, size_t index_count, const void* vertices, size_t vertex_count, size_t vertex_size)
+{
+	unsigned char* copy = NULL;
+	if (destination == vertices)
+	{
+		copy = (unsigned char*)malloc(vertex_count * vertex_size + 1);
+		memcpy(copy, vertices, vertex_count * vertex_size);
+		vertices = copy;
+	}
+	unsigned int* order = (unsigned int*)malloc((vertex_count ? vertex_count : 1) * sizeof(unsigned int));
+	size_t used = mo_optimizeVertexFetchRemap(order, indices, index_count, vertex_count);
+	for (size_t v = 0; v < vertex_count; ++v)
+		if (order[v] != ~0u)
+			memcpy((unsigned char*)destination + (size_t)order[v] * vertex_size, (const unsigned char*)vertices + v * vertex_size, vertex_size);
+	for (size_t i = 0; i < index_count; ++i)
+		indices[i] = order[indices[i]];
+	free(order);
+	free(copy);
+	return used;
+}
+
+/* meshopt_generatePositionRemap (src/indexgenerator.cpp:555-578): the smallest vertex index
+ * whose position compares equal (float ==) to each vertex's; the remap half of the
+ * simplifier's position remap */
+void mo_generatePositionRemap(unsigned int* destination, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride)
+{
+	unsigned int* wedge = (unsigned int*)malloc((vertex_count ? vertex_count : 1) * sizeof(unsigned int));
+	mo_position_remap(destination, wedge, vertex_positions, vertex_count, vertex_positions_stride / sizeof(float), NULL);
+	free(wedge);
+}

@@ -106,6 +106,13 @@ size_t mo_simplify_edge_f64(unsigned int* destination, const unsigned int* indic
     const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options,
     double* result_error, mo_stats* stats);
 
+/* The compaction step after the simplifier in its callers: same signatures as
+ * meshoptimizer.h's meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch and
+ * meshopt_generatePositionRemap. */
+size_t mo_optimizeVertexFetchRemap(unsigned int* destination, const unsigned int* indices, size_t index_count, size_t vertex_count);
+size_t mo_optimizeVertexFetch(void* destination, unsigned int* indices, size_t index_count, const void* vertices, size_t vertex_count, size_t vertex_size);
+void mo_generatePositionRemap(unsigned int* destination, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride);
+
 #ifdef __cplusplus
 }
 #endif

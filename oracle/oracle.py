@@ -207,6 +207,52 @@ def simplify(kind, indices, positions, target_index_count, target_error, options
     return out[:n].copy(), float(err.value)
 
 
+def _bind_compaction(o, prefix):
+    lib = o.lib
+    r = getattr(lib, prefix + "optimizeVertexFetchRemap")
+    r.restype = C.c_size_t
+    r.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t]
+    f = getattr(lib, prefix + "optimizeVertexFetch")
+    f.restype = C.c_size_t
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t]
+    g = getattr(lib, prefix + "generatePositionRemap")
+    g.restype = None
+    g.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t]
+    return r, f, g
+
+
+def optimize_vertex_fetch_remap(kind, indices, vertex_count):
+    """meshopt_optimizeVertexFetchRemap: (remap uint32 [vertex_count], used count)."""
+    o = load(kind)
+    r, _, _ = _bind_compaction(o, "mo_" if kind == "port" else "meshopt_")
+    indices = np.ascontiguousarray(indices, dtype=np.uint32)
+    out = np.zeros(max(vertex_count, 1), np.uint32)
+    n = r(_ptr(out), _ptr(indices), len(indices), vertex_count)
+    return out[:vertex_count], int(n)
+
+
+def optimize_vertex_fetch(kind, indices, vertices):
+    """meshopt_optimizeVertexFetch on a [V, k] array of vertices (any dtype, one row per vertex):
+    returns (new indices, new vertices[:used], used)."""
+    o = load(kind)
+    _, f, _ = _bind_compaction(o, "mo_" if kind == "port" else "meshopt_")
+    idx = np.array(indices, dtype=np.uint32, copy=True)
+    verts = np.ascontiguousarray(vertices)
+    dst = np.zeros_like(verts)
+    n = f(_ptr(dst), _ptr(idx), len(idx), _ptr(verts), verts.shape[0], verts.strides[0] if verts.ndim > 1 else verts.itemsize)
+    return idx, dst[:n], int(n)
+
+
+def generate_position_remap(kind, positions):
+    """meshopt_generatePositionRemap: uint32 [V]."""
+    o = load(kind)
+    _, _, g = _bind_compaction(o, "mo_" if kind == "port" else "meshopt_")
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    out = np.zeros(max(positions.shape[0], 1), np.uint32)
+    g(_ptr(out), _ptr(positions), positions.shape[0], positions.shape[1] * 4)
+    return out[:positions.shape[0]]
+
+
 def simplify_scale(kind, positions):
     o = load(kind)
     positions = np.ascontiguousarray(positions, dtype=np.float32)

@@ -34,3 +34,14 @@ def seeded_cases():
             d[k] = z[key] if key in z else None
         out.append(d)
     return out
+
+
+def compaction_cases():
+    z = np.load(os.path.join(GOLDEN, "compaction_cases.npz"))
+    out = []
+    for i in range(int(z["count"])):
+        prefix = f"{i}_"
+        d = {k[len(prefix):]: z[k] for k in z.files if k.startswith(prefix)}
+        d["kind"] = str(d["kind"])
+        out.append(d)
+    return out

@@ -14,6 +14,9 @@ It writes two files next to this script:
   the assertion the reference test makes (exact buffer, count or error bound).
 * ``seeded_cases.npz`` -- seeded synthetic meshes (heightfields, attribute spheres,
   lock-border patches, random lattice soups) with the reference library's outputs.
+* ``compaction_cases.npz`` -- seeded inputs of the compaction step after the simplifier
+  (meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch,
+  meshopt_generatePositionRemap) with the reference library's outputs.
 
 The GPU machine has no reference tree; these fixtures carry its results there.
 """
@@ -251,6 +254,38 @@ def seeded_cases():
     return cases
 
 
+def compaction_cases():
+    """Seeded inputs for meshopt_optimizeVertexFetchRemap / meshopt_optimizeVertexFetch /
+    meshopt_generatePositionRemap: index soups with unused vertices, a simplified heightfield,
+    an empty index buffer, vertex sizes 1..256 bytes, positions with duplicates, -0 and NaN."""
+    rng = np.random.default_rng(2024)
+    cases = []
+    for vc, ic, size in ((1, 3, 12), (17, 30, 7), (1000, 2400, 16), (300, 0, 4), (600, 3000, 256), (64, 96, 1)):
+        idx = rng.integers(0, vc, size=ic).astype(np.uint32)
+        verts = rng.integers(0, 256, size=(vc, size)).astype(np.uint8)
+        cases.append(dict(kind="fetch", indices=idx, vertices=verts))
+    hi, hp = W.heightfield(64, seed=9)
+    out, _ = oracle.simplify("reference", hi, hp, W.target_count(len(hi), 0.2), 1e-2, 0)
+    cases.append(dict(kind="fetch", indices=out, vertices=np.ascontiguousarray(hp).view(np.uint8).reshape(len(hp), 12)))
+    for vc, k in ((1, 3), (200, 3), (3000, 4), (777, 8)):
+        pos = rng.integers(-2, 3, size=(vc, k)).astype(np.float32) * 0.5
+        pos[rng.random(vc) < 0.05, 0] = np.nan
+        pos[rng.random(vc) < 0.1, 1] = -0.0
+        cases.append(dict(kind="remap", positions=pos))
+    for c in cases:
+        if c["kind"] == "fetch":
+            vc = c["vertices"].shape[0]
+            c["remap"], c["count"] = oracle.optimize_vertex_fetch_remap("reference", c["indices"], vc)
+            c["new_indices"], new_vertices, n = oracle.optimize_vertex_fetch("reference", c["indices"], c["vertices"])
+            assert n == c["count"]
+            # the moved vertex buffer follows from the remap (vertex v lands at remap[v])
+            used = c["remap"] != 0xFFFFFFFF
+            assert np.array_equal(new_vertices[c["remap"][used]], c["vertices"][used])
+        else:
+            c["remap"] = oracle.generate_position_remap("reference", c["positions"])
+    return cases
+
+
 def main():
     ka = known_answer_cases()
     js = []
@@ -277,6 +312,15 @@ def main():
     blob["meta"] = np.array(json.dumps(meta))
     np.savez_compressed(os.path.join(HERE, "seeded_cases.npz"), **blob)
     print(f"seeded cases: {len(sc)}")
+
+    cc = compaction_cases()
+    blob = {}
+    for i, c in enumerate(cc):
+        for k, v in c.items():
+            blob[f"{i}_{k}"] = np.asarray(v)
+    blob["count"] = np.array(len(cc))
+    np.savez_compressed(os.path.join(HERE, "compaction_cases.npz"), **blob)
+    print(f"compaction cases: {len(cc)}")
 
 
 if __name__ == "__main__":

@@ -67,3 +67,21 @@ def test_port_fp64_close(port):
 def test_port_empty(port):
     out, err = port.simplify("port", np.zeros(0, np.uint32), np.zeros((3, 3), np.float32), 0, 1e-2, 0)
     assert len(out) == 0 and err == 0
+
+
+def test_compaction_port_matches_golden(port):
+    """The oracle's restatement of the compaction step after the simplifier
+    (optimizeVertexFetchRemap / optimizeVertexFetch / generatePositionRemap) against the
+    reference library's outputs on the committed seeded cases."""
+    from fixtures import compaction_cases
+
+    for i, c in enumerate(compaction_cases()):
+        if c["kind"] == "fetch":
+            remap, n = port.optimize_vertex_fetch_remap("port", c["indices"], c["vertices"].shape[0])
+            assert np.array_equal(remap, c["remap"]) and n == int(c["count"]), i
+            idx, verts, n2 = port.optimize_vertex_fetch("port", c["indices"], c["vertices"])
+            assert np.array_equal(idx, c["new_indices"]) and n2 == n, i
+            used = c["remap"] != 0xFFFFFFFF
+            assert np.array_equal(verts[c["remap"][used]], c["vertices"][used]), i
+        else:
+            assert np.array_equal(port.generate_position_remap("port", c["positions"]), c["remap"]), i
