@@ -150,6 +150,30 @@ MESHOPTGPU_API int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, 
  * copied once, results copied back once. */
 MESHOPTGPU_API int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh_count, size_t* result_index_counts, float* result_errors);
 
+/* One level of a cluster-LOD build on device data: the boundary locks between groups
+ * (lockBoundary, demo/clusterlod.h:372-418), then every group simplified in one batch
+ * launch as clusterlod's simplify() does (demo/clusterlod.h:455-479). No counterpart in the
+ * library itself: it replaces the demo's per-level loop body (demo/clusterlod.h:642-690)
+ * up to re-clusterization.
+ *   indices            group g's merged cluster indices are indices[group_offsets[g] ..
+ *                      group_offsets[g+1]) (device; group_offsets is host, group_count + 1)
+ *   destination        group g's result at the same offsets (device; may alias indices)
+ *   position_remap     meshopt_generatePositionRemap of the vertex buffer (device), e.g. from
+ *                      meshoptgpu_generatePositionRemapDevice
+ *   locks              vertex_count bytes (device), kept by the caller across levels: on entry
+ *                      its Protect bits (seams to keep in permissive mode) are kept; on return it
+ *                      holds this level's locks (Lock where a position is used by two or more
+ *                      groups, | Protect, | vertex_lock), as clusterlod's locks array does
+ *   vertex_lock        optional user locks (device), ORed in
+ *   attribute_weights  host; target_index_counts host, one per group
+ * options are ORed with meshopt_SimplifySparse (groups address a shared vertex buffer); Prune is
+ * not supported. Results per group go to result_index_counts / result_errors (host). Returns a
+ * meshoptgpu_Status* value. */
+MESHOPTGPU_API int meshoptgpu_simplifyGroups(unsigned int* destination, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
+    const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride,
+    const float* attribute_weights, size_t attribute_count, const unsigned int* position_remap, unsigned char* locks, const unsigned char* vertex_lock,
+    const size_t* target_index_counts, float target_error, unsigned int options, size_t* result_index_counts, float* result_errors, void* stream);
+
 /* Batch launch shape: threads per CTA (128, 256 or 512; 0 = autotune, the default) and the
  * shared-memory budget per CTA in bytes (0 = default). The autotuner times each thread count
  * on the first batch of a size class and keeps the fastest for that class. */

@@ -49,6 +49,7 @@ EXPORTS = [
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
     "meshoptgpu_optimizeVertexFetchRemapDevice", "meshoptgpu_optimizeVertexFetchDevice", "meshoptgpu_generatePositionRemapDevice",
+    "meshoptgpu_simplifyGroups",
 ]
 
 
@@ -132,6 +133,8 @@ def load():
     lib.meshoptgpu_optimizeVertexFetchDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp]
     lib.meshoptgpu_generatePositionRemapDevice.restype = C.c_int
     lib.meshoptgpu_generatePositionRemapDevice.argtypes = [vp, vp, sz, sz, vp]
+    lib.meshoptgpu_simplifyGroups.restype = C.c_int
+    lib.meshoptgpu_simplifyGroups.argtypes = [vp, vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, vp, vp, vp, f32, u32, vp, vp, vp]
     _lib = lib
     return lib
 
@@ -381,6 +384,27 @@ def generate_position_remap_device(d_destination, d_positions, vertex_count, pos
     if check and st != STATUS_OK:
         raise SimplifyError(st, last_status()[1])
     return int(st)
+
+
+def simplify_groups_device(d_destination, d_indices, group_offsets, d_positions, vertex_count, positions_stride, d_remap, d_locks, targets,
+                           target_error, options, d_attributes=None, attributes_stride=0, weights=None, d_vertex_lock=None, stream=0, check=True):
+    """meshoptgpu_simplifyGroups: one cluster-LOD level (boundary locks, then every group simplified
+    in one batch launch). group_offsets: host ints (group_count + 1); targets: host ints per group;
+    weights: host floats. Returns (counts uint64 array, errors float32 array)."""
+    off = np.ascontiguousarray(group_offsets, dtype=np.uint64)
+    tg = np.ascontiguousarray(targets, dtype=np.uint64)
+    n = len(off) - 1
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    counts = np.zeros(max(n, 1), np.uint64)
+    errs = np.zeros(max(n, 1), np.float32)
+    st = load().meshoptgpu_simplifyGroups(d_destination, d_indices, off.ctypes.data, n, d_positions, vertex_count, positions_stride,
+                                          d_attributes if w is not None else None, attributes_stride if w is not None else 0,
+                                          w.ctypes.data if w is not None else None, len(w) if w is not None else 0, d_remap, d_locks,
+                                          d_vertex_lock, tg.ctypes.data, target_error, options, counts.ctypes.data, errs.ctypes.data,
+                                          C.c_void_p(stream or None))
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, last_status()[1])
+    return counts[:n], errs[:n]
 
 
 def set_batch_config(threads=0, smem_bytes=0):

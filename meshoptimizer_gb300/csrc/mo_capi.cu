@@ -11,6 +11,7 @@
 #include "mo_simplify.cuh"
 #include "mo_batch.cuh"
 #include "mo_vfetch.cuh"
+#include "mo_groups.cuh"
 
 #include <chrono>
 #include <condition_variable>
@@ -91,7 +92,7 @@ struct ThreadState
 	PhaseTimes times;
 	bool timing = false;
 	// batched path
-	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch;
+	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch, group_scratch;
 	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
 	unsigned int batch_smem = 0;    // 0: default budget
@@ -800,6 +801,91 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		MO_CUDA_CHECK(cudaStreamSynchronize(st));
 		for (size_t i = 0; i < mesh_count; ++i)
 			memcpy(meshes[i].destination, hout + off_out[i], size_t(res[i].index_count) * 4);
+		return finishBatch(res, result_index_counts, result_errors);
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
+int meshoptgpu_simplifyGroups(unsigned int* destination, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
+    const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride,
+    const float* attribute_weights, size_t attribute_count, const unsigned int* position_remap, unsigned char* locks, const unsigned char* vertex_lock,
+    const size_t* target_index_counts, float target_error, unsigned int options, size_t* result_index_counts, float* result_errors, void* stream)
+{
+	if (!position_remap || !locks || (group_count && (!group_offsets || !target_index_counts)))
+	{
+		setStatus(meshoptgpu_StatusInvalidArgument, "position_remap, locks, group_offsets and target_index_counts are required");
+		return meshoptgpu_StatusInvalidArgument;
+	}
+	std::vector<meshoptgpu_BatchMesh> meshes(group_count);
+	for (size_t g = 0; g < group_count; ++g)
+	{
+		meshoptgpu_BatchMesh& m = meshes[g];
+		m = meshoptgpu_BatchMesh{};
+		if (group_offsets[g + 1] < group_offsets[g])
+		{
+			setStatus(meshoptgpu_StatusInvalidArgument, "group_offsets must not decrease");
+			return meshoptgpu_StatusInvalidArgument;
+		}
+		m.indices = indices + group_offsets[g];
+		m.index_count = group_offsets[g + 1] - group_offsets[g];
+		m.vertex_positions = vertex_positions;
+		m.vertex_count = vertex_count;
+		m.vertex_positions_stride = vertex_positions_stride;
+		m.target_index_count = target_index_counts[g];
+		m.target_error = target_error;
+		m.options = options | kOptSparse;
+		m.destination = destination + group_offsets[g];
+		m.vertex_attributes = vertex_attributes;
+		m.vertex_attributes_stride = vertex_attributes_stride;
+		m.attribute_weights = attribute_weights;
+		m.attribute_count = attribute_count;
+		m.vertex_lock = locks;
+		std::string bad = checkBatchMesh(m);
+		if (!bad.empty())
+		{
+			int st = batchCheckStatus(m);
+			setStatus(st, "group " + std::to_string(g) + ": " + bad);
+			return st;
+		}
+	}
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		// offsets (device, 64-bit), the claim tables, the error word
+		const size_t lock_bytes = groupLockScratchBytes(vertex_count, group_count);
+		char* base = static_cast<char*>(s.group_scratch.ensure(lock_bytes + (group_count + 1) * 8 + 512));
+		unsigned long long* d_off = reinterpret_cast<unsigned long long*>(base + lock_bytes);
+		unsigned int* d_bad = reinterpret_cast<unsigned int*>(base + lock_bytes + ((group_count + 1) * 8 + 255) / 256 * 256);
+		std::vector<unsigned long long> off(group_offsets, group_offsets + group_count + 1);
+		unsigned long long* h_off = static_cast<unsigned long long*>(s.batch_host.ensure(off.size() * 8));
+		memcpy(h_off, off.data(), off.size() * 8);
+		MO_CUDA_CHECK(cudaMemcpyAsync(d_off, h_off, off.size() * 8, cudaMemcpyHostToDevice, st));
+		groupLocks(locks, indices, d_off, group_count, position_remap, vertex_lock, vertex_count, base, d_bad, st);
+		std::vector<BatchDesc> descs(group_count);
+		std::vector<int> attr_of(group_count);
+		AttrMaps maps;
+		for (size_t g = 0; g < group_count; ++g)
+		{
+			const meshoptgpu_BatchMesh& m = meshes[g];
+			descs[g] = makeDesc(m, m.indices, m.vertex_positions, m.vertex_attributes, m.vertex_lock, m.destination, maps, attr_of[g]);
+		}
+		std::vector<BatchResult> res;
+		runBatch(s, descs, maps, attr_of, res, st);
+		unsigned int hbad = 0;
+		MO_CUDA_CHECK(cudaMemcpyAsync(h_off, d_bad, 4, cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		memcpy(&hbad, h_off, 4);
+		if (hbad)
+		{
+			setStatus(meshoptgpu_StatusInvalidArgument, "an index or a position_remap entry is out of range of vertex_count");
+			return meshoptgpu_StatusInvalidArgument;
+		}
 		return finishBatch(res, result_index_counts, result_errors);
 	}
 	catch (const std::exception& e)

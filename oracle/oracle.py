@@ -72,6 +72,8 @@ def build(with_reference: bool = True) -> None:
     ref_root = os.environ.get("REFERENCE_ROOT", "/root/reference")
     if with_reference and os.path.isfile(os.path.join(ref_root, "src", "simplifier.cpp")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE_ROOT={ref_root}"], check=True)
+        if os.path.isfile(os.path.join(ref_root, "demo", "clusterlod.h")):
+            subprocess.run(["make", "-s", "-C", HERE, "clod-ref", f"REFERENCE_ROOT={ref_root}"], check=True)
 
 
 _libs: dict = {}

@@ -45,3 +45,12 @@ def compaction_cases():
         d["kind"] = str(d["kind"])
         out.append(d)
     return out
+
+
+def clod_cases():
+    z = np.load(os.path.join(GOLDEN, "clod_cases.npz"))
+    out = []
+    for i in range(int(z["count"])):
+        prefix = f"{i}_"
+        out.append({k[len(prefix):]: z[k] for k in z.files if k.startswith(prefix)})
+    return out

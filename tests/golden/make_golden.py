@@ -2,7 +2,7 @@
 
 Run here, where the reference sources exist:
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref clod-ref && python tests/golden/make_golden.py
 
 It writes two files next to this script:
 
@@ -14,6 +14,9 @@ It writes two files next to this script:
   the assertion the reference test makes (exact buffer, count or error bound).
 * ``seeded_cases.npz`` -- seeded synthetic meshes (heightfields, attribute spheres,
   lock-border patches, random lattice soups) with the reference library's outputs.
+* ``clod_cases.npz`` -- two cluster-LOD levels (boundary locks from the reference builder's
+  lockBoundary through oracle/clod_ref.cpp, then every group through the reference
+  simplifier) over one shared vertex buffer.
 * ``compaction_cases.npz`` -- seeded inputs of the compaction step after the simplifier
   (meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch,
   meshopt_generatePositionRemap) with the reference library's outputs.
@@ -286,6 +289,42 @@ def compaction_cases():
     return cases
 
 
+def clod_cases():
+    """Two cluster-LOD levels over the attribute sphere's shared vertex buffer: level 1 groups
+    are latitude/longitude bands of triangles, level 2 groups concatenate pairs of level-1
+    results. Each level runs the reference builder's lockBoundary (through the
+    oracle/clod_ref.cpp harness) and then the reference simplifier on every group with
+    Sparse | ErrorAbsolute | Permissive and the level's locks (demo/clusterlod.h:461-479)."""
+    import clod
+
+    rng = np.random.default_rng(77)
+    cases = []
+    for levels, group_tris in ((4, 64), (5, 256)):
+        groups, pos, attr, w, _ = W.cluster_groups(levels, group_tris)
+        remap = oracle.generate_position_remap("reference", pos)
+        locks = np.where(np.any(attr != attr[remap], axis=1), 2, 0).astype(np.uint8)
+        vl = rng.choice(np.array([0, 1, 2, 4], np.uint8), size=len(pos), p=[0.96, 0.01, 0.01, 0.02])
+        c = dict(positions=pos, attributes=attr, weights=w, remap=remap, locks_in=locks.copy(), vertex_lock=vl,
+                 options=np.array(2 | 4 | 32), error=np.array(np.finfo(np.float32).max, np.float32))
+        for level in (1, 2):
+            locks = clod.reference_lock_boundary(locks, groups, remap, vl)
+            targets = [(len(g) // 6) * 3 for g in groups]
+            outs = [oracle.simplify("reference", g, pos, t, float(c["error"]), int(c["options"]), attributes=attr, weights=w, lock=locks)
+                    for g, t in zip(groups, targets)]
+            off = np.zeros(len(groups) + 1, np.uint64)
+            off[1:] = np.cumsum([len(g) for g in groups])
+            c[f"l{level}_indices"] = np.concatenate(groups).astype(np.uint32)
+            c[f"l{level}_offsets"] = off
+            c[f"l{level}_targets"] = np.array(targets, np.uint64)
+            c[f"l{level}_locks"] = locks.copy()
+            c[f"l{level}_out"] = np.concatenate([o for o, _ in outs]).astype(np.uint32)
+            c[f"l{level}_counts"] = np.array([len(o) for o, _ in outs], np.uint64)
+            c[f"l{level}_errors"] = np.array([e for _, e in outs], np.float32)
+            groups = [np.concatenate([outs[i][0], outs[i + 1][0]]) if i + 1 < len(outs) else outs[i][0] for i in range(0, len(outs), 2)]
+        cases.append(c)
+    return cases
+
+
 def main():
     ka = known_answer_cases()
     js = []
@@ -321,6 +360,15 @@ def main():
     blob["count"] = np.array(len(cc))
     np.savez_compressed(os.path.join(HERE, "compaction_cases.npz"), **blob)
     print(f"compaction cases: {len(cc)}")
+
+    kc = clod_cases()
+    blob = {}
+    for i, c in enumerate(kc):
+        for k, v in c.items():
+            blob[f"{i}_{k}"] = np.asarray(v)
+    blob["count"] = np.array(len(kc))
+    np.savez_compressed(os.path.join(HERE, "clod_cases.npz"), **blob)
+    print(f"cluster-LOD cases: {len(kc)}")
 
 
 if __name__ == "__main__":

@@ -85,3 +85,23 @@ def test_compaction_port_matches_golden(port):
             assert np.array_equal(verts[c["remap"][used]], c["vertices"][used]), i
         else:
             assert np.array_equal(port.generate_position_remap("port", c["positions"]), c["remap"]), i
+
+
+def test_clod_level_port_matches_golden(port):
+    """The oracle's cluster-LOD level (lockBoundary restatement + the port simplifier on every
+    group) against the reference builder's locks and the reference simplifier's outputs."""
+    import clod
+    from fixtures import clod_cases
+
+    for c in clod_cases():
+        locks = c["locks_in"]
+        for level in (1, 2):
+            off = c[f"l{level}_offsets"].astype(np.int64)
+            idx = c[f"l{level}_indices"]
+            groups = [idx[off[g]:off[g + 1]] for g in range(len(off) - 1)]
+            locks, res = clod.simplify_level("port", groups, c["positions"], c["attributes"], c["weights"], c["remap"], locks, c["vertex_lock"],
+                                             c[f"l{level}_targets"], float(c["error"]), int(c["options"]))
+            assert np.array_equal(locks, c[f"l{level}_locks"])
+            assert np.array_equal(np.concatenate([o for o, _ in res]), c[f"l{level}_out"])
+            assert np.array_equal(np.array([len(o) for o, _ in res]), c[f"l{level}_counts"].astype(np.int64))
+            assert np.array_equal(np.array([e for _, e in res], np.float32), c[f"l{level}_errors"])
