@@ -55,6 +55,7 @@ def kperform_bytes(p, vertices, next_triangles):
 WORKLOADS = {
     "groups_4096": None,  # cluster groups: handled by bench_groups()
     "serving": None,      # request loop: handled by bench_serving()
+    "cluster_lod_level": None,  # one cluster-LOD level: handled by bench_clod_level()
     "sphere_attr_2m": lambda: W.config_sphere_attr(9),
     "sphere_attr_524k": lambda: W.config_sphere_attr(8),
     "heightfield_256": W.config_heightfield_256,
@@ -183,6 +184,114 @@ def bench_groups(args, mg, torch, seed_offset=0):
         "cpu_baseline": cpu, "bit_exact_vs_plain_and_oracle": bool(exact), "clocks": clocks.summary(), "gpu_launches": int(launches),
     }
     return line
+
+
+def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
+    """One cluster-LOD level over the 2,097,152-triangle attribute sphere: 2048 groups of 1024
+    triangles over one shared vertex buffer, boundary locks on the device, every group simplified
+    to half with Sparse | ErrorAbsolute | Permissive (meshoptgpu_simplifyGroups, one call)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    groups, pos, attr, w, _ = W.cluster_groups(levels, group_tris)
+    tris = sum(len(g) // 3 for g in groups)
+    idx = np.concatenate(groups).astype(np.uint32)
+    off = np.zeros(len(groups) + 1, np.uint64)
+    off[1:] = np.cumsum([len(g) for g in groups])
+    targets = np.array([(len(g) // 6) * 3 for g in groups], np.uint64)
+    options = mg.SimplifySparse | mg.SimplifyErrorAbsolute | mg.SimplifyPermissive
+    error = float(np.finfo(np.float32).max)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    di = torch.from_numpy(idx.view(np.int32)).to(dev)
+    dp = torch.from_numpy(pos).to(dev)
+    da = torch.from_numpy(attr).to(dev)
+    do = torch.empty_like(di)
+    dremap = torch.empty(len(pos), dtype=torch.int32, device=dev)
+    mg.generate_position_remap_device(dremap.data_ptr(), dp.data_ptr(), len(pos), 12, stream=stream.cuda_stream)
+    remap = dremap.cpu().numpy().view(np.uint32)
+    locks0 = np.where(np.any(attr != attr[remap], axis=1), 2, 0).astype(np.uint8)   # protected seams, as the builder sets up
+    dl = torch.from_numpy(locks0).to(dev)
+
+    def level():
+        return mg.simplify_groups_device(do.data_ptr(), di.data_ptr(), off, dp.data_ptr(), len(pos), 12, dremap.data_ptr(), dl.data_ptr(), targets,
+                                         error, options, d_attributes=da.data_ptr(), attributes_stride=attr.shape[1] * 4, weights=w,
+                                         stream=stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 1)):
+        level()
+    launches0 = mg.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            counts, errs = level()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    launches = mg.launch_count() - launches0
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    out = do.cpu().numpy().view(np.uint32)
+    locks = dl.cpu().numpy()
+
+    # e2e: the level's inputs from pinned host memory and its outputs back inside the timed region
+    h_idx = torch.from_numpy(idx.view(np.int32)).pin_memory()
+    h_pos = torch.from_numpy(pos).pin_memory()
+    h_attr = torch.from_numpy(attr).pin_memory()
+    h_out = torch.empty(len(idx), dtype=torch.int32).pin_memory()
+    tt = 0.0
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        di.copy_(h_idx, non_blocking=True)
+        dp.copy_(h_pos, non_blocking=True)
+        da.copy_(h_attr, non_blocking=True)
+        level()
+        h_out.copy_(do, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            tt += time.perf_counter() - t0
+
+    cpu, exact = None, None
+    if not args.no_cpu_baseline:
+        import concurrent.futures as cf
+
+        import clod
+        import oracle
+
+        if not oracle.available("port"):
+            oracle.build(with_reference=False)
+        oracle.load("port")
+        ref_locks = clod.lock_boundary(locks0, groups, remap)
+        threads = os.cpu_count() or 1
+
+        def work(gs):
+            return [oracle.simplify("port", groups[g], pos, int(targets[g]), error, options, attributes=attr, weights=w, lock=ref_locks) for g in gs]
+
+        chunks = [list(range(i, len(groups), threads)) for i in range(threads)]
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            parts = list(ex.map(work, chunks))
+        dt = time.perf_counter() - t0
+        exact = bool(np.array_equal(locks, ref_locks))
+        for ch, part in zip(chunks, parts):
+            for g, (o, e) in zip(ch, part):
+                exact = exact and int(counts[g]) == len(o) and np.array_equal(out[int(off[g]):int(off[g]) + len(o)], o) and float(errs[g]) == e
+        cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
+               "sample": f"the whole level once: lockBoundary restatement, then all {len(groups)} groups split statically over {threads} threads"}
+    h2d = idx.nbytes + pos.nbytes + attr.nbytes
+    return {
+        "metric": "input Mtris/s simplified (bit-exact)", "value": round(tris * args.steps / (total_ms / 1e3) / 1e6, 4), "unit": "Mtris/s",
+        "ms_per_step": round(total_ms / args.steps, 3),
+        "config": {"workload": f"cluster_lod_level_{tris}", "groups": len(groups), "tris_per_group": group_tris, "input_tris": tris,
+                   "output_tris": int(counts.sum()) // 3, "attributes": attr.shape[1], "options": "Sparse|ErrorAbsolute|Permissive",
+                   "target": "50% per group", "locks": "boundary (device) + protected seams",
+                   "batch_threads_per_cta": mg.batch_threads(), "l2": "flushed between steps (512 MiB write, outside the timed events)"},
+        "e2e": {"value": round(tris * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(idx.nbytes), "ms_per_step": round(1e3 * tt / args.steps, 3)},
+        "cpu_baseline": cpu, "bit_exact_vs_oracle": exact, "clocks": clocks.summary(), "gpu_launches": int(launches),
+    }
 
 
 def bench_serving(args, mg, torch):
@@ -432,6 +541,9 @@ def main():
     if args.workload == "serving":
         print(json.dumps(bench_serving(args, mg, torch)))
         return
+    if args.workload == "cluster_lod_level":
+        print(json.dumps(bench_clod_level(args, mg, torch)))
+        return
     c = load_workload(args.workload)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
@@ -579,6 +691,8 @@ def main():
         sv = bench_serving(argparse.Namespace(requests=2000, rates="500,1000", plain_rates=1, serve_workers=16, serve_blocks=0, serve_large=0,
                                               serve_batch_workers=0), mg, torch)
         line["serving"] = {k: sv[k] for k in ("served", "plain", "served_equals_plain", "config")}
+        cl = bench_clod_level(argparse.Namespace(steps=3, warmup=3, no_cpu_baseline=args.no_cpu_baseline), mg, torch)
+        line["cluster_lod_level"] = {k: cl[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "cpu_baseline", "bit_exact_vs_oracle")}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
