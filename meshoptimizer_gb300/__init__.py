@@ -338,17 +338,27 @@ def _device_mesh(m, keep):
                      m.get("attr_stride", 0) if wc else 0, wp, wc, m.get("d_lock"))
 
 
+class BatchDescriptors:
+    """A prebuilt meshoptgpu_BatchMesh array (and the host weight arrays it points to), for callers
+    that launch the same batch repeatedly without rebuilding it."""
+
+    def __init__(self, descs):
+        self.keep = []
+        self.n = len(descs)
+        self.arr = (BatchMesh * max(self.n, 1))()
+        for i, m in enumerate(descs):
+            self.arr[i] = _device_mesh(m, self.keep)
+
+
 def simplify_batch_device(descs, stream=0, check=True):
-    """meshoptgpu_simplifyBatch with device pointers: descs is a list of dicts with keys
-    d_indices, index_count, d_positions, vertex_count, stride, target, error, options, d_destination,
-    and optionally d_attributes, attr_stride (bytes), weights (host floats), d_lock.
+    """meshoptgpu_simplifyBatch with device pointers: descs is a BatchDescriptors or a list of dicts
+    with keys d_indices, index_count, d_positions, vertex_count, stride, target, error, options,
+    d_destination, and optionally d_attributes, attr_stride (bytes), weights (host floats), d_lock.
     Returns (counts uint64 array, errors float32 array)."""
     lib = load()
-    n = len(descs)
-    arr = (BatchMesh * max(n, 1))()
-    keep = []
-    for i, m in enumerate(descs):
-        arr[i] = _device_mesh(m, keep)
+    if not isinstance(descs, BatchDescriptors):
+        descs = BatchDescriptors(descs)
+    n, arr = descs.n, descs.arr
     counts = np.zeros(max(n, 1), np.uint64)
     errs = np.zeros(max(n, 1), np.float32)
     st = lib.meshoptgpu_simplifyBatch(C.cast(arr, C.c_void_p), n, counts.ctypes.data, errs.ctypes.data, C.c_void_p(stream or None))

@@ -84,8 +84,9 @@ __host__ __device__ inline size_t localVertexBound(size_t I, size_t vertex_count
 }
 
 // Carves the workspace of a mesh with I indices, V (local) vertices and ac attributes from
-// `base` (nullptr: size only).
-__host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t V, size_t ac, bool sparse)
+// `base` (nullptr: size only). The decision-round state (rounds = true) is only carved for
+// meshes in a global slab: meshes in shared memory run the serial warp loop without it.
+__host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t V, size_t ac, bool sparse, bool rounds)
 {
 	size_t off = 0;
 	size_t H = hashBucketsFor(V ? V : 1);
@@ -124,12 +125,12 @@ __host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t
 	w.order = reinterpret_cast<unsigned int*>(take(cap * 4));
 	w.hist = reinterpret_cast<unsigned int*>(take(kSortBinsC * 4));
 	w.red = reinterpret_cast<unsigned int*>(take(64 * 4));
-	w.minT = reinterpret_cast<unsigned long long*>(take(V * 8));
-	w.minS = reinterpret_cast<unsigned long long*>(take(V * 8));
-	w.moved = reinterpret_cast<unsigned long long*>(take(V * 8));
-	w.status = reinterpret_cast<unsigned char*>(take(cap));
-	w.list0 = reinterpret_cast<unsigned int*>(take(cap * 4));
-	w.list1 = reinterpret_cast<unsigned int*>(take(cap * 4));
+	w.minT = rounds ? reinterpret_cast<unsigned long long*>(take(V * 8)) : nullptr;
+	w.minS = rounds ? reinterpret_cast<unsigned long long*>(take(V * 8)) : nullptr;
+	w.moved = rounds ? reinterpret_cast<unsigned long long*>(take(V * 8)) : nullptr;
+	w.status = rounds ? reinterpret_cast<unsigned char*>(take(cap)) : nullptr;
+	w.list0 = rounds ? reinterpret_cast<unsigned int*>(take(cap * 4)) : nullptr;
+	w.list1 = rounds ? reinterpret_cast<unsigned int*>(take(cap * 4)) : nullptr;
 	return off > after_table ? off : after_table;
 }
 
@@ -192,15 +193,18 @@ __device__ __forceinline__ float fmax_l(float l, float r)
 
 // ---------------------------------------------------------------- one mesh
 
-template <int NT>
+// FULL = false compiles out the sparse subset, attributes, vertex_lock and Permissive, so that
+// positions-only batches run the lean instantiation
+template <int NT, bool FULL>
 __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, bool serial)
 {
 	const unsigned int tid = threadIdx.x;
 	const unsigned int I = d.index_count;
 	const float* P = d.positions;
 	const unsigned int sf = d.stride_f;
-	const unsigned int ac = d.ac;
-	unsigned int* const back = w.back; // sparse: local vertex -> vertex of the shared buffer
+	const unsigned int ac = FULL ? d.ac : 0;
+	const unsigned char* const vlock = FULL ? d.lock : nullptr;
+	unsigned int* const back = FULL ? w.back : nullptr; // sparse: local vertex -> vertex of the shared buffer
 	__shared__ unsigned int s_flag, s_unique;
 	__shared__ float s_mm[NT / 32][6];
 	__shared__ float s_minv[3], s_scale, s_extent;
@@ -404,12 +408,13 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 			w.pos[i] = make_float4((p[0] - s_minv[0]) * s_scale, (p[1] - s_minv[1]) * s_scale, (p[2] - s_minv[2]) * s_scale, 0.f);
 		}
 		// rescaleAttributes (:605-621): weighted copies of the used attributes
-		if (ac)
-			for (unsigned int x = tid; x < V * ac; x += NT)
-			{
-				unsigned int i = x / ac, k = x - i * ac;
-				w.attr[x] = d.attributes[(size_t)src(i) * d.attr_stride_f + d.amap->src[k]] * d.amap->weight[k];
-			}
+		if constexpr (FULL)
+			if (ac)
+				for (unsigned int x = tid; x < V * ac; x += NT)
+				{
+					unsigned int i = x / ac, k = x - i * ac;
+					w.attr[x] = d.attributes[(size_t)src(i) * d.attr_stride_f + d.amap->src[k]] * d.amap->weight[k];
+				}
 	}
 
 	// ---- raw adjacency (updateEdgeAdjacency :52-109, no remap): corner lists, unordered
@@ -489,7 +494,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		w.kind[i] = k;
 	}
 	__syncthreads();
-	if (d.options & kOptPermissive)
+	if (FULL && (d.options & kOptPermissive))
 	{
 		// Permissive (:481-515): a seam or locked primary becomes Complex unless a wedge is
 		// protected or has a half-edge with no opposite in position space (hasEdge :345-362);
@@ -504,7 +509,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 				unsigned int v = i;
 				do
 				{
-					protect |= d.lock && (d.lock[src(v)] & kVertexProtect) != 0;
+					protect |= vlock && (vlock[src(v)] & kVertexProtect) != 0;
 					v = w.wedge[v];
 				} while (v != i);
 				do
@@ -537,11 +542,11 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		}
 		__syncthreads();
 	}
-	if (d.lock)
+	if (vlock)
 	{
 		// vertex_lock (:517-531): a locked wedge locks its whole position
 		for (unsigned int i = tid; i < V; i += NT)
-			if (d.lock[src(i)] & kVertexLock)
+			if (vlock[src(i)] & kVertexLock)
 				w.kind[w.remap[i]] = kLocked;
 		__syncthreads();
 		for (unsigned int i = tid; i < V; i += NT)
@@ -627,7 +632,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 				Quadric F = qtriangle(V3{a0.x, a0.y, a0.z}, V3{a1.x, a1.y, a1.z}, V3{a2.x, a2.y, a2.z}, 1.f);
 				qadd(Q, F);
 			}
-			bool priority = d.lock && (d.lock[src(r)] & kVertexPriority) != 0;
+			bool priority = vlock && (vlock[src(r)] & kVertexPriority) != 0;
 			float wt = Q.w * (priority ? 1.0f : factor);
 			float4 pr = w.pos[r];
 			Quadric Pq = qpoint(pr.x, pr.y, pr.z, wt);
@@ -671,28 +676,31 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		}
 	}
 	__syncthreads();
-	if (ac)
+	if constexpr (FULL)
 	{
-		// fillAttributeQuadrics (:1159-1179): per wedge over its faces in face order; the
-		// gradients accumulate in place (each vertex is owned by one thread)
-		cornerLists(false);
-		for (unsigned int v = tid; v < V; v += NT)
+		if (ac)
 		{
-			float4* G = w.ag + (size_t)v * ac;
-			for (unsigned int k = 0; k < ac; ++k)
-				G[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-			Quadric Q = qzero();
-			for (unsigned int j = w.adj_off[v]; j < w.adj_off[v + 1]; ++j)
+			// fillAttributeQuadrics (:1159-1179): per wedge over its faces in face order; the
+			// gradients accumulate in place (each vertex is owned by one thread)
+			cornerLists(false);
+			for (unsigned int v = tid; v < V; v += NT)
 			{
-				unsigned int f = w.adj[j].x / 3;
-				unsigned int i0 = w.idx[f * 3 + 0], i1 = w.idx[f * 3 + 1], i2 = w.idx[f * 3 + 2];
-				float4 a0 = w.pos[i0], a1 = w.pos[i1], a2 = w.pos[i2];
-				addAttributeQuadric<32>(Q, G, (int)ac, V3{a0.x, a0.y, a0.z}, V3{a1.x, a1.y, a1.z}, V3{a2.x, a2.y, a2.z}, w.attr + (size_t)i0 * ac,
-				    w.attr + (size_t)i1 * ac, w.attr + (size_t)i2 * ac);
+				float4* G = w.ag + (size_t)v * ac;
+				for (unsigned int k = 0; k < ac; ++k)
+					G[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+				Quadric Q = qzero();
+				for (unsigned int j = w.adj_off[v]; j < w.adj_off[v + 1]; ++j)
+				{
+					unsigned int f = w.adj[j].x / 3;
+					unsigned int i0 = w.idx[f * 3 + 0], i1 = w.idx[f * 3 + 1], i2 = w.idx[f * 3 + 2];
+					float4 a0 = w.pos[i0], a1 = w.pos[i1], a2 = w.pos[i2];
+					addAttributeQuadric<32>(Q, G, (int)ac, V3{a0.x, a0.y, a0.z}, V3{a1.x, a1.y, a1.z}, V3{a2.x, a2.y, a2.z}, w.attr + (size_t)i0 * ac,
+					    w.attr + (size_t)i1 * ac, w.attr + (size_t)i2 * ac);
+				}
+				stquadric(w.aq, v, Q);
 			}
-			stquadric(w.aq, v, Q);
+			__syncthreads();
 		}
-		__syncthreads();
 	}
 
 	// ---- pass loop (:2493-2541)
@@ -808,10 +816,10 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 				}
 				else
 				{
-					if (w.kind[i0] == kComplex)
+					if (FULL && w.kind[i0] == kComplex)
 						for (unsigned int v = w.wedge[i0]; v != i0; v = w.wedge[v])
 							ei += term(v, complexTarget(v, i1, w.remap, w.loop, w.loopback));
-					if (w.kind[i1] == kComplex && bidi)
+					if (FULL && w.kind[i1] == kComplex && bidi)
 						for (unsigned int v = w.wedge[i1]; v != i1; v = w.wedge[v])
 							ej += term(v, complexTarget(v, i0, w.remap, w.loop, w.loopback));
 				}
@@ -905,7 +913,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 					}
 					if (lane == 0)
 					{
-						if (kd == kComplex)
+						if (FULL && kd == kComplex)
 						{
 							unsigned int v = i0;
 							do
@@ -1023,7 +1031,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 										else
 										{
 											unsigned int target = i1;
-											if (w.kind[i0] == kComplex)
+											if (FULL && w.kind[i0] == kComplex)
 												target = complexTarget(r0, i1, w.remap, w.loop, w.loopback);
 											else if (w.kind[i0] == kSeam)
 											{
@@ -1158,7 +1166,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 						continue;
 					unsigned int c = w.order[k];
 					unsigned int i0 = w.cv0[c], i1 = w.cv1[c];
-					if (w.kind[i0] == kComplex)
+					if (FULL && w.kind[i0] == kComplex)
 					{
 						unsigned int v = i0;
 						do
@@ -1217,36 +1225,39 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 			Quadric Q = ldquadric(w.vq, r1);
 			qadd(Q, ldquadric(w.vq, i));
 			stquadric(w.vq, r1, Q);
-			if (ac)
+			if constexpr (FULL)
 			{
-				unsigned int last = 0;
-				bool firstw = true;
-				for (;;)
+				if (ac)
 				{
-					unsigned int best = ~0u, v = i;
-					do
+					unsigned int last = 0;
+					bool firstw = true;
+					for (;;)
 					{
-						if ((firstw || v > last) && v < best)
-							best = v;
-						v = w.wedge[v];
-					} while (v != i);
-					if (best == ~0u)
-						break;
-					unsigned int tb = w.cr[best];
-					if (tb != best)
-					{
-						Quadric A = ldquadric(w.aq, tb);
-						qadd(A, ldquadric(w.aq, best));
-						stquadric(w.aq, tb, A);
-						for (unsigned int q = 0; q < ac; ++q)
+						unsigned int best = ~0u, v = i;
+						do
 						{
-							float4 g = w.ag[(size_t)tb * ac + q], h = w.ag[(size_t)best * ac + q];
-							g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
-							w.ag[(size_t)tb * ac + q] = g;
+							if ((firstw || v > last) && v < best)
+								best = v;
+							v = w.wedge[v];
+						} while (v != i);
+						if (best == ~0u)
+							break;
+						unsigned int tb = w.cr[best];
+						if (tb != best)
+						{
+							Quadric A = ldquadric(w.aq, tb);
+							qadd(A, ldquadric(w.aq, best));
+							stquadric(w.aq, tb, A);
+							for (unsigned int q = 0; q < ac; ++q)
+							{
+								float4 g = w.ag[(size_t)tb * ac + q], h = w.ag[(size_t)best * ac + q];
+								g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
+								w.ag[(size_t)tb * ac + q] = g;
+							}
 						}
+						last = best;
+						firstw = false;
 					}
-					last = best;
-					firstw = false;
 				}
 			}
 		}
@@ -1303,7 +1314,7 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		*out = BatchResult{result_count, sqrtf(result_error) * error_scale, passes, s_stall ? 3u : 0u};
 }
 
-template <int NT>
+template <int NT, bool FULL>
 __global__ void __launch_bounds__(NT) kBatch(const BatchDesc* __restrict__ descs, unsigned int count, unsigned int* ticket, BatchResult* results,
     char* slabs, size_t slab_bytes, unsigned int smem_bytes)
 {
@@ -1319,22 +1330,23 @@ __global__ void __launch_bounds__(NT) kBatch(const BatchDesc* __restrict__ descs
 			break;
 		BatchDesc d = descs[job];
 		CtaWork w;
-		const bool sparse = (d.options & kOptSparse) != 0;
+		const bool sparse = FULL && (d.options & kOptSparse) != 0;
 		const size_t vb = localVertexBound(d.index_count, d.vertex_count, sparse);
-		size_t need = carve(w, nullptr, d.index_count, vb, d.ac, sparse);
-		char* base = need <= smem_bytes ? smem : slabs + (size_t)blockIdx.x * slab_bytes;
-		carve(w, base, d.index_count, vb, d.ac, sparse);
-		simplifyMesh<NT>(d, w, &results[job], base == smem);
+		const unsigned int ac = FULL ? d.ac : 0;
+		const bool in_smem = carve(w, nullptr, d.index_count, vb, ac, sparse, false) <= smem_bytes;
+		char* base = in_smem ? smem : slabs + (size_t)blockIdx.x * slab_bytes;
+		carve(w, base, d.index_count, vb, ac, sparse, !in_smem);
+		simplifyMesh<NT, FULL>(d, w, &results[job], in_smem);
 		__syncthreads();
 	}
 }
 
 } // namespace
 
-size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count, size_t ac, bool sparse)
+size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count, size_t ac, bool sparse, bool rounds)
 {
 	CtaWork w;
-	return carve(w, nullptr, index_count, localVertexBound(index_count, vertex_count, sparse), ac, sparse);
+	return carve(w, nullptr, index_count, localVertexBound(index_count, vertex_count, sparse), ac, sparse, rounds);
 }
 
 // the dynamic shared-memory limit of every batch kernel instance is raised once, to the
@@ -1348,49 +1360,62 @@ void raiseSmemLimits()
 		cudaGetDevice(&dev);
 		cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
 		int limit = optin - 4096; // room for the kernel's static shared memory
-		cudaFuncSetAttribute(kBatch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
-		cudaFuncSetAttribute(kBatch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
-		cudaFuncSetAttribute(kBatch<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+		cudaFuncSetAttribute(kBatch<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
 	});
 }
 
-void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
+template <bool FULL>
+void launchBatchT(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
     unsigned int smem_bytes, unsigned int blocks, int threads, cudaStream_t stream)
+{
+	switch (threads)
+	{
+	case 128:
+		MO_LAUNCH((kBatch<128, FULL>), blocks, 128, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
+		break;
+	case 512:
+		MO_LAUNCH((kBatch<512, FULL>), blocks, 512, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
+		break;
+	default:
+		MO_LAUNCH((kBatch<256, FULL>), blocks, 256, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
+		break;
+	}
+}
+
+void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
+    unsigned int smem_bytes, unsigned int blocks, int threads, bool full, cudaStream_t stream)
 {
 	raiseSmemLimits();
 	MO_CUDA_CHECK(cudaMemsetAsync(d_ticket, 0, sizeof(unsigned int), stream));
-	switch (threads)
-	{
-	case 128:
-		MO_LAUNCH(kBatch<128>, blocks, 128, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
-		break;
-	case 512:
-		MO_LAUNCH(kBatch<512>, blocks, 512, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
-		break;
-	default:
-		MO_LAUNCH(kBatch<256>, blocks, 256, smem_bytes, stream, d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes);
-		break;
-	}
+	if (full)
+		launchBatchT<true>(d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes, blocks, threads, stream);
+	else
+		launchBatchT<false>(d_descs, count, d_ticket, d_results, d_slabs, slab_bytes, smem_bytes, blocks, threads, stream);
 	MO_CUDA_CHECK(cudaGetLastError());
 }
 
-int batchBlocksPerSM(int threads, unsigned int smem_bytes)
+template <bool FULL>
+int blocksPerSMT(int threads, unsigned int smem_bytes)
+{
+	int n = 0;
+	if (threads == 128)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<128, FULL>, 128, smem_bytes);
+	else if (threads == 512)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<512, FULL>, 512, smem_bytes);
+	else
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<256, FULL>, 256, smem_bytes);
+	return n;
+}
+
+int batchBlocksPerSM(int threads, unsigned int smem_bytes, bool full)
 {
 	raiseSmemLimits();
-	int n = 0;
-	switch (threads)
-	{
-	case 128:
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<128>, 128, smem_bytes);
-		break;
-	case 512:
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<512>, 512, smem_bytes);
-		break;
-	default:
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kBatch<256>, 256, smem_bytes);
-		break;
-	}
-	return n;
+	return full ? blocksPerSMT<true>(threads, smem_bytes) : blocksPerSMT<false>(threads, smem_bytes);
 }
 
 } // namespace mogpu

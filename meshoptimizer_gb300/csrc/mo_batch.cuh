@@ -42,14 +42,23 @@ struct BatchResult
 	unsigned int status; // 0 ok, 2 invalid index, 3 a decision round made no progress
 };
 
-// scratch bytes one mesh needs (shared memory when it fits, else a global slab); a sparse mesh
-// has at most min(index_count, vertex_count) vertices of its own
-size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count, size_t ac, bool sparse);
+// scratch bytes one mesh needs: without the decision-round state (rounds = false) in shared
+// memory, where it runs when that size fits the launch's budget, else with it in a global slab.
+// A sparse mesh has at most min(index_count, vertex_count) vertices of its own.
+size_t batchWorkspaceBytes(size_t index_count, size_t vertex_count, size_t ac, bool sparse, bool rounds);
 
-// resident CTAs per SM for a thread count and dynamic shared memory size
-int batchBlocksPerSM(int threads, unsigned int smem_bytes);
+// whether a mesh needs the full-option kernel: a sparse subset (option bit 1), attributes,
+// vertex_lock or Permissive (option bit 5)
+inline bool batchNeedsFull(const BatchDesc& d)
+{
+	return d.ac || d.lock || (d.options & ((1u << 1) | (1u << 5)));
+}
 
+// resident CTAs per SM for a thread count, dynamic shared memory size and kernel form
+int batchBlocksPerSM(int threads, unsigned int smem_bytes, bool full);
+
+// full: the instantiation with every option; otherwise the positions-only one
 void launchBatch(const BatchDesc* d_descs, unsigned int count, unsigned int* d_ticket, BatchResult* d_results, char* d_slabs, size_t slab_bytes,
-    unsigned int smem_bytes, unsigned int blocks, int threads, cudaStream_t stream);
+    unsigned int smem_bytes, unsigned int blocks, int threads, bool full, cudaStream_t stream);
 
 } // namespace mogpu

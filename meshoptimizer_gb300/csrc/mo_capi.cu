@@ -337,9 +337,10 @@ BatchDesc makeDesc(const meshoptgpu_BatchMesh& m, const unsigned int* indices, c
 	return d;
 }
 
-size_t descWorkspace(const BatchDesc& d)
+// workspace of a batched mesh in shared memory (serial perform) and in a global slab (rounds)
+size_t descWorkspace(const BatchDesc& d, bool rounds)
 {
-	return batchWorkspaceBytes(d.index_count, d.vertex_count, d.ac, (d.options & kOptSparse) != 0);
+	return batchWorkspaceBytes(d.index_count, d.vertex_count, d.ac, (d.options & kOptSparse) != 0, rounds);
 }
 
 // Runs descs (device pointers) through the persistent kernel; results in the same order.
@@ -361,8 +362,11 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 	for (size_t i = 0; i < n; ++i)
 	{
 		ordered[i] = descs[perm[i]];
-		size_t ws = descWorkspace(ordered[i]);
-		(ws <= budget ? maxfit : maxslab) = std::max(ws <= budget ? maxfit : maxslab, ws);
+		size_t ws = descWorkspace(ordered[i], false);
+		if (ws <= budget)
+			maxfit = std::max(maxfit, ws);
+		else
+			maxslab = std::max(maxslab, descWorkspace(ordered[i], true));
 		maxidx = std::max<size_t>(maxidx, ordered[i].index_count);
 	}
 	unsigned int smem = unsigned((maxfit + 15) & ~size_t(15));
@@ -390,13 +394,16 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 	if (nm)
 		MO_CUDA_CHECK(cudaMemcpyAsync(d_maps, hmeta + off_maps, nm * sizeof(BatchAttr), cudaMemcpyHostToDevice, st));
 
+	bool full = false;
+	for (const BatchDesc& d : ordered)
+		full = full || batchNeedsFull(d);
 	auto launch = [&](int threads) {
-		int per_sm = std::max(1, batchBlocksPerSM(threads, smem));
+		int per_sm = std::max(1, batchBlocksPerSM(threads, smem, full));
 		unsigned int blocks = unsigned(std::min<size_t>(size_t(per_sm) * sms, n));
 		if (maxslab)
 			blocks = unsigned(std::max<size_t>(1, std::min<size_t>(blocks, kBatchSlabTotal / maxslab)));
 		char* slabs = maxslab ? static_cast<char*>(s.batch_slabs.ensure(size_t(blocks) * maxslab)) : nullptr;
-		launchBatch(d_descs, unsigned(n), d_ticket, d_res, slabs, maxslab, smem, blocks, threads, st);
+		launchBatch(d_descs, unsigned(n), d_ticket, d_res, slabs, maxslab, smem, blocks, threads, full, st);
 	};
 
 	int threads = s.batch_threads;
@@ -521,8 +528,7 @@ const size_t kServerBudgetDefault = size_t(40) << 30;
 // fit shared memory hold none) or on the single-mesh path (its arena)
 size_t batchReserve(const ServerRequest& r)
 {
-	size_t ws = descWorkspace(r.desc);
-	return ws <= kBatchSmemDefault ? 4096 : ws;
+	return descWorkspace(r.desc, false) <= kBatchSmemDefault ? 4096 : descWorkspace(r.desc, true);
 }
 
 void publish(ServerImpl& S, std::vector<ServerRequest*>& done_reqs, size_t release)

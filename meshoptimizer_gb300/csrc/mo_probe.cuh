@@ -34,6 +34,8 @@ inline cudaEvent_t probeBegin(const char* name, cudaStream_t stream)
 {
 	LaunchProbe& p = probe();
 	p.launches++;
+	while (*name == '(' || *name == ' ') // template kernels are passed parenthesised
+		++name;
 	if (p.selected.empty() || p.selected.compare(0, p.selected.size(), name, 0, p.selected.size()) != 0)
 		return nullptr;
 	cudaEvent_t e = p.take();
