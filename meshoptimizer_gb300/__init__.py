@@ -287,6 +287,50 @@ def _weights(m, keep):
     return w.ctypes.data, len(w)
 
 
+class HostBatch:
+    """meshoptgpu_simplifyBatchHost over a fixed list of host meshes (dicts as simplify_batch takes):
+    the descriptor array and the output buffers are built once; run() makes the C-ABI call, which
+    packs the inputs into pinned memory, copies them to the device, simplifies, and copies the
+    results back into the output buffers. outputs[i][:counts[i]] is mesh i's result."""
+
+    def __init__(self, meshes):
+        self.keep = []
+        self.n = len(meshes)
+        self.arr = (BatchMesh * max(self.n, 1))()
+        self.outputs = []
+        arrays = {}
+
+        def shared(a, dtype):
+            key = id(a)
+            if key not in arrays:
+                arrays[key] = np.ascontiguousarray(a, dtype=dtype)
+                self.keep.append(arrays[key])
+            return arrays[key]
+
+        for i, m in enumerate(meshes):
+            idx = shared(m["indices"], np.uint32)
+            pos = shared(m["positions"], np.float32)
+            out = np.empty(max(len(idx), 1), np.uint32)
+            self.outputs.append(out)
+            wp, wc = _weights(m, self.keep)
+            attr = shared(m["attributes"], np.float32) if wc else None
+            lock = shared(m["lock"], np.uint8) if m.get("lock") is not None else None
+            self.arr[i] = BatchMesh(idx.ctypes.data, len(idx), pos.ctypes.data, pos.shape[0], pos.shape[1] * 4, int(m["target"]),
+                                    float(m["error"]), int(m.get("options", 0)), out.ctypes.data, attr.ctypes.data if wc else None,
+                                    attr.shape[1] * 4 if wc else 0, wp, wc, lock.ctypes.data if lock is not None else None)
+        self.counts = np.zeros(max(self.n, 1), np.uint64)
+        self.errors = np.zeros(max(self.n, 1), np.float32)
+
+    def run(self, check=True):
+        st = load().meshoptgpu_simplifyBatchHost(C.cast(self.arr, C.c_void_p), self.n, self.counts.ctypes.data, self.errors.ctypes.data)
+        if check and st != STATUS_OK:
+            raise SimplifyError(st, last_status()[1])
+        return st
+
+    def results(self):
+        return [(self.outputs[i][:int(self.counts[i])].copy(), float(self.errors[i])) for i in range(self.n)]
+
+
 def simplify_batch(meshes, check=True):
     """meshoptgpu_simplifyBatchHost on host arrays.
 
@@ -296,39 +340,9 @@ def simplify_batch(meshes, check=True):
     are uploaded once. Returns a list of (indices, result_error), identical to per-mesh
     meshopt_simplifyWithAttributes calls.
     """
-    lib = load()
-    n = len(meshes)
-    arr = (BatchMesh * max(n, 1))()
-    keep = []
-    outs = []
-    arrays = {}
-
-    def shared(a, dtype):
-        # the same array object for several meshes gives the same pointer (deduplicated natively)
-        key = id(a)
-        if key not in arrays:
-            arrays[key] = np.ascontiguousarray(a, dtype=dtype)
-            keep.append(a)
-        return arrays[key]
-
-    for i, m in enumerate(meshes):
-        idx = np.ascontiguousarray(m["indices"], dtype=np.uint32)
-        pos = shared(m["positions"], np.float32)
-        out = np.empty(max(len(idx), 1), np.uint32)
-        keep.append(idx)
-        outs.append(out)
-        wp, wc = _weights(m, keep)
-        attr = shared(m["attributes"], np.float32) if wc else None
-        lock = shared(m["lock"], np.uint8) if m.get("lock") is not None else None
-        arr[i] = BatchMesh(idx.ctypes.data, len(idx), pos.ctypes.data, pos.shape[0], pos.shape[1] * 4, int(m["target"]), float(m["error"]),
-                           int(m.get("options", 0)), out.ctypes.data, attr.ctypes.data if wc else None, attr.shape[1] * 4 if wc else 0, wp, wc,
-                           lock.ctypes.data if lock is not None else None)
-    counts = np.zeros(max(n, 1), np.uint64)
-    errs = np.zeros(max(n, 1), np.float32)
-    st = lib.meshoptgpu_simplifyBatchHost(C.cast(arr, C.c_void_p), n, counts.ctypes.data, errs.ctypes.data)
-    if check and st != STATUS_OK:
-        raise SimplifyError(st, last_status()[1])
-    return [(outs[i][:int(counts[i])].copy(), float(errs[i])) for i in range(n)]
+    b = HostBatch(meshes)
+    b.run(check)
+    return b.results()
 
 
 def _device_mesh(m, keep):

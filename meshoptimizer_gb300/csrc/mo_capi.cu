@@ -199,6 +199,49 @@ size_t align256(size_t v)
 	return (v + 255) & ~size_t(255);
 }
 
+struct HostCopy
+{
+	void* dst;
+	const void* src;
+	size_t bytes;
+};
+
+// Host memcpy of many pieces, spread over up to 8 threads in contiguous runs of about equal
+// bytes when there is enough to copy (packing a batch into pinned staging and scattering its
+// results are memory-bound host loops).
+void parallelCopies(const std::vector<HostCopy>& copies)
+{
+	size_t total = 0;
+	for (const HostCopy& c : copies)
+		total += c.bytes;
+	unsigned int hw = std::max(1u, std::thread::hardware_concurrency());
+	size_t threads = std::min<size_t>(std::min<size_t>(8, hw), total >> 21); // one thread per 2 MiB at least
+	auto run = [&](size_t b, size_t e) {
+		for (size_t i = b; i < e; ++i)
+			memcpy(copies[i].dst, copies[i].src, copies[i].bytes);
+	};
+	if (threads <= 1)
+	{
+		run(0, copies.size());
+		return;
+	}
+	std::vector<size_t> cut(1, 0);
+	size_t acc = 0, share = total / threads;
+	for (size_t i = 0; i < copies.size() && cut.size() < threads; ++i)
+	{
+		acc += copies[i].bytes;
+		if (acc >= share * cut.size())
+			cut.push_back(i + 1);
+	}
+	cut.push_back(copies.size());
+	std::vector<std::thread> pool;
+	for (size_t t = 0; t + 2 < cut.size(); ++t)
+		pool.emplace_back(run, cut[t], cut[t + 1]);
+	run(cut[cut.size() - 2], cut.back());
+	for (std::thread& th : pool)
+		th.join();
+}
+
 size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions, size_t vertex_count,
     size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
     const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error)
@@ -780,12 +823,15 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		}
 		char* h = static_cast<char*>(s.batch_host.ensure(in_bytes + 16));
 		{
+			std::vector<HostCopy> copies;
+			copies.reserve(pieces.size());
 			size_t at = 0;
 			for (auto& pc : pieces)
 			{
-				memcpy(h + at, pc.first, pc.second);
+				copies.push_back(HostCopy{h + at, pc.first, pc.second});
 				at = (at + pc.second + 15) & ~size_t(15);
 			}
+			parallelCopies(copies);
 		}
 		char* d = static_cast<char*>(s.batch_io.ensure(align256(in_bytes) + out_words * 4 + 256));
 		unsigned int* d_out = reinterpret_cast<unsigned int*>(d + align256(in_bytes));
@@ -805,8 +851,10 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		unsigned int* hout = static_cast<unsigned int*>(s.batch_host.ensure(std::max(in_bytes + 16, out_words * 4 + 16)));
 		MO_CUDA_CHECK(cudaMemcpyAsync(hout, d_out, out_words * 4, cudaMemcpyDeviceToHost, st));
 		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		std::vector<HostCopy> copies(mesh_count);
 		for (size_t i = 0; i < mesh_count; ++i)
-			memcpy(meshes[i].destination, hout + off_out[i], size_t(res[i].index_count) * 4);
+			copies[i] = HostCopy{meshes[i].destination, hout + off_out[i], size_t(res[i].index_count) * 4};
+		parallelCopies(copies);
 		return finishBatch(res, result_index_counts, result_errors);
 	}
 	catch (const std::exception& e)
