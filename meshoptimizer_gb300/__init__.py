@@ -49,7 +49,7 @@ EXPORTS = [
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
     "meshoptgpu_optimizeVertexFetchRemapDevice", "meshoptgpu_optimizeVertexFetchDevice", "meshoptgpu_generatePositionRemapDevice",
-    "meshoptgpu_simplifyGroups",
+    "meshoptgpu_simplifyGroups", "meshoptgpu_setDropinBatchLimit",
 ]
 
 
@@ -133,6 +133,7 @@ def load():
     lib.meshoptgpu_optimizeVertexFetchDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp]
     lib.meshoptgpu_generatePositionRemapDevice.restype = C.c_int
     lib.meshoptgpu_generatePositionRemapDevice.argtypes = [vp, vp, sz, sz, vp]
+    lib.meshoptgpu_setDropinBatchLimit.argtypes = [sz]
     lib.meshoptgpu_simplifyGroups.restype = C.c_int
     lib.meshoptgpu_simplifyGroups.argtypes = [vp, vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, vp, vp, vp, f32, u32, vp, vp, vp]
     _lib = lib
@@ -434,6 +435,11 @@ def simplify_groups_device(d_destination, d_indices, group_offsets, d_positions,
 def set_batch_config(threads=0, smem_bytes=0):
     """Threads per CTA of the batch kernel (128/256/512, 0 = autotune) and shared-memory budget."""
     load().meshoptgpu_setBatchConfig(int(threads), int(smem_bytes))
+
+
+def set_dropin_batch_limit(max_index_count=24000):
+    """Drop-in calls on meshes with at most this many indices run on the batch kernel (0: never)."""
+    load().meshoptgpu_setDropinBatchLimit(int(max_index_count))
 
 
 def batch_threads():

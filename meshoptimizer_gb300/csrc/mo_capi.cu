@@ -96,6 +96,9 @@ struct ThreadState
 	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
 	unsigned int batch_smem = 0;    // 0: default budget
+	// drop-in calls with at most this many indices run on the batch kernel as a batch of one
+	// (measured crossover on GB300: about 8k triangles, with or without attributes)
+	size_t dropin_batch_limit = 24000;
 
 	~ThreadState()
 	{
@@ -242,6 +245,10 @@ void parallelCopies(const std::vector<HostCopy>& copies)
 		th.join();
 }
 
+// Runs a small mesh (device pointers) on the batch kernel when the calling thread's drop-in
+// limit and the mesh's options allow; returns false to leave it to the single-mesh path.
+bool smallMeshOnBatch(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st);
+
 size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions, size_t vertex_count,
     size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
     const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error)
@@ -290,7 +297,8 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		m.target_index_count = target_index_count;
 		m.target_error = target_error;
 		m.options = options;
-		s.last = s.simplifier->run(m, d_out, st, s.timing ? &s.times : nullptr);
+		if (!smallMeshOnBatch(s, m, d_out, st))
+			s.last = s.simplifier->run(m, d_out, st, s.timing ? &s.times : nullptr);
 		if (s.last.index_count)
 			MO_CUDA_CHECK(cudaMemcpyAsync(destination, d_out, s.last.index_count * 4, cudaMemcpyDeviceToHost, st));
 		MO_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -494,6 +502,36 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 
 // argument checks of a batched mesh: those of meshopt_simplifyEdge (:2348-2357), then the
 // batch kernel's option set unless the mesh may take the single-mesh path
+bool smallMeshOnBatch(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st)
+{
+	if (s.timing || m.index_count == 0 || m.index_count > s.dropin_batch_limit || (m.options & ~kBatchOptions) ||
+	    m.vertex_count >= (size_t(1) << 32))
+		return false;
+	meshoptgpu_BatchMesh bm{};
+	bm.index_count = m.index_count;
+	bm.vertex_count = m.vertex_count;
+	bm.vertex_positions_stride = m.positions_stride;
+	bm.target_index_count = m.target_index_count;
+	bm.target_error = m.target_error;
+	bm.options = m.options;
+	bm.vertex_attributes_stride = m.attributes_stride;
+	bm.attribute_weights = m.weights;
+	bm.attribute_count = m.attribute_count;
+	AttrMaps maps;
+	std::vector<int> attr_of(1);
+	std::vector<BatchDesc> descs{makeDesc(bm, m.indices, m.positions, m.attributes, m.lock, d_out, maps, attr_of[0])};
+	std::vector<BatchResult> res;
+	runBatch(s, descs, maps, attr_of, res, st);
+	if (res[0].status == 2)
+		throw std::invalid_argument("index out of range of vertex_count");
+	if (res[0].status == 3)
+		throw std::runtime_error("collapse decision round made no progress");
+	s.last = RunResult();
+	s.last.index_count = res[0].index_count;
+	s.last.result_error = res[0].result_error;
+	return true;
+}
+
 std::string checkBatchMesh(const meshoptgpu_BatchMesh& m, bool any_option = false)
 {
 	if (m.attribute_count && (!m.vertex_attributes || !m.attribute_weights))
@@ -1183,6 +1221,11 @@ void meshoptgpu_setBatchConfig(int threads, unsigned int smem_bytes)
 	s.batch_smem = smem_bytes;
 }
 
+void meshoptgpu_setDropinBatchLimit(size_t max_index_count)
+{
+	state().dropin_batch_limit = max_index_count;
+}
+
 int meshoptgpu_getBatchThreads(void)
 {
 	ThreadState& s = state();
@@ -1325,7 +1368,8 @@ size_t meshoptgpu_simplifyDevice(unsigned int* destination, const unsigned int* 
 		m.target_index_count = target_index_count;
 		m.target_error = target_error;
 		m.options = options;
-		s.last = s.simplifier->run(m, destination, st, s.timing ? &s.times : nullptr);
+		if (!smallMeshOnBatch(s, m, destination, st))
+			s.last = s.simplifier->run(m, destination, st, s.timing ? &s.times : nullptr);
 		if (result_error)
 			*result_error = s.last.result_error;
 		setStatus(meshoptgpu_StatusOk, "");

@@ -29,6 +29,11 @@ def built():
 
     build.build()
     mg.load()
+    # this module checks the multi-CTA single-mesh path (and its per-pass counters) on every
+    # size; small drop-in calls routed to the batch kernel are covered by test_gpu_dropin.py
+    mg.set_dropin_batch_limit(0)
+    yield
+    mg.set_dropin_batch_limit()
 
 
 def supported(options):
