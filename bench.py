@@ -152,7 +152,21 @@ def bench_groups(args, mg, torch, seed_offset=0):
     h2d = sum(m["indices"].nbytes + m["positions"].nbytes for m in meshes)
     d2h = sum(len(r[0]) * 4 for r in host_res)
 
-    # plain: one drop-in call per group (host pointers), and one device-resident call per group
+    plain_gpu, exact = None, True
+    if not getattr(args, "no_plain", False):
+        plain_gpu, exact, plain = _groups_plain(args, mg, torch, meshes, raw_descs, stream, batched_out, host_res)
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dt, ref = cpu_groups(meshes, threads)
+        exact = exact and all(np.array_equal(a, r[0]) for a, r in zip(batched_out, ref))
+        cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
+               "sample": f"all {len(meshes)} groups once, independent groups split statically over {threads} threads"}
+    return _groups_line(args, mg, meshes, tris, out_tris, total_ms, tt, h2d, d2h, plain_gpu, cpu, exact, clocks, launches)
+
+
+def _groups_plain(args, mg, torch, meshes, raw_descs, stream, batched_out, host_res):
+    """plain: one drop-in call per group (host pointers), and one device-resident call per group"""
     for m in meshes[:64]:
         mg.simplify(m["indices"], m["positions"], m["target"], m["error"], m["options"])
     torch.cuda.synchronize()
@@ -167,13 +181,15 @@ def bench_groups(args, mg, torch, seed_offset=0):
     t_plain_dev = time.perf_counter() - t0
 
     exact = all(np.array_equal(a, b[0]) for a, b in zip(batched_out, plain)) and all(np.array_equal(a[0], b[0]) for a, b in zip(host_res, plain))
-    cpu = None
-    if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        dt, ref = cpu_groups(meshes, threads)
-        exact = exact and all(np.array_equal(a, r[0]) for a, r in zip(batched_out, ref))
-        cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
-               "sample": f"all {len(meshes)} groups once, independent groups split statically over {threads} threads"}
+    tris = sum(len(m["indices"]) // 3 for m in meshes)
+    plain_gpu = {"dropin_host_mtris_s": round(tris / t_plain / 1e6, 4), "dropin_host_ms": round(1e3 * t_plain, 1),
+                 "device_resident_mtris_s": round(tris / t_plain_dev / 1e6, 4), "device_resident_ms": round(1e3 * t_plain_dev, 1),
+                 "calls": len(meshes)}
+    return plain_gpu, exact, plain
+
+
+def _groups_line(args, mg, meshes, tris, out_tris, total_ms, tt, h2d, d2h, plain_gpu, cpu, exact, clocks, launches):
+    value = tris * args.steps / (total_ms / 1e3) / 1e6
     line = {
         "metric": "input Mtris/s simplified (bit-exact)", "value": round(value, 4), "unit": "Mtris/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -183,9 +199,7 @@ def bench_groups(args, mg, torch, seed_offset=0):
                    "batch_threads_per_cta": mg.batch_threads(), "l2": "flushed between steps (512 MiB write, outside the timed events)"},
         "e2e": {"value": round(tris * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": round(1e3 * tt / args.steps, 3)},
-        "plain_gpu": {"dropin_host_mtris_s": round(tris / t_plain / 1e6, 4), "dropin_host_ms": round(1e3 * t_plain, 1),
-                      "device_resident_mtris_s": round(tris / t_plain_dev / 1e6, 4), "device_resident_ms": round(1e3 * t_plain_dev, 1),
-                      "calls": len(meshes)},
+        "plain_gpu": plain_gpu,
         "cpu_baseline": cpu, "bit_exact_vs_plain_and_oracle": bool(exact), "clocks": clocks.summary(), "gpu_launches": int(launches),
     }
     return line
@@ -436,6 +450,21 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def kernel_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` on `workload` from a committed ncu summary
+    (profiles/traffic.json: dram__bytes_read.sum + dram__bytes_write.sum averaged over the
+    captured launches), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.isfile(path):
+        return None
+    with open(path) as f:
+        entries = json.load(f)
+    for e in entries:
+        if e.get("kernel") == kernel and e.get("workload") == workload:
+            return {"dram_bytes_per_launch": int(e["dram_bytes_per_launch"]), "source": e["source"]}
+    return None
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.isfile(p):
@@ -510,6 +539,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched-groups and serving summaries of the default line")
+    ap.add_argument("--no-plain", action="store_true", help="groups: skip the separate one-call-per-group comparison leg")
     ap.add_argument("--requests", type=int, default=10000, help="serving: requests per arrival rate")
     ap.add_argument("--rates", default="250,500,1000,2000", help="serving: Poisson arrival rates (requests/s)")
     ap.add_argument("--plain-rates", type=int, default=2, help="serving: how many of the rates also run the plain path")
@@ -569,7 +599,6 @@ def main():
     for _ in range(max(args.warmup, 0)):
         n_out, err = step()
 
-    mg.set_kernel_profile(args.kernel)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = mg.launch_count()
     if dist:
@@ -585,9 +614,24 @@ def main():
     if dist:
         dist.barrier()
     launches = mg.launch_count() - launches0
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+
+    # per-launch CUDA-event timing of the roofline kernel: the same steps replayed with the
+    # host-driven pass loop (events cannot be recorded inside the device-resident loop's graph)
+    mg.set_device_loop(False)
+    step()
+    mg.set_kernel_profile(args.kernel)
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        kev[i][0].record(stream)
+        step()
+        kev[i][1].record(stream)
+    torch.cuda.synchronize()
     k_launches, k_ms = mg.kernel_profile()
     mg.set_kernel_profile(None)
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    mg.set_device_loop(True)
+    host_loop_ms = sum(a.elapsed_time(b) for a, b in kev)
     from meshoptimizer_gb300 import replicas
 
     rate, secs, _ = replicas.aggregate(total_ms / 1e3, float(c["tris"] * args.steps), dist=dist, device=dev)
@@ -657,7 +701,13 @@ def main():
                     "algorithmic_bytes_per_launch": int(bytes_per_launch),
                     "unit_definition": "kperform_bytes(): rounds 29 B/active candidate, stop 12 B/evaluated, apply 164 B/commit, "
                                        "25 B/vertex, 24 B/triangle + 12 B/kept triangle",
-                    "share_of_step": round(k_ms / total_ms, 4)}
+                    "share_of_step": round(k_ms / host_loop_ms, 4) if host_loop_ms else None,
+                    "kernel_timing": "CUDA events around every launch on its stream, over the same steps replayed with the host-driven "
+                                     "pass loop (the timed steps run the device-resident loop, whose graph cannot hold events)"}
+        tr = kernel_traffic(args.kernel, c["name"])
+        if tr:
+            roofline["traffic"] = tr["dram_bytes_per_launch"]
+            roofline["traffic_source"] = tr["source"]
 
     cpu = None
     bit_exact = None

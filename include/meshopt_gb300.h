@@ -187,6 +187,15 @@ MESHOPTGPU_API void meshoptgpu_setBatchConfig(int threads, unsigned int smem_byt
  * (meshoptgpu_setTiming(1) keeps every call on the single-mesh path). Per calling thread;
  * default 24000, 0 disables. */
 MESHOPTGPU_API void meshoptgpu_setDropinBatchLimit(size_t max_index_count);
+
+/* The single-mesh path runs its pass loop (src/simplifier.cpp:2493-2541) on the device: one
+ * pass is recorded into a CUDA graph as the body of a WHILE conditional node and replayed
+ * until the loop ends, with no host round trip between passes. enabled = 0 switches the
+ * calling thread to the host-driven loop (one host read per pass), which per-launch kernel
+ * timing (meshoptgpu_setKernelProfile) needs. Pruning, the debug bit and
+ * meshoptgpu_setTiming(1) always use the host loop. Results are identical. Returns a
+ * meshoptgpu_Status* value. */
+MESHOPTGPU_API int meshoptgpu_setDeviceLoop(int enabled);
 MESHOPTGPU_API int meshoptgpu_getBatchThreads(void);
 
 /* ---- serving: continuous batching of simplify requests ---- */

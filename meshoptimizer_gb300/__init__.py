@@ -49,7 +49,7 @@ EXPORTS = [
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
     "meshoptgpu_optimizeVertexFetchRemapDevice", "meshoptgpu_optimizeVertexFetchDevice", "meshoptgpu_generatePositionRemapDevice",
-    "meshoptgpu_simplifyGroups", "meshoptgpu_setDropinBatchLimit",
+    "meshoptgpu_simplifyGroups", "meshoptgpu_setDropinBatchLimit", "meshoptgpu_setDeviceLoop",
 ]
 
 
@@ -134,6 +134,8 @@ def load():
     lib.meshoptgpu_generatePositionRemapDevice.restype = C.c_int
     lib.meshoptgpu_generatePositionRemapDevice.argtypes = [vp, vp, sz, sz, vp]
     lib.meshoptgpu_setDropinBatchLimit.argtypes = [sz]
+    lib.meshoptgpu_setDeviceLoop.restype = C.c_int
+    lib.meshoptgpu_setDeviceLoop.argtypes = [C.c_int]
     lib.meshoptgpu_simplifyGroups.restype = C.c_int
     lib.meshoptgpu_simplifyGroups.argtypes = [vp, vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, vp, vp, vp, f32, u32, vp, vp, vp]
     _lib = lib
@@ -440,6 +442,11 @@ def set_batch_config(threads=0, smem_bytes=0):
 def set_dropin_batch_limit(max_index_count=24000):
     """Drop-in calls on meshes with at most this many indices run on the batch kernel (0: never)."""
     load().meshoptgpu_setDropinBatchLimit(int(max_index_count))
+
+
+def set_device_loop(enabled=True):
+    """Pass loop of the single-mesh path on the device (CUDA graph, default) or driven by the host."""
+    return int(load().meshoptgpu_setDeviceLoop(1 if enabled else 0))
 
 
 def batch_threads():

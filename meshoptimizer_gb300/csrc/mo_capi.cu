@@ -1226,6 +1226,24 @@ void meshoptgpu_setDropinBatchLimit(size_t max_index_count)
 	state().dropin_batch_limit = max_index_count;
 }
 
+int meshoptgpu_setDeviceLoop(int enabled)
+{
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		Tuning t = s.simplifier->tuning();
+		t.device_loop = enabled != 0;
+		s.simplifier->setTuning(t);
+		return meshoptgpu_StatusOk;
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
 int meshoptgpu_getBatchThreads(void)
 {
 	ThreadState& s = state();

@@ -91,9 +91,20 @@ void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int
 	MO_LAUNCH(kScanApply, (unsigned)tiles, kScanThreads, 0, stream, in, out, n, sums, total, aligned);
 }
 
-__global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* __restrict__ keys, size_t n, int shift, unsigned int* __restrict__ hist, unsigned int tiles)
+// n_dev (optional): the live element count on the device, at most n; the grid covers n
+__device__ __forceinline__ size_t liveCount(size_t n, const unsigned int* n_dev)
+{
+	if (!n_dev)
+		return n;
+	size_t d = *n_dev;
+	return d < n ? d : n;
+}
+
+__global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* __restrict__ keys, size_t n, const unsigned int* n_dev, int shift,
+    unsigned int* __restrict__ hist, unsigned int tiles)
 {
 	__shared__ unsigned int sh[kSortBins];
+	n = liveCount(n, n_dev);
 	sh[threadIdx.x] = 0;
 	__syncthreads();
 	size_t base = (size_t)blockIdx.x * kSortTile + threadIdx.x;
@@ -112,9 +123,11 @@ __global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* _
 // j*256 .. j*256+255 of the tile; within it, warp w and lane l give the order), so equal
 // digits keep their input order; tiles are laid out by the digit-major scanned histogram.
 __global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
-    unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, size_t n, int shift, const unsigned int* __restrict__ hist, unsigned int tiles)
+    unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, size_t n, const unsigned int* n_dev, int shift, const unsigned int* __restrict__ hist,
+    unsigned int tiles)
 {
 	// vin == nullptr stands for the identity values 0..n-1
+	n = liveCount(n, n_dev);
 	__shared__ unsigned int base[kSortBins];
 	__shared__ unsigned int wcnt[2][kSortThreads / 32][kSortBins];
 
@@ -198,13 +211,15 @@ size_t radixScratchWords(size_t n)
 }
 
 void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
-    unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream)
+    unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream, const unsigned int* n_dev)
 {
 	if (n == 0)
 		return;
 	int passes = (bits + 7) / 8;
 	if (passes == 0)
 	{
+		if (n_dev)
+			throw std::invalid_argument("radixSortPairs: a device count needs at least one digit pass");
 		MO_CUDA_CHECK(cudaMemcpyAsync(keys_out, keys_in, n * 4, cudaMemcpyDeviceToDevice, stream));
 		MO_CUDA_CHECK(cudaMemcpyAsync(vals_out, vals_in, n * 4, cudaMemcpyDeviceToDevice, stream));
 		return;
@@ -222,9 +237,9 @@ void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, un
 		unsigned int* kd = to_out ? keys_out : keys_tmp;
 		unsigned int* vd = to_out ? vals_out : vals_tmp;
 		int shift = p * 8;
-		MO_LAUNCH(kRadixHist, tiles, kSortThreads, 0, stream, ks, n, shift, hist, tiles);
+		MO_LAUNCH(kRadixHist, tiles, kSortThreads, 0, stream, ks, n, n_dev, shift, hist, tiles);
 		scanExclusive(hist, hist, size_t(tiles) * kSortBins, nullptr, sscratch, stream);
-		MO_LAUNCH(kRadixScatter, tiles, kSortThreads, 0, stream, ks, vs, kd, vd, n, shift, hist, tiles);
+		MO_LAUNCH(kRadixScatter, tiles, kSortThreads, 0, stream, ks, vs, kd, vd, n, n_dev, shift, hist, tiles);
 		ks = kd;
 		vs = vd;
 	}

@@ -22,6 +22,7 @@ struct LaunchProbe
 	std::vector<cudaEvent_t> pool;
 	unsigned long long timed_launches = 0;
 	double timed_ms = 0;
+	bool capturing = false; // launches are being recorded into a graph: count them, record no events
 
 	~LaunchProbe();
 	cudaEvent_t take();
@@ -36,7 +37,7 @@ inline cudaEvent_t probeBegin(const char* name, cudaStream_t stream)
 	p.launches++;
 	while (*name == '(' || *name == ' ') // template kernels are passed parenthesised
 		++name;
-	if (p.selected.empty() || p.selected.compare(0, p.selected.size(), name, 0, p.selected.size()) != 0)
+	if (p.capturing || p.selected.empty() || p.selected.compare(0, p.selected.size(), name, 0, p.selected.size()) != 0)
 		return nullptr;
 	cudaEvent_t e = p.take();
 	cudaEventRecord(e, stream);

@@ -38,6 +38,26 @@ constexpr int kStopTile = 1024; // sorted candidates per block in the stop-rule 
 constexpr size_t kPinnedBytes = 16384; // host readback buffer of the scalars block
 constexpr unsigned int kApplyTile = 4096; // sorted positions compacted per block step in the apply phase
 
+// State of the device-resident pass loop: the counts each pass's kernels read instead of
+// launch parameters, so that one recorded pass can be replayed until the loop ends.
+struct PassLive
+{
+	const unsigned int* res;  // current index buffer
+	unsigned int* res_next;   // the next pass's
+	unsigned int indices;     // current index count
+	unsigned int tris;
+	unsigned int count;       // candidates of the pass
+	unsigned int stop;        // nonzero: the loop has ended; the pass's kernels return at once
+	unsigned long long goal;  // triangle goal of the pass
+	unsigned int first_window;
+	unsigned int round_base;
+	unsigned int passes;
+	unsigned int iterations;
+	unsigned int target;      // target_index_count
+	unsigned int pad;
+	double window_factor;
+};
+
 struct Scalars
 {
 	float minv[3];
@@ -69,6 +89,8 @@ struct Scalars
 	unsigned long long phase_cycles[8]; // kPerform phases, SM cycles of block 0, summed over the run
 	unsigned int trace_count;           // decision rounds traced so far in the run
 	unsigned int trace[2 * 512];        // per round: active candidates, SM cycles / 16
+	PassLive live;                      // device-resident pass loop
+	PassStats pstats[kMaxPassStats];    // its per-pass counters
 };
 
 static_assert(sizeof(Scalars) <= kPinnedBytes, "the scalars block must fit the pinned readback buffer");
@@ -324,8 +346,17 @@ __global__ void kCompactFlagged(const unsigned int* __restrict__ flags, const un
 
 // ---------------------------------------------------------------- setup: CSR
 
-__global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ cnt)
+// lv (device-resident pass loop, else nullptr): the index buffer and count come from it
+__global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ cnt,
+    const PassLive* lv = nullptr)
 {
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		idx = lv->res;
+		n = lv->indices;
+	}
 	size_t i = gtid();
 	if (i >= n)
 		return;
@@ -723,8 +754,15 @@ __global__ void kCapacity(size_t index_count, Scalars* sc)
 // ---------------------------------------------------------------- pass: adjacency
 
 __global__ void kAdjFill(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ off,
-    unsigned int* __restrict__ fill, uint2* __restrict__ adj)
+    unsigned int* __restrict__ fill, uint2* __restrict__ adj, const PassLive* lv)
 {
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		res = lv->res;
+		tris = lv->tris;
+	}
 	size_t t = gtid();
 	if (t >= tris)
 		return;
@@ -769,10 +807,21 @@ __device__ __forceinline__ bool pickEdge(unsigned int i0, unsigned int i1, const
 	return true;
 }
 
+// lv: counts of the live pass; the grid covers the first pass's triangles and the slots past
+// the live count are cleared, so the scan over the full range is the scan of the live one
 __global__ void kPickCount(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
-    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ cnt)
+    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ cnt, const PassLive* lv)
 {
 	size_t t = gtid();
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		if (t < tris && t >= lv->tris)
+			cnt[t] = 0;
+		res = lv->res;
+		tris = lv->tris;
+	}
 	if (t >= tris)
 		return;
 	unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
@@ -790,8 +839,15 @@ __global__ void kPickCount(const unsigned int* __restrict__ res, size_t tris, co
 // (the capacity check at :1319-1320 stops at the first triangle that does not)
 __global__ void kPickEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
     const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, const unsigned int* __restrict__ offs, Scalars* sc,
-    unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr)
+    unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr, const PassLive* lv)
 {
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		res = lv->res;
+		tris = lv->tris;
+	}
 	size_t t = gtid();
 	if (t >= tris)
 		return;
@@ -822,8 +878,15 @@ __global__ void kPickEmit(const unsigned int* __restrict__ res, size_t tris, con
 __global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr,
     unsigned int* __restrict__ ckey, const float4* __restrict__ pos, const Quadric* __restrict__ vq, const unsigned int* __restrict__ remap,
     const unsigned int* __restrict__ wedge, const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop,
-    const unsigned int* __restrict__ loopback, const float* __restrict__ attr, const Quadric* __restrict__ aq, const float4* __restrict__ ag, int ac)
+    const unsigned int* __restrict__ loopback, const float* __restrict__ attr, const Quadric* __restrict__ aq, const float4* __restrict__ ag, int ac,
+    const PassLive* lv)
 {
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		count = lv->count;
+	}
 	size_t c = gtid();
 	if (c >= count)
 		return;
@@ -879,8 +942,14 @@ __global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int
 __global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ order, const unsigned int* __restrict__ cv0, const unsigned int* __restrict__ cv1,
     const unsigned int* __restrict__ cerr, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
     const unsigned int* __restrict__ adj_off, uint4* __restrict__ srec, uint2* __restrict__ sidx, unsigned int* __restrict__ serr,
-    unsigned char* __restrict__ skind, unsigned char* __restrict__ status)
+    unsigned char* __restrict__ skind, unsigned char* __restrict__ status, const PassLive* lv)
 {
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		count = lv->count;
+	}
 	size_t k = gtid();
 	if (k >= count)
 		return;
@@ -955,6 +1024,9 @@ struct PerformArgs
 	unsigned int tris;
 	uint4* blk;
 	Scalars* sc;
+	// device-resident pass loop (else nullptr): count, goal, first_window, round_base, tris, res,
+	// res_next and the previous result error come from here instead of the fields above
+	const PassLive* live;
 };
 
 // Decision rule: candidate k is decided once nothing earlier in sorted order can change its
@@ -1261,6 +1333,26 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 	const size_t gthreads = (size_t)G * blockDim.x;
 	const unsigned int lane = threadIdx.x & 31;
 
+	// per-pass scalars: the launch parameters, or the device-resident loop's live state
+	unsigned int count = a.count, tris = a.tris, first_window = a.first_window, round_base = a.round_base, prev_err = a.prev_err_bits;
+	unsigned long long goal = a.goal;
+	const unsigned int* res = a.res;
+	unsigned int* res_next = a.res_next;
+	if (a.live)
+	{
+		const PassLive* lv = a.live;
+		if (lv->stop)
+			return;
+		count = lv->count;
+		tris = lv->tris;
+		first_window = lv->first_window;
+		round_base = lv->round_base;
+		goal = lv->goal;
+		res = lv->res;
+		res_next = lv->res_next;
+		prev_err = sc->result_error_bits;
+	}
+
 	for (size_t i = gtid(); i < a.vcount; i += gthreads)
 	{
 		a.touched[i] = 0;
@@ -1268,10 +1360,10 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		a.cr[i] = (unsigned int)i;
 	}
 
-	unsigned int round = a.round_base;
+	unsigned int round = round_base;
 	unsigned long long active_sum = 0;
-	unsigned int K0 = 0, K1 = min(a.count, a.first_window);
-	unsigned int carryT = 0, carryF = 0, carryM = a.prev_err_bits;
+	unsigned int K0 = 0, K1 = min(count, first_window);
+	unsigned int carryT = 0, carryF = 0, carryM = prev_err;
 	unsigned int windows = 0;
 
 	for (;;)
@@ -1305,7 +1397,7 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		while (n)
 		{
 			++round;
-			if (++guard > a.count + 1 || __ldcg(&sc->grid_error))
+			if (++guard > count + 1 || __ldcg(&sc->grid_error))
 				break;
 			active_sum += n;
 			const unsigned int* cur = a.list[round & 1] + region;
@@ -1414,20 +1506,20 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 			unsigned long long T = (unsigned long long)bb.x + eT;
 			unsigned long long F = (unsigned long long)bb.y + eF;
 			unsigned int M = max(bb.z, eM);
-			const unsigned long long egoal0 = a.goal / 2;
+			const unsigned long long egoal0 = goal / 2;
 			for (unsigned int k = t0; k < t1; ++k)
 			{
 				float e = __uint_as_float(__ldg(a.serr + k));
 				unsigned int reason = 0;
 				if (e > a.error_limit)
 					reason = 1;
-				else if (T >= a.goal)
+				else if (T >= goal)
 					reason = 2;
 				else
 				{
 					unsigned long long eg = egoal0 + F;
-					float error_goal = eg < a.count ? 1.5f * __uint_as_float(__ldg(a.serr + eg)) : FLT_MAX;
-					if (e > error_goal && e > __uint_as_float(M) && T > a.goal / 6)
+					float error_goal = eg < count ? 1.5f * __uint_as_float(__ldg(a.serr + eg)) : FLT_MAX;
+					if (e > error_goal && e > __uint_as_float(M) && T > goal / 6)
 						reason = 3;
 				}
 				if (reason)
@@ -1443,13 +1535,13 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		gridBarrier(sc->bar, &sc->grid_error);
 		if (timer)
 			pc.lap(kPhStop);
-		if (__ldcg(&sc->cut) != ~0ull || K1 == a.count || __ldcg(&sc->grid_error))
+		if (__ldcg(&sc->cut) != ~0ull || K1 == count || __ldcg(&sc->grid_error))
 			break;
 		carryT = __ldcg(&sc->carry[0]);
 		carryF = __ldcg(&sc->carry[1]);
 		carryM = __ldcg(&sc->carry[2]);
 		K0 = K1;
-		K1 = (unsigned int)min((unsigned long long)a.count, 2ull * K1);
+		K1 = (unsigned int)min((unsigned long long)count, 2ull * K1);
 	}
 	if (__ldcg(&sc->grid_error))
 		return;
@@ -1457,7 +1549,7 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 	// ---- apply the committed prefix: each block compacts the commits of its chunk of [0, cut)
 	// in shared memory, 4096 sorted positions at a time, so every lane applies a commit
 	const unsigned long long cutv = __ldcg(&sc->cut);
-	const unsigned int cut = cutv == ~0ull ? a.count : (unsigned int)(cutv >> 2);
+	const unsigned int cut = cutv == ~0ull ? count : (unsigned int)(cutv >> 2);
 	unsigned int nd = 0, ns = 0, ni = 0, em = 0, dm = 0;
 	{
 		__shared__ unsigned int clist[kApplyTile];
@@ -1526,7 +1618,7 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 				atomicAdd(&sc->phase_cycles[i], (unsigned long long)pc.acc[i]);
 		if (gtid() == 0)
 		{
-			sc->rounds = round - a.round_base;
+			sc->rounds = round - round_base;
 			sc->active_sum = active_sum;
 			sc->windows = windows;
 		}
@@ -1553,15 +1645,15 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 				L[i] = r;
 		}
 	}
-	const unsigned int tper_block = (a.tris + G - 1) / G;
-	const unsigned int tb0 = min(a.tris, blockIdx.x * tper_block), tb1 = min(a.tris, tb0 + tper_block);
+	const unsigned int tper_block = (tris + G - 1) / G;
+	const unsigned int tb0 = min(tris, blockIdx.x * tper_block), tb1 = min(tris, tb0 + tper_block);
 	const unsigned int tper_thread = (tb1 - tb0 + blockDim.x - 1) / blockDim.x;
 	const unsigned int tt0 = min(tb1, tb0 + threadIdx.x * tper_thread), tt1 = min(tb1, tt0 + tper_thread);
 	unsigned int kept = 0;
 	for (unsigned int t = tt0; t < tt1; ++t)
 	{
 		uint3 o;
-		kept += keepTriangle(a.res, t, a.cr, a.remap, o);
+		kept += keepTriangle(res, t, a.cr, a.remap, o);
 	}
 	unsigned int ek = kept, d1 = 0, d2 = 0;
 	uint3 ktot = blockScan3(ek, d1, d2, sm);
@@ -1585,7 +1677,7 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		if (threadIdx.x == 0)
 		{
 			sc->tri_total = run;
-			sc->rounds = round - a.round_base;
+			sc->rounds = round - round_base;
 			sc->active_sum = active_sum;
 			sc->windows = windows;
 		}
@@ -1598,11 +1690,11 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 		for (unsigned int t = tt0; t < tt1; ++t)
 		{
 			uint3 o;
-			if (keepTriangle(a.res, t, a.cr, a.remap, o))
+			if (keepTriangle(res, t, a.cr, a.remap, o))
 			{
-				a.res_next[(size_t)w * 3 + 0] = o.x;
-				a.res_next[(size_t)w * 3 + 1] = o.y;
-				a.res_next[(size_t)w * 3 + 2] = o.z;
+				res_next[(size_t)w * 3 + 0] = o.x;
+				res_next[(size_t)w * 3 + 1] = o.y;
+				res_next[(size_t)w * 3 + 2] = o.z;
 				w++;
 			}
 		}
@@ -1632,6 +1724,96 @@ __device__ __forceinline__ unsigned int ufFind(unsigned int* parent, unsigned in
 }
 
 // lock-free union-find over the welded edges: the larger root is linked under the smaller, so
+
+// ---------------------------------------------------------------- device-resident pass loop
+//
+// The pass loop (src/simplifier.cpp:2493-2541) recorded once into a CUDA graph as the body of
+// a WHILE conditional node: every kernel of a pass reads the pass's counts from PassLive, the
+// grids cover the first (largest) pass, and kPassEnd decides on the device whether another
+// pass runs, so the loop needs no host round trip.
+
+// After the pick: the pass's candidate count, triangle goal and first window (the host loop's
+// arithmetic), and the per-pass resets of kPerform's scalars. No candidate ends the loop (the
+// host loop's break at C == 0).
+__global__ void kPassPrep(Scalars* sc)
+{
+	PassLive& lv = sc->live;
+	if (lv.stop)
+		return;
+	unsigned int C = min(sc->pick_total, sc->pick_trunc);
+	lv.count = C;
+	if (C == 0)
+	{
+		lv.stop = 1;
+		return;
+	}
+	unsigned long long goal = (unsigned long long)(lv.indices - lv.target) / 3;
+	lv.goal = goal;
+	double wf = lv.window_factor * double(goal / 2) + 4096.0;
+	lv.first_window = unsigned(double(C) < wf ? double(C) : wf);
+	sc->bar[0] = 0;
+	sc->bar[1] = 0;
+	sc->grid_error = 0;
+	sc->cut = ~0ull;
+	sc->done = 0;
+	sc->skipped = 0;
+	sc->invalid = 0;
+}
+
+// After kPerform: the pass's counters (as the host loop records them), the next pass's index
+// buffer and counts, and the loop condition.
+__global__ void kPassEnd(Scalars* sc, cudaGraphConditionalHandle handle, unsigned int max_passes)
+{
+	PassLive& lv = sc->live;
+	lv.iterations++;
+	if (!lv.stop)
+	{
+		if (sc->grid_error)
+			lv.stop = 1; // reported by the host after the loop
+		else
+		{
+			const unsigned long long cutv = sc->cut;
+			const unsigned int C = lv.count;
+			const unsigned int cut = cutv == ~0ull ? C : (unsigned int)(cutv >> 2);
+			if (lv.passes < kMaxPassStats)
+			{
+				PassStats& ps = sc->pstats[lv.passes];
+				ps.triangles = lv.tris;
+				ps.candidates = C;
+				ps.evaluated = cut < C ? cut + 1 : C;
+				ps.done = sc->done;
+				ps.skipped = sc->skipped;
+				ps.invalid = sc->invalid;
+				ps.stop = cutv == ~0ull ? 0u : (unsigned int)(cutv & 3);
+				ps.rounds = sc->rounds;
+				ps.active = (unsigned int)sc->active_sum;
+				ps.windows = sc->windows;
+			}
+			lv.round_base += sc->rounds;
+			lv.passes++;
+			if (sc->done == 0)
+				lv.stop = 1;
+			else
+			{
+				lv.tris = sc->tri_total;
+				lv.indices = sc->tri_total * 3;
+				const unsigned int* r = lv.res;
+				lv.res = lv.res_next;
+				lv.res_next = const_cast<unsigned int*>(r);
+				if (lv.indices <= lv.target)
+					lv.stop = 1;
+				else if (lv.passes >= max_passes)
+				{
+					lv.stop = 1;
+					sc->grid_error |= 4u;
+				}
+			}
+		}
+	}
+	cudaGraphSetConditional(handle, lv.stop ? 0u : 1u);
+}
+
+
 // a component's root is its smallest primary vertex, as the reference's union-find leaves it
 __global__ void kUnionEdges(const unsigned int* __restrict__ idx, size_t tris, const unsigned int* __restrict__ remap, unsigned int* parent)
 {
@@ -1928,6 +2110,8 @@ Tuning Tuning::fromEnvironment()
 		t.perform_blocks_per_sm = std::max(1, atoi(v));
 	if (const char* v = getenv("MESHOPTGPU_WINDOW_FACTOR"))
 		t.window_factor = std::max(0.0, atof(v));
+	if (const char* v = getenv("MESHOPTGPU_DEVICE_LOOP"))
+		t.device_loop = atoi(v) != 0;
 	return t;
 }
 
@@ -1962,6 +2146,7 @@ Simplifier::Simplifier(int device) : device_(device)
 {
 	MO_CUDA_CHECK(cudaSetDevice(device));
 	MO_CUDA_CHECK(cudaMallocHost(&pinned_, kPinnedBytes));
+	MO_CUDA_CHECK(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking));
 	int sms = 0, per_sm = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
@@ -1973,6 +2158,8 @@ Simplifier::Simplifier(int device) : device_(device)
 
 Simplifier::~Simplifier()
 {
+	if (capture_)
+		cudaStreamDestroy(capture_);
 	if (pinned_)
 		cudaFreeHost(pinned_);
 }
@@ -2334,6 +2521,141 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	MO_CUDA_CHECK(cudaMemsetAsync(w.minT, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
 	MO_CUDA_CHECK(cudaMemsetAsync(w.minS, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
 
+	// ---- the pass loop on the device: one pass recorded into the body of a WHILE conditional
+	// node, replayed until kPassEnd ends it (pruning, the debug bit and per-phase event timing
+	// need the host between passes and take the host loop below)
+	if (tuning_.device_loop && !timed && !(m.options & (kOptPrune | kOptInternalDebug)) && result_count > m.target_index_count)
+	{
+		const size_t T0 = I / 3, capn = std::max<size_t>(hs->capacity, 1);
+		PassLive init{};
+		init.res = w.res0;
+		init.res_next = w.res1;
+		init.indices = unsigned(I);
+		init.tris = unsigned(T0);
+		init.target = unsigned(m.target_index_count);
+		init.window_factor = tuning_.window_factor;
+		MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->live, &init, sizeof(init), cudaMemcpyHostToDevice, stream));
+		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->result_error_bits, 0, 4, stream));
+		const PassLive* lv = &w.sc->live;
+
+		cudaGraph_t graph = nullptr;
+		cudaGraphExec_t exec = nullptr;
+		MO_CUDA_CHECK(cudaGraphCreate(&graph, 0));
+		cudaGraphConditionalHandle handle;
+		MO_CUDA_CHECK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+		cudaGraphNodeParams cp = {};
+		cp.type = cudaGraphNodeTypeConditional;
+		cp.conditional.handle = handle;
+		cp.conditional.type = cudaGraphCondTypeWhile;
+		cp.conditional.size = 1;
+		cudaGraphNode_t loop_node;
+		MO_CUDA_CHECK(cudaGraphAddNode(&loop_node, graph, nullptr, nullptr, 0, &cp));
+		cudaGraph_t body = cp.conditional.phGraph_out[0];
+
+		LaunchProbe& lp = probe();
+		const unsigned long long launches0 = lp.launches;
+		cudaStream_t cs = capture_; // recording only: nothing runs on it
+		MO_CUDA_CHECK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+		lp.capturing = true;
+		try
+		{
+			const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads), gC = gridFor(capn, kThreads);
+			MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, cs));
+			MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, cs));
+			MO_LAUNCH(kCountKeys, gI, kThreads, 0, cs, nullptr, w.remap, I, w.cnt, lv);
+			scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs);
+			MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, w.fill, w.adj, lv);
+			MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
+			scanExclusive(w.tcnt, w.tcnt, T0, &w.sc->pick_total, w.scratch, cs);
+			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
+			MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, lv);
+			MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
+			MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+			    w.attr, w.aq, w.ag, ac, lv);
+			radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count);
+			MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr,
+			    w.skind, w.status, lv);
+			PerformArgs pa;
+			pa.count = 0;
+			pa.srec = w.srec;
+			pa.sidx = w.sidx;
+			pa.skind = w.skind;
+			pa.serr = w.serr;
+			pa.status = w.status;
+			pa.vcount = unsigned(V);
+			pa.minT[0] = w.minT;
+			pa.minT[1] = w.minT + (V + 1);
+			pa.minS[0] = w.minS;
+			pa.minS[1] = w.minS + (V + 1);
+			pa.touched = w.touched;
+			pa.moved = w.moved;
+			pa.cr = w.cr;
+			pa.list[0] = w.act0;
+			pa.list[1] = w.act1;
+			pa.adj_off = w.adj_off;
+			pa.adj = w.adj;
+			pa.pos = w.pos;
+			pa.remap = w.remap;
+			pa.wedge = w.wedge;
+			pa.loop = w.loop;
+			pa.loopback = w.loopback;
+			pa.vq = w.vq;
+			pa.aq = w.aq;
+			pa.ag = w.ag;
+			pa.ac = ac;
+			pa.prev_err_bits = 0;
+			pa.error_limit = error_limit;
+			pa.goal = 0;
+			pa.first_window = 0;
+			pa.round_base = 0;
+			pa.res = nullptr;
+			pa.res_next = nullptr;
+			pa.tris = 0;
+			pa.blk = w.blk;
+			pa.sc = w.sc;
+			pa.live = lv;
+			unsigned int want = gridFor(std::max(std::max(capn, V), T0), kThreads);
+			unsigned int blocks = std::max(1u, std::min(perform_blocks_, want));
+			if (tuning_.perform_grid_cap > 0)
+				blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
+			if (size_t(blocks) * kThreads > kListSlack)
+				throw std::runtime_error("kPerform grid exceeds the candidate list slack");
+			void* params[] = {&pa};
+			lp.launches++;
+			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, cs));
+			MO_LAUNCH(kPassEnd, 1, 1, 0, cs, w.sc, handle, unsigned(T0 + 1));
+		}
+		catch (...)
+		{
+			lp.capturing = false;
+			cudaGraph_t dead = nullptr;
+			cudaStreamEndCapture(cs, &dead);
+			cudaGraphDestroy(graph);
+			throw;
+		}
+		lp.capturing = false;
+		cudaGraph_t captured = nullptr;
+		MO_CUDA_CHECK(cudaStreamEndCapture(cs, &captured));
+		const unsigned long long body_launches = lp.launches - launches0;
+		MO_CUDA_CHECK(cudaGraphInstantiate(&exec, graph, 0));
+		MO_CUDA_CHECK(cudaGraphLaunch(exec, stream));
+		readScalars();
+		cudaGraphExecDestroy(exec);
+		cudaGraphDestroy(graph);
+		// every replay of the body launched its kernels again
+		if (hs->live.iterations > 1)
+			lp.launches += body_launches * (hs->live.iterations - 1);
+		if (hs->grid_error)
+			throw std::runtime_error(hs->grid_error & 4 ? "pass loop did not converge"
+			                                            : (hs->grid_error & 2 ? "collapse decision round made no progress" : "grid barrier wait limit reached"));
+		passes = int(hs->live.passes);
+		for (int p = 0; p < passes && p < kMaxPassStats; ++p)
+			rr.pass[p] = hs->pstats[p];
+		result_error_bits = hs->result_error_bits;
+		result_count = hs->live.indices;
+		res = const_cast<unsigned int*>(hs->live.res);
+	}
+	else
 	while (result_count > m.target_index_count)
 	{
 		const size_t T = result_count / 3;
@@ -2346,15 +2668,15 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
 		MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
 		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream);
-		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj);
+		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[3], stream));
 
 		// pick
-		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt);
+		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, nullptr);
 		scanExclusive(w.tcnt, w.tcnt, T, &w.sc->pick_total, w.scratch, stream);
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, stream));
-		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr);
+		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, nullptr);
 		readScalars();
 		const size_t C = std::min<size_t>(hs->pick_total, hs->pick_trunc);
 		if (timed)
@@ -2365,12 +2687,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 
 		// rank + sort
 		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback, w.attr, w.aq,
-		    w.ag, ac);
+		    w.ag, ac, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
 		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream);
 		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr, w.skind,
-		    w.status);
+		    w.status, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
@@ -2415,6 +2737,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.res_next = res_next;
 			pa.tris = unsigned(T);
 			pa.blk = w.blk;
+			pa.live = nullptr;
 			pa.sc = w.sc;
 			MO_CUDA_CHECK(cudaMemsetAsync(w.sc->bar, 0, sizeof(unsigned int) * 3, stream));
 			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->cut, 0xFF, 8, stream));

@@ -100,13 +100,15 @@ private:
 };
 
 // Launch-shape parameters (picked by the autotuner, or set with environment variables
-// MESHOPTGPU_PERFORM_BLOCKS_PER_SM and MESHOPTGPU_WINDOW_FACTOR).
+// MESHOPTGPU_PERFORM_BLOCKS_PER_SM, MESHOPTGPU_WINDOW_FACTOR and MESHOPTGPU_DEVICE_LOOP).
 struct Tuning
 {
 	int perform_blocks_per_sm = 4;  // resident blocks per SM of the cooperative pass kernel
 	double window_factor = 2.0;     // first decision window = factor * (triangle goal / 2) + 4096
 	int perform_grid_cap = 0;       // at most this many blocks for the pass kernel (0: no cap); lets
 	                                // concurrent simplifications share the GPU
+	bool device_loop = true;        // run the pass loop as a device-resident CUDA graph (off: one host
+	                                // round trip per pass, needed for per-kernel event timing)
 	static Tuning fromEnvironment();
 };
 
@@ -136,6 +138,8 @@ private:
 	DeviceArena arena_;
 	DeviceArena sparse_arena_; // compact copy of a sparse subset
 	unsigned int* pinned_ = nullptr; // small pinned readback buffer
+	cudaStream_t capture_ = nullptr; // records the device-resident pass loop (the caller's stream may be
+	                                 // the legacy default stream, which cannot capture)
 	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative pass kernel (occupancy)
 	unsigned int perform_blocks_ = 1;
 	int sms_ = 1;
