@@ -76,9 +76,18 @@ size_t mo_simplifyWithAttributes(unsigned int* destination, const unsigned int* 
 	    target_index_count, target_error, options, result_error, NULL, NULL);
 }
 
+size_t mo_simplifyWithUpdate(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
+    float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
+    size_t target_index_count, float target_error, unsigned int options, float* result_error)
+{
+	return simplify_edge_f32(indices, indices, index_count, vertex_positions, vertex_count, vertex_positions_stride, vertex_attributes,
+	    vertex_attributes_stride, attribute_weights, attribute_count, vertex_lock, target_index_count, target_error, options | MO_InternalSolve,
+	    result_error, NULL, NULL);
+}
+
 float mo_simplifyScale(const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride)
 {
-	return rescale_positions_f32(NULL, vertex_positions, vertex_count, vertex_positions_stride / sizeof(float), NULL);
+	return rescale_positions_f32(NULL, vertex_positions, vertex_count, vertex_positions_stride / sizeof(float), NULL, NULL);
 }
 
 /* ---- the step after the simplifier in its callers (compaction of the vertex buffer) ---- */

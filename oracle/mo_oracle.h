@@ -29,6 +29,7 @@ enum
 	MO_Regularize = 1 << 4,
 	MO_Permissive = 1 << 5,
 	MO_RegularizeLight = 1 << 6,
+	MO_InternalSolve = 1 << 29,  /* meshopt_simplifyWithUpdate's mode (src/simplifier.cpp:2340) */
 	MO_InternalDebug = 1 << 30,
 };
 
@@ -92,6 +93,12 @@ size_t mo_simplifyWithAttributes(unsigned int* destination, const unsigned int* 
     const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
     const float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
     const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error);
+
+/* meshoptimizer.h:560: simplifies indices in place and writes the optimal positions (and
+ * attributes) of the vertices the result uses back into the caller's buffers */
+size_t mo_simplifyWithUpdate(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
+    float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
+    size_t target_index_count, float target_error, unsigned int options, float* result_error);
 
 /* meshoptimizer.h:611 */
 float mo_simplifyScale(const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride);

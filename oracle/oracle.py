@@ -255,6 +255,44 @@ def generate_position_remap(kind, positions):
     return out[:positions.shape[0]]
 
 
+def simplify_with_update(kind, indices, positions, target_index_count, target_error, options=0, attributes=None, weights=None, lock=None):
+    """meshopt_simplifyWithUpdate on copies of the inputs: returns (indices, positions, attributes,
+    result_error) with the positions (and attributes) as the call leaves them."""
+    o = load(kind)
+    f = getattr(o.lib, ("mo_" if kind == "port" else "meshopt_") + "simplifyWithUpdate")
+    f.restype = C.c_size_t
+    f.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                  C.c_size_t, C.c_float, C.c_uint, C.c_void_p]
+    idx = np.array(indices, dtype=np.uint32, copy=True)
+    pos = np.array(positions, dtype=np.float32, copy=True)
+    attr = None if attributes is None else np.array(attributes, dtype=np.float32, copy=True)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    lk = None if lock is None else np.ascontiguousarray(lock, dtype=np.uint8)
+    err = C.c_float(0)
+    n = f(_ptr(idx), len(idx), _ptr(pos), pos.shape[0], pos.shape[1] * 4, _ptr(attr), 0 if attr is None else attr.shape[1] * 4, _ptr(w),
+          0 if w is None else len(w), _ptr(lk), int(target_index_count), float(target_error), int(options), C.byref(err))
+    return idx[:n].copy(), pos, attr, float(err.value)
+
+
+def simplify_with_update_interleaved(kind, indices, vertices, stride_f, attr_offset, weights, lock, target_index_count, target_error, options=0):
+    """meshopt_simplifyWithUpdate on one interleaved float vertex buffer (positions first, the
+    attributes attr_offset floats into each stride_f-float vertex), on copies: returns
+    (indices, vertices, result_error)."""
+    o = load(kind)
+    f = getattr(o.lib, ("mo_" if kind == "port" else "meshopt_") + "simplifyWithUpdate")
+    f.restype = C.c_size_t
+    f.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                  C.c_size_t, C.c_float, C.c_uint, C.c_void_p]
+    ib = np.array(indices, np.uint32, copy=True)
+    v = np.array(vertices, np.float32, copy=True).reshape(-1)
+    w = np.ascontiguousarray(weights, np.float32)
+    lk = None if lock is None else np.ascontiguousarray(lock, np.uint8)
+    err = C.c_float(0)
+    n = f(_ptr(ib), len(ib), _ptr(v), len(v) // stride_f, stride_f * 4, v.ctypes.data + attr_offset * 4, stride_f * 4, _ptr(w), len(w), _ptr(lk),
+          int(target_index_count), float(target_error), int(options), C.byref(err))
+    return ib[:n].copy(), v, float(err.value)
+
+
 def simplify_scale(kind, positions):
     o = load(kind)
     positions = np.ascontiguousarray(positions, dtype=np.float32)

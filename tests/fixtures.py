@@ -54,3 +54,15 @@ def clod_cases():
         prefix = f"{i}_"
         out.append({k[len(prefix):]: z[k] for k in z.files if k.startswith(prefix)})
     return out
+
+
+def update_cases():
+    z = np.load(os.path.join(GOLDEN, "update_cases.npz"))
+    out = []
+    for i in range(int(z["count"])):
+        prefix = f"{i}_"
+        d = {k[len(prefix):]: z[k] for k in z.files if k.startswith(prefix)}
+        d["name"] = str(d["name"])
+        d["kind"] = str(d["kind"])
+        out.append(d)
+    return out

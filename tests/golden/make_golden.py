@@ -17,6 +17,9 @@ It writes two files next to this script:
 * ``clod_cases.npz`` -- two cluster-LOD levels (boundary locks from the reference builder's
   lockBoundary through oracle/clod_ref.cpp, then every group through the reference
   simplifier) over one shared vertex buffer.
+* ``update_cases.npz`` -- meshopt_simplifyWithUpdate: the reference's simplifyUpdate tests
+  (asserted here) and seeded meshes, with the indices, positions and attributes the reference
+  leaves.
 * ``compaction_cases.npz`` -- seeded inputs of the compaction step after the simplifier
   (meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch,
   meshopt_generatePositionRemap) with the reference library's outputs.
@@ -325,6 +328,51 @@ def clod_cases():
     return cases
 
 
+def update_cases():
+    """meshopt_simplifyWithUpdate: the reference's simplifyUpdate / simplifyUpdateLocked tests
+    (demo/tests.cpp:2590-2665; one interleaved buffer, their asserts checked here) and seeded
+    meshes with separate position and attribute arrays."""
+    body = _function_body(open(TESTS_CPP).read(), "simplifyUpdate")
+    vb = np.array(_np(_arrays(body), "vb"), np.float32)
+    ib = np.array(_np(_arrays(body), "ib"), np.uint32)
+    expected = np.array([0, 1, 3, 3, 1, 2, 0, 3, 2], np.uint32)
+    cases = []
+    for name, lock, options in (("simplifyUpdate", None, 0), ("simplifyUpdateLocked", np.array([0, 0, 0, 1, 0], np.uint8), 0),
+                                ("simplifyUpdateLocked_sparse", np.array([0, 0, 0, 1, 0], np.uint8), 2)):
+        out, v, err = oracle.simplify_with_update_interleaved("reference", ib, vb, 4, 3, [1.0], lock, 9, 1.0, options)
+        assert np.array_equal(out, expected), name
+        vv = v.reshape(-1, 4)
+        assert all(abs(vv[i][3]) < 1e-6 for i in range(3)), name
+        if lock is None:
+            assert abs(vv[3][0] - 0.88) < 1e-2 and abs(vv[3][1] - 0.19) < 1e-2 and abs(vv[3][2] - 0.11) < 1e-2 and abs(vv[3][3] - 0.18) < 1e-2
+        else:
+            assert vv[3][0] == np.float32(0.9) and vv[3][1] == np.float32(0.2) and vv[3][2] == np.float32(0.1) and vv[3][3] == np.float32(0.2)
+        cases.append(dict(name=name, kind="interleaved", indices=ib, vertices=vb, lock=lock, options=np.array(options), target=np.array(9),
+                          error=np.array(1.0, np.float32), out=out, out_vertices=v, out_error=np.array(err, np.float32)))
+    rng = np.random.default_rng(99)
+    seeded = []
+    for n in (16, 33):
+        idx, pos = W.heightfield(n, seed=n)
+        seeded.append((f"update_hf{n}", idx, pos, None, None, None, W.target_count(len(idx), 0.3), 1e-1, 0))
+    for lv in (3, 4):
+        idx, pos, attr, w = W.octa_sphere(lv, seed=lv)
+        lock = rng.choice(np.array([0, 0, 0, 1, 2, 4], np.uint8), size=len(pos))
+        seeded.append((f"update_sphere{lv}_attr", idx, pos, attr, w, None, W.target_count(len(idx), 0.25), 5e-2, 0))
+        seeded.append((f"update_sphere{lv}_attr_lock_permissive", idx, pos, attr, w, lock, W.target_count(len(idx), 0.25), 5e-2, 32))
+        half = idx[: (len(idx) // 6) * 3]
+        seeded.append((f"update_sphere{lv}_sparse", half, pos, attr, w, None, W.target_count(len(half), 0.25), 5e-2, 2 | 4))
+    for name, idx, pos, attr, w, lock, target, error, options in seeded:
+        out, p2, a2, err = oracle.simplify_with_update("reference", idx, pos, target, error, options, attributes=attr, weights=w, lock=lock)
+        c = dict(name=name, kind="separate", indices=idx, positions=pos, target=np.array(target), error=np.array(error, np.float32),
+                 options=np.array(options), out=out, out_positions=p2, out_error=np.array(err, np.float32))
+        if attr is not None:
+            c.update(attributes=attr, weights=w, out_attributes=a2)
+        if lock is not None:
+            c["lock"] = lock
+        cases.append(c)
+    return cases
+
+
 def main():
     ka = known_answer_cases()
     js = []
@@ -369,6 +417,16 @@ def main():
     blob["count"] = np.array(len(kc))
     np.savez_compressed(os.path.join(HERE, "clod_cases.npz"), **blob)
     print(f"cluster-LOD cases: {len(kc)}")
+
+    uc = update_cases()
+    blob = {}
+    for i, c in enumerate(uc):
+        for k, v in c.items():
+            if v is not None:
+                blob[f"{i}_{k}"] = np.asarray(v)
+    blob["count"] = np.array(len(uc))
+    np.savez_compressed(os.path.join(HERE, "update_cases.npz"), **blob)
+    print(f"update cases: {len(uc)}")
 
 
 if __name__ == "__main__":

@@ -105,3 +105,25 @@ def test_clod_level_port_matches_golden(port):
             assert np.array_equal(np.concatenate([o for o, _ in res]), c[f"l{level}_out"])
             assert np.array_equal(np.array([len(o) for o, _ in res]), c[f"l{level}_counts"].astype(np.int64))
             assert np.array_equal(np.array([e for _, e in res], np.float32), c[f"l{level}_errors"])
+
+
+def test_update_port_matches_golden(port):
+    """meshopt_simplifyWithUpdate's restatement against the reference library's indices,
+    rewritten positions and attributes, and error (the reference's own simplifyUpdate tests and
+    seeded meshes), bit for bit."""
+    from fixtures import update_cases
+
+    for c in update_cases():
+        if c["kind"] == "interleaved":
+            out, v, err = port.simplify_with_update_interleaved("port", c["indices"], c["vertices"], 4, 3, [1.0], c.get("lock"), int(c["target"]),
+                                                                float(c["error"]), int(c["options"]))
+            assert np.array_equal(out, c["out"]), c["name"]
+            assert np.array_equal(v.view(np.uint32), c["out_vertices"].reshape(-1).view(np.uint32)), c["name"]
+        else:
+            out, p2, a2, err = port.simplify_with_update("port", c["indices"], c["positions"], int(c["target"]), float(c["error"]), int(c["options"]),
+                                                         attributes=c.get("attributes"), weights=c.get("weights"), lock=c.get("lock"))
+            assert np.array_equal(out, c["out"]), c["name"]
+            assert np.array_equal(p2.view(np.uint32), c["out_positions"].view(np.uint32)), c["name"]
+            if "out_attributes" in c:
+                assert np.array_equal(a2.view(np.uint32), c["out_attributes"].view(np.uint32)), c["name"]
+        assert np.float32(err) == c["out_error"], c["name"]
