@@ -101,6 +101,21 @@ MESHOPTGPU_API void meshoptgpu_setTiming(int enabled);
 MESHOPTGPU_API int meshoptgpu_getLastRoundTrace(unsigned int* active, float* micros, int max_rounds);
 MESHOPTGPU_API int meshoptgpu_getLastPhaseTimes(float* out16);
 
+/* meshoptimizer.h:560 (src/simplifier.cpp:2642): simplifies indices in place and writes the
+ * optimal positions (and attributes) of the vertices the result uses back into the caller's
+ * buffers. Same results as the reference. Prune and the debug bit are not implemented here
+ * (they return meshoptgpu_StatusUnsupported with the buffers unchanged). */
+MESHOPTGPU_API size_t meshopt_simplifyWithUpdate(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count,
+    size_t vertex_positions_stride, float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
+    const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error);
+
+/* Device-resident form of meshopt_simplifyWithUpdate: indices, positions, attributes and
+ * vertex_lock are DEVICE pointers (updated in place), attribute_weights is host; work on
+ * `stream`, returning once the result count is known. */
+MESHOPTGPU_API size_t meshoptgpu_simplifyWithUpdateDevice(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count,
+    size_t vertex_positions_stride, float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
+    const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error, void* stream);
+
 /* Device-resident form of meshopt_simplifyWithAttributes: every array pointer is a DEVICE
  * pointer on the current device, except attribute_weights (host, at most 32 floats).
  * destination must hold index_count indices and may alias indices. Work is queued on

@@ -40,7 +40,8 @@ STATUS_OUT_OF_MEMORY = 4
 
 # every symbol include/meshopt_gb300.h declares
 EXPORTS = [
-    "meshopt_simplify", "meshopt_simplifyWithAttributes", "meshopt_simplifyScale",
+    "meshopt_simplify", "meshopt_simplifyWithAttributes", "meshopt_simplifyScale", "meshopt_simplifyWithUpdate",
+    "meshoptgpu_simplifyWithUpdateDevice",
     "meshoptgpu_getLastStatus", "meshoptgpu_getLastMessage", "meshoptgpu_getLastPassStats",
     "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
     "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
@@ -134,6 +135,10 @@ def load():
     lib.meshoptgpu_generatePositionRemapDevice.restype = C.c_int
     lib.meshoptgpu_generatePositionRemapDevice.argtypes = [vp, vp, sz, sz, vp]
     lib.meshoptgpu_setDropinBatchLimit.argtypes = [sz]
+    lib.meshopt_simplifyWithUpdate.restype = sz
+    lib.meshopt_simplifyWithUpdate.argtypes = [vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp]
+    lib.meshoptgpu_simplifyWithUpdateDevice.restype = sz
+    lib.meshoptgpu_simplifyWithUpdateDevice.argtypes = [vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp, vp]
     lib.meshoptgpu_setDeviceLoop.restype = C.c_int
     lib.meshoptgpu_setDeviceLoop.argtypes = [C.c_int]
     lib.meshoptgpu_simplifyGroups.restype = C.c_int
@@ -190,6 +195,53 @@ def simplify(indices, positions, target_index_count, target_error, options=0, at
                                                float(target_error), int(options), C.byref(err))
     _check(check)
     return out[:n].copy(), float(err.value)
+
+
+def simplify_with_update(indices, positions, target_index_count, target_error, options=0, attributes=None, weights=None, lock=None, check=True):
+    """meshopt_simplifyWithUpdate on copies of host arrays: returns (indices, positions, attributes,
+    result_error) as the call leaves them (positions float32 [V, k>=3]; attributes float32 [V, a])."""
+    lib = load()
+    idx = np.array(indices, dtype=np.uint32, copy=True)
+    pos = np.array(positions, dtype=np.float32, copy=True)
+    attr = None if attributes is None else np.array(attributes, dtype=np.float32, copy=True)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    lk = None if lock is None else np.ascontiguousarray(lock, dtype=np.uint8)
+    err = C.c_float(0)
+    n = lib.meshopt_simplifyWithUpdate(_p(idx), len(idx), _p(pos), pos.shape[0], pos.shape[1] * 4, _p(attr), 0 if attr is None else attr.shape[1] * 4,
+                                       _p(w), 0 if w is None else len(w), _p(lk), int(target_index_count), float(target_error), int(options),
+                                       C.byref(err))
+    _check(check)
+    return idx[:n].copy(), pos, attr, float(err.value)
+
+
+def simplify_with_update_interleaved(indices, vertices, stride_f, attr_offset, weights, lock, target_index_count, target_error, options=0, check=True):
+    """meshopt_simplifyWithUpdate on one interleaved float vertex buffer (positions first, the
+    attributes attr_offset floats into each stride_f-float vertex), on copies: returns
+    (indices, vertices, result_error)."""
+    lib = load()
+    ib = np.array(indices, np.uint32, copy=True)
+    v = np.array(vertices, np.float32, copy=True).reshape(-1)
+    w = np.ascontiguousarray(weights, np.float32)
+    lk = None if lock is None else np.ascontiguousarray(lock, np.uint8)
+    err = C.c_float(0)
+    n = lib.meshopt_simplifyWithUpdate(_p(ib), len(ib), _p(v), len(v) // stride_f, stride_f * 4, C.c_void_p(v.ctypes.data + attr_offset * 4),
+                                       stride_f * 4, _p(w), len(w), _p(lk), int(target_index_count), float(target_error), int(options), C.byref(err))
+    _check(check)
+    return ib[:n].copy(), v, float(err.value)
+
+
+def simplify_with_update_device(d_indices, index_count, d_positions, vertex_count, positions_stride, target_index_count, target_error, options=0,
+                                d_attributes=0, attributes_stride=0, weights=None, d_lock=0, stream=0, check=True):
+    """meshoptgpu_simplifyWithUpdateDevice with raw device pointers (updated in place)."""
+    lib = load()
+    err = C.c_float(0)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    n = lib.meshoptgpu_simplifyWithUpdateDevice(C.c_void_p(d_indices), index_count, C.c_void_p(d_positions), vertex_count, positions_stride,
+                                                C.c_void_p(d_attributes or None), attributes_stride, _p(w), 0 if w is None else len(w),
+                                                C.c_void_p(d_lock or None), int(target_index_count), float(target_error), int(options), C.byref(err),
+                                                C.c_void_p(stream or None))
+    _check(check)
+    return int(n), float(err.value)
 
 
 def simplify_raw(destination, indices, index_count, positions, vertex_count, positions_stride, target_index_count, target_error,

@@ -92,7 +92,7 @@ struct ThreadState
 	PhaseTimes times;
 	bool timing = false;
 	// batched path
-	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch, group_scratch;
+	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch, group_scratch, update_io;
 	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
 	unsigned int batch_smem = 0;    // 0: default budget
@@ -310,6 +310,85 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 	catch (const std::exception& e)
 	{
 		return failHost(destination, indices, index_count, result_error, statusOf(e), e.what());
+	}
+}
+
+// ---------------------------------------------------------------- the update mode
+
+// meshopt_simplifyWithUpdate on host buffers. The vertex data goes to the device as one region
+// when positions and attributes overlap (one interleaved buffer, as the reference's tests pass
+// it) or as two, and comes back the same way after the write-back.
+size_t updateHost(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
+    float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
+    size_t target_index_count, float target_error, unsigned int options, float* result_error)
+{
+	std::string bad = checkArgs(index_count, vertex_positions_stride, target_index_count, target_error, vertex_attributes_stride, attribute_weights,
+	    attribute_count, options);
+	if (!bad.empty())
+		return failHost(indices, indices, index_count, result_error,
+		    (options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument, bad);
+	if (options & (kOptPrune | kOptInternalDebug))
+		return failHost(indices, indices, index_count, result_error, meshoptgpu_StatusUnsupported,
+		    "meshopt_simplifyWithUpdate with Prune or the debug bit is not implemented on the GPU path");
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		const size_t pbytes = vertex_count * vertex_positions_stride;
+		const size_t abytes = attribute_count ? vertex_count * vertex_attributes_stride : 0;
+		const char* P = reinterpret_cast<const char*>(vertex_positions);
+		const char* A = reinterpret_cast<const char*>(vertex_attributes);
+		const bool joint = abytes && A < P + pbytes && P < A + abytes;
+		const char* lo = joint ? std::min(P, A) : P;
+		const size_t span = joint ? size_t(std::max(P + pbytes, A + abytes) - lo) : pbytes;
+		size_t b_idx = align256(index_count * 4), b_v = align256(span), b_a = joint ? 0 : align256(abytes), b_lock = vertex_lock ? align256(vertex_count) : 0;
+		char* base = static_cast<char*>(s.update_io.ensure(b_idx + b_v + b_a + b_lock + 256));
+		unsigned int* d_idx = reinterpret_cast<unsigned int*>(base);
+		char* d_v = base + b_idx;
+		float* d_pos = reinterpret_cast<float*>(d_v + (P - lo));
+		float* d_attr = abytes ? (joint ? reinterpret_cast<float*>(d_v + (A - lo)) : reinterpret_cast<float*>(base + b_idx + b_v)) : nullptr;
+		unsigned char* d_lock = vertex_lock ? reinterpret_cast<unsigned char*>(base + b_idx + b_v + b_a) : nullptr;
+		cudaStream_t st = s.stream;
+		if (index_count)
+			MO_CUDA_CHECK(cudaMemcpyAsync(d_idx, indices, index_count * 4, cudaMemcpyHostToDevice, st));
+		if (span)
+			MO_CUDA_CHECK(cudaMemcpyAsync(d_v, lo, span, cudaMemcpyHostToDevice, st));
+		if (abytes && !joint)
+			MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, A, abytes, cudaMemcpyHostToDevice, st));
+		if (d_lock)
+			MO_CUDA_CHECK(cudaMemcpyAsync(d_lock, vertex_lock, vertex_count, cudaMemcpyHostToDevice, st));
+		MeshDesc m;
+		m.indices = d_idx;
+		m.index_count = index_count;
+		m.positions = d_pos;
+		m.vertex_count = vertex_count;
+		m.positions_stride = vertex_positions_stride;
+		m.attributes = d_attr;
+		m.attributes_stride = vertex_attributes_stride;
+		m.weights = attribute_weights;
+		m.attribute_count = attribute_count;
+		m.lock = d_lock;
+		m.target_index_count = target_index_count;
+		m.target_error = target_error;
+		m.options = options | kOptInternalSolve;
+		m.update_positions = d_pos;
+		m.update_attributes = d_attr;
+		s.last = s.simplifier->run(m, d_idx, st, s.timing ? &s.times : nullptr);
+		if (s.last.index_count)
+			MO_CUDA_CHECK(cudaMemcpyAsync(indices, d_idx, s.last.index_count * 4, cudaMemcpyDeviceToHost, st));
+		if (span)
+			MO_CUDA_CHECK(cudaMemcpyAsync(const_cast<char*>(lo), d_v, span, cudaMemcpyDeviceToHost, st));
+		if (abytes && !joint)
+			MO_CUDA_CHECK(cudaMemcpyAsync(vertex_attributes, d_attr, abytes, cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		if (result_error)
+			*result_error = s.last.result_error;
+		setStatus(meshoptgpu_StatusOk, "");
+		return s.last.index_count;
+	}
+	catch (const std::exception& e)
+	{
+		return failHost(indices, indices, index_count, result_error, statusOf(e), e.what());
 	}
 }
 
@@ -774,6 +853,68 @@ void largeWorker(ServerImpl* S)
 } // namespace
 
 extern "C" {
+
+size_t meshopt_simplifyWithUpdate(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride,
+    float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count, const unsigned char* vertex_lock,
+    size_t target_index_count, float target_error, unsigned int options, float* result_error)
+{
+	return updateHost(indices, index_count, vertex_positions, vertex_count, vertex_positions_stride, vertex_attributes, vertex_attributes_stride,
+	    attribute_weights, attribute_count, vertex_lock, target_index_count, target_error, options, result_error);
+}
+
+size_t meshoptgpu_simplifyWithUpdateDevice(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count,
+    size_t vertex_positions_stride, float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
+    const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error, void* stream)
+{
+	std::string bad = checkArgs(index_count, vertex_positions_stride, target_index_count, target_error, vertex_attributes_stride, attribute_weights,
+	    attribute_count, options);
+	if (bad.empty() && (options & (kOptPrune | kOptInternalDebug)))
+		bad = "meshopt_simplifyWithUpdate with Prune or the debug bit is not implemented on the GPU path";
+	if (!bad.empty())
+	{
+		setStatus((options & ~kSupportedOptions) || (options & (kOptPrune | kOptInternalDebug)) ? meshoptgpu_StatusUnsupported
+		                                                                                      : meshoptgpu_StatusInvalidArgument,
+		    bad);
+		if (result_error)
+			*result_error = 0.f;
+		return index_count;
+	}
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		MeshDesc m;
+		m.indices = indices;
+		m.index_count = index_count;
+		m.positions = vertex_positions;
+		m.vertex_count = vertex_count;
+		m.positions_stride = vertex_positions_stride;
+		m.attributes = attribute_count ? vertex_attributes : nullptr;
+		m.attributes_stride = vertex_attributes_stride;
+		m.weights = attribute_weights;
+		m.attribute_count = attribute_count;
+		m.lock = vertex_lock;
+		m.target_index_count = target_index_count;
+		m.target_error = target_error;
+		m.options = options | kOptInternalSolve;
+		m.update_positions = vertex_positions;
+		m.update_attributes = attribute_count ? vertex_attributes : nullptr;
+		s.last = s.simplifier->run(m, indices, st, s.timing ? &s.times : nullptr);
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		if (result_error)
+			*result_error = s.last.result_error;
+		setStatus(meshoptgpu_StatusOk, "");
+		return s.last.index_count;
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		if (result_error)
+			*result_error = 0.f;
+		return index_count;
+	}
+}
 
 int meshoptgpu_simplifyBatch(const meshoptgpu_BatchMesh* meshes, size_t mesh_count, size_t* result_index_counts, float* result_errors, void* stream)
 {

@@ -33,6 +33,7 @@ enum : unsigned int
 	kOptRegularize = 1u << 4,
 	kOptPermissive = 1u << 5,
 	kOptRegularizeLight = 1u << 6,
+	kOptInternalSolve = 1u << 29, // meshopt_simplifyWithUpdate's mode (src/simplifier.cpp:2340)
 	kOptInternalDebug = 1u << 30,
 };
 
@@ -315,6 +316,98 @@ __device__ __forceinline__ float qerrorAttr(const Quadric& Q, const float4* __re
 		r += a * (a * Q.w - 2 * g);
 	}
 	return fabsf(r);
+}
+
+// ---- the update mode (meshopt_simplifyWithUpdate)
+
+// quadricVolumeGradient, :952-965: gradient of the signed volume under a face
+__device__ __forceinline__ float4 qvolumeGrad(const V3& p0, const V3& p1, const V3& p2)
+{
+	V3 p10 = {p1.x - p0.x, p1.y - p0.y, p1.z - p0.z};
+	V3 p20 = {p2.x - p0.x, p2.y - p0.y, p2.z - p0.z};
+	V3 n = {p10.y * p20.z - p10.z * p20.y, p10.z * p20.x - p10.x * p20.z, p10.x * p20.y - p10.y * p20.x};
+	float area = vnormalize(n) * 0.5f;
+	return make_float4(n.x * area, n.y * area, n.z * area, (-p0.x * n.x - p0.y * n.y - p0.z * n.z) * area);
+}
+
+__device__ __forceinline__ void gadd(float4& g, const float4& h)
+{
+	g.x += h.x;
+	g.y += h.y;
+	g.z += h.z;
+	g.w += h.w;
+}
+
+// quadricSolve, :967-1022: LDL^T solve of the quadric's 3x3 system, augmented with the volume
+// constraint GV as a Lagrange row; false when a pivot is too small
+__device__ __forceinline__ bool qsolve(V3& p, const Quadric& Q, const float4& GV)
+{
+	float a00 = Q.a00, a11 = Q.a11, a22 = Q.a22;
+	float a10 = Q.a10, a20 = Q.a20, a21 = Q.a21;
+	float x0 = -Q.b0, x1 = -Q.b1, x2 = -Q.b2;
+	float eps = 1e-6f * Q.w;
+
+	float d0 = a00;
+	float l10 = a10 / d0;
+	float l20 = a20 / d0;
+	float d1 = a11 - a10 * l10;
+	float dl21 = a21 - a20 * l10;
+	float l21 = dl21 / d1;
+	float d2 = a22 - a20 * l20 - dl21 * l21;
+
+	float y0 = x0;
+	float y1 = x1 - l10 * y0;
+	float y2 = x2 - l20 * y0 - l21 * y1;
+	float z0 = y0 / d0;
+	float z1 = y1 / d1;
+	float z2 = y2 / d2;
+
+	float a30 = GV.x, a31 = GV.y, a32 = GV.z;
+	float x3 = -GV.w;
+	float l30 = a30 / d0;
+	float dl31 = a31 - a30 * l10;
+	float l31 = dl31 / d1;
+	float dl32 = a32 - a30 * l20 - dl31 * l21;
+	float l32 = dl32 / d2;
+	float d3 = 0.f - a30 * l30 - dl31 * l31 - dl32 * l32;
+	float y3 = x3 - l30 * y0 - l31 * y1 - l32 * y2;
+	float z3 = fabsf(d3) > eps ? y3 / d3 : 0.f;
+
+	float lambda = z3;
+	float pz = z2 - l32 * lambda;
+	float py = z1 - l21 * pz - l31 * lambda;
+	float px = z0 - l10 * py - l20 * pz - l30 * lambda;
+	p = V3{px, py, pz};
+	return fabsf(d0) > eps && fabsf(d1) > eps && fabsf(d2) > eps;
+}
+
+// quadricReduceAttributes, :1024-1050: one wedge's attribute quadric folded into the position
+// system (its gradients enter as B B^T / a)
+__device__ __forceinline__ void qreduceAttr(Quadric& Q, const Quadric& A, const float4* G, int count)
+{
+	Q.a00 += A.a00 * Q.w;
+	Q.a11 += A.a11 * Q.w;
+	Q.a22 += A.a22 * Q.w;
+	Q.a10 += A.a10 * Q.w;
+	Q.a20 += A.a20 * Q.w;
+	Q.a21 += A.a21 * Q.w;
+	Q.b0 += A.b0 * Q.w;
+	Q.b1 += A.b1 * Q.w;
+	Q.b2 += A.b2 * Q.w;
+	float iaw = A.w == 0 ? 0.f : Q.w / A.w;
+	for (int k = 0; k < count; ++k)
+	{
+		float4 g = G[k];
+		Q.a00 -= (g.x * g.x) * iaw;
+		Q.a11 -= (g.y * g.y) * iaw;
+		Q.a22 -= (g.z * g.z) * iaw;
+		Q.a10 -= (g.x * g.y) * iaw;
+		Q.a20 -= (g.x * g.z) * iaw;
+		Q.a21 -= (g.y * g.z) * iaw;
+		Q.b0 -= (g.x * g.w) * iaw;
+		Q.b1 -= (g.y * g.w) * iaw;
+		Q.b2 -= (g.z * g.w) * iaw;
+	}
 }
 
 // getComplexTarget, :1278-1290

@@ -91,6 +91,8 @@ struct Scalars
 	unsigned int trace[2 * 512];        // per round: active candidates, SM cycles / 16
 	PassLive live;                      // device-resident pass loop
 	PassStats pstats[kMaxPassStats];    // its per-pass counters
+	unsigned int solve_pending[3];      // update mode: position-solve candidates left, rotating by round
+	unsigned int solve_rounds;
 };
 
 static_assert(sizeof(Scalars) <= kPinnedBytes, "the scalars block must fit the pinned readback buffer");
@@ -604,6 +606,24 @@ __global__ void kSparseGather(const unsigned int* __restrict__ sparse_remap, siz
 		lock_out[d] = lock[v];
 }
 
+// the update mode on a sparse subset: the compact copies (updated in place by the inner run)
+// back into the caller's buffers; vertices the solve left alone carry their gathered bits back
+__global__ void kSparseScatterBack(const unsigned int* __restrict__ sparse_remap, size_t u, const float* __restrict__ cpos, const float* __restrict__ cattr,
+    size_t acount, float* pos, size_t pstride_f, float* attr, size_t astride_f)
+{
+	size_t d = gtid();
+	if (d >= u)
+		return;
+	unsigned int v = sparse_remap[d];
+	float* p = pos + (size_t)v * pstride_f;
+	p[0] = cpos[d * 3 + 0];
+	p[1] = cpos[d * 3 + 1];
+	p[2] = cpos[d * 3 + 2];
+	if (attr)
+		for (size_t k = 0; k < acount; ++k)
+			attr[(size_t)v * astride_f + k] = cattr[d * acount + k];
+}
+
 __global__ void kSparseOut(const unsigned int* __restrict__ in, size_t n, const unsigned int* __restrict__ sparse_remap, unsigned int* __restrict__ out)
 {
 	size_t p = gtid();
@@ -620,7 +640,7 @@ __global__ void kSparseOut(const unsigned int* __restrict__ in, size_t n, const 
 // list with corners in increasing order.
 __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ off, const unsigned int* __restrict__ csr, size_t n,
     const float4* __restrict__ pos, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop,
-    const unsigned int* __restrict__ loopback, const unsigned char* __restrict__ lock, float factor, Quadric* __restrict__ vq)
+    const unsigned int* __restrict__ loopback, const unsigned char* __restrict__ lock, float factor, Quadric* __restrict__ vq, float4* __restrict__ vg)
 {
 	size_t vi = gtid();
 	if (vi >= n)
@@ -629,17 +649,25 @@ __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsign
 	if (remap[r] != r)
 	{
 		stquadric(vq, r, qzero());
+		if (vg)
+			vg[r] = make_float4(0.f, 0.f, 0.f, 0.f);
 		return;
 	}
 	unsigned int b = off[r], e = off[r + 1];
 	Quadric Q = qzero();
+	float4 G = make_float4(0.f, 0.f, 0.f, 0.f); // volume gradient (update mode with attributes), the same face order
 	for (unsigned int j = b; j < e; ++j)
 	{
 		unsigned int f = csr[j] / 3;
 		unsigned int i0 = idx[f * 3 + 0], i1 = idx[f * 3 + 1], i2 = idx[f * 3 + 2];
-		Quadric F = qtriangle(ldpos(pos, i0), ldpos(pos, i1), ldpos(pos, i2), 1.f);
+		V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1), p2 = ldpos(pos, i2);
+		Quadric F = qtriangle(p0, p1, p2, 1.f);
 		qadd(Q, F);
+		if (vg)
+			gadd(G, qvolumeGrad(p0, p1, p2));
 	}
+	if (vg)
+		vg[r] = G;
 	bool priority = lock && (lock[r] & kVertexPriority) != 0;
 	float w = Q.w * (priority ? 1.0f : factor);
 	V3 p = ldpos(pos, r);
@@ -1012,6 +1040,7 @@ struct PerformArgs
 	Quadric* aq;
 	float4* ag;
 	int ac;
+	float4* vg; // volume gradients (update mode with attributes), else nullptr
 	// stop rules
 	unsigned int prev_err_bits;
 	float error_limit;
@@ -1253,6 +1282,12 @@ __device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& 
 
 	qadd(Q1, Q0);
 	stquadric(a.vq, r1, Q1);
+	if (a.vg)
+	{
+		float4 g = a.vg[r1];
+		gadd(g, a.vg[r0]);
+		a.vg[r1] = g;
+	}
 	errbits = e == e ? __float_as_uint(e) : 0u;
 
 	if (a.ac)
@@ -1725,6 +1760,267 @@ __device__ __forceinline__ unsigned int ufFind(unsigned int* parent, unsigned in
 
 // lock-free union-find over the welded edges: the larger root is linked under the smaller, so
 
+// ---------------------------------------------------------------- the update mode (meshopt_simplifyWithUpdate)
+//
+// After the passes the vertices the result still uses get the optimal position of their
+// quadric (solvePositions :1675-1763) and attributes (solveAttributes :1765-1809), written back
+// to the caller's buffers (finalizeVertices :623-665). The reference solves positions in
+// vertex order, in place: a vertex's checks see the new positions of lower-index neighbours
+// and the old ones of higher-index neighbours. Here a vertex is solved once every lower-index
+// neighbour that is solved at all is final, reading final positions below its index and the
+// original ones above it: the same values, in rounds (the lowest pending vertex is always
+// ready, so every round makes progress).
+
+// vertices the result uses, and their positions' primaries (:2580-2587)
+__global__ void kMarkUpdate(const unsigned int* __restrict__ res, size_t n, const unsigned int* __restrict__ remap, unsigned char* update)
+{
+	size_t i = gtid();
+	if (i >= n)
+		return;
+	unsigned int v = res[i];
+	update[remap[v]] = 1;
+	update[v] = 1;
+}
+
+__device__ __forceinline__ bool positionSolved(unsigned char k)
+{
+	return !(k == kLocked || k == kSeam || k == kBorder);
+}
+
+// solved primaries go to the first list; every other vertex keeps its position and is final
+__global__ void kSolveList(size_t n, const unsigned char* __restrict__ update, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
+    unsigned int* __restrict__ done, unsigned int* __restrict__ list, unsigned int* count)
+{
+	size_t vi = gtid();
+	if (vi >= n)
+		return;
+	unsigned int i = (unsigned int)vi;
+	bool cand = update[i] && remap[i] == i && positionSolved(kind[i]);
+	done[i] = cand ? 0u : 1u;
+	if (cand)
+		list[atomicAdd(count, 1u)] = i;
+}
+
+struct SolveArgs
+{
+	unsigned int* list[2];
+	unsigned int* done;
+	const unsigned int* adj_off;
+	const uint2* adj;
+	const float4* pos;   // positions before the solve
+	float4* pos_new;     // solved positions (starts as a copy of pos)
+	const Quadric* vq;
+	const Quadric* aq;
+	const float4* ag;
+	const float4* vg;
+	int ac;
+	const unsigned int* wedge;
+	unsigned int max_rounds;
+	Scalars* sc;
+};
+
+// the reference's checks for one vertex (:1698-1759); true with the accepted position in p
+__device__ bool solveVertex(const SolveArgs& a, unsigned int i, V3& p)
+{
+	const V3 vp = ldpos(a.pos, i);
+	Quadric Q = ldquadric(a.vq, i);
+	Quadric R = qpoint(vp.x, vp.y, vp.z, Q.w * 1e-4f);
+	qadd(Q, R);
+	float4 GV = make_float4(0.f, 0.f, 0.f, 0.f);
+	if (a.ac)
+	{
+		unsigned int v = i;
+		do
+		{
+			qreduceAttr(Q, ldquadric(a.aq, v), a.ag + (size_t)v * a.ac, a.ac);
+			v = a.wedge[v];
+		} while (v != i);
+		if (a.vg)
+			GV = a.vg[i];
+	}
+	if (!qsolve(p, Q, GV))
+		return false;
+
+	// neighbours as the reference's loop sees them at i's turn
+	auto npos = [&](unsigned int x) {
+		if (x < i)
+		{
+			float4 q = __ldcg(a.pos_new + x);
+			return V3{q.x, q.y, q.z};
+		}
+		return ldpos(a.pos, x);
+	};
+	const unsigned int b = a.adj_off[i], e = a.adj_off[i + 1];
+	float radius = 0.f;
+	for (unsigned int j = b; j < e; ++j)
+	{
+		uint2 ed = a.adj[j];
+		V3 va = npos(ed.x), vb = npos(ed.y);
+		float da = (va.x - vp.x) * (va.x - vp.x) + (va.y - vp.y) * (va.y - vp.y) + (va.z - vp.z) * (va.z - vp.z);
+		float db = (vb.x - vp.x) * (vb.x - vp.x) + (vb.y - vp.y) * (vb.y - vp.y) + (vb.z - vp.z) * (vb.z - vp.z);
+		radius = radius < da ? da : radius;
+		radius = radius < db ? db : radius;
+	}
+	float nr = sqrtf(radius);
+	float dp = (p.x - vp.x) * (p.x - vp.x) + (p.y - vp.y) * (p.y - vp.y) + (p.z - vp.z) * (p.z - vp.z);
+	if (dp > nr * nr)
+		return false;
+	for (unsigned int j = b; j < e; ++j)
+	{
+		uint2 ed = a.adj[j];
+		if (triFlip(npos(ed.x), npos(ed.y), vp, p))
+			return false;
+	}
+	const Quadric Q0 = ldquadric(a.vq, i);
+	if (qerror(Q0, p) > qerror(Q0, vp) * 1.5f + 1e-6f)
+		return false;
+	return true;
+}
+
+__global__ void __launch_bounds__(kThreads) kSolvePositions(SolveArgs a)
+{
+	Scalars* sc = a.sc;
+	const size_t gthreads = (size_t)gridDim.x * blockDim.x;
+	const unsigned int lane = threadIdx.x & 31;
+	unsigned int n = __ldcg(&sc->solve_pending[1]);
+	unsigned int round = 0;
+	while (n)
+	{
+		++round;
+		if (round > a.max_rounds || __ldcg(&sc->grid_error))
+		{
+			if (gtid() == 0)
+				atomicOr(&sc->grid_error, 2u);
+			break;
+		}
+		const unsigned int* cur = a.list[round & 1];
+		unsigned int* next = a.list[(round + 1) & 1];
+		unsigned int* next_count = &sc->solve_pending[(round + 1) % 3];
+		if (gtid() == 0)
+			sc->solve_pending[(round + 2) % 3] = 0;
+		for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += gthreads)
+		{
+			size_t x = base + threadIdx.x;
+			bool keep = false;
+			unsigned int i = 0;
+			if (x < n)
+			{
+				i = __ldcg(cur + x);
+				bool ready = true;
+				for (unsigned int j = a.adj_off[i], e = a.adj_off[i + 1]; j < e && ready; ++j)
+				{
+					uint2 ed = a.adj[j];
+					ready = !((ed.x < i && __ldcg(a.done + ed.x) == 0) || (ed.y < i && __ldcg(a.done + ed.y) == 0));
+				}
+				if (ready)
+				{
+					__threadfence(); // the final positions behind the flags read above
+					V3 p;
+					if (solveVertex(a, i, p))
+						a.pos_new[i] = make_float4(p.x, p.y, p.z, 0.f);
+					__threadfence();
+					atomicExch(a.done + i, 1u);
+				}
+				else
+					keep = true;
+			}
+			unsigned int m = __ballot_sync(0xffffffffu, keep);
+			if (m)
+			{
+				unsigned int leader = __ffs(m) - 1, o = 0;
+				if (lane == leader)
+					o = atomicAdd(next_count, __popc(m));
+				o = __shfl_sync(0xffffffffu, o, leader);
+				if (keep)
+					next[o + __popc(m & ((1u << lane) - 1u))] = i;
+			}
+		}
+		gridBarrier(sc->bar, &sc->grid_error);
+		unsigned int nn = __ldcg(next_count);
+		if (nn >= n)
+		{
+			if (gtid() == 0)
+				atomicOr(&sc->grid_error, 2u);
+			break;
+		}
+		n = nn;
+	}
+	if (gtid() == 0)
+		sc->solve_rounds = round;
+}
+
+// wedges take their primary's solved position (:1691-1695)
+__global__ void kSolveWedges(size_t n, const unsigned char* __restrict__ update, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
+    float4* pos_new)
+{
+	size_t vi = gtid();
+	if (vi >= n)
+		return;
+	unsigned int i = (unsigned int)vi;
+	if (update[i] && remap[i] != i && positionSolved(kind[i]))
+		pos_new[i] = pos_new[remap[i]];
+}
+
+// solveAttributes :1765-1809, one thread per solved primary over its wedges
+__global__ void kSolveAttributes(size_t n, const unsigned char* __restrict__ update, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge,
+    const unsigned char* __restrict__ kind, const float4* __restrict__ pos_new, const Quadric* __restrict__ aq, const float4* __restrict__ ag, int ac,
+    float* attr)
+{
+	size_t vi = gtid();
+	if (vi >= n)
+		return;
+	unsigned int i = (unsigned int)vi;
+	if (!update[i] || remap[i] != i)
+		return;
+	const float4 pn = pos_new[i];
+	for (int k = 0; k < ac; ++k)
+	{
+		unsigned int shared = ~0u;
+		if (kind[i] == kComplex)
+		{
+			shared = i;
+			for (unsigned int v = wedge[i]; v != i; v = wedge[v])
+				if (attr[(size_t)v * ac + k] != attr[(size_t)i * ac + k])
+					shared = ~0u;
+				else if (shared != ~0u && ldquadric(aq, v).w > ldquadric(aq, shared).w)
+					shared = v;
+		}
+		unsigned int v = i;
+		do
+		{
+			unsigned int r = shared == ~0u ? v : shared;
+			float aw = ldquadric(aq, r).w;
+			float4 g = ag[(size_t)r * ac + k];
+			float iw = aw == 0 ? 0.f : 1.f / aw;
+			attr[(size_t)v * ac + k] = (g.x * pn.x + g.y * pn.y + g.z * pn.z + g.w) * iw;
+			v = wedge[v];
+		} while (v != i);
+	}
+}
+
+// finalizeVertices :623-665: undo the rescale and the attribute weights into the caller's buffers
+__global__ void kFinalizeVertices(size_t n, const unsigned char* __restrict__ update, const unsigned char* __restrict__ lock, const unsigned char* __restrict__ kind,
+    const float4* __restrict__ pos_new, const Scalars* __restrict__ sc, float* positions, size_t pstride_f, const float* __restrict__ attr, AttrMap am,
+    float* attributes, size_t astride_f)
+{
+	size_t vi = gtid();
+	if (vi >= n)
+		return;
+	if (!update[vi] || (lock && (lock[vi] & kVertexLock)))
+		return;
+	if (kind[vi] != kLocked)
+	{
+		const float4 p = pos_new[vi];
+		const float scale = sc->extent;
+		float* v = positions + vi * pstride_f;
+		v[0] = p.x * scale + sc->minv[0];
+		v[1] = p.y * scale + sc->minv[1];
+		v[2] = p.z * scale + sc->minv[2];
+	}
+	for (int k = 0; k < am.count; ++k)
+		attributes[vi * astride_f + am.src[k]] = attr[vi * am.count + k] / am.weight[k];
+}
+
 // ---------------------------------------------------------------- device-resident pass loop
 //
 // The pass loop (src/simplifier.cpp:2493-2541) recorded once into a CUDA graph as the body of
@@ -2004,6 +2300,12 @@ struct Work
 	unsigned int* blkcnt;
 	unsigned int* scratch;
 	unsigned int hash_mask;
+	// the update mode only
+	float4* vg;              // volume gradients (with attributes)
+	float4* pos_new;         // solved positions
+	unsigned char* vupdate;  // vertices the result uses (and their positions' primaries)
+	unsigned int* sdone;     // position solve: 0 while the vertex is a pending candidate
+	unsigned int *slist0, *slist1;
 };
 
 inline float __uint_as_float_host(unsigned int u)
@@ -2025,7 +2327,7 @@ size_t hashBuckets(size_t count)
 // at most the window plus one tile per block
 constexpr size_t kListSlack = size_t(1) << 19;
 
-size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
+size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = false)
 {
 	Carver c{base};
 	size_t Vp = V + 1;
@@ -2088,6 +2390,13 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac)
 	w.blkcnt = c.take<unsigned int>(T / kThreads + 2);
 	size_t sw = std::max(std::max(scanScratchWords(I + Vp + 2), radixScratchWords(big)), scanScratchWords(T + 2));
 	w.scratch = c.take<unsigned int>(sw);
+	const size_t Vs = solve ? Vp : 0;
+	w.vg = (solve && ac) ? c.take<float4>(Vp) : nullptr;
+	w.pos_new = c.take<float4>(Vs);
+	w.vupdate = c.take<unsigned char>(Vs);
+	w.sdone = c.take<unsigned int>(Vs);
+	w.slist0 = c.take<unsigned int>(Vs + kListSlack * (solve ? 1 : 0));
+	w.slist1 = c.take<unsigned int>(Vs + kListSlack * (solve ? 1 : 0));
 	return c.off;
 }
 
@@ -2233,7 +2542,16 @@ RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStre
 	cm.attributes_stride = ac * 4;
 	cm.lock = m.lock ? clock : nullptr;
 	cm.options = m.options & ~(kOptSparse | kOptInternalDebug); // debug bits are not produced for sparse subsets (:2602)
+	const bool solve = (m.options & kOptInternalSolve) != 0;
+	if (solve)
+	{
+		cm.update_positions = cpos;
+		cm.update_attributes = ac ? cattr : nullptr;
+	}
 	RunResult rr = run(cm, cres, stream, times, dump);
+	if (solve && U)
+		MO_LAUNCH(kSparseScatterBack, gridFor(U, kThreads), kThreads, 0, stream, smap, U, cpos, cattr, ac, m.update_positions, m.positions_stride / 4,
+		    ac ? m.update_attributes : nullptr, m.attributes_stride / 4);
 	if (rr.index_count)
 		MO_LAUNCH(kSparseOut, gridFor(rr.index_count, kThreads), kThreads, 0, stream, cres, rr.index_count, smap, d_out);
 	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
@@ -2281,11 +2599,14 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			am.count++;
 		}
 	const int ac = am.count;
+	const bool solve = (m.options & kOptInternalSolve) != 0;
+	if (solve && (!m.update_positions || (ac && !m.update_attributes)))
+		throw std::invalid_argument("the update mode needs writable position (and attribute) buffers");
 
 	Work w;
-	size_t bytes = layout(w, nullptr, I, V, ac);
+	size_t bytes = layout(w, nullptr, I, V, ac, solve);
 	arena_.reserve(bytes);
-	layout(w, arena_.base(), I, V, ac);
+	layout(w, arena_.base(), I, V, ac, solve);
 
 	Scalars* hs = reinterpret_cast<Scalars*>(pinned_);
 	auto readScalars = [&]() {
@@ -2398,7 +2719,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// quadrics
 	float factor = (m.options & kOptRegularizeLight) ? 1e-2f : ((m.options & kOptRegularize) ? 1e-1f : 1e-7f);
 	if (V)
-		MO_LAUNCH(kFillQuadrics, gV, kThreads, 0, stream, w.res0, off_rm, csr_rm, V, w.pos, w.remap, w.kind, w.loop, w.loopback, m.lock, factor, w.vq);
+		MO_LAUNCH(kFillQuadrics, gV, kThreads, 0, stream, w.res0, off_rm, csr_rm, V, w.pos, w.remap, w.kind, w.loop, w.loopback, m.lock, factor, w.vq,
+		    (solve && ac) ? w.vg : nullptr);
 	if (ac && V)
 	{
 		if (ac <= 4)
@@ -2603,6 +2925,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.aq = w.aq;
 			pa.ag = w.ag;
 			pa.ac = ac;
+			pa.vg = (solve && ac) ? w.vg : nullptr;
 			pa.prev_err_bits = 0;
 			pa.error_limit = error_limit;
 			pa.goal = 0;
@@ -2727,6 +3050,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.aq = w.aq;
 			pa.ag = w.ag;
 			pa.ac = ac;
+			pa.vg = (solve && ac) ? w.vg : nullptr;
 			pa.prev_err_bits = result_error_bits;
 			pa.error_limit = error_limit;
 			pa.goal = goal;
@@ -2818,6 +3142,60 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		vertex_error = vertex_error < maxerr ? maxerr : vertex_error;
 	}
 
+	// the update mode (:2575-2599): solve the vertices the result uses and write them back
+	if (solve && V)
+	{
+		const size_t T = result_count / 3;
+		MO_CUDA_CHECK(cudaMemsetAsync(w.vupdate, 0, V, stream));
+		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
+		MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
+		MO_CUDA_CHECK(cudaMemsetAsync(w.sc->solve_pending, 0, sizeof(w.sc->solve_pending), stream));
+		if (result_count)
+		{
+			MO_LAUNCH(kMarkUpdate, gridFor(result_count, kThreads), kThreads, 0, stream, res, result_count, w.remap, w.vupdate);
+			MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
+		}
+		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream);
+		if (T)
+			MO_LAUNCH(kAdjFill, gridFor(T, kThreads), kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj, nullptr);
+		MO_CUDA_CHECK(cudaMemcpyAsync(w.pos_new, w.pos, V * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
+		const unsigned int gV = gridFor(V, kThreads);
+		MO_LAUNCH(kSolveList, gV, kThreads, 0, stream, V, w.vupdate, w.remap, w.kind, w.sdone, w.slist1, &w.sc->solve_pending[1]);
+		{
+			SolveArgs sa;
+			sa.list[0] = w.slist0;
+			sa.list[1] = w.slist1;
+			sa.done = w.sdone;
+			sa.adj_off = w.adj_off;
+			sa.adj = w.adj;
+			sa.pos = w.pos;
+			sa.pos_new = w.pos_new;
+			sa.vq = w.vq;
+			sa.aq = w.aq;
+			sa.ag = w.ag;
+			sa.vg = ac ? w.vg : nullptr;
+			sa.ac = ac;
+			sa.wedge = w.wedge;
+			sa.max_rounds = unsigned(V + 2);
+			sa.sc = w.sc;
+			// co-resident blocks of this kernel (its own register count), as many as the pass kernel's at most
+			int per_sm = 0;
+			MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kSolvePositions, kThreads, 0));
+			unsigned int resident = unsigned(std::max(1, per_sm * sms_));
+			unsigned int blocks = std::max(1u, std::min(std::min(perform_blocks_, resident), gV));
+			MO_CUDA_CHECK(cudaMemsetAsync(w.sc->bar, 0, sizeof(unsigned int) * 3, stream));
+			void* params[] = {&sa};
+			cudaEvent_t e0 = probeBegin("kSolvePositions", stream);
+			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kSolvePositions, dim3(blocks), dim3(kThreads), params, 0, stream));
+			probeEnd(e0, stream);
+		}
+		MO_LAUNCH(kSolveWedges, gV, kThreads, 0, stream, V, w.vupdate, w.remap, w.kind, w.pos_new);
+		if (ac)
+			MO_LAUNCH(kSolveAttributes, gV, kThreads, 0, stream, V, w.vupdate, w.remap, w.wedge, w.kind, w.pos_new, w.aq, w.ag, ac, w.attr);
+		MO_LAUNCH(kFinalizeVertices, gV, kThreads, 0, stream, V, w.vupdate, m.lock, w.kind, w.pos_new, w.sc, m.update_positions, m.positions_stride / 4,
+		    w.attr, am, ac ? m.update_attributes : nullptr, m.attributes_stride / 4);
+	}
+
 	if ((m.options & kOptInternalDebug) && result_count)
 		MO_LAUNCH(kDebugBits, gridFor(result_count / 3, kThreads), kThreads, 0, stream, res, result_count / 3, w.kind, w.loop, w.loopback);
 
@@ -2840,6 +3218,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		rr.round_trace.clear();
 		for (unsigned int i = 0; i < hs->trace_count && i < 512; ++i)
 			rr.round_trace.push_back({hs->trace[2 * i], khz ? float(double(hs->trace[2 * i + 1]) * 16.0 / khz * 1e3) : 0.f});
+		if (solve && hs->grid_error)
+			throw std::runtime_error(hs->grid_error & 2 ? "position solve made no progress" : "grid barrier wait limit reached in the position solve");
 	}
 	rr.index_count = result_count;
 	rr.result_error_sq = rerr;

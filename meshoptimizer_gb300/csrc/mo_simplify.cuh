@@ -32,6 +32,11 @@ struct MeshDesc
 	size_t target_index_count = 0;
 	float target_error = 0.f;
 	unsigned int options = 0;
+	// the update mode (options with kOptInternalSolve): the buffers the solved positions and
+	// attributes are written back to, same layout as positions / attributes (may be the same
+	// device buffers)
+	float* update_positions = nullptr;
+	float* update_attributes = nullptr;
 };
 
 // Per-pass counters, the same quantities the reference prints under TRACE

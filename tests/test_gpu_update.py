@@ -1,0 +1,96 @@
+"""meshopt_simplifyWithUpdate on the GPU against the reference library (the committed fixtures:
+its simplifyUpdate tests and seeded meshes) and, on larger meshes, the oracle: the index buffer,
+the positions and attributes written back, and the error, bit for bit."""
+import numpy as np
+import pytest
+
+import fixtures
+import meshoptimizer_gb300 as mg
+from meshoptimizer_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from meshoptimizer_gb300 import build
+
+    build.build()
+    mg.load()
+
+
+def _same(a, b):
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
+
+
+@pytest.mark.parametrize("case", fixtures.update_cases(), ids=lambda c: c["name"])
+@pytest.mark.parametrize("device_loop", [True, False])
+def test_update_fixtures(case, device_loop):
+    mg.set_device_loop(device_loop)
+    try:
+        if case["kind"] == "interleaved":
+            out, v, err = mg.simplify_with_update_interleaved(case["indices"], case["vertices"], 4, 3, [1.0], case.get("lock"), int(case["target"]),
+                                                              float(case["error"]), int(case["options"]))
+            assert np.array_equal(out, case["out"])
+            assert _same(v, case["out_vertices"].reshape(-1))
+        else:
+            out, p2, a2, err = mg.simplify_with_update(case["indices"], case["positions"], int(case["target"]), float(case["error"]),
+                                                       int(case["options"]), attributes=case.get("attributes"), weights=case.get("weights"),
+                                                       lock=case.get("lock"))
+            assert np.array_equal(out, case["out"])
+            assert _same(p2, case["out_positions"])
+            if "out_attributes" in case:
+                assert _same(a2, case["out_attributes"])
+        assert np.float32(err) == case["out_error"]
+    finally:
+        mg.set_device_loop(True)
+
+
+def _cases():
+    rng = np.random.default_rng(12)
+    out = []
+    idx, pos = W.heightfield(128, seed=5)
+    out.append(("hf128", idx, pos, None, None, None, W.target_count(len(idx), 0.2), 2e-2, 0))
+    idx, pos, attr, w = W.octa_sphere(6, seed=6)
+    lock = rng.choice(np.array([0, 0, 0, 0, 1, 2, 4], np.uint8), size=len(pos))
+    out.append(("sphere6_attr", idx, pos, attr, w, None, W.target_count(len(idx), 0.1), 5e-3, 0))
+    out.append(("sphere6_attr_lock_permissive", idx, pos, attr, w, lock, W.target_count(len(idx), 0.1), 5e-3, mg.SimplifyPermissive))
+    half = idx[: (len(idx) // 6) * 3]
+    out.append(("sphere6_sparse_abs", half, pos, attr, w, None, W.target_count(len(half), 0.2), 1e-2, mg.SimplifySparse | mg.SimplifyErrorAbsolute))
+    return out
+
+
+@pytest.mark.parametrize("name,idx,pos,attr,w,lock,target,error,options", _cases(), ids=lambda x: x if isinstance(x, str) else "")
+def test_update_matches_oracle(port, name, idx, pos, attr, w, lock, target, error, options):
+    ref = port.simplify_with_update("port", idx, pos, target, error, options, attributes=attr, weights=w, lock=lock)
+    got = mg.simplify_with_update(idx, pos, target, error, options, attributes=attr, weights=w, lock=lock)
+    assert np.array_equal(got[0], ref[0])
+    assert _same(got[1], ref[1])
+    if attr is not None:
+        assert _same(got[2], ref[2])
+    assert got[3] == ref[3]
+    moved = int(np.sum(np.any(got[1].view(np.uint32) != np.asarray(pos, np.float32).view(np.uint32), axis=1)))
+    assert moved > 0 or name == "hf128"
+
+
+def test_update_device_entry(port):
+    torch = pytest.importorskip("torch")
+    idx, pos, attr, w = W.octa_sphere(5, seed=8)
+    target = W.target_count(len(idx), 0.15)
+    ref = port.simplify_with_update("port", idx, pos, target, 1e-2, 0, attributes=attr, weights=w)
+    di = torch.from_numpy(idx.view(np.int32).copy()).cuda()
+    dp = torch.from_numpy(pos.copy()).cuda()
+    da = torch.from_numpy(attr.copy()).cuda()
+    n, err = mg.simplify_with_update_device(di.data_ptr(), len(idx), dp.data_ptr(), len(pos), 12, target, 1e-2, 0, d_attributes=da.data_ptr(),
+                                            attributes_stride=attr.shape[1] * 4, weights=w)
+    assert np.array_equal(di[:n].cpu().numpy().view(np.uint32), ref[0])
+    assert _same(dp.cpu().numpy(), ref[1])
+    assert _same(da.cpu().numpy(), ref[2])
+    assert err == ref[3]
+
+
+def test_update_rejects_prune():
+    idx, pos = W.heightfield(8, seed=1)
+    with pytest.raises(mg.SimplifyError) as e:
+        mg.simplify_with_update(idx, pos, 0, 1e-2, mg.SimplifyPrune)
+    assert e.value.status == mg.STATUS_UNSUPPORTED
