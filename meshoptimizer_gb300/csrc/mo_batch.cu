@@ -58,6 +58,7 @@ struct CtaWork
 	unsigned char* status;     // cap: decision per sorted position
 	unsigned int* list0;       // cap: undecided candidates of the round
 	unsigned int* list1;       // cap
+	unsigned int* sort_tmp;    // cap: the sort's first digit pass
 	unsigned int* back;        // V: sparse meshes, local vertex -> vertex of the shared buffer
 	float* attr;               // V * ac: rescaled attributes
 	Quadric* aq;               // V: attribute quadrics (per wedge)
@@ -123,8 +124,9 @@ __host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t
 	w.cv1 = reinterpret_cast<unsigned int*>(take(cap * 4));
 	w.cerr = reinterpret_cast<unsigned int*>(take(cap * 4));
 	w.order = reinterpret_cast<unsigned int*>(take(cap * 4));
-	w.hist = reinterpret_cast<unsigned int*>(take(kSortBinsC * 4));
+	w.hist = reinterpret_cast<unsigned int*>(take(kSortBinsC * 4)); // >= 8 warps x 256 digit counters
 	w.red = reinterpret_cast<unsigned int*>(take(64 * 4));
+	w.sort_tmp = reinterpret_cast<unsigned int*>(take(cap * 4));
 	w.minT = rounds ? reinterpret_cast<unsigned long long*>(take(V * 8)) : nullptr;
 	w.minS = rounds ? reinterpret_cast<unsigned long long*>(take(V * 8)) : nullptr;
 	w.moved = rounds ? reinterpret_cast<unsigned long long*>(take(V * 8)) : nullptr;
@@ -140,19 +142,72 @@ __host__ __device__ inline size_t carve(CtaWork& w, char* base, size_t I, size_t
 template <int NT>
 __device__ unsigned int blockScanArray(unsigned int* data, unsigned int n, unsigned int* red)
 {
-	unsigned int carry = 0;
-	for (unsigned int base = 0; base < n; base += NT)
+	// each thread scans a contiguous run; one block scan of the run totals
+	const unsigned int per = (n + NT - 1) / NT;
+	const unsigned int b = min(n, threadIdx.x * per), e = min(n, b + per);
+	unsigned int sum = 0;
+	for (unsigned int i = b; i < e; ++i)
+		sum += data[i];
+	unsigned int tot;
+	unsigned int run = blockExclusiveScan<NT>(sum, red, &tot);
+	for (unsigned int i = b; i < e; ++i)
 	{
-		unsigned int i = base + threadIdx.x;
-		unsigned int v = i < n ? data[i] : 0u;
-		unsigned int tot;
-		unsigned int ex = blockExclusiveScan<NT>(v, red, &tot);
-		if (i < n)
-			data[i] = carry + ex;
-		carry += tot;
-		__syncthreads();
+		unsigned int v = data[i];
+		data[i] = run;
+		run += v;
 	}
-	return carry;
+	__syncthreads();
+	return tot;
+}
+
+// One pass of a stable LSD radix sort of candidate indices on 8 bits of their sort key: up to 8
+// warps each own a contiguous segment, count its digits (counters digit-major, then warp, so
+// one scan gives every (digit, warp) its start), and scatter the segment in order. Equal digits
+// keep segment order and index order inside a segment. src == nullptr: the identity.
+template <int NT>
+__device__ void blockDigitPass(const unsigned int* cerr, const unsigned int* src, unsigned int* dst, unsigned int C, int shift, unsigned int* cnt,
+    unsigned int* red)
+{
+	constexpr unsigned int NW = NT / 32 < 8 ? NT / 32 : 8; // counters: NW * 256 words
+	const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const unsigned int seg = (C + NW - 1) / NW;
+	const unsigned int s0 = min(C, warp * seg), s1 = warp < NW ? min(C, s0 + seg) : s0;
+	for (unsigned int i = threadIdx.x; i < NW * 256; i += NT)
+		cnt[i] = 0;
+	__syncthreads();
+	for (unsigned int b = s0; b < s1; b += 32)
+	{
+		unsigned int x = b + lane;
+		bool valid = x < s1;
+		unsigned int v = valid ? (src ? src[x] : x) : 0u;
+		unsigned int d = valid ? ((sortKey(cerr[v]) >> shift) & 255u) : 256u + lane;
+		unsigned int peers = __match_any_sync(0xffffffffu, d);
+		if (valid && lane == (unsigned int)(__ffs(peers) - 1))
+			cnt[d * NW + warp] += __popc(peers);
+		__syncwarp();
+	}
+	__syncthreads();
+	blockScanArray<NT>(cnt, NW * 256, red);
+	for (unsigned int b = s0; b < s1; b += 32)
+	{
+		unsigned int x = b + lane;
+		bool valid = x < s1;
+		unsigned int v = valid ? (src ? src[x] : x) : 0u;
+		unsigned int d = valid ? ((sortKey(cerr[v]) >> shift) & 255u) : 256u + lane;
+		unsigned int peers = __match_any_sync(0xffffffffu, d);
+		unsigned int leader = __ffs(peers) - 1;
+		unsigned int base = 0;
+		if (valid && lane == leader)
+		{
+			base = cnt[d * NW + warp];
+			cnt[d * NW + warp] = base + __popc(peers);
+		}
+		base = __shfl_sync(0xffffffffu, base, leader);
+		if (valid)
+			dst[base + __popc(peers & ((1u << lane) - 1u))] = v;
+		__syncwarp();
+	}
+	__syncthreads();
 }
 
 template <int NT>
@@ -735,54 +790,62 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 		}
 		__syncthreads();
 
-		// pick (pickEdgeCollapses :1310-1372), chunked block scan over triangles
+		// pick (pickEdgeCollapses :1310-1372): each thread takes a contiguous run of triangles,
+		// counts its candidates, and after one block scan emits them in triangle order; the
+		// capacity check stops at the first triangle that has no room for three more
 		if (tid == 0)
-			s_count = 0, s_trunc = ~0u;
-		__syncthreads();
-		for (unsigned int base = 0; base < T; base += NT)
+			s_trunc = ~0u;
 		{
-			unsigned int t = base + tid;
-			unsigned int v0[3], v1[3], bd[3], n = 0;
-			if (t < T)
-			{
-				unsigned int a[3] = {w.idx[t * 3], w.idx[t * 3 + 1], w.idx[t * 3 + 2]};
+			auto pickEdgeB = [&](unsigned int i0, unsigned int i1, unsigned int& v0, unsigned int& v1, unsigned int& bd) {
+				unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
+				if (r0 == r1)
+					return false;
+				unsigned int k0 = w.kind[i0], k1 = w.kind[i1];
+				bool c01 = canCollapse(k0, k1), c10 = canCollapse(k1, k0);
+				if (!(c01 | c10))
+					return false;
+				if (hasOpposite(k0, k1) && r1 > r0)
+					return false;
+				if ((k0 == kBorder || k0 == kSeam) && k1 != kManifold && w.loop[i0] != i1)
+					return false;
+				if ((k1 == kBorder || k1 == kSeam) && k0 != kManifold && w.loopback[i1] != i0)
+					return false;
+				if (c01 & c10)
+					v0 = i0, v1 = i1, bd = 1;
+				else
+					v0 = c01 ? i0 : i1, v1 = c01 ? i1 : i0, bd = 0;
+				return true;
+			};
+			const unsigned int per = (T + NT - 1) / NT;
+			const unsigned int t0 = min(T, tid * per), t1 = min(T, t0 + per);
+			unsigned int n = 0;
+			for (unsigned int t = t0; t < t1; ++t)
 				for (int e = 0; e < 3; ++e)
 				{
-					unsigned int i0 = a[e], i1 = a[e == 2 ? 0 : e + 1];
-					unsigned int r0 = w.remap[i0], r1 = w.remap[i1];
-					if (r0 == r1)
-						continue;
-					unsigned int k0 = w.kind[i0], k1 = w.kind[i1];
-					bool c01 = canCollapse(k0, k1), c10 = canCollapse(k1, k0);
-					if (!(c01 | c10))
-						continue;
-					if (hasOpposite(k0, k1) && r1 > r0)
-						continue;
-					if ((k0 == kBorder || k0 == kSeam) && k1 != kManifold && w.loop[i0] != i1)
-						continue;
-					if ((k1 == kBorder || k1 == kSeam) && k0 != kManifold && w.loopback[i1] != i0)
-						continue;
-					if (c01 & c10)
-						v0[n] = i0, v1[n] = i1, bd[n] = 1;
-					else
-						v0[n] = c01 ? i0 : i1, v1[n] = c01 ? i1 : i0, bd[n] = 0;
-					n++;
+					unsigned int v0, v1, bd;
+					n += pickEdgeB(w.idx[t * 3 + e], w.idx[t * 3 + (e == 2 ? 0 : e + 1)], v0, v1, bd);
 				}
-			}
 			unsigned int tot;
-			unsigned int ex = blockExclusiveScan<NT>(n, w.red, &tot);
-			unsigned int o = s_count + ex;
-			if (t < T)
+			unsigned int o = blockExclusiveScan<NT>(n, w.red, &tot);
+			if (tid == 0)
+				s_count = tot;
+			for (unsigned int t = t0; t < t1; ++t)
 			{
 				if (o + 3 > s_cap)
+				{
 					atomicMin(&s_trunc, o);
-				else
-					for (unsigned int q = 0; q < n; ++q)
-						w.cv0[o + q] = v0[q], w.cv1[o + q] = v1[q], w.cerr[o + q] = bd[q];
+					break;
+				}
+				for (int e = 0; e < 3; ++e)
+				{
+					unsigned int v0, v1, bd;
+					if (pickEdgeB(w.idx[t * 3 + e], w.idx[t * 3 + (e == 2 ? 0 : e + 1)], v0, v1, bd))
+					{
+						w.cv0[o] = v0, w.cv1[o] = v1, w.cerr[o] = bd;
+						o++;
+					}
+				}
 			}
-			__syncthreads();
-			if (tid == 0)
-				s_count += tot;
 			__syncthreads();
 		}
 		const unsigned int C = min(s_count, s_trunc);
@@ -829,36 +892,10 @@ __device__ void simplifyMesh(const BatchDesc& d, CtaWork& w, BatchResult* out, b
 			w.cv1[c] = rev ? i0 : i1;
 			w.cerr[c] = __float_as_uint(ej < ei ? ej : ei);
 		}
-		// sort (sortEdgeCollapses :1452-1496): histogram, scan, stable scatter by warp 0
-		for (unsigned int i = tid; i < kSortBinsC; i += NT)
-			w.hist[i] = 0;
-		__syncthreads();
-		for (unsigned int c = tid; c < C; c += NT)
-			atomicAdd(&w.hist[sortKey(w.cerr[c])], 1u);
-		__syncthreads();
-		blockScanArray<NT>(w.hist, kSortBinsC, w.red);
-		if (tid < 32)
-		{
-			const unsigned int lane = tid;
-			for (unsigned int base = 0; base < C; base += 32)
-			{
-				unsigned int c = base + lane;
-				unsigned int key = c < C ? sortKey(w.cerr[c]) : 0x10000u + lane;
-				unsigned int peers = __match_any_sync(0xffffffffu, key);
-				unsigned int rank = __popc(peers & ((1u << lane) - 1u));
-				unsigned int leader = __ffs(peers) - 1;
-				unsigned int basepos = 0;
-				if (c < C && lane == leader)
-				{
-					basepos = w.hist[key];
-					w.hist[key] = basepos + __popc(peers);
-				}
-				basepos = __shfl_sync(0xffffffffu, basepos, leader);
-				if (c < C)
-					w.order[basepos + rank] = c;
-				__syncwarp();
-			}
-		}
+		// sort (sortEdgeCollapses :1452-1496): the same stable order on the 12-bit key as two
+		// stable 8-bit digit passes (low byte, then the high four bits)
+		blockDigitPass<NT>(w.cerr, nullptr, w.sort_tmp, C, 0, w.hist, w.red);
+		blockDigitPass<NT>(w.cerr, w.sort_tmp, w.order, C, 8, w.hist, w.red);
 		for (unsigned int i = tid; i < V; i += NT)
 			w.cr[i] = i, w.locked[i] = 0;
 		__syncthreads();
