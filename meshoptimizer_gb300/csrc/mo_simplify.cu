@@ -93,6 +93,7 @@ struct Scalars
 	PassStats pstats[kMaxPassStats];    // its per-pass counters
 	unsigned int solve_pending[3];      // update mode: position-solve candidates left, rotating by round
 	unsigned int solve_rounds;
+	unsigned int max_degree[2];         // corners of the busiest vertex: raw, remapped
 };
 
 static_assert(sizeof(Scalars) <= kPinnedBytes, "the scalars block must fit the pinned readback buffer");
@@ -366,6 +367,54 @@ __global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned 
 	if (remap)
 		v = remap[v];
 	atomicAdd(&cnt[v], 1u);
+}
+
+// the largest count of corners[v] = off[v+1] - off[v]
+__global__ void kMaxDegree(const unsigned int* __restrict__ off, size_t n, unsigned int* out)
+{
+	size_t i = gtid();
+	unsigned int d = i < n ? off[i + 1] - off[i] : 0u;
+	for (int o = 16; o > 0; o >>= 1)
+		d = max(d, __shfl_down_sync(0xffffffffu, d, o));
+	if ((threadIdx.x & 31) == 0 && d)
+		atomicMax(out, d);
+}
+
+// vertex -> corner lists: every corner into its vertex's range (arbitrary order within it), then
+// each range sorted by corner index, which is the order a stable sort by vertex gives
+__global__ void kCornerFill(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, const unsigned int* __restrict__ off,
+    unsigned int* fill, unsigned int* __restrict__ csr)
+{
+	size_t p = gtid();
+	if (p >= n)
+		return;
+	unsigned int v = idx[p];
+	if (remap)
+		v = remap[v];
+	csr[off[v] + atomicAdd(&fill[v], 1u)] = (unsigned int)p;
+}
+
+// insertion sort of each vertex's corners (only used when no vertex has more than
+// kCornerSortMax corners)
+constexpr unsigned int kCornerSortMax = 64;
+
+__global__ void kCornerSort(const unsigned int* __restrict__ off, size_t n, unsigned int* csr)
+{
+	size_t v = gtid();
+	if (v >= n)
+		return;
+	const unsigned int b = off[v], e = off[v + 1];
+	for (unsigned int j = b + 1; j < e; ++j)
+	{
+		unsigned int x = csr[j];
+		unsigned int q = j;
+		while (q > b && csr[q - 1] > x)
+		{
+			csr[q] = csr[q - 1];
+			--q;
+		}
+		csr[q] = x;
+	}
 }
 
 __global__ void kIota(unsigned int* __restrict__ out, size_t n)
@@ -2648,6 +2697,22 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.flags);
 		scanExclusive(w.flags, w.flags, V, &w.sc->dup_count, w.scratch, stream);
 	}
+	// vertex -> corner lists in corner order: raw (classification, attribute quadrics) and
+	// remapped (position quadrics). Their offsets and largest degrees come before the host read
+	// below, which decides how the lists are filled.
+	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
+	if (I)
+		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt);
+	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream);
+	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
+	if (I)
+		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt);
+	scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream);
+	if (V)
+	{
+		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_raw, V, &w.sc->max_degree[0]);
+		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_rm, V, &w.sc->max_degree[1]);
+	}
 	// flags now hold offsets; recompute flags from remap in the compaction kernel
 	readScalars();
 	if (hs->bad_index)
@@ -2664,24 +2729,33 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_LAUNCH(kWedgeLink, gridFor(D, kThreads), kThreads, 0, stream, w.keys_a, w.vals_a, D, w.wedge);
 	}
 
-	// vertex -> corner lists in corner order: raw (classification, attribute quadrics) and
-	// remapped (position quadrics)
 	const int vbits = bitsFor(V ? V - 1 : 0);
-	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
-	if (I)
-		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt);
-	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream);
-	radixSortPairs(w.res0, nullptr, w.keys_a, w.csr_raw, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
-	if (D)
+	if (hs->max_degree[0] <= kCornerSortMax && hs->max_degree[1] <= kCornerSortMax)
 	{
-		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
-		if (I)
+		// few corners per vertex: fill and sort each list in place
+		if (I && V)
 		{
-			MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt);
-			MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.ckey);
+			MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
+			MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, nullptr, I, w.off_raw, w.fill, w.csr_raw);
+			MO_LAUNCH(kCornerSort, gV, kThreads, 0, stream, w.off_raw, V, w.csr_raw);
+			if (D)
+			{
+				MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
+				MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, w.remap, I, w.off_rm, w.fill, w.csr_rm);
+				MO_LAUNCH(kCornerSort, gV, kThreads, 0, stream, w.off_rm, V, w.csr_rm);
+			}
 		}
-		scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream);
-		radixSortPairs(w.ckey, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
+	}
+	else
+	{
+		// a vertex with many corners: stable radix sorts by vertex
+		radixSortPairs(w.res0, nullptr, w.keys_a, w.csr_raw, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
+		if (D)
+		{
+			if (I)
+				MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.ckey);
+			radixSortPairs(w.ckey, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
+		}
 	}
 	const unsigned int* off_rm = D ? w.off_rm : w.off_raw;
 	const unsigned int* csr_rm = D ? w.csr_rm : w.csr_raw;

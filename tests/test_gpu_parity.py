@@ -240,3 +240,15 @@ def test_unsupported_option_reports_status():
     out, err = mg.simplify(idx, pos, 0, 1e-2, 1 << 29, check=False)  # the internal solve bit (simplifyWithUpdate)
     st, msg = mg.last_status()
     assert st == mg.STATUS_UNSUPPORTED and np.array_equal(out, idx)
+
+
+def test_high_degree_fan(port):
+    """A vertex with more corners than the per-vertex list sort takes (the stable radix sort
+    builds the corner lists instead): a 300-triangle fan around one vertex plus a wavy rim."""
+    n = 300
+    ang = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    rim = np.stack([np.cos(ang), np.sin(ang), 0.05 * np.sin(7 * ang)], axis=1)
+    pos = np.concatenate([[[0.0, 0.0, 0.2]], rim]).astype(np.float32)
+    idx = np.array([[0, 1 + i, 1 + (i + 1) % n] for i in range(n)], np.uint32).reshape(-1)
+    for opt in (0, mg.SimplifyLockBorder):
+        _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.3), 1.0, opt)
