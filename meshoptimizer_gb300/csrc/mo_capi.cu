@@ -789,6 +789,10 @@ void largeWorker(ServerImpl* S)
 		ts.ensure();
 		Tuning t = ts.simplifier->tuning();
 		t.perform_grid_cap = S->cfg.perform_blocks;
+		// requests come in every shape, so a recorded pass graph is never replayed for a second
+		// request, and concurrent workers instantiating graphs contend in the driver: the
+		// single-mesh workers drive their pass loops from the host
+		t.device_loop = false;
 		ts.simplifier->setTuning(t);
 	}
 	catch (const std::exception& e)
