@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 from meshoptimizer_gb300 import workloads as W  # noqa: E402
 
 # Algorithmic bytes of the dominant kernel, kPerform (one cooperative launch per pass), from
-# the per-pass counters the library reports (see DESIGN.md section 5):
+# the per-pass counters the library reports:
 #   decision rounds   29 B per active candidate (id 4, record 16, status 1, touched 2, append 4, pad 2)
 #   stop-rule scan    12 B per evaluated candidate (status, kind, error bits, read twice)
 #   per-vertex init   9 B per vertex (touched, moved_by, collapse_remap)

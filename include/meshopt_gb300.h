@@ -64,7 +64,7 @@ MESHOPTGPU_API float meshopt_simplifyScale(const float* vertex_positions, size_t
 enum
 {
 	meshoptgpu_StatusOk = 0,
-	meshoptgpu_StatusUnsupported = 1, /* an option this build does not implement on the GPU */
+	meshoptgpu_StatusUnsupported = 1, /* an option the GPU path does not implement */
 	meshoptgpu_StatusInvalidArgument = 2,
 	meshoptgpu_StatusCudaError = 3,
 	meshoptgpu_StatusOutOfMemory = 4,
