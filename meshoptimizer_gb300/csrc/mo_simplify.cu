@@ -2934,9 +2934,21 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->result_error_bits, 0, 4, stream));
 		const PassLive* lv = &w.sc->live;
 
-		cudaGraph_t graph = nullptr;
-		cudaGraphExec_t exec = nullptr;
-		MO_CUDA_CHECK(cudaGraphCreate(&graph, 0));
+		// the graph and its executable are released on every way out of this block
+		struct GraphGuard
+		{
+			cudaGraph_t graph = nullptr;
+			cudaGraphExec_t exec = nullptr;
+			~GraphGuard()
+			{
+				if (exec)
+					cudaGraphExecDestroy(exec);
+				if (graph)
+					cudaGraphDestroy(graph);
+			}
+		} guard;
+		MO_CUDA_CHECK(cudaGraphCreate(&guard.graph, 0));
+		cudaGraph_t graph = guard.graph;
 		cudaGraphConditionalHandle handle;
 		MO_CUDA_CHECK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
 		cudaGraphNodeParams cp = {};
@@ -3027,18 +3039,15 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			lp.capturing = false;
 			cudaGraph_t dead = nullptr;
 			cudaStreamEndCapture(cs, &dead);
-			cudaGraphDestroy(graph);
 			throw;
 		}
 		lp.capturing = false;
 		cudaGraph_t captured = nullptr;
 		MO_CUDA_CHECK(cudaStreamEndCapture(cs, &captured));
 		const unsigned long long body_launches = lp.launches - launches0;
-		MO_CUDA_CHECK(cudaGraphInstantiate(&exec, graph, 0));
-		MO_CUDA_CHECK(cudaGraphLaunch(exec, stream));
+		MO_CUDA_CHECK(cudaGraphInstantiate(&guard.exec, graph, 0));
+		MO_CUDA_CHECK(cudaGraphLaunch(guard.exec, stream));
 		readScalars();
-		cudaGraphExecDestroy(exec);
-		cudaGraphDestroy(graph);
 		// every replay of the body launched its kernels again
 		if (hs->live.iterations > 1)
 			lp.launches += body_launches * (hs->live.iterations - 1);
