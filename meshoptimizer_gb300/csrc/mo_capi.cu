@@ -327,9 +327,6 @@ size_t updateHost(unsigned int* indices, size_t index_count, float* vertex_posit
 	if (!bad.empty())
 		return failHost(indices, indices, index_count, result_error,
 		    (options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument, bad);
-	if (options & (kOptPrune | kOptInternalDebug))
-		return failHost(indices, indices, index_count, result_error, meshoptgpu_StatusUnsupported,
-		    "meshopt_simplifyWithUpdate with Prune or the debug bit is not implemented on the GPU path");
 	try
 	{
 		ThreadState& s = state();
@@ -872,13 +869,9 @@ size_t meshoptgpu_simplifyWithUpdateDevice(unsigned int* indices, size_t index_c
 {
 	std::string bad = checkArgs(index_count, vertex_positions_stride, target_index_count, target_error, vertex_attributes_stride, attribute_weights,
 	    attribute_count, options);
-	if (bad.empty() && (options & (kOptPrune | kOptInternalDebug)))
-		bad = "meshopt_simplifyWithUpdate with Prune or the debug bit is not implemented on the GPU path";
 	if (!bad.empty())
 	{
-		setStatus((options & ~kSupportedOptions) || (options & (kOptPrune | kOptInternalDebug)) ? meshoptgpu_StatusUnsupported
-		                                                                                      : meshoptgpu_StatusInvalidArgument,
-		    bad);
+		setStatus((options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument, bad);
 		if (result_error)
 			*result_error = 0.f;
 		return index_count;

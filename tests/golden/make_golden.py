@@ -328,6 +328,20 @@ def clod_cases():
     return cases
 
 
+def _parts(seed):
+    """Several disconnected heightfield pieces of different sizes and scales in one buffer."""
+    rng = np.random.default_rng(seed)
+    parts_idx, parts_pos, base = [], [], 0
+    for p in range(int(rng.integers(3, 7))):
+        n = int(rng.integers(3, 14))
+        idx, pos = W.heightfield(n, seed=seed * 10 + p, amp=0.05)
+        pos = pos * np.float32(rng.uniform(0.05, 1.0)) + rng.uniform(-2, 2, size=3).astype(np.float32)
+        parts_idx.append(idx + base)
+        parts_pos.append(pos)
+        base += len(pos)
+    return np.concatenate(parts_idx).astype(np.uint32), np.concatenate(parts_pos).astype(np.float32)
+
+
 def update_cases():
     """meshopt_simplifyWithUpdate: the reference's simplifyUpdate / simplifyUpdateLocked tests
     (demo/tests.cpp:2590-2665; one interleaved buffer, their asserts checked here) and seeded
@@ -361,6 +375,13 @@ def update_cases():
         seeded.append((f"update_sphere{lv}_attr_lock_permissive", idx, pos, attr, w, lock, W.target_count(len(idx), 0.25), 5e-2, 32))
         half = idx[: (len(idx) // 6) * 3]
         seeded.append((f"update_sphere{lv}_sparse", half, pos, attr, w, None, W.target_count(len(half), 0.25), 5e-2, 2 | 4))
+    # Prune (8) removes whole pieces before the solve; the debug bit (1 << 30) tags the indices after it
+    # (LockBorder keeps open pieces from collapsing away on their own, so pruning decides the result)
+    for seed, ratio, error, options in ((201, 0.1, 0.2, 8 | 1), (203, 0.2, 5e-2, 8 | 1), (205, 0.1, 0.5, 8 | 1 | 4), (202, 0.1, 0.2, 8 | 1)):
+        idx, pos = _parts(seed)
+        seeded.append((f"update_parts{seed}_prune_{options}", idx, pos, None, None, None, W.target_count(len(idx), ratio), error, options))
+    idx, pos = W.heightfield(12, seed=4)
+    seeded.append(("update_hf12_debug", idx, pos, None, None, None, W.target_count(len(idx), 0.3), 5e-2, 1 << 30))
     for name, idx, pos, attr, w, lock, target, error, options in seeded:
         out, p2, a2, err = oracle.simplify_with_update("reference", idx, pos, target, error, options, attributes=attr, weights=w, lock=lock)
         c = dict(name=name, kind="separate", indices=idx, positions=pos, target=np.array(target), error=np.array(error, np.float32),

@@ -57,7 +57,24 @@ def _cases():
     out.append(("sphere6_attr_lock_permissive", idx, pos, attr, w, lock, W.target_count(len(idx), 0.1), 5e-3, mg.SimplifyPermissive))
     half = idx[: (len(idx) // 6) * 3]
     out.append(("sphere6_sparse_abs", half, pos, attr, w, None, W.target_count(len(half), 0.2), 1e-2, mg.SimplifySparse | mg.SimplifyErrorAbsolute))
+    out.append(("sphere6_attr_debug", idx, pos, attr, w, None, W.target_count(len(idx), 0.1), 5e-3, 1 << 30))
+    pidx, ppos = _parts(77)
+    out.append(("parts_prune_lockborder", pidx, ppos, None, None, None, W.target_count(len(pidx), 0.05), 0.5, mg.SimplifyPrune | mg.SimplifyLockBorder))
+    out.append(("parts_prune_sparse", pidx[: (len(pidx) // 6) * 3], ppos, None, None, None, W.target_count(len(pidx) // 2, 0.02), 0.5,
+                mg.SimplifyPrune | mg.SimplifyLockBorder | mg.SimplifySparse))
     return out
+
+
+def _parts(seed):
+    """Disconnected heightfield pieces of different sizes and scales in one vertex buffer."""
+    rng = np.random.default_rng(seed)
+    parts_idx, parts_pos, base = [], [], 0
+    for p in range(int(rng.integers(4, 9))):
+        idx, pos = W.heightfield(int(rng.integers(4, 60)), seed=seed * 10 + p, amp=0.05)
+        parts_idx.append(idx + base)
+        parts_pos.append(pos * np.float32(rng.uniform(0.05, 1.0)) + rng.uniform(-2, 2, size=3).astype(np.float32))
+        base += len(pos)
+    return np.concatenate(parts_idx).astype(np.uint32), np.concatenate(parts_pos).astype(np.float32)
 
 
 @pytest.mark.parametrize("name,idx,pos,attr,w,lock,target,error,options", _cases(), ids=lambda x: x if isinstance(x, str) else "")
@@ -70,7 +87,12 @@ def test_update_matches_oracle(port, name, idx, pos, attr, w, lock, target, erro
         assert _same(got[2], ref[2])
     assert got[3] == ref[3]
     moved = int(np.sum(np.any(got[1].view(np.uint32) != np.asarray(pos, np.float32).view(np.uint32), axis=1)))
-    assert moved > 0 or name == "hf128"
+    assert moved > 0 or name == "hf128" or len(got[0]) == 0
+    if options & mg.SimplifyPrune:
+        unpruned = port.simplify_with_update("port", idx, pos, target, error, options & ~mg.SimplifyPrune)
+        assert len(unpruned[0]) > len(got[0])  # the case removes pieces
+    if options & (1 << 30):
+        assert np.any(got[0] >> 28)
 
 
 def test_update_device_entry(port):
@@ -89,8 +111,24 @@ def test_update_device_entry(port):
     assert err == ref[3]
 
 
-def test_update_rejects_prune():
+def test_update_device_entry_prune(port):
+    """Prune through the device entry: pieces removed before the solve, survivors written back."""
+    torch = pytest.importorskip("torch")
+    idx, pos = _parts(78)
+    target = W.target_count(len(idx), 0.05)
+    opts = mg.SimplifyPrune | mg.SimplifyLockBorder
+    ref = port.simplify_with_update("port", idx, pos, target, 0.5, opts)
+    di = torch.from_numpy(idx.view(np.int32).copy()).cuda()
+    dp = torch.from_numpy(pos.copy()).cuda()
+    n, err = mg.simplify_with_update_device(di.data_ptr(), len(idx), dp.data_ptr(), len(pos), 12, target, 0.5, opts)
+    assert n < len(port.simplify_with_update("port", idx, pos, target, 0.5, mg.SimplifyLockBorder)[0])
+    assert np.array_equal(di[:n].cpu().numpy().view(np.uint32), ref[0])
+    assert _same(dp.cpu().numpy(), ref[1])
+    assert err == ref[3]
+
+
+def test_update_rejects_unknown_option():
     idx, pos = W.heightfield(8, seed=1)
     with pytest.raises(mg.SimplifyError) as e:
-        mg.simplify_with_update(idx, pos, 0, 1e-2, mg.SimplifyPrune)
+        mg.simplify_with_update(idx, pos, 0, 1e-2, 1 << 12)
     assert e.value.status == mg.STATUS_UNSUPPORTED
