@@ -441,6 +441,9 @@ __device__ __forceinline__ void cornerNeighbours(const unsigned int* __restrict_
 
 // ---------------------------------------------------------------- setup: classification
 
+constexpr unsigned int kOpenEdgesRegs = 12; // vertices with at most this many corners search in registers
+constexpr unsigned int kFillBatch = 4;      // corners whose loads kFillQuadrics issues together
+
 // openout (stored in loop) and openinc (stored in loopback) of classifyVertices :370-396,
 // from the vertex's own raw half-edge list: ~0u for none, the unique open neighbour, or the
 // vertex itself for several / a degenerate triangle.
@@ -452,6 +455,49 @@ __global__ void kOpenEdges(const unsigned int* __restrict__ idx, const unsigned 
 		return;
 	unsigned int v = (unsigned int)vi;
 	unsigned int b = off[v], e = off[v + 1];
+	if (e - b <= kOpenEdgesRegs)
+	{
+		// the corners' neighbours in registers (all loads issued together), then the same
+		// search over them
+		unsigned int nxs[kOpenEdgesRegs], pvs[kOpenEdgesRegs];
+		const unsigned int d = e - b;
+#pragma unroll
+		for (unsigned int q = 0; q < kOpenEdgesRegs; ++q)
+			nxs[q] = q < d ? csr[b + q] : 0u;
+#pragma unroll
+		for (unsigned int q = 0; q < kOpenEdgesRegs; ++q)
+		{
+			if (q < d)
+				cornerNeighbours(idx, nxs[q], nxs[q], pvs[q]);
+			else
+				nxs[q] = pvs[q] = ~0u;
+		}
+		bool degen = false;
+#pragma unroll
+		for (unsigned int q = 0; q < kOpenEdgesRegs; ++q)
+			degen |= q < d && nxs[q] == v;
+		unsigned int outc = 0, outt = ~0u, inc = 0, ins = ~0u;
+#pragma unroll
+		for (unsigned int j = 0; j < kOpenEdgesRegs; ++j)
+		{
+			if (j >= d)
+				break;
+			bool has_back = false, has_fwd = false;
+#pragma unroll
+			for (unsigned int q = 0; q < kOpenEdgesRegs; ++q)
+			{
+				has_back |= q < d && pvs[q] == nxs[j];
+				has_fwd |= q < d && nxs[q] == pvs[j];
+			}
+			if (!has_back)
+				outc++, outt = nxs[j];
+			if (!has_fwd)
+				inc++, ins = pvs[j];
+		}
+		loop[v] = degen ? v : (outc == 0 ? ~0u : (outc == 1 ? outt : v));
+		loopback[v] = degen ? v : (inc == 0 ? ~0u : (inc == 1 ? ins : v));
+		return;
+	}
 	bool degen = false;
 	for (unsigned int j = b; j < e; ++j)
 	{
@@ -705,15 +751,34 @@ __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsign
 	unsigned int b = off[r], e = off[r + 1];
 	Quadric Q = qzero();
 	float4 G = make_float4(0.f, 0.f, 0.f, 0.f); // volume gradient (update mode with attributes), the same face order
-	for (unsigned int j = b; j < e; ++j)
+	// corners in groups of kFillBatch: the group's loads are issued together (past the end the
+	// last corner is loaded again), then its faces fold in corner order
+	for (unsigned int j = b; j < e; j += kFillBatch)
 	{
-		unsigned int f = csr[j] / 3;
-		unsigned int i0 = idx[f * 3 + 0], i1 = idx[f * 3 + 1], i2 = idx[f * 3 + 2];
-		V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1), p2 = ldpos(pos, i2);
-		Quadric F = qtriangle(p0, p1, p2, 1.f);
-		qadd(Q, F);
-		if (vg)
-			gadd(G, qvolumeGrad(p0, p1, p2));
+		uint3 t[kFillBatch];
+#pragma unroll
+		for (unsigned int q = 0; q < kFillBatch; ++q)
+		{
+			unsigned int f = csr[min(j + q, e - 1)] / 3;
+			t[q] = make_uint3(idx[f * 3 + 0], idx[f * 3 + 1], idx[f * 3 + 2]);
+		}
+		V3 p[kFillBatch][3];
+#pragma unroll
+		for (unsigned int q = 0; q < kFillBatch; ++q)
+		{
+			p[q][0] = ldpos(pos, t[q].x);
+			p[q][1] = ldpos(pos, t[q].y);
+			p[q][2] = ldpos(pos, t[q].z);
+		}
+#pragma unroll
+		for (unsigned int q = 0; q < kFillBatch; ++q)
+			if (j + q < e)
+			{
+				Quadric F = qtriangle(p[q][0], p[q][1], p[q][2], 1.f);
+				qadd(Q, F);
+				if (vg)
+					gadd(G, qvolumeGrad(p[q][0], p[q][1], p[q][2]));
+			}
 	}
 	if (vg)
 		vg[r] = G;
@@ -724,38 +789,58 @@ __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsign
 	qadd(Q, P);
 
 	unsigned int lastf = ~0u;
-	for (unsigned int j = b; j < e; ++j)
+	for (unsigned int j = b; j < e; j += kFillBatch)
 	{
-		unsigned int f = csr[j] / 3;
-		if (f == lastf)
-			continue;
-		lastf = f;
-		for (int ed = 0; ed < 3; ++ed)
+		unsigned int fs[kFillBatch];
+		unsigned int tv[kFillBatch][3];
+		unsigned char tk[kFillBatch][3];
+#pragma unroll
+		for (unsigned int q = 0; q < kFillBatch; ++q)
 		{
-			unsigned int i0 = idx[f * 3 + ed];
-			unsigned int i1 = idx[f * 3 + (ed == 2 ? 0 : ed + 1)];
-			unsigned char k0 = kind[i0], k1 = kind[i1];
-			bool b0 = k0 == kBorder || k0 == kSeam, b1 = k1 == kBorder || k1 == kSeam;
-			if (!b0 && !b1)
+			fs[q] = csr[min(j + q, e - 1)] / 3;
+#pragma unroll
+			for (int c = 0; c < 3; ++c)
+				tv[q][c] = idx[fs[q] * 3 + c];
+		}
+#pragma unroll
+		for (unsigned int q = 0; q < kFillBatch; ++q)
+#pragma unroll
+			for (int c = 0; c < 3; ++c)
+				tk[q][c] = kind[tv[q][c]];
+#pragma unroll
+		for (unsigned int q = 0; q < kFillBatch; ++q)
+		{
+			if (j + q >= e || fs[q] == lastf)
 				continue;
-			if (b0 && loop[i0] != i1)
-				continue;
-			if (b1 && loopback[i1] != i0)
-				continue;
-			bool to0 = remap[i0] == r, to1 = remap[i1] == r;
-			if (!to0 && !to1)
-				continue;
-			unsigned int i2 = idx[f * 3 + (ed == 0 ? 2 : ed - 1)];
-			float weight = (k0 == kBorder || k1 == kBorder) ? 10.f : 0.5f;
-			V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1), p2 = ldpos(pos, i2);
-			Quadric E = qedge(p0, p1, p2, weight);
-			Quadric T = qtriangle(p0, p1, p2, weight);
-			T.w = 0;
-			qadd(E, T);
-			if (to0)
-				qadd(Q, E);
-			if (to1)
-				qadd(Q, E);
+			lastf = fs[q];
+#pragma unroll
+			for (int ed = 0; ed < 3; ++ed)
+			{
+				const int ne = ed == 2 ? 0 : ed + 1, pe = ed == 0 ? 2 : ed - 1;
+				unsigned int i0 = tv[q][ed], i1 = tv[q][ne];
+				unsigned char k0 = tk[q][ed], k1 = tk[q][ne];
+				bool b0 = k0 == kBorder || k0 == kSeam, b1 = k1 == kBorder || k1 == kSeam;
+				if (!b0 && !b1)
+					continue;
+				if (b0 && loop[i0] != i1)
+					continue;
+				if (b1 && loopback[i1] != i0)
+					continue;
+				bool to0 = remap[i0] == r, to1 = remap[i1] == r;
+				if (!to0 && !to1)
+					continue;
+				unsigned int i2 = tv[q][pe];
+				float weight = (k0 == kBorder || k1 == kBorder) ? 10.f : 0.5f;
+				V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1), p2 = ldpos(pos, i2);
+				Quadric E = qedge(p0, p1, p2, weight);
+				Quadric T = qtriangle(p0, p1, p2, weight);
+				T.w = 0;
+				qadd(E, T);
+				if (to0)
+					qadd(Q, E);
+				if (to1)
+					qadd(Q, E);
+			}
 		}
 	}
 	stquadric(vq, r, Q);
@@ -792,12 +877,44 @@ __global__ void kFillAttributeQuadrics(const unsigned int* __restrict__ idx, con
 #pragma unroll
 	for (int k = 0; k < MAXA; ++k)
 		G[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-	for (unsigned int j = off[v]; j < off[v + 1]; ++j)
+	// up to 8 attributes: two faces' loads (positions and attributes into registers) are issued
+	// together, then the two fold in corner order; wider attribute sets go one face at a time
+	constexpr unsigned int B = MAXA <= 8 ? 2 : 1;
+	const unsigned int b = off[v], e = off[v + 1];
+	for (unsigned int j = b; j < e; j += B)
 	{
-		unsigned int f = csr[j] / 3;
-		unsigned int i0 = idx[f * 3 + 0], i1 = idx[f * 3 + 1], i2 = idx[f * 3 + 2];
-		addAttributeQuadric<MAXA>(Q, G, count, ldpos(pos, i0), ldpos(pos, i1), ldpos(pos, i2), attr + (size_t)i0 * count, attr + (size_t)i1 * count,
-		    attr + (size_t)i2 * count);
+		uint3 t[B];
+#pragma unroll
+		for (unsigned int q = 0; q < B; ++q)
+		{
+			unsigned int f = csr[min(j + q, e - 1)] / 3;
+			t[q] = make_uint3(idx[f * 3 + 0], idx[f * 3 + 1], idx[f * 3 + 2]);
+		}
+		if constexpr (MAXA <= 8)
+		{
+			V3 p[B][3];
+			float at[B][3][MAXA];
+#pragma unroll
+			for (unsigned int q = 0; q < B; ++q)
+			{
+				const unsigned int tc[3] = {t[q].x, t[q].y, t[q].z};
+#pragma unroll
+				for (int c = 0; c < 3; ++c)
+				{
+					p[q][c] = ldpos(pos, tc[c]);
+#pragma unroll
+					for (int k = 0; k < MAXA; ++k)
+						at[q][c][k] = k < count ? __ldg(attr + (size_t)tc[c] * count + k) : 0.f;
+				}
+			}
+#pragma unroll
+			for (unsigned int q = 0; q < B; ++q)
+				if (j + q < e)
+					addAttributeQuadric<MAXA>(Q, G, count, p[q][0], p[q][1], p[q][2], at[q][0], at[q][1], at[q][2]);
+		}
+		else
+			addAttributeQuadric<MAXA>(Q, G, count, ldpos(pos, t[0].x), ldpos(pos, t[0].y), ldpos(pos, t[0].z), attr + (size_t)t[0].x * count,
+			    attr + (size_t)t[0].y * count, attr + (size_t)t[0].z * count);
 	}
 	stquadric(aq, v, Q);
 #pragma unroll
@@ -1115,6 +1232,31 @@ struct PerformArgs
 //    and no undecided earlier candidate moves a vertex of its one-ring (minS); then the flip
 //    test runs against the one-ring as moved by earlier commits only (moving commit < k).
 // Returns true if k stays undecided.
+
+// the commit of a decided candidate: r0 moves to its target and both endpoints lock
+__device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int k, unsigned int r0, unsigned int r1)
+{
+	uint2 ii = __ldg(a.sidx + k);
+	const unsigned int i0 = ii.x, i1 = ii.y;
+	unsigned char kd = __ldg(a.skind + k);
+	unsigned int target;
+	if (kd == kComplex)
+		target = complexTarget(r0, i1, a.remap, a.loop, a.loopback);
+	else if (kd == kSeam)
+	{
+		unsigned int s0 = a.wedge[i0];
+		unsigned int s1 = a.loop[i0] == i1 ? a.loopback[s0] : a.loop[s0];
+		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
+		target = (s0 == r0) ? s1 : i1;
+	}
+	else
+		target = i1;
+	a.moved[r0] = ((unsigned long long)k << 32) | target;
+	a.touched[r0] = 1;
+	a.touched[r1] = 1;
+	a.status[k] = kCommit;
+}
+
 __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
 {
 	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
@@ -1197,25 +1339,7 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 			}
 		}
 	}
-	uint2 ii = __ldg(a.sidx + k);
-	const unsigned int i0 = ii.x, i1 = ii.y;
-	unsigned char kd = __ldg(a.skind + k);
-	unsigned int target;
-	if (kd == kComplex)
-		target = complexTarget(r0, i1, a.remap, a.loop, a.loopback);
-	else if (kd == kSeam)
-	{
-		unsigned int s0 = a.wedge[i0];
-		unsigned int s1 = a.loop[i0] == i1 ? a.loopback[s0] : a.loop[s0];
-		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
-		target = (s0 == r0) ? s1 : i1;
-	}
-	else
-		target = i1;
-	a.moved[r0] = ((unsigned long long)k << 32) | target;
-	a.touched[r0] = 1;
-	a.touched[r1] = 1;
-	a.status[k] = kCommit;
+	commitOne(a, k, r0, r1);
 	return false;
 }
 
@@ -1280,6 +1404,21 @@ __device__ __forceinline__ bool keepTriangle(const unsigned int* __restrict__ re
 	return r0 != r1 && r0 != r2 && r1 != r2;
 }
 
+// attribute quadric and gradient rows of vertex v added into those of vertex t (t != v)
+__device__ __forceinline__ void mergeRows(const Quadric* __restrict__ vq, Quadric* __restrict__ tq, const float4* __restrict__ vg, float4* __restrict__ tg,
+    int ac)
+{
+	Quadric A = ldquadric(tq, 0);
+	qadd(A, ldquadric(vq, 0));
+	stquadric(tq, 0, A);
+	for (int q = 0; q < ac; ++q)
+	{
+		float4 g = tg[q], h = vg[q];
+		g.x += h.x, g.y += h.y, g.z += h.z, g.w += h.w;
+		tg[q] = g;
+	}
+}
+
 __device__ __forceinline__ void mergeAttributes(const PerformArgs& a, unsigned int v, unsigned int t)
 {
 	Quadric A = ldquadric(a.aq, t);
@@ -1295,40 +1434,20 @@ __device__ __forceinline__ void mergeAttributes(const PerformArgs& a, unsigned i
 }
 
 // the collapse_remap writes and quadric merges of one committed candidate; attribute sources
-// of one commit merge in increasing vertex order, as updateQuadrics' vertex loop does
-__device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& errbits, unsigned int& derrbits)
+// of one commit merge in increasing vertex order, as updateQuadrics' vertex loop does.
+// Commits of one pass touch disjoint vertices (no two share an endpoint, and every vertex
+// written belongs to the position of r0 or r1), so a commit reads only values that no other
+// commit of the pass writes.
+__device__ void applyComplexCommit(const PerformArgs& a, unsigned int r0, unsigned int r1, unsigned int i0, unsigned int i1, unsigned int& derrbits)
 {
-	uint4 rec = __ldg(a.srec + k);
-	uint2 ii = __ldg(a.sidx + k);
-	const unsigned int r0 = rec.x, r1 = rec.y, i0 = ii.x, i1 = ii.y;
-	unsigned char kd = __ldg(a.skind + k);
 	Quadric Q1 = ldquadric(a.vq, r1);
 	Quadric Q0 = ldquadric(a.vq, r0);
-	float e = __uint_as_float(__ldg(a.serr + k));
-
-	unsigned int mv0 = i0, mv1 = ~0u; // moved vertices of a non-complex commit, at most two
-	if (kd == kComplex)
+	unsigned int v = i0;
+	do
 	{
-		unsigned int v = i0;
-		do
-		{
-			a.cr[v] = complexTarget(v, i1, a.remap, a.loop, a.loopback);
-			v = a.wedge[v];
-		} while (v != i0);
-	}
-	else if (kd == kSeam)
-	{
-		unsigned int s0 = a.wedge[i0];
-		unsigned int s1 = a.loop[i0] == i1 ? a.loopback[s0] : a.loop[s0];
-		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
-		a.cr[i0] = i1;
-		a.cr[s0] = s1;
-		if (s0 != i0)
-			mv0 = min(i0, s0), mv1 = max(i0, s0);
-	}
-	else
-		a.cr[i0] = i1;
-
+		a.cr[v] = complexTarget(v, i1, a.remap, a.loop, a.loopback);
+		v = a.wedge[v];
+	} while (v != i0);
 	qadd(Q1, Q0);
 	stquadric(a.vq, r1, Q1);
 	if (a.vg)
@@ -1337,40 +1456,100 @@ __device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& 
 		gadd(g, a.vg[r0]);
 		a.vg[r1] = g;
 	}
-	errbits = e == e ? __float_as_uint(e) : 0u;
-
 	if (a.ac)
 	{
-		if (kd == kComplex)
+		// all wedges of the source, in increasing vertex order (selection by repeated minimum)
+		unsigned int last = 0;
+		bool first = true;
+		for (;;)
 		{
-			// all wedges of the source, in increasing vertex order (selection by repeated minimum)
-			unsigned int last = 0;
-			bool first = true;
-			for (;;)
+			unsigned int best = ~0u;
+			v = i0;
+			do
 			{
-				unsigned int best = ~0u, v = i0;
-				do
-				{
-					if ((first || v > last) && v < best)
-						best = v;
-					v = a.wedge[v];
-				} while (v != i0);
-				if (best == ~0u)
-					break;
-				mergeAttributes(a, best, a.cr[best]);
-				last = best;
-				first = false;
-			}
-		}
-		else
-		{
-			mergeAttributes(a, mv0, a.cr[mv0]);
-			if (mv1 != ~0u)
-				mergeAttributes(a, mv1, a.cr[mv1]);
+				if ((first || v > last) && v < best)
+					best = v;
+				v = a.wedge[v];
+			} while (v != i0);
+			if (best == ~0u)
+				break;
+			mergeAttributes(a, best, a.cr[best]);
+			last = best;
+			first = false;
 		}
 		float d = qerror(Q0, ldpos(a.pos, a.remap[a.cr[r0]]));
 		derrbits = d == d ? __float_as_uint(d) : 0u;
 	}
+}
+
+__device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& errbits, unsigned int& derrbits)
+{
+	uint4 rec = __ldg(a.srec + k);
+	uint2 ii = __ldg(a.sidx + k);
+	const unsigned int r0 = rec.x, r1 = rec.y, i0 = ii.x, i1 = ii.y;
+	unsigned char kd = __ldg(a.skind + k);
+	float e = __uint_as_float(__ldg(a.serr + k));
+	errbits = e == e ? __float_as_uint(e) : 0u;
+	if (kd == kComplex)
+	{
+		applyComplexCommit(a, r0, r1, i0, i1, derrbits);
+		return;
+	}
+
+	// collapse_remap: cr[i0] = i1, then for a seam cr[s0] = s1 (s0 may be i0 itself, which
+	// then ends at s1); the targets are known here, so nothing is read back from cr
+	unsigned int s0 = ~0u, s1 = ~0u;
+	if (kd == kSeam)
+	{
+		s0 = a.wedge[i0];
+		unsigned int li = a.loop[i0];
+		s1 = li == i1 ? a.loopback[s0] : a.loop[s0];
+		s1 = (s1 != ~0u) ? s1 : a.wedge[i1];
+	}
+	unsigned int mv0 = i0, mv1 = ~0u; // moved vertices, at most two, in increasing order
+	if (s0 != ~0u && s0 != i0)
+		mv0 = min(i0, s0), mv1 = max(i0, s0);
+	const unsigned int t0 = mv0 == s0 ? s1 : i1;
+
+	// the rows read and written below belong to distinct vertices (r0 != r1, and t0 is a wedge
+	// of r1 while mv0 is one of r0), which the restrict-qualified row pointers tell the compiler,
+	// so it can issue the loads ahead of the stores; cr is written last
+	const Quadric* __restrict__ q0 = a.vq + r0;
+	Quadric* __restrict__ q1 = a.vq + r1;
+	const int ac = a.ac;
+	V3 pr = {0.f, 0.f, 0.f};
+	if (ac)
+	{
+		const unsigned int tr = r0 == s0 ? s1 : (r0 == i0 ? i1 : __ldcg(a.cr + r0));
+		pr = ldpos(a.pos, __ldg(a.remap + tr));
+	}
+	Quadric Q1 = ldquadric(q1, 0);
+	Quadric Q0 = ldquadric(q0, 0);
+	qadd(Q1, Q0);
+	stquadric(q1, 0, Q1);
+	if (a.vg)
+	{
+		const float4* __restrict__ g0 = a.vg + r0;
+		float4* __restrict__ g1 = a.vg + r1;
+		float4 g = *g1;
+		gadd(g, *g0);
+		*g1 = g;
+	}
+	if (ac)
+	{
+		mergeRows(a.aq + mv0, a.aq + t0, a.ag + (size_t)mv0 * ac, a.ag + (size_t)t0 * ac, ac);
+		if (mv1 != ~0u)
+		{
+			// after the first merge: both may share a target
+			const unsigned int t1 = mv1 == s0 ? s1 : i1;
+			mergeRows(a.aq + mv1, a.aq + t1, a.ag + (size_t)mv1 * ac, a.ag + (size_t)t1 * ac, ac);
+		}
+		float d = qerror(Q0, pr);
+		derrbits = d == d ? __float_as_uint(d) : 0u;
+	}
+	a.cr[i0] = i1;
+	if (s0 != ~0u)
+		a.cr[s0] = s1;
 }
 
 // kPerform phases timed by block 0 between grid barriers (SM clock cycles)
@@ -1404,7 +1583,11 @@ struct PhaseClock
 	}
 };
 
-__global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
+#ifndef MO_PERFORM_MIN_BLOCKS
+#define MO_PERFORM_MIN_BLOCKS 4 // resident blocks per SM the pass kernel is compiled for (64 registers)
+#endif
+
+__global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(PerformArgs a)
 {
 	__shared__ unsigned int s_app[33];
 	PhaseClock pc;
@@ -1630,38 +1813,39 @@ __global__ void __launch_bounds__(kThreads, 4) kPerform(PerformArgs a)
 	if (__ldcg(&sc->grid_error))
 		return;
 
-	// ---- apply the committed prefix: each block compacts the commits of its chunk of [0, cut)
-	// in shared memory, 4096 sorted positions at a time, so every lane applies a commit
+	// ---- apply the committed prefix. Commits are independent (no two share an endpoint), so
+	// any order gives the same result. Sorted order is cut into slices of blockDim positions and
+	// block b takes slices b, b + G, b + 2G, ...: commits are densest at the front of sorted
+	// order, and interleaving spreads them evenly over the blocks. Each block compacts the commits
+	// of 16 slices at a time in shared memory, so every lane applies a commit.
 	const unsigned long long cutv = __ldcg(&sc->cut);
 	const unsigned int cut = cutv == ~0ull ? count : (unsigned int)(cutv >> 2);
 	unsigned int nd = 0, ns = 0, ni = 0, em = 0, dm = 0;
 	{
+		constexpr unsigned int per = kApplyTile / kThreads; // slices per block step
 		__shared__ unsigned int clist[kApplyTile];
-		const unsigned int per_block = (cut + G - 1) / G;
-		const unsigned int c0 = min(cut, blockIdx.x * per_block), c1 = min(cut, c0 + per_block);
-		for (unsigned int base = c0; base < c1; base += kApplyTile)
+		const unsigned int slices = (cut + kThreads - 1) / kThreads;
+		for (unsigned int s0 = blockIdx.x; s0 < slices; s0 += G * per)
 		{
-			const unsigned int lim = min(c1, base + kApplyTile);
-			const unsigned int per = kApplyTile / kThreads; // 16 consecutive positions per thread
-			const unsigned int p0 = base + threadIdx.x * per;
-			unsigned int mine = 0;
+			unsigned int mine = 0, mask = 0;
 			for (unsigned int q = 0; q < per; ++q)
 			{
-				unsigned int k = p0 + q;
-				if (k < lim)
+				unsigned int s = s0 + q * G;
+				unsigned int k = s * kThreads + threadIdx.x;
+				if (s < slices && k < cut)
 				{
 					unsigned char st = __ldcg(a.status + k);
 					nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
 					mine += st == kCommit;
+					mask |= (st == kCommit ? 1u : 0u) << q;
 				}
 			}
 			unsigned int off = mine, d1 = 0, d2 = 0;
 			uint3 tot = blockScan3(off, d1, d2, sm);
-			for (unsigned int q = 0; q < per; ++q)
+			for (; mask; mask &= mask - 1)
 			{
-				unsigned int k = p0 + q;
-				if (k < lim && __ldcg(a.status + k) == kCommit)
-					clist[off++] = k;
+				unsigned int q = __ffs(mask) - 1;
+				clist[off++] = (s0 + q * G) * kThreads + threadIdx.x;
 			}
 			__syncthreads();
 			for (unsigned int x = threadIdx.x; x < tot.x; x += blockDim.x)
