@@ -122,29 +122,46 @@ __global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* _
 // Stable scatter: elements are ranked in index order (sub-round j holds elements
 // j*256 .. j*256+255 of the tile; within it, warp w and lane l give the order), so equal
 // digits keep their input order; tiles are laid out by the digit-major scanned histogram.
+// The tile is first put in digit order in shared memory and then written out front to back,
+// so each digit's elements of the tile leave as one contiguous run (coalesced stores).
 __global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
     unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, size_t n, const unsigned int* n_dev, int shift, const unsigned int* __restrict__ hist,
     unsigned int tiles)
 {
 	// vin == nullptr stands for the identity values 0..n-1
 	n = liveCount(n, n_dev);
-	__shared__ unsigned int base[kSortBins];
-	__shared__ unsigned int wcnt[2][kSortThreads / 32][kSortBins];
+	__shared__ unsigned int base[kSortBins];  // next tile-local slot per digit
+	__shared__ unsigned int lbase[kSortBins]; // tile-local start per digit
+	__shared__ unsigned int gbase[kSortBins]; // global position of the tile's first element per digit
+	// per warp and digit: the sub-round's count, then its first slot; zero between sub-rounds
+	__shared__ unsigned int wcnt[kSortThreads / 32][kSortBins];
+	__shared__ unsigned int sk[kSortTile], sv[kSortTile];
 
 	const unsigned int t = threadIdx.x, w = t >> 5, lane = t & 31;
-	base[t] = hist[(size_t)t * tiles + blockIdx.x];
+	const size_t tile0 = (size_t)blockIdx.x * kSortTile;
+	if (tile0 >= n)
+		return;
+	const unsigned int tile_n = (unsigned int)min((size_t)kSortTile, n - tile0);
+	{
+		// the tile's count of digit t: the scanned histogram's next entry (digit-major, so the
+		// entry after (t, last tile) is (t + 1, first tile); after the last one comes n)
+		const size_t at = (size_t)t * tiles + blockIdx.x;
+		const unsigned int g = hist[at];
+		const unsigned int next = at + 1 < (size_t)kSortBins * tiles ? hist[at + 1] : (unsigned int)n;
+		gbase[t] = g;
+		unsigned int total;
+		unsigned int l = blockExclusiveScan<kSortThreads>(next - g, wcnt[0], &total);
+		__syncthreads();
+		lbase[t] = l;
+		base[t] = l;
+	}
 #pragma unroll
 	for (int q = 0; q < kSortThreads / 32; ++q)
-	{
-		wcnt[0][q][t] = 0;
-		wcnt[1][q][t] = 0;
-	}
+		wcnt[q][t] = 0;
 	__syncthreads();
 
-	size_t tile0 = (size_t)blockIdx.x * kSortTile;
 	for (int j = 0; j < kSortItems; ++j)
 	{
-		const int b = j & 1;
 		size_t i = tile0 + (size_t)j * kSortThreads + t;
 		bool valid = i < n;
 		unsigned int k = valid ? __ldg(kin + i) : 0u;
@@ -152,28 +169,42 @@ __global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int
 		unsigned int d = valid ? ((k >> shift) & 0xFFu) : (0x100u + lane);
 		unsigned int peers = __match_any_sync(0xffffffffu, d);
 		unsigned int rank = __popc(peers & ((1u << lane) - 1u));
-		if (valid && lane == (unsigned)(__ffs(peers) - 1))
-			wcnt[b][w][d] = __popc(peers);
+		bool leader = valid && lane == (unsigned)(__ffs(peers) - 1);
+		if (leader)
+			wcnt[w][d] = __popc(peers);
 		__syncthreads();
 		{
+			// counts to first slots, in warp order; entries without elements stay zero
 			unsigned int run = base[t];
 #pragma unroll
 			for (int q = 0; q < kSortThreads / 32; ++q)
 			{
-				unsigned int c = wcnt[b][q][t];
-				wcnt[b][q][t] = run;
+				unsigned int c = wcnt[q][t];
+				if (c)
+					wcnt[q][t] = run;
 				run += c;
-				wcnt[b ^ 1][q][t] = 0;
 			}
 			base[t] = run;
 		}
 		__syncthreads();
+		unsigned int lp = valid ? wcnt[w][d] + rank : 0u;
+		__syncwarp();
+		if (leader)
+			wcnt[w][d] = 0; // only this warp's lanes read it
 		if (valid)
 		{
-			unsigned int pos = wcnt[b][w][d] + rank;
-			kout[pos] = k;
-			vout[pos] = v;
+			sk[lp] = k;
+			sv[lp] = v;
 		}
+	}
+	__syncthreads();
+	for (unsigned int x = t; x < tile_n; x += kSortThreads)
+	{
+		unsigned int k = sk[x];
+		unsigned int d = (k >> shift) & 0xFFu;
+		unsigned int pos = gbase[d] + (x - lbase[d]);
+		kout[pos] = k;
+		vout[pos] = sv[x];
 	}
 }
 

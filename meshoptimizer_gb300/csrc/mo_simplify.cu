@@ -54,7 +54,7 @@ struct PassLive
 	unsigned int passes;
 	unsigned int iterations;
 	unsigned int target;      // target_index_count
-	unsigned int pad;
+	float error_limit;        // squared, in the rescaled space (:2489-2491)
 	double window_factor;
 };
 
@@ -372,12 +372,22 @@ __global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned 
 // the largest count of corners[v] = off[v+1] - off[v]
 __global__ void kMaxDegree(const unsigned int* __restrict__ off, size_t n, unsigned int* out)
 {
+	__shared__ unsigned int wmax[32];
 	size_t i = gtid();
 	unsigned int d = i < n ? off[i + 1] - off[i] : 0u;
 	for (int o = 16; o > 0; o >>= 1)
 		d = max(d, __shfl_down_sync(0xffffffffu, d, o));
-	if ((threadIdx.x & 31) == 0 && d)
-		atomicMax(out, d);
+	if ((threadIdx.x & 31) == 0)
+		wmax[threadIdx.x >> 5] = d;
+	__syncthreads();
+	if (threadIdx.x < 32)
+	{
+		d = threadIdx.x < blockDim.x / 32 ? wmax[threadIdx.x] : 0u;
+		for (int o = 16; o > 0; o >>= 1)
+			d = max(d, __shfl_down_sync(0xffffffffu, d, o));
+		if (threadIdx.x == 0 && d)
+			atomicMax(out, d); // one atomic per block
+	}
 }
 
 // vertex -> corner lists: every corner into its vertex's range (arbitrary order within it), then
@@ -397,6 +407,7 @@ __global__ void kCornerFill(const unsigned int* __restrict__ idx, const unsigned
 // insertion sort of each vertex's corners (only used when no vertex has more than
 // kCornerSortMax corners)
 constexpr unsigned int kCornerSortMax = 64;
+constexpr unsigned int kCornerRegs = 16; // lists up to this long are sorted in registers
 
 __global__ void kCornerSort(const unsigned int* __restrict__ off, size_t n, unsigned int* csr)
 {
@@ -404,6 +415,26 @@ __global__ void kCornerSort(const unsigned int* __restrict__ off, size_t n, unsi
 	if (v >= n)
 		return;
 	const unsigned int b = off[v], e = off[v + 1];
+	if (e - b <= kCornerRegs)
+	{
+		// in registers: corner indices are distinct, so each one's rank is the count of smaller ones
+		const unsigned int d = e - b;
+		unsigned int c[kCornerRegs];
+#pragma unroll
+		for (unsigned int q = 0; q < kCornerRegs; ++q)
+			c[q] = q < d ? csr[b + q] : ~0u;
+#pragma unroll
+		for (unsigned int q = 0; q < kCornerRegs; ++q)
+			if (q < d)
+			{
+				unsigned int r = 0;
+#pragma unroll
+				for (unsigned int p = 0; p < kCornerRegs; ++p)
+					r += c[p] < c[q];
+				csr[b + r] = c[q];
+			}
+		return;
+	}
 	for (unsigned int j = b + 1; j < e; ++j)
 	{
 		unsigned int x = csr[j];
@@ -1603,6 +1634,7 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 	// per-pass scalars: the launch parameters, or the device-resident loop's live state
 	unsigned int count = a.count, tris = a.tris, first_window = a.first_window, round_base = a.round_base, prev_err = a.prev_err_bits;
 	unsigned long long goal = a.goal;
+	float error_limit = a.error_limit;
 	const unsigned int* res = a.res;
 	unsigned int* res_next = a.res_next;
 	if (a.live)
@@ -1618,6 +1650,7 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		res = lv->res;
 		res_next = lv->res_next;
 		prev_err = sc->result_error_bits;
+		error_limit = lv->error_limit;
 	}
 
 	for (size_t i = gtid(); i < a.vcount; i += gthreads)
@@ -1778,7 +1811,7 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 			{
 				float e = __uint_as_float(__ldg(a.serr + k));
 				unsigned int reason = 0;
-				if (e > a.error_limit)
+				if (e > error_limit)
 					reason = 1;
 				else if (T >= goal)
 					reason = 2;
@@ -2264,6 +2297,14 @@ __global__ void kFinalizeVertices(size_t n, const unsigned char* __restrict__ up
 // After the pick: the pass's candidate count, triangle goal and first window (the host loop's
 // arithmetic), and the per-pass resets of kPerform's scalars. No candidate ends the loop (the
 // host loop's break at C == 0).
+// the pass loop's squared error limit (:2489-2491) from the extent kMinMaxFinal left, with the
+// host's operations: target_error^2 / scale^2, scale = the extent for ErrorAbsolute, else 1
+__global__ void kErrorLimit(Scalars* sc, float target_error, int absolute)
+{
+	const float s = absolute ? sc->extent : 1.f;
+	sc->live.error_limit = (target_error * target_error) / (s * s);
+}
+
 __global__ void kPassPrep(Scalars* sc)
 {
 	PassLive& lv = sc->live;
@@ -2698,8 +2739,18 @@ Simplifier::Simplifier(int device) : device_(device)
 	perform_blocks_ = std::min(coop_blocks_, unsigned(std::max(1, sms * tuning_.perform_blocks_per_sm)));
 }
 
+void Simplifier::dropLoopGraph()
+{
+	if (loop_.exec)
+		cudaGraphExecDestroy(loop_.exec);
+	if (loop_.graph)
+		cudaGraphDestroy(loop_.graph);
+	loop_ = LoopGraph{};
+}
+
 Simplifier::~Simplifier()
 {
+	dropLoopGraph();
 	if (capture_)
 		cudaStreamDestroy(capture_);
 	if (pinned_)
@@ -3012,9 +3063,24 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_LAUNCH(kDualCount, gV, kThreads, 0, stream, w.off_raw, w.kind, V, &w.sc->dual);
 	MO_LAUNCH(kCapacity, 1, 32, 0, stream, I, w.sc);
 	MO_CUDA_CHECK(cudaGetLastError());
-	readScalars();
-	const float vertex_scale = hs->extent;
-	rr.scale = vertex_scale;
+
+	// The device-resident pass loop (below) takes no host values from setup: its graph is
+	// recorded and instantiated while the setup kernels run, and the extent is read after it.
+	// Pruning, the debug bit and per-phase event timing need the host between passes.
+	const bool device_loop =
+	    tuning_.device_loop && !timed && !dump && !(m.options & (kOptPrune | kOptInternalDebug)) && I > m.target_index_count;
+	float vertex_scale = 0.f, error_scale = 1.f, error_limit = 0.f;
+	auto takeScale = [&]() {
+		vertex_scale = hs->extent;
+		rr.scale = vertex_scale;
+		error_scale = (m.options & kOptErrorAbsolute) ? vertex_scale : 1.f;
+		error_limit = (m.target_error * m.target_error) / (error_scale * error_scale);
+	};
+	if (!device_loop)
+	{
+		readScalars();
+		takeScale();
+	}
 
 	if (dump)
 	{
@@ -3059,8 +3125,6 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaEventRecord(ev[1], stream));
 
 	// ---- pass loop (src/simplifier.cpp:2493-2541)
-	const float error_scale = (m.options & kOptErrorAbsolute) ? vertex_scale : 1.f;
-	const float error_limit = (m.target_error * m.target_error) / (error_scale * error_scale);
 	size_t result_count = I;
 	unsigned int* res = w.res0;
 	unsigned int* res_next = w.res1;
@@ -3102,11 +3166,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	MO_CUDA_CHECK(cudaMemsetAsync(w.minS, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
 
 	// ---- the pass loop on the device: one pass recorded into the body of a WHILE conditional
-	// node, replayed until kPassEnd ends it (pruning, the debug bit and per-phase event timing
-	// need the host between passes and take the host loop below)
-	if (tuning_.device_loop && !timed && !(m.options & (kOptPrune | kOptInternalDebug)) && result_count > m.target_index_count)
+	// node, replayed until kPassEnd ends it
+	if (device_loop)
 	{
-		const size_t T0 = I / 3, capn = std::max<size_t>(hs->capacity, 1);
+		// grids cover the capacity bound (boundEdgeCollapses <= I + 3); the kernels stop at the
+		// live counts
+		const size_t T0 = I / 3, capn = I + 3;
 		PassLive init{};
 		init.res = w.res0;
 		init.res_next = w.res1;
@@ -3116,125 +3181,143 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		init.window_factor = tuning_.window_factor;
 		MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->live, &init, sizeof(init), cudaMemcpyHostToDevice, stream));
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->result_error_bits, 0, 4, stream));
+		MO_LAUNCH(kErrorLimit, 1, 1, 0, stream, w.sc, m.target_error, (m.options & kOptErrorAbsolute) ? 1 : 0);
 		const PassLive* lv = &w.sc->live;
 
-		// the graph and its executable are released on every way out of this block
-		struct GraphGuard
-		{
-			cudaGraph_t graph = nullptr;
-			cudaGraphExec_t exec = nullptr;
-			~GraphGuard()
-			{
-				if (exec)
-					cudaGraphExecDestroy(exec);
-				if (graph)
-					cudaGraphDestroy(graph);
-			}
-		} guard;
-		MO_CUDA_CHECK(cudaGraphCreate(&guard.graph, 0));
-		cudaGraph_t graph = guard.graph;
-		cudaGraphConditionalHandle handle;
-		MO_CUDA_CHECK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
-		cudaGraphNodeParams cp = {};
-		cp.type = cudaGraphNodeTypeConditional;
-		cp.conditional.handle = handle;
-		cp.conditional.type = cudaGraphCondTypeWhile;
-		cp.conditional.size = 1;
-		cudaGraphNode_t loop_node;
-		MO_CUDA_CHECK(cudaGraphAddNode(&loop_node, graph, nullptr, nullptr, 0, &cp));
-		cudaGraph_t body = cp.conditional.phGraph_out[0];
+		// grid of the pass kernel
+		unsigned int blocks = std::max(1u, std::min(perform_blocks_, gridFor(std::max(std::max(capn, V), T0), kThreads)));
+		if (tuning_.perform_grid_cap > 0)
+			blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
+		if (size_t(blocks) * kThreads > kListSlack)
+			throw std::runtime_error("kPerform grid exceeds the candidate list slack");
 
 		LaunchProbe& lp = probe();
-		const unsigned long long launches0 = lp.launches;
-		cudaStream_t cs = capture_; // recording only: nothing runs on it
-		MO_CUDA_CHECK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-		lp.capturing = true;
-		try
+		const bool reuse = loop_.exec && loop_.base == arena_.base() && loop_.I == I && loop_.V == V && loop_.ac == ac && loop_.solve == solve &&
+		                   loop_.blocks == blocks;
+		if (!reuse)
 		{
-			const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads), gC = gridFor(capn, kThreads);
-			MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, cs));
-			MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, cs));
-			MO_LAUNCH(kCountKeys, gI, kThreads, 0, cs, nullptr, w.remap, I, w.cnt, lv);
-			scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs);
-			MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, w.fill, w.adj, lv);
-			MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
-			scanExclusive(w.tcnt, w.tcnt, T0, &w.sc->pick_total, w.scratch, cs);
-			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
-			MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, lv);
-			MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
-			MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
-			    w.attr, w.aq, w.ag, ac, lv);
-			radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count);
-			MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr,
-			    w.skind, w.status, lv);
-			PerformArgs pa;
-			pa.count = 0;
-			pa.srec = w.srec;
-			pa.sidx = w.sidx;
-			pa.skind = w.skind;
-			pa.serr = w.serr;
-			pa.status = w.status;
-			pa.vcount = unsigned(V);
-			pa.minT[0] = w.minT;
-			pa.minT[1] = w.minT + (V + 1);
-			pa.minS[0] = w.minS;
-			pa.minS[1] = w.minS + (V + 1);
-			pa.touched = w.touched;
-			pa.moved = w.moved;
-			pa.cr = w.cr;
-			pa.list[0] = w.act0;
-			pa.list[1] = w.act1;
-			pa.adj_off = w.adj_off;
-			pa.adj = w.adj;
-			pa.pos = w.pos;
-			pa.remap = w.remap;
-			pa.wedge = w.wedge;
-			pa.loop = w.loop;
-			pa.loopback = w.loopback;
-			pa.vq = w.vq;
-			pa.aq = w.aq;
-			pa.ag = w.ag;
-			pa.ac = ac;
-			pa.vg = (solve && ac) ? w.vg : nullptr;
-			pa.prev_err_bits = 0;
-			pa.error_limit = error_limit;
-			pa.goal = 0;
-			pa.first_window = 0;
-			pa.round_base = 0;
-			pa.res = nullptr;
-			pa.res_next = nullptr;
-			pa.tris = 0;
-			pa.blk = w.blk;
-			pa.sc = w.sc;
-			pa.live = lv;
-			unsigned int want = gridFor(std::max(std::max(capn, V), T0), kThreads);
-			unsigned int blocks = std::max(1u, std::min(perform_blocks_, want));
-			if (tuning_.perform_grid_cap > 0)
-				blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
-			if (size_t(blocks) * kThreads > kListSlack)
-				throw std::runtime_error("kPerform grid exceeds the candidate list slack");
-			void* params[] = {&pa};
-			lp.launches++;
-			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, cs));
-			MO_LAUNCH(kPassEnd, 1, 1, 0, cs, w.sc, handle, unsigned(T0 + 1));
-		}
-		catch (...)
-		{
+			dropLoopGraph();
+			// the new graph and its executable are released if recording or instantiation fails
+			struct GraphGuard
+			{
+				cudaGraph_t graph = nullptr;
+				cudaGraphExec_t exec = nullptr;
+				~GraphGuard()
+				{
+					if (exec)
+						cudaGraphExecDestroy(exec);
+					if (graph)
+						cudaGraphDestroy(graph);
+				}
+			} guard;
+			MO_CUDA_CHECK(cudaGraphCreate(&guard.graph, 0));
+			cudaGraph_t graph = guard.graph;
+			cudaGraphConditionalHandle handle;
+			MO_CUDA_CHECK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+			cudaGraphNodeParams cp = {};
+			cp.type = cudaGraphNodeTypeConditional;
+			cp.conditional.handle = handle;
+			cp.conditional.type = cudaGraphCondTypeWhile;
+			cp.conditional.size = 1;
+			cudaGraphNode_t loop_node;
+			MO_CUDA_CHECK(cudaGraphAddNode(&loop_node, graph, nullptr, nullptr, 0, &cp));
+			cudaGraph_t body = cp.conditional.phGraph_out[0];
+
+			const unsigned long long launches0 = lp.launches;
+			cudaStream_t cs = capture_; // recording only: nothing runs on it
+			MO_CUDA_CHECK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+			lp.capturing = true;
+			try
+			{
+				const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads), gC = gridFor(capn, kThreads);
+				MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, cs));
+				MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, cs));
+				MO_LAUNCH(kCountKeys, gI, kThreads, 0, cs, nullptr, w.remap, I, w.cnt, lv);
+				scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs);
+				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, w.fill, w.adj, lv);
+				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
+				scanExclusive(w.tcnt, w.tcnt, T0, &w.sc->pick_total, w.scratch, cs);
+				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
+				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, lv);
+				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
+				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+				    w.attr, w.aq, w.ag, ac, lv);
+				radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count);
+				MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr,
+				    w.skind, w.status, lv);
+				PerformArgs pa;
+				pa.count = 0;
+				pa.srec = w.srec;
+				pa.sidx = w.sidx;
+				pa.skind = w.skind;
+				pa.serr = w.serr;
+				pa.status = w.status;
+				pa.vcount = unsigned(V);
+				pa.minT[0] = w.minT;
+				pa.minT[1] = w.minT + (V + 1);
+				pa.minS[0] = w.minS;
+				pa.minS[1] = w.minS + (V + 1);
+				pa.touched = w.touched;
+				pa.moved = w.moved;
+				pa.cr = w.cr;
+				pa.list[0] = w.act0;
+				pa.list[1] = w.act1;
+				pa.adj_off = w.adj_off;
+				pa.adj = w.adj;
+				pa.pos = w.pos;
+				pa.remap = w.remap;
+				pa.wedge = w.wedge;
+				pa.loop = w.loop;
+				pa.loopback = w.loopback;
+				pa.vq = w.vq;
+				pa.aq = w.aq;
+				pa.ag = w.ag;
+				pa.ac = ac;
+				pa.vg = (solve && ac) ? w.vg : nullptr;
+				pa.prev_err_bits = 0;
+				pa.error_limit = 0.f; // the live state's
+				pa.goal = 0;
+				pa.first_window = 0;
+				pa.round_base = 0;
+				pa.res = nullptr;
+				pa.res_next = nullptr;
+				pa.tris = 0;
+				pa.blk = w.blk;
+				pa.sc = w.sc;
+				pa.live = lv;
+				void* params[] = {&pa};
+				lp.launches++;
+				MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, cs));
+				MO_LAUNCH(kPassEnd, 1, 1, 0, cs, w.sc, handle, unsigned(T0 + 1));
+			}
+			catch (...)
+			{
+				lp.capturing = false;
+				cudaGraph_t dead = nullptr;
+				cudaStreamEndCapture(cs, &dead);
+				throw;
+			}
 			lp.capturing = false;
-			cudaGraph_t dead = nullptr;
-			cudaStreamEndCapture(cs, &dead);
-			throw;
+			cudaGraph_t captured = nullptr;
+			MO_CUDA_CHECK(cudaStreamEndCapture(cs, &captured));
+			MO_CUDA_CHECK(cudaGraphInstantiate(&guard.exec, graph, 0));
+			loop_.body_launches = lp.launches - launches0;
+			lp.launches = launches0; // counted below, once per replay
+			loop_.graph = guard.graph;
+			loop_.exec = guard.exec;
+			guard.graph = nullptr;
+			guard.exec = nullptr;
+			loop_.base = arena_.base();
+			loop_.I = I;
+			loop_.V = V;
+			loop_.ac = ac;
+			loop_.solve = solve;
+			loop_.blocks = blocks;
 		}
-		lp.capturing = false;
-		cudaGraph_t captured = nullptr;
-		MO_CUDA_CHECK(cudaStreamEndCapture(cs, &captured));
-		const unsigned long long body_launches = lp.launches - launches0;
-		MO_CUDA_CHECK(cudaGraphInstantiate(&guard.exec, graph, 0));
-		MO_CUDA_CHECK(cudaGraphLaunch(guard.exec, stream));
+		MO_CUDA_CHECK(cudaGraphLaunch(loop_.exec, stream));
 		readScalars();
-		// every replay of the body launched its kernels again
-		if (hs->live.iterations > 1)
-			lp.launches += body_launches * (hs->live.iterations - 1);
+		takeScale();
+		lp.launches += loop_.body_launches * hs->live.iterations;
 		if (hs->grid_error)
 			throw std::runtime_error(hs->grid_error & 4 ? "pass loop did not converge"
 			                                            : (hs->grid_error & 2 ? "collapse decision round made no progress" : "grid barrier wait limit reached"));

@@ -149,6 +149,21 @@ private:
 	unsigned int perform_blocks_ = 1;
 	int sms_ = 1;
 	Tuning tuning_;
+	// The device-resident pass loop's executable graph, kept for the next run of the same shape:
+	// the graph holds workspace pointers (fixed by the arena base and the layout's sizes) and
+	// grid sizes; everything else it reads (targets, counts, the error limit) is on the device.
+	struct LoopGraph
+	{
+		const void* base = nullptr;
+		size_t I = 0, V = 0;
+		int ac = 0;
+		bool solve = false;
+		unsigned int blocks = 0;
+		unsigned long long body_launches = 0; // kernels one replay of the body launches
+		cudaGraph_t graph = nullptr;
+		cudaGraphExec_t exec = nullptr;
+	} loop_;
+	void dropLoopGraph();
 
 public:
 	void setTuning(const Tuning& t)

@@ -87,6 +87,19 @@ def test_heightfield(port, n, opt):
     _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.25), 1e-2, opt)
 
 
+def test_same_shape_sequence(port):
+    """Calls on one mesh shape reuse the recorded pass loop: targets, error limits (including
+    ErrorAbsolute, whose limit depends on the mesh extent) and lock options change per call; a
+    different shape in between records a new loop."""
+    idx, pos = W.heightfield(96, seed=41, amp=0.05)
+    idx2, pos2 = W.heightfield(80, seed=42, amp=0.05)
+    scaled = pos * np.float32(3.0)
+    runs = [(idx, pos, 0.25, 1e-2, 0), (idx, pos, 0.1, 5e-2, 0), (idx, scaled, 0.1, 0.1, mg.SimplifyErrorAbsolute),
+            (idx2, pos2, 0.3, 1e-2, 0), (idx, pos, 0.2, 2e-2, mg.SimplifyLockBorder), (idx, scaled, 0.05, 0.3, mg.SimplifyErrorAbsolute)]
+    for i, p, ratio, error, opt in runs:
+        _compare_with_oracle(port, i, p, W.target_count(len(i), ratio), error, opt)
+
+
 @pytest.mark.parametrize("levels", [3, 5, 7])
 def test_sphere_attributes(port, levels):
     idx, pos, attr, w = W.octa_sphere(levels, seed=levels)
