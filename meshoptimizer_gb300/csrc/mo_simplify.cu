@@ -37,6 +37,8 @@ constexpr int kThreads = 256;
 constexpr int kStopTile = 1024; // sorted candidates per block in the stop-rule scan
 constexpr size_t kPinnedBytes = 16384; // host readback buffer of the scalars block
 constexpr unsigned int kApplyTile = 4096; // sorted positions compacted per block step in the apply phase
+constexpr unsigned int kStageChunk = 2048; // candidates of a block taken through the decision stages at a time
+constexpr unsigned int kStageItems = 4;    // candidates per thread in the first decision stage
 
 // State of the device-resident pass loop: the counts each pass's kernels read instead of
 // launch parameters, so that one recorded pass can be replayed until the loop ends.
@@ -1262,7 +1264,6 @@ struct PerformArgs
 //  * otherwise it waits until it is the earliest undecided candidate on both endpoints (minT)
 //    and no undecided earlier candidate moves a vertex of its one-ring (minS); then the flip
 //    test runs against the one-ring as moved by earlier commits only (moving commit < k).
-// Returns true if k stays undecided.
 
 // the commit of a decided candidate: r0 moves to its target and both endpoints lock
 __device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int k, unsigned int r0, unsigned int r1)
@@ -1288,30 +1289,22 @@ __device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int k, 
 	a.status[k] = kCommit;
 }
 
-__device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
+// The rule runs in three stages per round, each over the candidates the stage before left (so
+// lanes stay busy): the lock flags and endpoint marks (in the rounds loop), then the one-ring's
+// marks (ringWaits), then the flip test and the commit (flipOrCommit).
+
+// no undecided earlier candidate may move a vertex of the one-ring (its sources): true if one does
+__device__ __forceinline__ bool ringWaits(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
 {
-	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
+	const unsigned int r0 = rec.x, b = rec.z, e = rec.w;
 	const unsigned long long tag = roundTag(round);
-	const unsigned long long mine = tag | k;
-	const unsigned long long* minT = a.minT[round & 1];
 	const unsigned long long* minS = a.minS[round & 1];
-	// issued together: lock flags, endpoint marks and the first four half-edges of the one-ring
-	unsigned char t0 = __ldcg(a.touched + r0), t1 = __ldcg(a.touched + r1);
-	unsigned long long m0 = __ldcg(minT + r0), m1 = __ldcg(minT + r1);
-	uint2 ed[4];
+	for (unsigned int j = b; j < e; j += 4)
+	{
+		uint2 ed[4];
 #pragma unroll
-	for (int q = 0; q < 4; ++q)
-		ed[q] = b + q < e ? __ldg(a.adj + b + q) : make_uint2(r0, r0);
-	if (t0 | t1)
-	{
-		a.status[k] = kSkipLocked;
-		return false;
-	}
-	if (m0 != mine || m1 != mine)
-		return true;
-	// no undecided earlier candidate may move a vertex of the one-ring (its sources)
-	for (unsigned int j = b;;)
-	{
+		for (int q = 0; q < 4; ++q)
+			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
 		unsigned long long sx[4], sy[4];
 #pragma unroll
 		for (int q = 0; q < 4; ++q)
@@ -1325,23 +1318,25 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 			wait |= earlierThan(sx[q], tag, k) | earlierThan(sy[q], tag, k);
 		if (wait)
 			return true;
-		j += 4;
-		if (j >= e)
-			break;
-#pragma unroll
-		for (int q = 0; q < 4; ++q)
-			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
 	}
-	#ifndef MO_FLIP_BATCH
+	return false;
+}
+
+#ifndef MO_FLIP_BATCH
 #define MO_FLIP_BATCH 2
 #endif
-	// flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232);
-	// the neighbours' own positions are loaded with their moved records (a moved neighbour's
-	// target position is loaded after)
+
+// flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232), then
+// the commit; the neighbours' own positions are loaded with their moved records (a moved
+// neighbour's target position is loaded after)
+__device__ __forceinline__ void flipOrCommit(const PerformArgs& a, unsigned int k, const uint4& rec)
+{
+	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
 	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
 	constexpr int FB = MO_FLIP_BATCH;
 	for (unsigned int j = b; j < e; j += FB)
 	{
+		uint2 ed[FB];
 		unsigned long long mx[FB], my[FB];
 		float4 px[FB], py[FB];
 #pragma unroll
@@ -1366,12 +1361,11 @@ __device__ __forceinline__ bool decideOne(const PerformArgs& a, unsigned int k, 
 			if (triFlip(pa, pb, v0, v1))
 			{
 				a.status[k] = kSkipFlip;
-				return false;
+				return;
 			}
 		}
 	}
 	commitOne(a, k, r0, r1);
-	return false;
 }
 
 __device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
@@ -1621,6 +1615,7 @@ struct PhaseClock
 __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(PerformArgs a)
 {
 	__shared__ unsigned int s_app[33];
+	__shared__ unsigned int s_stage[2][kStageChunk]; // candidates passed to the next decision stage
 	PhaseClock pc;
 	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
 	if (timer)
@@ -1709,33 +1704,108 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 				sc->act_count[(round + 2) % 3] = 0;
 			if (threadIdx.x == 0)
 				s_app[0] = 0;
-			__syncthreads();
-			for (unsigned int base = 0; base < nb; base += blockDim.x)
-			{
-				unsigned int x = base + threadIdx.x;
-				unsigned int g = first ? base * G + blockIdx.x * blockDim.x + threadIdx.x : x;
-				bool keep = false;
-				unsigned int k = 0;
-				if (first ? g < wlen : x < nb)
-				{
-					k = first ? K0 + g : __ldcg(cur + x);
-					uint4 rec = __ldg(a.srec + k);
-					keep = decideOne(a, k, rec, round);
-					if (keep)
-						markCandidate(a, k, rec, round + 1);
-				}
-				unsigned int m = __ballot_sync(0xffffffffu, keep);
+			// warp-aggregated append of the lanes whose flag is set to dst at the shared counter
+			auto append = [&](bool flag, unsigned int k, unsigned int* counter, unsigned int* dst) {
+				unsigned int m = __ballot_sync(0xffffffffu, flag);
 				if (m)
 				{
 					unsigned int leader = __ffs(m) - 1, o = 0;
 					if (lane == leader)
-						o = atomicAdd(&s_app[0], __popc(m));
+						o = atomicAdd(counter, __popc(m));
 					o = __shfl_sync(0xffffffffu, o, leader);
-					if (keep)
-						next[o + __popc(m & ((1u << lane) - 1u))] = k;
+					if (flag)
+						dst[o + __popc(m & ((1u << lane) - 1u))] = k;
 				}
+			};
+			for (unsigned int c0 = 0; c0 < nb; c0 += kStageChunk)
+			{
+				const unsigned int c1 = min(nb, c0 + kStageChunk);
+				if (threadIdx.x == 0)
+					s_app[1] = 0, s_app[2] = 0;
+				__syncthreads();
+				// stage A: lock flags and endpoint marks; kStageItems candidates per thread, their
+				// loads issued together
+				const unsigned long long tag = roundTag(round);
+				const unsigned long long* minT = a.minT[round & 1];
+				for (unsigned int base = c0; base < c1; base += blockDim.x * kStageItems)
+				{
+					unsigned int kk[kStageItems];
+					bool ok[kStageItems];
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+					{
+						const unsigned int x = base + q * blockDim.x + threadIdx.x;
+						const unsigned int g = (x - threadIdx.x) * G + blockIdx.x * blockDim.x + threadIdx.x;
+						ok[q] = x < c1 && (!first || g < wlen);
+						kk[q] = ok[q] ? (first ? K0 + g : __ldcg(cur + x)) : 0u;
+					}
+					uint2 ends[kStageItems];
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+					{
+						uint4 rec = ok[q] ? __ldg(a.srec + kk[q]) : make_uint4(0, 0, 0, 0);
+						ends[q] = make_uint2(rec.x, rec.y);
+					}
+					unsigned char t[kStageItems];
+					unsigned long long m0[kStageItems], m1[kStageItems];
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+					{
+						t[q] = ok[q] ? (unsigned char)(__ldcg(a.touched + ends[q].x) | __ldcg(a.touched + ends[q].y)) : (unsigned char)0;
+						m0[q] = ok[q] ? __ldcg(minT + ends[q].x) : 0ull;
+						m1[q] = ok[q] ? __ldcg(minT + ends[q].y) : 0ull;
+					}
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+					{
+						const unsigned long long mine = tag | kk[q];
+						const bool locked = ok[q] && t[q];
+						const bool keep = ok[q] && !t[q] && (m0[q] != mine || m1[q] != mine);
+						const bool pass = ok[q] && !t[q] && !keep;
+						if (locked)
+							a.status[kk[q]] = kSkipLocked;
+						if (keep)
+						{
+							unsigned long long key = roundTag(round + 1) | kk[q];
+							atomicMin(&a.minT[(round + 1) & 1][ends[q].x], key);
+							atomicMin(&a.minT[(round + 1) & 1][ends[q].y], key);
+							atomicMin(&a.minS[(round + 1) & 1][ends[q].x], key);
+						}
+						append(keep, kk[q], &s_app[0], next);
+						append(pass, kk[q], &s_app[1], s_stage[0]);
+					}
+				}
+				__syncthreads();
+				// stage B: the one-ring's marks
+				const unsigned int nB = s_app[1];
+				for (unsigned int base = 0; base < nB; base += blockDim.x)
+				{
+					const unsigned int x = base + threadIdx.x;
+					bool keep = false, pass = false;
+					unsigned int k = 0;
+					if (x < nB)
+					{
+						k = s_stage[0][x];
+						uint4 rec = __ldg(a.srec + k);
+						keep = ringWaits(a, k, rec, round);
+						pass = !keep;
+						if (keep)
+							markCandidate(a, k, rec, round + 1);
+					}
+					append(keep, k, &s_app[0], next);
+					append(pass, k, &s_app[2], s_stage[1]);
+				}
+				__syncthreads();
+				// stage C: the flip test and the commit
+				const unsigned int nC = s_app[2];
+				for (unsigned int x = threadIdx.x; x < nC; x += blockDim.x)
+				{
+					const unsigned int k = s_stage[1][x];
+					flipOrCommit(a, k, __ldg(a.srec + k));
+				}
+				__syncthreads();
 			}
-			__syncthreads();
+			__syncthreads(); // the counter's reset is seen when the block had no candidates
 			nb = s_app[0];
 			if (threadIdx.x == 0 && nb)
 				atomicAdd(next_total, nb);
