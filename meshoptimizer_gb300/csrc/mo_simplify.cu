@@ -57,8 +57,21 @@ struct PassLive
 	unsigned int iterations;
 	unsigned int target;      // target_index_count
 	float error_limit;        // squared, in the rescaled space (:2489-2491)
-	double window_factor;
+	double window_factor;     // this pass's first decision window, in units of the triangle goal / 2
+	double window_base;       // its smallest value
 };
+
+// The sorted positions a pass decides before its stop rules cut grow from pass to pass relative to
+// its triangle goal; the next pass's first window is this much larger than the last pass needed,
+// so that it rarely needs a second window (a second window costs a full set of decision rounds).
+constexpr double kWindowMargin = 1.5;
+
+__host__ __device__ inline double nextWindowFactor(double base, unsigned long long goal, unsigned long long evaluated)
+{
+	const double half = double(goal / 2 ? goal / 2 : 1);
+	const double f = kWindowMargin * double(evaluated) / half;
+	return f > base ? f : base;
+}
 
 struct Scalars
 {
@@ -2429,6 +2442,7 @@ __global__ void kPassEnd(Scalars* sc, cudaGraphConditionalHandle handle, unsigne
 				ps.active = (unsigned int)sc->active_sum;
 				ps.windows = sc->windows;
 			}
+			lv.window_factor = nextWindowFactor(lv.window_base, lv.goal, cut < C ? cut + 1 : C);
 			lv.round_base += sc->rounds;
 			lv.passes++;
 			if (sc->done == 0)
@@ -3231,6 +3245,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	else if (m.options & kOptPrune)
 		comp_next = FLT_MAX;
 	int passes = 0;
+	double window_factor = tuning_.window_factor; // the host loop's first-window factor, as kPassEnd adapts it
 	unsigned int round_base = 0; // decision rounds are numbered across the run (mark tags never repeat)
 	MO_CUDA_CHECK(cudaMemsetAsync(w.minT, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
 	MO_CUDA_CHECK(cudaMemsetAsync(w.minS, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
@@ -3249,6 +3264,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		init.tris = unsigned(T0);
 		init.target = unsigned(m.target_index_count);
 		init.window_factor = tuning_.window_factor;
+		init.window_base = tuning_.window_factor;
 		MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->live, &init, sizeof(init), cudaMemcpyHostToDevice, stream));
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->result_error_bits, 0, 4, stream));
 		MO_LAUNCH(kErrorLimit, 1, 1, 0, stream, w.sc, m.target_error, (m.options & kOptErrorAbsolute) ? 1 : 0);
@@ -3474,7 +3490,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.prev_err_bits = result_error_bits;
 			pa.error_limit = error_limit;
 			pa.goal = goal;
-			double wf = tuning_.window_factor * double(goal / 2) + 4096.0;
+			double wf = window_factor * double(goal / 2) + 4096.0;
 			pa.first_window = unsigned(std::min<double>(double(C), wf));
 			pa.round_base = round_base;
 			pa.res = res;
@@ -3521,6 +3537,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			ps.active = unsigned(hs->active_sum);
 			ps.windows = hs->windows;
 		}
+		window_factor = nextWindowFactor(tuning_.window_factor, goal, cut < C ? cut + 1 : C);
 		passes++;
 		result_error_bits = hs->result_error_bits;
 		if (hs->done == 0)
