@@ -68,6 +68,7 @@ enum
 	meshoptgpu_StatusInvalidArgument = 2,
 	meshoptgpu_StatusCudaError = 3,
 	meshoptgpu_StatusOutOfMemory = 4,
+	meshoptgpu_StatusInternal = 5, /* a bound the GPU path keeps was exceeded (a defect: please report) */
 };
 
 /* Status and message of the calling thread's last simplifier call. */
@@ -188,6 +189,25 @@ MESHOPTGPU_API int meshoptgpu_simplifyGroups(unsigned int* destination, const un
     const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride,
     const float* attribute_weights, size_t attribute_count, const unsigned int* position_remap, unsigned char* locks, const unsigned char* vertex_lock,
     const size_t* target_index_counts, float target_error, unsigned int options, size_t* result_index_counts, float* result_errors, void* stream);
+
+/* Re-clusterization of a cluster-LOD level, on device data: meshopt_buildMeshletsFlex
+ * (src/clusterizer.cpp:1035; the clusterize step of demo/clusterlod.h:266-296) for every group,
+ * one warp per group, each group's result equal to a separate call's on its indices.
+ *   indices            group g is indices[group_offsets[g] .. group_offsets[g+1]) (device;
+ *                      group_offsets host, group_count + 1 entries); each count a multiple of 3
+ *   meshlets           {vertex_offset, triangle_offset, vertex_count, triangle_count} rows
+ *                      (meshopt_Meshlet, device); group g's start at row meshlet_offsets[g] (host,
+ *                      group_count + 1) and have room for at least
+ *                      meshopt_buildMeshletsBound(index_count, max_vertices, min_triangles) rows;
+ *                      offsets inside the rows are relative to the group's own arrays
+ *   meshlet_vertices   group g's at group_offsets[g] (device; index_count entries each)
+ *   meshlet_triangles  group g's at group_offsets[g] (device; index_count bytes each)
+ *   meshlet_counts     meshlets per group (host, out)
+ * The other arguments are meshopt_buildMeshletsFlex's. Returns a meshoptgpu_Status* value. */
+MESHOPTGPU_API int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles,
+    const size_t* meshlet_offsets, size_t* meshlet_counts, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
+    const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles, size_t max_triangles,
+    float cone_weight, float split_factor, void* stream);
 
 /* Batch launch shape: threads per CTA (128, 256 or 512; 0 = autotune, the default) and the
  * shared-memory budget per CTA in bytes (0 = default). The autotuner times each thread count

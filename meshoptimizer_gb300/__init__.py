@@ -37,6 +37,7 @@ STATUS_UNSUPPORTED = 1
 STATUS_INVALID_ARGUMENT = 2
 STATUS_CUDA_ERROR = 3
 STATUS_OUT_OF_MEMORY = 4
+STATUS_INTERNAL = 5
 
 # every symbol include/meshopt_gb300.h declares
 EXPORTS = [
@@ -50,7 +51,7 @@ EXPORTS = [
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
     "meshoptgpu_optimizeVertexFetchRemapDevice", "meshoptgpu_optimizeVertexFetchDevice", "meshoptgpu_generatePositionRemapDevice",
-    "meshoptgpu_simplifyGroups", "meshoptgpu_setDropinBatchLimit", "meshoptgpu_setDeviceLoop",
+    "meshoptgpu_simplifyGroups", "meshoptgpu_buildMeshletsFlexGroups", "meshoptgpu_setDropinBatchLimit", "meshoptgpu_setDeviceLoop",
 ]
 
 
@@ -143,6 +144,8 @@ def load():
     lib.meshoptgpu_setDeviceLoop.argtypes = [C.c_int]
     lib.meshoptgpu_simplifyGroups.restype = C.c_int
     lib.meshoptgpu_simplifyGroups.argtypes = [vp, vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, vp, vp, vp, f32, u32, vp, vp, vp]
+    lib.meshoptgpu_buildMeshletsFlexGroups.restype = C.c_int
+    lib.meshoptgpu_buildMeshletsFlexGroups.argtypes = [vp, vp, vp, vp, vp, vp, vp, sz, vp, sz, sz, sz, sz, sz, f32, f32, vp]
     _lib = lib
     return lib
 
@@ -484,6 +487,76 @@ def simplify_groups_device(d_destination, d_indices, group_offsets, d_positions,
     if check and st != STATUS_OK:
         raise SimplifyError(st, last_status()[1])
     return counts[:n], errs[:n]
+
+
+def meshlets_bound(index_count, max_vertices, max_triangles):
+    """meshopt_buildMeshletsBound (src/clusterizer.cpp:1017-1033)."""
+    by_vertices = (index_count + max_vertices - 2 - 1) // (max_vertices - 2)
+    by_triangles = (index_count // 3 + max_triangles - 1) // max_triangles
+    return max(by_vertices, by_triangles)
+
+
+def meshlet_rows(group_offsets, max_vertices, min_triangles):
+    """Row offsets (group_count + 1) with each group's meshopt_buildMeshletsBound rows."""
+    off = np.asarray(group_offsets, dtype=np.int64)
+    rows = [meshlets_bound(int(off[g + 1] - off[g]), max_vertices, min_triangles) for g in range(len(off) - 1)]
+    return np.concatenate([[0], np.cumsum(rows, dtype=np.int64)]).astype(np.uint64)
+
+
+def build_meshlets_flex_groups_device(d_meshlets, d_meshlet_vertices, d_meshlet_triangles, meshlet_offsets, d_indices, group_offsets, d_positions,
+                                      vertex_count, positions_stride, max_vertices, min_triangles, max_triangles, cone_weight=0.0,
+                                      split_factor=2.0, stream=0, check=True):
+    """meshoptgpu_buildMeshletsFlexGroups: meshopt_buildMeshletsFlex for every group of a level on device
+    data, one warp per group. meshlet_offsets / group_offsets: host ints (group_count + 1).
+    Returns the meshlet count per group (uint64 array)."""
+    off = np.ascontiguousarray(group_offsets, dtype=np.uint64)
+    mo = np.ascontiguousarray(meshlet_offsets, dtype=np.uint64)
+    n = len(off) - 1
+    counts = np.zeros(max(n, 1), np.uint64)
+    st = load().meshoptgpu_buildMeshletsFlexGroups(d_meshlets, d_meshlet_vertices, d_meshlet_triangles, mo.ctypes.data, counts.ctypes.data, d_indices,
+                                                   off.ctypes.data, n, d_positions, vertex_count, positions_stride, max_vertices, min_triangles,
+                                                   max_triangles, C.c_float(cone_weight), C.c_float(split_factor), C.c_void_p(stream or None))
+    if check and st != STATUS_OK:
+        raise SimplifyError(st, last_status()[1])
+    return counts[:n]
+
+
+def build_meshlets_flex_groups(groups, positions, max_vertices, min_triangles, max_triangles, cone_weight=0.0, split_factor=2.0):
+    """Host convenience over build_meshlets_flex_groups_device (torch for device memory): groups is
+    a list of index arrays into `positions`. Returns, per group, (meshlets [n, 4] uint32,
+    meshlet_vertices uint32, meshlet_triangles uint8) trimmed as meshopt_buildMeshletsFlex leaves them."""
+    import torch
+
+    idx = [np.ascontiguousarray(g, dtype=np.uint32).reshape(-1) for g in groups]
+    off = np.concatenate([[0], np.cumsum([len(g) for g in idx], dtype=np.int64)]).astype(np.uint64)
+    rows = meshlet_rows(off, max_vertices, min_triangles)
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    flat = np.concatenate(idx) if idx else np.zeros(0, np.uint32)
+    total = max(int(off[-1]), 1)
+    d_idx = torch.from_numpy(flat.view(np.int32).copy() if len(flat) else np.zeros(1, np.int32)).cuda()
+    d_pos = torch.from_numpy(pos.reshape(len(pos), -1)).cuda()
+    d_m = torch.zeros(max(int(rows[-1]), 1) * 4, dtype=torch.int32, device="cuda")
+    d_v = torch.zeros(total, dtype=torch.int32, device="cuda")
+    d_t = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    counts = build_meshlets_flex_groups_device(d_m.data_ptr(), d_v.data_ptr(), d_t.data_ptr(), rows, d_idx.data_ptr(), off, d_pos.data_ptr(),
+                                               len(pos), pos.reshape(len(pos), -1).shape[1] * 4, max_vertices, min_triangles, max_triangles,
+                                               cone_weight, split_factor)
+    torch.cuda.synchronize()
+    m = d_m.cpu().numpy().view(np.uint32).reshape(-1, 4)
+    v = d_v.cpu().numpy().view(np.uint32)
+    t = d_t.cpu().numpy()
+    out = []
+    for g in range(len(idx)):
+        n = int(counts[g])
+        mg = m[int(rows[g]): int(rows[g]) + n].copy()
+        if n:
+            last = mg[-1]
+            vv = v[int(off[g]): int(off[g]) + int(last[0] + last[2])].copy()
+            tt = t[int(off[g]): int(off[g]) + int(last[1] + last[3] * 3)].copy()
+        else:
+            vv, tt = np.zeros(0, np.uint32), np.zeros(0, np.uint8)
+        out.append((mg, vv, tt))
+    return out
 
 
 def set_batch_config(threads=0, smem_bytes=0):

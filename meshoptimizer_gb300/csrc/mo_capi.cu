@@ -12,6 +12,7 @@
 #include "mo_batch.cuh"
 #include "mo_vfetch.cuh"
 #include "mo_groups.cuh"
+#include "mo_meshlets.cuh"
 
 #include <chrono>
 #include <condition_variable>
@@ -92,7 +93,7 @@ struct ThreadState
 	PhaseTimes times;
 	bool timing = false;
 	// batched path
-	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch, group_scratch, update_io;
+	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch, group_scratch, update_io, meshlet_scratch;
 	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
 	unsigned int batch_smem = 0;    // 0: default budget
@@ -1117,6 +1118,120 @@ int meshoptgpu_simplifyGroups(unsigned int* destination, const unsigned int* ind
 			return meshoptgpu_StatusInvalidArgument;
 		}
 		return finishBatch(res, result_index_counts, result_errors);
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
+int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles,
+    const size_t* meshlet_offsets, size_t* meshlet_counts, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
+    const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles, size_t max_triangles,
+    float cone_weight, float split_factor, void* stream)
+{
+	// the reference's argument checks (src/clusterizer.cpp:1039-1049), as errors
+	std::string bad;
+	if (group_count && (!group_offsets || !meshlet_offsets || !meshlet_counts))
+		bad = "group_offsets, meshlet_offsets and meshlet_counts are required";
+	else if (vertex_positions_stride < 12 || vertex_positions_stride > 256 || vertex_positions_stride % 4)
+		bad = "vertex_positions_stride must be 12..256 and a multiple of 4";
+	else if (max_vertices < 3 || max_vertices > 256)
+		bad = "max_vertices must be 3..256";
+	else if (min_triangles < 1 || min_triangles > max_triangles || max_triangles > 512)
+		bad = "need 1 <= min_triangles <= max_triangles <= 512";
+	else if (!(cone_weight >= 0.f && cone_weight <= 1.f))
+		bad = "cone_weight must be in [0, 1]";
+	else if (!(split_factor >= 0.f))
+		bad = "split_factor must be >= 0";
+	else if (vertex_count >= (size_t(1) << 32))
+		bad = "vertex_count must be below 2^32";
+	for (size_t g = 0; bad.empty() && g < group_count; ++g)
+	{
+		const size_t n = group_offsets[g + 1] - group_offsets[g];
+		if (group_offsets[g + 1] < group_offsets[g] || n % 3)
+			bad = "group " + std::to_string(g) + ": index counts must be multiples of 3 and offsets must not decrease";
+		else if (meshlet_offsets[g + 1] < meshlet_offsets[g] || meshlet_offsets[g + 1] - meshlet_offsets[g] < meshletBound(n, max_vertices, min_triangles))
+			bad = "group " + std::to_string(g) + ": fewer meshlet rows than meshopt_buildMeshletsBound(index_count, max_vertices, min_triangles)";
+		else if (n >= (size_t(1) << 31))
+			bad = "group " + std::to_string(g) + ": index count must be below 2^31";
+	}
+	if (!bad.empty())
+	{
+		setStatus(meshoptgpu_StatusInvalidArgument, bad);
+		return meshoptgpu_StatusInvalidArgument;
+	}
+	if (!group_count)
+	{
+		setStatus(meshoptgpu_StatusOk, "");
+		return meshoptgpu_StatusOk;
+	}
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		// per group: index offsets, meshlet rows, scratch offsets (64-bit, device); counts and the error word
+		const size_t G = group_count;
+		std::vector<unsigned long long> host((G + 1) * 3, 0);
+		unsigned long long scratch = 0;
+		for (size_t g = 0; g <= G; ++g)
+		{
+			host[g] = group_offsets[g];
+			host[(G + 1) + g] = meshlet_offsets[g];
+			host[2 * (G + 1) + g] = scratch;
+			if (g < G)
+				scratch += meshletScratchBytes(group_offsets[g + 1] - group_offsets[g]);
+		}
+		const size_t meta = ((host.size() * 8 + 255) / 256) * 256, words = ((G + 1) * 4 + 255) / 256 * 256;
+		char* base = static_cast<char*>(s.meshlet_scratch.ensure(meta + words + scratch + 256));
+		unsigned long long* d_meta = reinterpret_cast<unsigned long long*>(base);
+		unsigned int* d_counts = reinterpret_cast<unsigned int*>(base + meta);
+		unsigned int* d_err = d_counts + G;
+		char* d_scratch = base + meta + words;
+		void* h = s.batch_host.ensure(host.size() * 8 + (G + 1) * 4);
+		memcpy(h, host.data(), host.size() * 8);
+		MO_CUDA_CHECK(cudaMemcpyAsync(d_meta, h, host.size() * 8, cudaMemcpyHostToDevice, st));
+		MO_CUDA_CHECK(cudaMemsetAsync(d_err, 0, 4, st));
+		MeshletBatch b;
+		b.indices = indices;
+		b.offsets = d_meta;
+		b.groups = unsigned(G);
+		b.positions = vertex_positions;
+		b.stride_f = unsigned(vertex_positions_stride / 4);
+		b.vertex_count = unsigned(vertex_count);
+		b.max_vertices = unsigned(max_vertices);
+		b.min_triangles = unsigned(min_triangles);
+		b.max_triangles = unsigned(max_triangles);
+		b.cone_weight = cone_weight;
+		b.split_factor = split_factor;
+		b.meshlets = meshlets;
+		b.meshlet_base = d_meta + (G + 1);
+		b.mverts = meshlet_vertices;
+		b.mtris = meshlet_triangles;
+		b.counts = d_counts;
+		b.scratch = d_scratch;
+		b.scratch_off = d_meta + 2 * (G + 1);
+		b.error = d_err;
+		buildMeshletsBatch(b, st);
+		unsigned int* hc = reinterpret_cast<unsigned int*>(static_cast<char*>(h) + host.size() * 8);
+		MO_CUDA_CHECK(cudaMemcpyAsync(hc, d_counts, (G + 1) * 4, cudaMemcpyDeviceToHost, st));
+		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		if (hc[G] & 1u)
+		{
+			setStatus(meshoptgpu_StatusInvalidArgument, "an index is out of range of vertex_count");
+			return meshoptgpu_StatusInvalidArgument;
+		}
+		if (hc[G])
+		{
+			setStatus(meshoptgpu_StatusInternal, "meshlet construction exceeded a bound it keeps (tree depth or output size)");
+			return meshoptgpu_StatusInternal;
+		}
+		for (size_t g = 0; g < G; ++g)
+			meshlet_counts[g] = hc[g];
+		setStatus(meshoptgpu_StatusOk, "");
+		return meshoptgpu_StatusOk;
 	}
 	catch (const std::exception& e)
 	{

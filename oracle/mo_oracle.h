@@ -120,6 +120,14 @@ size_t mo_optimizeVertexFetchRemap(unsigned int* destination, const unsigned int
 size_t mo_optimizeVertexFetch(void* destination, unsigned int* indices, size_t index_count, const void* vertices, size_t vertex_count, size_t vertex_size);
 void mo_generatePositionRemap(unsigned int* destination, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride);
 
+/* Re-clusterization after a cluster-LOD level's simplify (mo_meshlet.c): same signatures as
+ * meshoptimizer.h's meshopt_buildMeshletsBound and meshopt_buildMeshletsFlex; `meshlets` holds
+ * {vertex_offset, triangle_offset, vertex_count, triangle_count} per meshlet. */
+size_t mo_buildMeshletsBound(size_t index_count, size_t max_vertices, size_t max_triangles);
+size_t mo_buildMeshletsFlex(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles, const unsigned int* indices,
+    size_t index_count, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles,
+    size_t max_triangles, float cone_weight, float split_factor);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,3 +66,18 @@ def update_cases():
         d["kind"] = str(d["kind"])
         out.append(d)
     return out
+
+
+def meshlet_cases():
+    """meshopt_buildMeshletsFlex golden cases: each with its mesh's indices and positions."""
+    z = np.load(os.path.join(GOLDEN, "meshlet_cases.npz"))
+    out = []
+    for i in range(int(z["count"])):
+        prefix = f"{i}_"
+        d = {k[len(prefix):]: z[k] for k in z.files if k.startswith(prefix)}
+        d["name"] = str(d["name"])
+        j = int(d["mesh"])
+        d["indices"] = z[f"mesh{j}_indices"]
+        d["positions"] = z[f"mesh{j}_positions"]
+        out.append(d)
+    return out

@@ -20,6 +20,9 @@ It writes two files next to this script:
 * ``update_cases.npz`` -- meshopt_simplifyWithUpdate: the reference's simplifyUpdate tests
   (asserted here) and seeded meshes, with the indices, positions and attributes the reference
   leaves.
+* ``meshlet_cases.npz`` -- meshopt_buildMeshletsFlex, the re-clusterization step of a
+  cluster-LOD level: seeded meshes (each stored once) and the reference's meshlets for six
+  parameter sets each, through the reference's own clusterizer.cpp in oracle/_ref/libclod_ref.so.
 * ``compaction_cases.npz`` -- seeded inputs of the compaction step after the simplifier
   (meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch,
   meshopt_generatePositionRemap) with the reference library's outputs.
@@ -394,6 +397,49 @@ def update_cases():
     return cases
 
 
+def meshlet_cases():
+    """meshopt_buildMeshletsFlex (src/clusterizer.cpp:1035), the reference's own build: dense and
+    sparse (index subsets of a larger buffer) meshes, degenerate and zero-area triangles, a NaN
+    position, and parameters from clusterlod's defaults to the extremes the asserts allow."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import meshlets as ML
+
+    rng = np.random.default_rng(77)
+    meshes = []
+    idx, pos = W.heightfield(24, seed=3)
+    meshes.append(("hf24", idx, pos))
+    idx, pos, _, _ = W.octa_sphere(4, seed=4)
+    meshes.append(("sphere4", idx, pos))
+    idx, pos, _, _ = W.octa_sphere(5, seed=2)
+    tri = idx.reshape(-1, 3)
+    for g in range(3):
+        s0 = int(rng.integers(0, len(tri) - 1100))
+        meshes.append((f"sphere5_subset{g}", tri[s0:s0 + int(rng.integers(200, 1000))].reshape(-1).copy(), pos))
+    idx, pos = W.heightfield(12, seed=5)
+    t = idx.reshape(-1, 3).copy()
+    t[::7, 1] = t[::7, 0]  # degenerate triangles (a repeated vertex)
+    meshes.append(("hf12_degenerate", t.reshape(-1), pos))
+    idx, pos = W.heightfield(10, seed=6, amp=0.0)
+    flat = pos.copy()
+    flat[:, 1] = 0.0  # every triangle has zero area
+    meshes.append(("hf10_zero_area", idx, flat))
+    idx, pos = W.heightfield(10, seed=7)
+    nanpos = pos.copy()
+    nanpos[5, 0] = np.nan
+    meshes.append(("hf10_nan", idx, nanpos))
+    meshes.append(("one_triangle", np.array([0, 1, 2], np.uint32), np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)))
+    params = [(128, 42, 128, 0.0, 2.0), (64, 21, 64, 0.0, 2.0), (64, 16, 124, 0.25, 0.0), (255, 85, 256, 1.0, 1.5), (3, 1, 1, 0.0, 2.0),
+              (256, 512, 512, 0.5, 4.0)]
+    cases = []
+    for j, (name, idx, pos) in enumerate(meshes):
+        for mv, mint, maxt, cw, sf in params:
+            m, v, tr = ML.build_meshlets_flex(idx, pos, mv, mint, maxt, cw, sf, kind="reference")
+            cases.append(dict(name=f"{name}_{mv}_{mint}_{maxt}_{cw}_{sf}", mesh=np.array(j), max_vertices=np.array(mv), min_triangles=np.array(mint),
+                              max_triangles=np.array(maxt), cone_weight=np.array(cw, np.float32), split_factor=np.array(sf, np.float32), meshlets=m,
+                              meshlet_vertices=v, meshlet_triangles=tr))
+    return [(np.asarray(idx, np.uint32), np.asarray(pos, np.float32)) for _, idx, pos in meshes], cases
+
+
 def main():
     ka = known_answer_cases()
     js = []
@@ -448,6 +494,18 @@ def main():
     blob["count"] = np.array(len(uc))
     np.savez_compressed(os.path.join(HERE, "update_cases.npz"), **blob)
     print(f"update cases: {len(uc)}")
+
+    mm, mc = meshlet_cases()
+    blob = {}
+    for j, (idx, pos) in enumerate(mm):
+        blob[f"mesh{j}_indices"] = idx
+        blob[f"mesh{j}_positions"] = pos
+    for i, c in enumerate(mc):
+        for k, v in c.items():
+            blob[f"{i}_{k}"] = np.asarray(v)
+    blob["count"] = np.array(len(mc))
+    np.savez_compressed(os.path.join(HERE, "meshlet_cases.npz"), **blob)
+    print(f"meshlet cases: {len(mc)}")
 
 
 if __name__ == "__main__":

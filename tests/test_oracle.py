@@ -127,3 +127,26 @@ def test_update_port_matches_golden(port):
             if "out_attributes" in c:
                 assert np.array_equal(a2.view(np.uint32), c["out_attributes"].view(np.uint32)), c["name"]
         assert np.float32(err) == c["out_error"], c["name"]
+
+
+def test_meshlet_port_matches_golden(port):
+    """mo_buildMeshletsFlex (oracle/mo_meshlet.c) against the reference's meshopt_buildMeshletsFlex
+    outputs: the meshlets, their vertices and their triangles, byte for byte."""
+    import meshlets as ML
+
+    cases = fixtures.meshlet_cases()
+    assert len(cases) >= 50
+    for c in cases:
+        m, v, t = ML.build_meshlets_flex(c["indices"], c["positions"], int(c["max_vertices"]), int(c["min_triangles"]), int(c["max_triangles"]),
+                                         float(c["cone_weight"]), float(c["split_factor"]), kind="port")
+        assert np.array_equal(m, c["meshlets"]), c["name"]
+        assert np.array_equal(v, c["meshlet_vertices"]), c["name"]
+        assert np.array_equal(t, c["meshlet_triangles"]), c["name"]
+
+
+def test_meshlet_port_bound():
+    import meshlets as ML
+
+    # meshopt_buildMeshletsBound: the larger of the vertex-limited and triangle-limited counts
+    assert ML.bound(3 * 1000, 64, 124, kind="port") == max((3000 + 61) // 62, (1000 + 123) // 124)
+    assert ML.bound(0, 64, 124, kind="port") == 0
