@@ -272,11 +272,46 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
         if i >= args.warmup:
             tt += time.perf_counter() - t0
 
-    cpu, exact = None, None
+    # ---- re-clusterization of the simplified groups (clusterlod's clusterize with its default
+    # configuration for 128-triangle clusters: meshopt_buildMeshletsFlex, 128 vertices, 42..128
+    # triangles, cone weight 0, split factor 2), the level's second step
+    cl_params = (128, 42, 128, 0.0, 2.0)
+    sgroups = [out[int(off[g]):int(off[g]) + int(counts[g])].copy() for g in range(len(groups))]
+    sidx = np.concatenate(sgroups).astype(np.uint32)
+    soff = np.zeros(len(groups) + 1, np.uint64)
+    soff[1:] = np.cumsum([len(sg) for sg in sgroups])
+    rows = mg.meshlet_rows(soff, cl_params[0], cl_params[1])
+    dsi = torch.from_numpy(sidx.view(np.int32)).to(dev)
+    dm = torch.empty(max(int(rows[-1]), 1) * 4, dtype=torch.int32, device=dev)
+    dmv = torch.empty(max(len(sidx), 1), dtype=torch.int32, device=dev)
+    dmt = torch.empty(max(len(sidx), 1), dtype=torch.uint8, device=dev)
+
+    def clusterize():
+        return mg.build_meshlets_flex_groups_device(dm.data_ptr(), dmv.data_ptr(), dmt.data_ptr(), rows, dsi.data_ptr(), soff, dp.data_ptr(),
+                                                    len(pos), 12, *cl_params, stream=stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 1)):
+        clusterize()
+    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.zero_()
+        cev[i][0].record(stream)
+        mcounts = clusterize()
+        cev[i][1].record(stream)
+    torch.cuda.synchronize()
+    cl_ms = sum(a.elapsed_time(b) for a, b in cev) / args.steps
+    stris = len(sidx) // 3
+    gm = dm.cpu().numpy().view(np.uint32).reshape(-1, 4)
+    gv = dmv.cpu().numpy().view(np.uint32)
+    gt = dmt.cpu().numpy()
+
+    cpu, exact, cl_cpu, cl_exact = None, None, None, None
     if not args.no_cpu_baseline:
         import concurrent.futures as cf
 
         import clod
+        import meshlets as ML
         import oracle
 
         if not oracle.available("port"):
@@ -299,6 +334,23 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
                 exact = exact and int(counts[g]) == len(o) and np.array_equal(out[int(off[g]):int(off[g]) + len(o)], o) and float(errs[g]) == e
         cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
                "sample": f"the whole level once: lockBoundary restatement, then all {len(groups)} groups split statically over {threads} threads"}
+
+        def cl_work(gs):
+            return [ML.build_meshlets_flex(sgroups[g], pos, *cl_params, kind="port") for g in gs]
+
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            cl_parts = list(ex.map(cl_work, chunks))
+        cdt = time.perf_counter() - t0
+        cl_exact = True
+        for ch, part in zip(chunks, cl_parts):
+            for g, (m, v, t) in zip(ch, part):
+                n = int(mcounts[g])
+                ok = n == len(m) and np.array_equal(gm[int(rows[g]):int(rows[g]) + n], m)
+                ok = ok and np.array_equal(gv[int(soff[g]):int(soff[g]) + len(v)], v) and np.array_equal(gt[int(soff[g]):int(soff[g]) + len(t)], t)
+                cl_exact = cl_exact and ok
+        cl_cpu = {"value": round(stris / cdt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
+                  "sample": f"all {len(groups)} simplified groups once, split statically over {threads} threads"}
     h2d = idx.nbytes + pos.nbytes + attr.nbytes
     return {
         "metric": "input Mtris/s simplified (bit-exact)", "value": round(tris * args.steps / (total_ms / 1e3) / 1e6, 4), "unit": "Mtris/s",
@@ -310,6 +362,13 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
         "e2e": {"value": round(tris * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(idx.nbytes), "ms_per_step": round(1e3 * tt / args.steps, 3)},
         "cpu_baseline": cpu, "bit_exact_vs_oracle": exact, "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "clusterize": {"metric": "simplified Mtris/s clusterized (bit-exact)", "value": round(stris / (cl_ms / 1e3) / 1e6, 4), "unit": "Mtris/s",
+                       "ms_per_step": round(cl_ms, 3), "meshlets": int(mcounts.sum()),
+                       "config": {"function": "meshopt_buildMeshletsFlex per group (meshoptgpu_buildMeshletsFlexGroups)", "input_tris": stris,
+                                  "max_vertices": cl_params[0], "min_triangles": cl_params[1], "max_triangles": cl_params[2],
+                                  "cone_weight": cl_params[3], "split_factor": cl_params[4], "one_warp_per_group": True},
+                       "cpu_baseline": cl_cpu, "bit_exact_vs_oracle": cl_exact},
+        "level_ms": round(total_ms / args.steps + cl_ms, 3),
     }
 
 

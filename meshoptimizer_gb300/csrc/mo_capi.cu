@@ -393,6 +393,7 @@ size_t updateHost(unsigned int* indices, size_t index_count, float* vertex_posit
 // ---------------------------------------------------------------- batched path
 
 const size_t kBatchSmemDefault = 104 * 1024;    // shared-memory budget per CTA (two CTAs per SM)
+const unsigned int kMeshletPoolDefault = 0;      // re-clusterization: all per-group arrays in global scratch
 const size_t kBatchSlabTotal = size_t(16) << 30; // global slabs for meshes beyond the budget
 
 struct BatchTuner
@@ -1126,6 +1127,18 @@ int meshoptgpu_simplifyGroups(unsigned int* destination, const unsigned int* ind
 	}
 }
 
+// shared memory per warp of the re-clusterization kernel (MESHOPTGPU_MESHLET_POOL bytes, at
+// most 48 KiB; default below)
+static unsigned int meshletPoolBytes()
+{
+	static const unsigned int bytes = [] {
+		const char* v = getenv("MESHOPTGPU_MESHLET_POOL");
+		long n = v ? atol(v) : long(kMeshletPoolDefault);
+		return unsigned(std::min(std::max(n, 0L), 48L * 1024) & ~15L);
+	}();
+	return bytes;
+}
+
 int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles,
     const size_t* meshlet_offsets, size_t* meshlet_counts, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
     const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles, size_t max_triangles,
@@ -1214,6 +1227,7 @@ int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* mes
 		b.scratch = d_scratch;
 		b.scratch_off = d_meta + 2 * (G + 1);
 		b.error = d_err;
+		b.pool_bytes = meshletPoolBytes();
 		buildMeshletsBatch(b, st);
 		unsigned int* hc = reinterpret_cast<unsigned int*>(static_cast<char*>(h) + host.size() * 8);
 		MO_CUDA_CHECK(cudaMemcpyAsync(hc, d_counts, (G + 1) * 4, cudaMemcpyDeviceToHost, st));

@@ -25,6 +25,7 @@
 #include "mo_probe.cuh"
 
 #include <float.h>
+#include <type_traits>
 
 namespace mogpu
 {
@@ -36,7 +37,7 @@ constexpr unsigned int kMaxSeeds = 256; // kMeshletMaxSeeds, :27
 constexpr unsigned int kAddSeeds = 4;   // kMeshletAddSeeds, :28
 constexpr int kMaxDepth = 50;           // kMeshletMaxTreeDepth, :31
 constexpr unsigned int kLeafSize = 8;   // :1090
-constexpr int kWarpsPerBlock = 4;
+constexpr int kMaxWarpsPerBlock = 4;
 
 struct Cone
 {
@@ -366,10 +367,10 @@ __device__ void kdNearest(const Scratch& s, const float* pos, unsigned int* resu
 	}
 }
 
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) kMeshletsFlex(MeshletBatch b)
+__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) kMeshletsFlex(MeshletBatch b)
 {
 	const unsigned int lane = threadIdx.x & 31;
-	const unsigned int g = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+	const unsigned int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
 	if (g >= b.groups)
 		return;
 	const unsigned long long i0 = b.offsets[g], i1 = b.offsets[g + 1];
@@ -432,6 +433,29 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) kMeshletsFlex(MeshletBatc
 			s.gid[id] = v < b.vertex_count ? v : 0u;
 		}
 		U += __popc(m);
+	}
+	// the arrays the greedy loop reads at every step move to this warp's shared memory, in the
+	// order of their use per step, while they fit (U is known now)
+	{
+		extern __shared__ __align__(16) char pool[];
+		char* base = pool + (threadIdx.x >> 5) * b.pool_bytes;
+		size_t used_bytes = 0;
+		auto promote = [&](auto*& ptr, size_t bytes) {
+			bytes = (bytes + 15) & ~size_t(15);
+			if (used_bytes + bytes <= b.pool_bytes)
+			{
+				ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(base + used_bytes);
+				used_bytes += bytes;
+			}
+		};
+		promote(s.cnt, size_t(U) * 4);
+		promote(s.off, size_t(U) * 4);
+		promote(s.used, size_t(U) * 2);
+		promote(s.lidx, size_t(I) * 4);
+		promote(s.adj, size_t(I) * 4);
+		promote(s.mvl, size_t(I) * 4);
+		promote(s.emitted, F);
+		promote(s.cones, size_t(F) * sizeof(Cone));
 	}
 	__syncwarp();
 	for (unsigned int p = lane; p < I; p += 32)
@@ -806,8 +830,10 @@ void buildMeshletsBatch(const MeshletBatch& b, cudaStream_t stream)
 {
 	if (!b.groups)
 		return;
-	const unsigned int blocks = (b.groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
-	MO_LAUNCH(kMeshletsFlex, blocks, kWarpsPerBlock * 32, 0, stream, b);
+	// with a shared pool, one warp per block (the pool sets how many fit on an SM); without, four
+	const unsigned int warps = b.pool_bytes ? 1 : kMaxWarpsPerBlock;
+	const unsigned int blocks = (b.groups + warps - 1) / warps;
+	MO_LAUNCH(kMeshletsFlex, blocks, warps * 32, warps * b.pool_bytes, stream, b);
 	MO_CUDA_CHECK(cudaGetLastError());
 }
 

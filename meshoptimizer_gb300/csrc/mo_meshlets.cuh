@@ -31,6 +31,9 @@ struct MeshletBatch
 	char* scratch;        // group g's at scratch_off[g] (meshletScratchBytes of its index count)
 	const unsigned long long* scratch_off;
 	unsigned int* error; // nonzero: an index out of range, or a bound the algorithm keeps was exceeded
+	// shared memory per warp (at most 48 KiB) for the arrays the greedy loop reads at every step,
+	// placed while they fit; 0: all in global scratch
+	unsigned int pool_bytes;
 };
 
 // meshopt_buildMeshletsBound (src/clusterizer.cpp:1017-1033)
