@@ -274,7 +274,8 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
 
     # ---- re-clusterization of the simplified groups (clusterlod's clusterize with its default
     # configuration for 128-triangle clusters: meshopt_buildMeshletsFlex, 128 vertices, 42..128
-    # triangles, cone weight 0, split factor 2), the level's second step
+    # triangles, cone weight 0, split factor 2, then meshopt_optimizeMeshletLevel(1) on every
+    # meshlet), the level's second step
     cl_params = (128, 42, 128, 0.0, 2.0)
     sgroups = [out[int(off[g]):int(off[g]) + int(counts[g])].copy() for g in range(len(groups))]
     sidx = np.concatenate(sgroups).astype(np.uint32)
@@ -288,7 +289,7 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
 
     def clusterize():
         return mg.build_meshlets_flex_groups_device(dm.data_ptr(), dmv.data_ptr(), dmt.data_ptr(), rows, dsi.data_ptr(), soff, dp.data_ptr(),
-                                                    len(pos), 12, *cl_params, stream=stream.cuda_stream)
+                                                    len(pos), 12, *cl_params, optimize_level=1, stream=stream.cuda_stream)
 
     for _ in range(max(args.warmup, 1)):
         clusterize()
@@ -336,7 +337,12 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
                "sample": f"the whole level once: lockBoundary restatement, then all {len(groups)} groups split statically over {threads} threads"}
 
         def cl_work(gs):
-            return [ML.build_meshlets_flex(sgroups[g], pos, *cl_params, kind="port") for g in gs]
+            res = []
+            for g in gs:
+                m, v, t = ML.build_meshlets_flex(sgroups[g], pos, *cl_params, kind="port")
+                v, t = ML.optimize_meshlets(m, v, t, 1, kind="port")
+                res.append((m, v, t))
+            return res
 
         t0 = time.perf_counter()
         with cf.ThreadPoolExecutor(threads) as ex:
@@ -364,7 +370,7 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
         "cpu_baseline": cpu, "bit_exact_vs_oracle": exact, "clocks": clocks.summary(), "gpu_launches": int(launches),
         "clusterize": {"metric": "simplified Mtris/s clusterized (bit-exact)", "value": round(stris / (cl_ms / 1e3) / 1e6, 4), "unit": "Mtris/s",
                        "ms_per_step": round(cl_ms, 3), "meshlets": int(mcounts.sum()),
-                       "config": {"function": "meshopt_buildMeshletsFlex per group (meshoptgpu_buildMeshletsFlexGroups)", "input_tris": stris,
+                       "config": {"function": "meshopt_buildMeshletsFlex per group, then meshopt_optimizeMeshletLevel(1) per meshlet (meshoptgpu_buildMeshletsFlexGroups)", "input_tris": stris,
                                   "max_vertices": cl_params[0], "min_triangles": cl_params[1], "max_triangles": cl_params[2],
                                   "cone_weight": cl_params[3], "split_factor": cl_params[4], "one_warp_per_group": True},
                        "cpu_baseline": cl_cpu, "bit_exact_vs_oracle": cl_exact},

@@ -203,11 +203,13 @@ MESHOPTGPU_API int meshoptgpu_simplifyGroups(unsigned int* destination, const un
  *   meshlet_vertices   group g's at group_offsets[g] (device; index_count entries each)
  *   meshlet_triangles  group g's at group_offsets[g] (device; index_count bytes each)
  *   meshlet_counts     meshlets per group (host, out)
+ *   optimize_level     0..9: meshopt_optimizeMeshletLevel (src/meshletutils.cpp:366) on every meshlet
+ *                      afterwards, as clusterize does with its optimize_clusters_level; -1: none
  * The other arguments are meshopt_buildMeshletsFlex's. Returns a meshoptgpu_Status* value. */
 MESHOPTGPU_API int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles,
     const size_t* meshlet_offsets, size_t* meshlet_counts, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
     const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles, size_t max_triangles,
-    float cone_weight, float split_factor, void* stream);
+    float cone_weight, float split_factor, int optimize_level, void* stream);
 
 /* Batch launch shape: threads per CTA (128, 256 or 512; 0 = autotune, the default) and the
  * shared-memory budget per CTA in bytes (0 = default). The autotuner times each thread count

@@ -145,7 +145,7 @@ def load():
     lib.meshoptgpu_simplifyGroups.restype = C.c_int
     lib.meshoptgpu_simplifyGroups.argtypes = [vp, vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, vp, vp, vp, f32, u32, vp, vp, vp]
     lib.meshoptgpu_buildMeshletsFlexGroups.restype = C.c_int
-    lib.meshoptgpu_buildMeshletsFlexGroups.argtypes = [vp, vp, vp, vp, vp, vp, vp, sz, vp, sz, sz, sz, sz, sz, f32, f32, vp]
+    lib.meshoptgpu_buildMeshletsFlexGroups.argtypes = [vp, vp, vp, vp, vp, vp, vp, sz, vp, sz, sz, sz, sz, sz, f32, f32, C.c_int, vp]
     _lib = lib
     return lib
 
@@ -505,9 +505,10 @@ def meshlet_rows(group_offsets, max_vertices, min_triangles):
 
 def build_meshlets_flex_groups_device(d_meshlets, d_meshlet_vertices, d_meshlet_triangles, meshlet_offsets, d_indices, group_offsets, d_positions,
                                       vertex_count, positions_stride, max_vertices, min_triangles, max_triangles, cone_weight=0.0,
-                                      split_factor=2.0, stream=0, check=True):
+                                      split_factor=2.0, optimize_level=-1, stream=0, check=True):
     """meshoptgpu_buildMeshletsFlexGroups: meshopt_buildMeshletsFlex for every group of a level on device
-    data, one warp per group. meshlet_offsets / group_offsets: host ints (group_count + 1).
+    data, one warp per group, then meshopt_optimizeMeshletLevel(optimize_level) on every meshlet
+    unless it is -1. meshlet_offsets / group_offsets: host ints (group_count + 1).
     Returns the meshlet count per group (uint64 array)."""
     off = np.ascontiguousarray(group_offsets, dtype=np.uint64)
     mo = np.ascontiguousarray(meshlet_offsets, dtype=np.uint64)
@@ -515,13 +516,14 @@ def build_meshlets_flex_groups_device(d_meshlets, d_meshlet_vertices, d_meshlet_
     counts = np.zeros(max(n, 1), np.uint64)
     st = load().meshoptgpu_buildMeshletsFlexGroups(d_meshlets, d_meshlet_vertices, d_meshlet_triangles, mo.ctypes.data, counts.ctypes.data, d_indices,
                                                    off.ctypes.data, n, d_positions, vertex_count, positions_stride, max_vertices, min_triangles,
-                                                   max_triangles, C.c_float(cone_weight), C.c_float(split_factor), C.c_void_p(stream or None))
+                                                   max_triangles, C.c_float(cone_weight), C.c_float(split_factor), int(optimize_level),
+                                                   C.c_void_p(stream or None))
     if check and st != STATUS_OK:
         raise SimplifyError(st, last_status()[1])
     return counts[:n]
 
 
-def build_meshlets_flex_groups(groups, positions, max_vertices, min_triangles, max_triangles, cone_weight=0.0, split_factor=2.0):
+def build_meshlets_flex_groups(groups, positions, max_vertices, min_triangles, max_triangles, cone_weight=0.0, split_factor=2.0, optimize_level=-1):
     """Host convenience over build_meshlets_flex_groups_device (torch for device memory): groups is
     a list of index arrays into `positions`. Returns, per group, (meshlets [n, 4] uint32,
     meshlet_vertices uint32, meshlet_triangles uint8) trimmed as meshopt_buildMeshletsFlex leaves them."""
@@ -540,7 +542,7 @@ def build_meshlets_flex_groups(groups, positions, max_vertices, min_triangles, m
     d_t = torch.zeros(total, dtype=torch.uint8, device="cuda")
     counts = build_meshlets_flex_groups_device(d_m.data_ptr(), d_v.data_ptr(), d_t.data_ptr(), rows, d_idx.data_ptr(), off, d_pos.data_ptr(),
                                                len(pos), pos.reshape(len(pos), -1).shape[1] * 4, max_vertices, min_triangles, max_triangles,
-                                               cone_weight, split_factor)
+                                               cone_weight, split_factor, optimize_level)
     torch.cuda.synchronize()
     m = d_m.cpu().numpy().view(np.uint32).reshape(-1, 4)
     v = d_v.cpu().numpy().view(np.uint32)

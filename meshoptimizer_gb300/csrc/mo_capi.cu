@@ -1142,7 +1142,7 @@ static unsigned int meshletPoolBytes()
 int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles,
     const size_t* meshlet_offsets, size_t* meshlet_counts, const unsigned int* indices, const size_t* group_offsets, size_t group_count,
     const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles, size_t max_triangles,
-    float cone_weight, float split_factor, void* stream)
+    float cone_weight, float split_factor, int optimize_level, void* stream)
 {
 	// the reference's argument checks (src/clusterizer.cpp:1039-1049), as errors
 	std::string bad;
@@ -1160,6 +1160,8 @@ int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* mes
 		bad = "split_factor must be >= 0";
 	else if (vertex_count >= (size_t(1) << 32))
 		bad = "vertex_count must be below 2^32";
+	else if (optimize_level < -1 || optimize_level > 9)
+		bad = "optimize_level must be -1 (none) or 0..9";
 	for (size_t g = 0; bad.empty() && g < group_count; ++g)
 	{
 		const size_t n = group_offsets[g + 1] - group_offsets[g];
@@ -1228,6 +1230,8 @@ int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, unsigned int* mes
 		b.scratch_off = d_meta + 2 * (G + 1);
 		b.error = d_err;
 		b.pool_bytes = meshletPoolBytes();
+		b.optimize_level = optimize_level;
+		b.rows = meshlet_offsets[G];
 		buildMeshletsBatch(b, st);
 		unsigned int* hc = reinterpret_cast<unsigned int*>(static_cast<char*>(h) + host.size() * 8);
 		MO_CUDA_CHECK(cudaMemcpyAsync(hc, d_counts, (G + 1) * 4, cudaMemcpyDeviceToHost, st));

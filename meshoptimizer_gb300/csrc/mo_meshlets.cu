@@ -367,6 +367,171 @@ __device__ void kdNearest(const Scratch& s, const float* pos, unsigned int* resu
 	}
 }
 
+// meshopt_optimizeMeshletLevel (src/meshletutils.cpp:366-554) on one meshlet, by one warp: at
+// every position the scan over the remaining triangles runs 32 at a time (the stop after the
+// level-th edge match found with a ballot, then the first best score up to it), the shift and
+// the bookkeeping on lane 0; 8-bit timestamps and valences wrap as the reference's do
+struct MeshletOpt
+{
+	unsigned char idx[512 * 3];
+	unsigned char cache[256];
+	unsigned int valence[256];
+	short remap[256];
+	unsigned int order[256];
+};
+
+__device__ void optimizeMeshletWarp(unsigned int* verts, unsigned char* tris, unsigned int vc, unsigned int tc, int level, MeshletOpt& o)
+{
+	const unsigned int lane = threadIdx.x & 31;
+	const unsigned char cutoff = 3;
+	for (unsigned int k = lane; k < tc * 3; k += 32)
+		o.idx[k] = tris[k];
+	for (unsigned int v = lane; v < vc; v += 32)
+	{
+		o.cache[v] = 0;
+		o.valence[v] = 0;
+	}
+	__syncwarp();
+	for (unsigned int k = lane; k < tc * 3; k += 32)
+		atomicAdd(&o.valence[o.idx[k]], 1u);
+	__syncwarp();
+	unsigned char cache_last = 128;
+	for (unsigned int i = 0; i < tc; ++i)
+	{
+		int next = -1, next_score = -1, edges = 0;
+		bool done = false;
+		for (unsigned int j0 = i; j0 < tc && !done; j0 += 32)
+		{
+			const unsigned int j = j0 + lane;
+			const bool valid = j < tc;
+			int score = -2, match = 0;
+			if (valid)
+			{
+				unsigned char a = o.idx[j * 3 + 0], b = o.idx[j * 3 + 1], c = o.idx[j * 3 + 2];
+				unsigned char ad = (unsigned char)(cache_last - o.cache[a]);
+				unsigned char bd = (unsigned char)(cache_last - o.cache[b]);
+				unsigned char cd = (unsigned char)(cache_last - o.cache[c]);
+				match = (ad < cutoff) + (bd < cutoff) + (cd < cutoff);
+				if (level)
+				{
+					int va = o.valence[a] & 0xFF, vb = o.valence[b] & 0xFF, vcc = o.valence[c] & 0xFF;
+					int vmin = va < vb ? va : vb;
+					vmin = vcc < vmin ? vcc : vmin;
+					score = (match * 1024 + (1023 - ad - bd - cd)) * 256 + (255 - vmin);
+				}
+				else
+					score = match;
+			}
+			// the scan stops at the edge match that makes `level` of them (the first one at level 0)
+			const unsigned int em = __ballot_sync(0xffffffffu, valid && match >= 2);
+			const int need = level ? level - edges : 1;
+			unsigned int last = 31;
+			if (__popc(em) >= need)
+			{
+				unsigned int m = em;
+				for (int q = 1; q < need; ++q)
+					m &= m - 1;
+				last = __ffs(m) - 1;
+				done = true;
+			}
+			edges += __popc(em & (last == 31 ? 0xffffffffu : ((2u << last) - 1u)));
+			// the first best score among the scanned ones
+			int bs = (valid && lane <= last) ? score : -2;
+			unsigned int bj = (valid && lane <= last) ? j : ~0u;
+			for (int off = 16; off > 0; off >>= 1)
+			{
+				int os = __shfl_xor_sync(0xffffffffu, bs, off);
+				unsigned int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+				if (os > bs || (os == bs && oj < bj))
+					bs = os, bj = oj;
+			}
+			if (bs > next_score)
+			{
+				next = int(bj);
+				next_score = bs;
+			}
+		}
+		if (lane == 0)
+		{
+			const unsigned int n = unsigned(next);
+			unsigned char a = o.idx[n * 3 + 0], b = o.idx[n * 3 + 1], c = o.idx[n * 3 + 2];
+			for (unsigned int k = n * 3; k > i * 3; --k) // the triangles before it shift forward
+				o.idx[k + 2] = o.idx[k - 1];
+			o.idx[i * 3 + 0] = a;
+			o.idx[i * 3 + 1] = b;
+			o.idx[i * 3 + 2] = c;
+			unsigned char stamp = (unsigned char)(cache_last + 1);
+			o.cache[a] = o.cache[b] = o.cache[c] = stamp;
+			o.valence[a] = (o.valence[a] - 1) & 0xFF;
+			o.valence[b] = (o.valence[b] - 1) & 0xFF;
+			o.valence[c] = (o.valence[c] - 1) & 0xFF;
+		}
+		cache_last++;
+		__syncwarp();
+	}
+	if (lane == 0)
+	{
+		if (level >= 1)
+		{
+			for (unsigned int v = 0; v < vc; ++v)
+				o.cache[v] = 0;
+			for (unsigned int i = 0; i < tc; ++i)
+			{
+				unsigned char a = o.idx[i * 3 + 0], b = o.idx[i * 3 + 1], c = o.idx[i * 3 + 2];
+				if (!o.cache[a] && o.cache[b] && !o.cache[c])
+				{
+					unsigned char t = a;
+					a = b, b = c, c = t;
+				}
+				else if (!o.cache[a] && !o.cache[b] && !o.cache[c])
+				{
+					bool ab = false, bc = false, ca = false;
+					for (unsigned int j = i + 1; j < tc && j <= i + cutoff; ++j)
+					{
+						unsigned char oa = o.idx[j * 3 + 0], ob = o.idx[j * 3 + 1], oc = o.idx[j * 3 + 2];
+						ab |= (oa == b && ob == a) || (ob == b && oc == a) || (oc == b && oa == a);
+						bc |= (oa == c && ob == b) || (ob == c && oc == b) || (oc == c && oa == b);
+						ca |= (oa == a && ob == c) || (ob == a && oc == c) || (oc == a && oa == c);
+					}
+					if (ab && !bc)
+					{
+						unsigned char t = a;
+						a = b, b = c, c = t;
+					}
+					else if ((ab && !ca) || (!ab && bc && !ca))
+					{
+						unsigned char t = c;
+						c = b, b = a, a = t;
+					}
+				}
+				o.idx[i * 3 + 0] = a, o.idx[i * 3 + 1] = b, o.idx[i * 3 + 2] = c;
+				o.cache[a] = o.cache[b] = o.cache[c] = 1;
+			}
+		}
+		// vertices renumbered in first-use order
+		for (unsigned int v = 0; v < vc; ++v)
+			o.remap[v] = -1;
+		unsigned int n = 0;
+		for (unsigned int k = 0; k < tc * 3; ++k)
+		{
+			short r = o.remap[o.idx[k]];
+			if (r < 0)
+			{
+				r = short(n);
+				o.remap[o.idx[k]] = r;
+				o.order[n++] = verts[o.idx[k]];
+			}
+			o.idx[k] = (unsigned char)r;
+		}
+		for (unsigned int v = 0; v < n; ++v)
+			verts[v] = o.order[v];
+	}
+	__syncwarp();
+	for (unsigned int k = lane; k < tc * 3; k += 32)
+		tris[k] = o.idx[k];
+	__syncwarp();
+}
+
 __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) kMeshletsFlex(MeshletBatch b)
 {
 	const unsigned int lane = threadIdx.x & 31;
@@ -810,6 +975,36 @@ __global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) kMeshletsFlex(MeshletB
 	}
 }
 
+// meshopt_optimizeMeshletLevel on every meshlet, as clusterize runs it (demo/clusterlod.h:292-300):
+// one warp per meshlet row of the batch; a row past its group's meshlet count has nothing to do
+__global__ void __launch_bounds__(kMaxWarpsPerBlock * 32) kOptimizeMeshlets(MeshletBatch b, unsigned long long rows)
+{
+	__shared__ MeshletOpt opt[kMaxWarpsPerBlock];
+	const unsigned long long r = (unsigned long long)blockIdx.x * kMaxWarpsPerBlock + (threadIdx.x >> 5);
+	if (r >= rows)
+		return;
+	// the group whose rows hold r: the last g with meshlet_base[g] <= r
+	unsigned int lo = 0, hi = b.groups;
+	while (hi - lo > 1)
+	{
+		unsigned int mid = (lo + hi) / 2;
+		if (b.meshlet_base[mid] <= r)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	const unsigned int g = lo;
+	const unsigned long long k = r - b.meshlet_base[g];
+	if (k >= b.counts[g])
+		return;
+	const unsigned long long i0 = b.offsets[g];
+	const unsigned int I = unsigned(b.offsets[g + 1] - i0) / 3 * 3;
+	const unsigned int* row = b.meshlets + r * 4;
+	const unsigned int vo = row[0], to = row[1], vc = row[2], tc = row[3];
+	if (vc <= 256 && tc <= 512 && vo + vc <= I && to + tc * 3 <= I)
+		optimizeMeshletWarp(b.mverts + i0 + vo, b.mtris + i0 + to, vc, tc, b.optimize_level, opt[threadIdx.x >> 5]);
+}
+
 } // namespace
 
 size_t meshletBound(size_t index_count, size_t max_vertices, size_t max_triangles)
@@ -834,6 +1029,8 @@ void buildMeshletsBatch(const MeshletBatch& b, cudaStream_t stream)
 	const unsigned int warps = b.pool_bytes ? 1 : kMaxWarpsPerBlock;
 	const unsigned int blocks = (b.groups + warps - 1) / warps;
 	MO_LAUNCH(kMeshletsFlex, blocks, warps * 32, warps * b.pool_bytes, stream, b);
+	if (b.optimize_level >= 0 && b.rows)
+		MO_LAUNCH(kOptimizeMeshlets, unsigned((b.rows + kMaxWarpsPerBlock - 1) / kMaxWarpsPerBlock), kMaxWarpsPerBlock * 32, 0, stream, b, b.rows);
 	MO_CUDA_CHECK(cudaGetLastError());
 }
 

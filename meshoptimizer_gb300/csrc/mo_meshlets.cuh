@@ -34,6 +34,8 @@ struct MeshletBatch
 	// shared memory per warp (at most 48 KiB) for the arrays the greedy loop reads at every step,
 	// placed while they fit; 0: all in global scratch
 	unsigned int pool_bytes;
+	int optimize_level; // meshopt_optimizeMeshletLevel level run on every meshlet after the build, -1: none
+	unsigned long long rows; // meshlet rows of the batch (meshlet_base[groups])
 };
 
 // meshopt_buildMeshletsBound (src/clusterizer.cpp:1017-1033)

@@ -64,3 +64,31 @@ def build_meshlets_flex(indices, positions, max_vertices, min_triangles, max_tri
         mverts = mverts[:0].copy()
         mtris = mtris[:0].copy()
     return meshlets, mverts, mtris
+
+
+def optimize_meshlets(meshlets, meshlet_vertices, meshlet_triangles, level, kind="port"):
+    """meshopt_optimizeMeshletLevel on every meshlet of a build result (copies returned), as a
+    cluster-LOD builder's clusterize step runs it (demo/clusterlod.h:292-300)."""
+    v = np.array(meshlet_vertices, dtype=np.uint32, copy=True)
+    t = np.array(meshlet_triangles, dtype=np.uint8, copy=True)
+    m = np.ascontiguousarray(meshlets, dtype=np.uint32)
+    if kind == "port":
+        # the whole loop in C (mo_optimizeMeshlets), so that timing it times the port
+        key = ("opt_all", kind)
+        if key not in _fns:
+            f = C.CDLL(PORT_PATH).mo_optimizeMeshlets
+            f.restype = None
+            f.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int]
+            _fns[key] = f
+        if len(m):
+            _fns[key](m.ctypes.data, len(m), v.ctypes.data, t.ctypes.data, int(level))
+        return v, t
+    key = ("opt_one", kind)
+    if key not in _fns:
+        f = C.CDLL(REF_PATH).meshopt_optimizeMeshletLevel
+        f.restype = None
+        f.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int]
+        _fns[key] = f
+    for vo, to, vc, tc in m.astype(np.uint64):
+        _fns[key](v.ctypes.data + int(vo) * 4, int(vc), t.ctypes.data + int(to), int(tc), int(level))
+    return v, t

@@ -598,3 +598,119 @@ size_t mo_buildMeshletsFlex(unsigned int* meshlets, unsigned int* meshlet_vertic
 	free(lidx);
 	return offset;
 }
+
+/* meshopt_optimizeMeshletLevel (src/meshletutils.cpp:366-554): triangles reordered for vertex
+ * reuse (a greedy pick over the remaining triangles with 8-bit cache timestamps and valences,
+ * which wrap as the reference's unsigned char counters do), rotated for compressibility at
+ * level >= 1, then vertices renumbered in first-use order. */
+void mo_optimizeMeshletLevel(unsigned int* meshlet_vertices, size_t vertex_count, unsigned char* meshlet_triangles, size_t triangle_count, int level)
+{
+	unsigned char* idx = meshlet_triangles;
+	unsigned char cache[256], valence[256];
+	memset(cache, 0, vertex_count);
+	memset(valence, 0, vertex_count);
+	unsigned char cache_last = 128;
+	const unsigned char cutoff = 3;
+	for (size_t i = 0; i < triangle_count * 3; ++i)
+		valence[idx[i]]++;
+	for (size_t i = 0; i < triangle_count; ++i)
+	{
+		int next = -1, next_score = -1, edges = 0;
+		for (size_t j = i; j < triangle_count; ++j)
+		{
+			unsigned char a = idx[j * 3 + 0], b = idx[j * 3 + 1], c = idx[j * 3 + 2];
+			unsigned char ad = (unsigned char)(cache_last - cache[a]);
+			unsigned char bd = (unsigned char)(cache_last - cache[b]);
+			unsigned char cd = (unsigned char)(cache_last - cache[c]);
+			int match = (ad < cutoff) + (bd < cutoff) + (cd < cutoff);
+			int score;
+			if (level)
+			{
+				int vmin = valence[a] < valence[b] ? valence[a] : valence[b];
+				vmin = valence[c] < vmin ? valence[c] : vmin;
+				score = (match * 1024 + (1023 - ad - bd - cd)) * 256 + (255 - vmin);
+			}
+			else
+				score = match;
+			if (score > next_score)
+			{
+				next = (int)j;
+				next_score = score;
+			}
+			if (level ? (match >= 2 && ++edges >= level) : (match >= 2))
+				break;
+		}
+		unsigned char a = idx[next * 3 + 0], b = idx[next * 3 + 1], c = idx[next * 3 + 2];
+		memmove(idx + (i + 1) * 3, idx + i * 3, (size_t)(next - (int)i) * 3);
+		idx[i * 3 + 0] = a;
+		idx[i * 3 + 1] = b;
+		idx[i * 3 + 2] = c;
+		cache_last++;
+		cache[a] = cache[b] = cache[c] = cache_last;
+		valence[a]--;
+		valence[b]--;
+		valence[c]--;
+	}
+	if (level >= 1)
+	{
+		memset(cache, 0, vertex_count);
+		for (size_t i = 0; i < triangle_count; ++i)
+		{
+			unsigned char a = idx[i * 3 + 0], b = idx[i * 3 + 1], c = idx[i * 3 + 2];
+			if (!cache[a] && cache[b] && !cache[c])
+			{
+				unsigned char t = a;
+				a = b, b = c, c = t;
+			}
+			else if (!cache[a] && !cache[b] && !cache[c])
+			{
+				int ab = 0, bc = 0, ca = 0;
+				for (size_t j = i + 1; j < triangle_count && j <= i + cutoff; ++j)
+				{
+					unsigned char oa = idx[j * 3 + 0], ob = idx[j * 3 + 1], oc = idx[j * 3 + 2];
+					ab |= (oa == b && ob == a) || (ob == b && oc == a) || (oc == b && oa == a);
+					bc |= (oa == c && ob == b) || (ob == c && oc == b) || (oc == c && oa == b);
+					ca |= (oa == a && ob == c) || (ob == a && oc == c) || (oc == a && oa == c);
+				}
+				if (ab && !bc)
+				{
+					unsigned char t = a;
+					a = b, b = c, c = t;
+				}
+				else if ((ab && !ca) || (!ab && bc && !ca))
+				{
+					unsigned char t = c;
+					c = b, b = a, a = t;
+				}
+			}
+			idx[i * 3 + 0] = a, idx[i * 3 + 1] = b, idx[i * 3 + 2] = c;
+			cache[a] = cache[b] = cache[c] = 1;
+		}
+	}
+	unsigned int order[256];
+	short remap[256];
+	for (size_t v = 0; v < vertex_count; ++v)
+		remap[v] = -1;
+	size_t n = 0;
+	for (size_t i = 0; i < triangle_count * 3; ++i)
+	{
+		short* r = &remap[idx[i]];
+		if (*r < 0)
+		{
+			*r = (short)n;
+			order[n++] = meshlet_vertices[idx[i]];
+		}
+		idx[i] = (unsigned char)*r;
+	}
+	memcpy(meshlet_vertices, order, n * sizeof(unsigned int));
+}
+
+/* the clusterize step's per-meshlet pass (demo/clusterlod.h:292-300) over a build's output */
+void mo_optimizeMeshlets(const unsigned int* meshlets, size_t meshlet_count, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles, int level)
+{
+	for (size_t i = 0; i < meshlet_count; ++i)
+	{
+		const unsigned int* m = meshlets + i * 4;
+		mo_optimizeMeshletLevel(meshlet_vertices + m[0], m[2], meshlet_triangles + m[1], m[3], level);
+	}
+}

@@ -127,6 +127,10 @@ size_t mo_buildMeshletsBound(size_t index_count, size_t max_vertices, size_t max
 size_t mo_buildMeshletsFlex(unsigned int* meshlets, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles, const unsigned int* indices,
     size_t index_count, const float* vertex_positions, size_t vertex_count, size_t vertex_positions_stride, size_t max_vertices, size_t min_triangles,
     size_t max_triangles, float cone_weight, float split_factor);
+/* meshopt_optimizeMeshletLevel (src/meshletutils.cpp:366), same signature */
+void mo_optimizeMeshletLevel(unsigned int* meshlet_vertices, size_t vertex_count, unsigned char* meshlet_triangles, size_t triangle_count, int level);
+/* mo_optimizeMeshletLevel on each of meshlet_count {vertex_offset, triangle_offset, vertex_count, triangle_count} rows */
+void mo_optimizeMeshlets(const unsigned int* meshlets, size_t meshlet_count, unsigned int* meshlet_vertices, unsigned char* meshlet_triangles, int level);
 
 #ifdef __cplusplus
 }

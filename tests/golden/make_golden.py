@@ -22,7 +22,8 @@ It writes two files next to this script:
   leaves.
 * ``meshlet_cases.npz`` -- meshopt_buildMeshletsFlex, the re-clusterization step of a
   cluster-LOD level: seeded meshes (each stored once) and the reference's meshlets for six
-  parameter sets each, through the reference's own clusterizer.cpp in oracle/_ref/libclod_ref.so.
+  parameter sets each, through the reference's own clusterizer.cpp in oracle/_ref/libclod_ref.so,
+  with the meshlets after the reference's meshopt_optimizeMeshletLevel (meshletutils.cpp).
 * ``compaction_cases.npz`` -- seeded inputs of the compaction step after the simplifier
   (meshopt_optimizeVertexFetchRemap, meshopt_optimizeVertexFetch,
   meshopt_generatePositionRemap) with the reference library's outputs.
@@ -434,9 +435,16 @@ def meshlet_cases():
     for j, (name, idx, pos) in enumerate(meshes):
         for mv, mint, maxt, cw, sf in params:
             m, v, tr = ML.build_meshlets_flex(idx, pos, mv, mint, maxt, cw, sf, kind="reference")
-            cases.append(dict(name=f"{name}_{mv}_{mint}_{maxt}_{cw}_{sf}", mesh=np.array(j), max_vertices=np.array(mv), min_triangles=np.array(mint),
-                              max_triangles=np.array(maxt), cone_weight=np.array(cw, np.float32), split_factor=np.array(sf, np.float32), meshlets=m,
-                              meshlet_vertices=v, meshlet_triangles=tr))
+            c = dict(name=f"{name}_{mv}_{mint}_{maxt}_{cw}_{sf}", mesh=np.array(j), max_vertices=np.array(mv), min_triangles=np.array(mint),
+                     max_triangles=np.array(maxt), cone_weight=np.array(cw, np.float32), split_factor=np.array(sf, np.float32), meshlets=m,
+                     meshlet_vertices=v, meshlet_triangles=tr)
+            # meshopt_optimizeMeshletLevel on every meshlet (src/meshletutils.cpp:366): clusterlod's
+            # level 1 everywhere, levels 0 and 5 on every other case
+            for level in ((1, 0, 5) if len(cases) % 2 == 0 else (1,)):
+                ov, ot = ML.optimize_meshlets(m, v, tr, level, kind="reference")
+                c[f"opt{level}_meshlet_vertices"] = ov
+                c[f"opt{level}_meshlet_triangles"] = ot
+            cases.append(c)
     return [(np.asarray(idx, np.uint32), np.asarray(pos, np.float32)) for _, idx, pos in meshes], cases
 
 

@@ -53,6 +53,28 @@ def test_golden_cases():
             base += len(c["positions"])
 
 
+@pytest.mark.parametrize("level", [1, 0, 5])
+def test_golden_cases_optimized(level):
+    """The fixtures with meshopt_optimizeMeshletLevel(level) run on every meshlet afterwards."""
+    cases = [c for c in fixtures.meshlet_cases() if f"opt{level}_meshlet_vertices" in c]
+    assert len(cases) >= 27
+    for c in cases:
+        key = (int(c["max_vertices"]), int(c["min_triangles"]), int(c["max_triangles"]), float(c["cone_weight"]), float(c["split_factor"]))
+        (m, v, t), = mg.build_meshlets_flex_groups([c["indices"]], c["positions"], *key, optimize_level=level)
+        _same((m, v, t), (c["meshlets"], c[f"opt{level}_meshlet_vertices"], c[f"opt{level}_meshlet_triangles"]), f"{c['name']} level {level}")
+
+
+def test_cluster_groups_optimized_match_oracle(port):
+    """clusterlod's clusterize with its defaults: build, then optimizeMeshletLevel(1) per meshlet."""
+    groups, pos, _, _, _ = W.cluster_groups(6, group_tris=512, seed=4)
+    got = mg.build_meshlets_flex_groups(groups, pos, 128, 42, 128, 0.0, 2.0, optimize_level=1)
+    ML = _ml()
+    for g, (idx, res) in enumerate(zip(groups, got)):
+        m, v, t = ML.build_meshlets_flex(idx, pos, 128, 42, 128, 0.0, 2.0, kind="port")
+        v, t = ML.optimize_meshlets(m, v, t, 1, kind="port")
+        _same(res, (m, v, t), f"group {g}")
+
+
 @pytest.mark.parametrize("params", [(128, 42, 128, 0.0, 2.0), (64, 21, 64, 0.25, 2.0), (96, 32, 96, 0.0, 0.0)])
 def test_cluster_groups_match_oracle(port, params):
     """Groups of a cluster-LOD level over one shared vertex buffer (clusterlod's default
@@ -115,15 +137,16 @@ def test_invalid_arguments():
     rows = mg.meshlet_rows(off, 64, 21)
 
     def call(**kw):
-        a = dict(meshlet_offsets=rows, group_offsets=off, vertex_count=len(pos), max_vertices=64, min_triangles=21, max_triangles=64)
+        a = dict(meshlet_offsets=rows, group_offsets=off, vertex_count=len(pos), max_vertices=64, min_triangles=21, max_triangles=64,
+                 optimize_level=-1)
         a.update(kw)
         return mg.build_meshlets_flex_groups_device(d_m.data_ptr(), d_v.data_ptr(), d_t.data_ptr(), a["meshlet_offsets"], d_idx.data_ptr(),
                                                     a["group_offsets"], d_pos.data_ptr(), a["vertex_count"], 12, a["max_vertices"],
-                                                    a["min_triangles"], a["max_triangles"], check=False)
+                                                    a["min_triangles"], a["max_triangles"], optimize_level=a["optimize_level"], check=False)
 
     for kw in (dict(max_vertices=2), dict(max_vertices=257), dict(min_triangles=0), dict(min_triangles=65), dict(max_triangles=513),
                dict(group_offsets=np.array([0, len(idx) - 1], np.uint64)), dict(meshlet_offsets=np.array([0, 1], np.uint64)),
-               dict(vertex_count=len(pos) - 1)):
+               dict(vertex_count=len(pos) - 1), dict(optimize_level=10), dict(optimize_level=-2)):
         call(**kw)
         assert mg.last_status()[0] == mg.STATUS_INVALID_ARGUMENT, kw
     call()

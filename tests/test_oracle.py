@@ -150,3 +150,19 @@ def test_meshlet_port_bound():
     # meshopt_buildMeshletsBound: the larger of the vertex-limited and triangle-limited counts
     assert ML.bound(3 * 1000, 64, 124, kind="port") == max((3000 + 61) // 62, (1000 + 123) // 124)
     assert ML.bound(0, 64, 124, kind="port") == 0
+
+
+def test_meshlet_optimize_port_matches_golden(port):
+    """mo_optimizeMeshletLevel against the reference's meshopt_optimizeMeshletLevel outputs."""
+    import meshlets as ML
+
+    checked = 0
+    for c in fixtures.meshlet_cases():
+        for level in (0, 1, 5):
+            if f"opt{level}_meshlet_vertices" not in c:
+                continue
+            v, t = ML.optimize_meshlets(c["meshlets"], c["meshlet_vertices"], c["meshlet_triangles"], level, kind="port")
+            assert np.array_equal(v, c[f"opt{level}_meshlet_vertices"]), (c["name"], level)
+            assert np.array_equal(t, c[f"opt{level}_meshlet_triangles"]), (c["name"], level)
+            checked += 1
+    assert checked >= 100
