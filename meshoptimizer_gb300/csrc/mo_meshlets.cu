@@ -190,7 +190,8 @@ __device__ unsigned int neighborSerial(const Scratch& s, unsigned int voff, unsi
 __device__ unsigned int neighborWarp(const Scratch& s, unsigned int voff, unsigned int vcount, const Cone& mc, float cone_weight, float radius, bool* nan)
 {
 	const unsigned int lane = threadIdx.x & 31;
-	unsigned int best = ~0u, key = ~0u;
+	unsigned int best = ~0u;
+	unsigned long long key = ~0ull; // scan position: (meshlet vertex, list entry)
 	int bp = 5;
 	float bs = FLT_MAX;
 	bool sawnan = false;
@@ -212,13 +213,14 @@ __device__ unsigned int neighborWarp(const Scratch& s, unsigned int voff, unsign
 				best = t;
 				bp = priority;
 				bs = score;
-				key = (i << 16) | j;
+				key = ((unsigned long long)i << 32) | j;
 			}
 		}
 	}
 	for (int o = 16; o > 0; o >>= 1)
 	{
-		unsigned int ob = __shfl_xor_sync(0xffffffffu, best, o), ok = __shfl_xor_sync(0xffffffffu, key, o);
+		unsigned int ob = __shfl_xor_sync(0xffffffffu, best, o);
+		unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
 		int op = __shfl_xor_sync(0xffffffffu, bp, o);
 		float os = __shfl_xor_sync(0xffffffffu, bs, o);
 		bool take = op < bp || (op == bp && (os < bs || (os == bs && ok < key)));

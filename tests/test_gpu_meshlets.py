@@ -151,3 +151,18 @@ def test_invalid_arguments():
         assert mg.last_status()[0] == mg.STATUS_INVALID_ARGUMENT, kw
     call()
     assert mg.last_status()[0] == mg.STATUS_OK
+
+
+def test_high_degree_fan(port):
+    """A vertex shared by 2000 triangles: its list is scanned by one lane at every step."""
+    n = 2000
+    ang = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    rim = np.stack([np.cos(ang), np.sin(ang), 0.05 * np.sin(9 * ang)], axis=1)
+    pos = np.concatenate([[[0.0, 0.0, 0.3]], rim]).astype(np.float32)
+    idx = np.array([[0, 1 + i, 1 + (i + 1) % n] for i in range(n)], np.uint32).reshape(-1)
+    ML = _ml()
+    for params in ((128, 42, 128, 0.0, 2.0), (64, 16, 124, 0.25, 0.0)):
+        (got,) = mg.build_meshlets_flex_groups([idx], pos, *params, optimize_level=1)
+        m, v, t = ML.build_meshlets_flex(idx, pos, *params, kind="port")
+        v, t = ML.optimize_meshlets(m, v, t, 1, kind="port")
+        _same(got, (m, v, t), f"fan {params}")
