@@ -100,10 +100,38 @@ struct ThreadState
 	// drop-in calls with at most this many indices run on the batch kernel as a batch of one
 	// (measured crossover on GB300: about 8k triangles, with or without attributes)
 	size_t dropin_batch_limit = 24000;
+	// drop-in copies of positions and attributes on streams of their own (another copy engine;
+	// the attributes are waited for only where they are first read)
+	cudaStream_t copy_stream[2] = {nullptr, nullptr};
+	cudaEvent_t copy_done[2] = {nullptr, nullptr};
+
+	void ensureCopyStreams()
+	{
+		for (int i = 0; i < 2; ++i)
+			if (!copy_stream[i])
+			{
+				MO_CUDA_CHECK(cudaStreamCreateWithFlags(&copy_stream[i], cudaStreamNonBlocking));
+				MO_CUDA_CHECK(cudaEventCreateWithFlags(&copy_done[i], cudaEventDisableTiming));
+			}
+	}
+
+	void releaseCopyStreams()
+	{
+		for (int i = 0; i < 2; ++i)
+		{
+			if (copy_done[i])
+				cudaEventDestroy(copy_done[i]);
+			if (copy_stream[i])
+				cudaStreamDestroy(copy_stream[i]);
+			copy_done[i] = nullptr;
+			copy_stream[i] = nullptr;
+		}
+	}
 
 	~ThreadState()
 	{
 		simplifier.reset();
+		releaseCopyStreams();
 		if (stream)
 			cudaStreamDestroy(stream);
 	}
@@ -115,6 +143,7 @@ struct ThreadState
 		if (simplifier && device == dev)
 			return;
 		simplifier.reset();
+		releaseCopyStreams();
 		if (stream)
 			cudaStreamDestroy(stream);
 		stream = nullptr;
@@ -259,6 +288,7 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 	if (!bad.empty())
 		return failHost(destination, indices, index_count, result_error,
 		    (options & ~kSupportedOptions) ? meshoptgpu_StatusUnsupported : meshoptgpu_StatusInvalidArgument, bad);
+	bool split = false; // inputs copied on the copy streams too
 	try
 	{
 		ThreadState& s = state();
@@ -275,12 +305,30 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		unsigned char* d_lock = vertex_lock ? reinterpret_cast<unsigned char*>(base + b_idx + b_pos + b_attr) : nullptr;
 		unsigned int* d_out = reinterpret_cast<unsigned int*>(base + b_idx + b_pos + b_attr + b_lock);
 		cudaStream_t st = s.stream;
+		// large meshes on the single-mesh path: positions and attributes on their own copy
+		// streams; the setup waits for the positions at once and for the attributes where it
+		// first reads them
+		const size_t attr_bytes = d_attr ? vertex_count * vertex_attributes_stride : 0;
+		split = attr_bytes >= (size_t(1) << 20) && index_count > s.dropin_batch_limit;
 		if (index_count)
 			MO_CUDA_CHECK(cudaMemcpyAsync(d_idx, indices, index_count * 4, cudaMemcpyHostToDevice, st));
-		if (vertex_count)
-			MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, vertex_count * vertex_positions_stride, cudaMemcpyHostToDevice, st));
-		if (d_attr)
-			MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, vertex_count * vertex_attributes_stride, cudaMemcpyHostToDevice, st));
+		if (split)
+		{
+			s.ensureCopyStreams();
+			if (vertex_count)
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, vertex_count * vertex_positions_stride, cudaMemcpyHostToDevice, s.copy_stream[0]));
+			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[0], s.copy_stream[0]));
+			MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, attr_bytes, cudaMemcpyHostToDevice, s.copy_stream[1]));
+			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[1], s.copy_stream[1]));
+			MO_CUDA_CHECK(cudaStreamWaitEvent(st, s.copy_done[0], 0));
+		}
+		else
+		{
+			if (vertex_count)
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, vertex_count * vertex_positions_stride, cudaMemcpyHostToDevice, st));
+			if (d_attr)
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, attr_bytes, cudaMemcpyHostToDevice, st));
+		}
 		if (d_lock)
 			MO_CUDA_CHECK(cudaMemcpyAsync(d_lock, vertex_lock, vertex_count, cudaMemcpyHostToDevice, st));
 
@@ -298,11 +346,14 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		m.target_index_count = target_index_count;
 		m.target_error = target_error;
 		m.options = options;
-		if (!smallMeshOnBatch(s, m, d_out, st))
+		m.attributes_ready = split ? s.copy_done[1] : nullptr;
+		if (split || !smallMeshOnBatch(s, m, d_out, st))
 			s.last = s.simplifier->run(m, d_out, st, s.timing ? &s.times : nullptr);
 		if (s.last.index_count)
 			MO_CUDA_CHECK(cudaMemcpyAsync(destination, d_out, s.last.index_count * 4, cudaMemcpyDeviceToHost, st));
 		MO_CUDA_CHECK(cudaStreamSynchronize(st));
+		if (split) // the caller's attribute buffer is read to the end before returning
+			MO_CUDA_CHECK(cudaEventSynchronize(s.copy_done[1]));
 		if (result_error)
 			*result_error = s.last.result_error;
 		setStatus(meshoptgpu_StatusOk, "");
@@ -310,6 +361,12 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 	}
 	catch (const std::exception& e)
 	{
+		if (split)
+		{
+			ThreadState& s = state();
+			cudaEventSynchronize(s.copy_done[0]);
+			cudaEventSynchronize(s.copy_done[1]);
+		}
 		return failHost(destination, indices, index_count, result_error, statusOf(e), e.what());
 	}
 }

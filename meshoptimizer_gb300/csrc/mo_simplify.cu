@@ -2897,6 +2897,8 @@ RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStre
 	MO_CUDA_CHECK(cudaMemcpyAsync(pinned_, total, 4, cudaMemcpyDeviceToHost, stream));
 	MO_CUDA_CHECK(cudaStreamSynchronize(stream));
 	const size_t U = pinned_[0];
+	if (ac && m.attributes_ready)
+		MO_CUDA_CHECK(cudaStreamWaitEvent(stream, m.attributes_ready, 0));
 	if (U)
 		MO_LAUNCH(kSparseGather, gridFor(U, kThreads), kThreads, 0, stream, smap, U, m.positions, m.positions_stride / 4, ac ? m.attributes : nullptr,
 		    m.attributes_stride / 4, ac, m.lock, cpos, cattr, m.lock ? clock : nullptr);
@@ -2907,6 +2909,7 @@ RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStre
 	cm.positions = cpos;
 	cm.positions_stride = 12;
 	cm.attributes = ac ? cattr : nullptr;
+	cm.attributes_ready = nullptr;
 	cm.attributes_stride = ac * 4;
 	cm.lock = m.lock ? clock : nullptr;
 	cm.options = m.options & ~(kOptSparse | kOptInternalDebug); // debug bits are not produced for sparse subsets (:2602)
@@ -3107,7 +3110,11 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	if (V)
 		MO_LAUNCH(kRescale, gV, kThreads, 0, stream, w.pos_raw, V, w.sc, w.pos);
 	if (ac && V)
+	{
+		if (m.attributes_ready)
+			MO_CUDA_CHECK(cudaStreamWaitEvent(stream, m.attributes_ready, 0));
 		MO_LAUNCH(kRescaleAttributes, gV, kThreads, 0, stream, m.attributes, m.attributes_stride / 4, V, am, w.attr);
+	}
 
 	// quadrics
 	float factor = (m.options & kOptRegularizeLight) ? 1e-2f : ((m.options & kOptRegularize) ? 1e-1f : 1e-7f);

@@ -37,6 +37,9 @@ struct MeshDesc
 	// device buffers)
 	float* update_positions = nullptr;
 	float* update_attributes = nullptr;
+	// when set, the attributes are still arriving: the stream waits for this event before it
+	// first reads them (their copy overlaps the setup that does not need them)
+	cudaEvent_t attributes_ready = nullptr;
 };
 
 // Per-pass counters, the same quantities the reference prints under TRACE
