@@ -10,36 +10,30 @@
 namespace mogpu
 {
 
-constexpr unsigned int kBarrierSpinLimit = 1u << 25; // x ~64 ns sleep: seconds, never reached in a normal run
+constexpr unsigned int kBarrierSpinLimit = 1u << 25; // x >= 32 ns sleep: seconds, never reached in a normal run
 
-// bar[0]: arrivals, bar[1]: generation. Both zero before the launch.
+// bar[0] counts the arrivals of all barriers of the launch and is zero before it. Barrier i ends
+// when the count reaches (i + 1) * gridDim.x: no block can arrive at barrier i + 1 before every
+// block has arrived at barrier i, so an arrival that reads old = n belongs to barrier n / G.
+// Waiting blocks poll the count itself, so the last arrival releases them with its own add.
 __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err)
 {
 	__syncthreads();
 	if (threadIdx.x == 0)
 	{
-		volatile unsigned int* gen = bar + 1;
-		unsigned int g = *gen;
+		volatile unsigned int* count = bar;
 		__threadfence();
-		unsigned int arrived = atomicAdd(bar, 1u);
-		if (arrived == gridDim.x - 1)
+		const unsigned int old = atomicAdd(bar, 1u);
+		const unsigned int target = (old / gridDim.x + 1) * gridDim.x;
+		unsigned int spins = 0;
+		while ((int)(*count - target) < 0)
 		{
-			atomicExch(bar, 0u);
-			__threadfence();
-			atomicAdd(bar + 1, 1u);
-		}
-		else
-		{
-			unsigned int spins = 0;
-			while (*gen == g)
+			if (++spins > kBarrierSpinLimit)
 			{
-				if (++spins > kBarrierSpinLimit)
-				{
-					atomicOr(err, 1u);
-					break;
-				}
-				__nanosleep(64);
+				atomicOr(err, 1u);
+				break;
 			}
+			__nanosleep(32);
 		}
 		__threadfence();
 	}
