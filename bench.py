@@ -812,7 +812,7 @@ def main():
                                               serve_batch_workers=0), mg, torch)
         line["serving"] = {k: sv[k] for k in ("served", "plain", "served_equals_plain", "config")}
         cl = bench_clod_level(argparse.Namespace(steps=3, warmup=3, no_cpu_baseline=args.no_cpu_baseline), mg, torch)
-        line["cluster_lod_level"] = {k: cl[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "cpu_baseline", "bit_exact_vs_oracle")}
+        line["cluster_lod_level"] = {k: cl[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "cpu_baseline", "bit_exact_vs_oracle", "clusterize", "level_ms")}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -17,6 +17,8 @@
 #include "mo_prims.cuh"
 #include "mo_probe.cuh"
 #include "mo_batch.cuh"
+#include <tuple>
+#include <map>
 
 #include <algorithm>
 #include <cstring>
@@ -1449,10 +1451,26 @@ int blocksPerSMT(int threads, unsigned int smem_bytes)
 	return n;
 }
 
+// occupancy per (device, threads, shared memory, variant), queried once each: driver queries
+// are not free, and a batch call makes one
 int batchBlocksPerSM(int threads, unsigned int smem_bytes, bool full)
 {
 	raiseSmemLimits();
-	return full ? blocksPerSMT<true>(threads, smem_bytes) : blocksPerSMT<false>(threads, smem_bytes);
+	static std::mutex lock;
+	static std::map<std::tuple<int, int, unsigned int, bool>, int> known;
+	int dev = 0;
+	cudaGetDevice(&dev);
+	const auto key = std::make_tuple(dev, threads, smem_bytes, full);
+	{
+		std::lock_guard<std::mutex> g(lock);
+		auto it = known.find(key);
+		if (it != known.end())
+			return it->second;
+	}
+	const int n = full ? blocksPerSMT<true>(threads, smem_bytes) : blocksPerSMT<false>(threads, smem_bytes);
+	std::lock_guard<std::mutex> g(lock);
+	known[key] = n;
+	return n;
 }
 
 } // namespace mogpu

@@ -96,6 +96,7 @@ struct ThreadState
 	DeviceBuffer batch_meta, batch_slabs, batch_io, compact_scratch, group_scratch, update_io, meshlet_scratch;
 	HostStaging batch_host, batch_meta_host;
 	int batch_threads = 0;          // 0: autotune
+	int sms = 1;                    // the device's SM count
 	unsigned int batch_smem = 0;    // 0: default budget
 	// drop-in calls with at most this many indices run on the batch kernel as a batch of one
 	// (measured crossover on GB300: about 8k triangles, with or without attributes)
@@ -149,6 +150,7 @@ struct ThreadState
 		stream = nullptr;
 		device = dev;
 		MO_CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+		MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 		simplifier.reset(new Simplifier(dev));
 	}
 };
@@ -556,8 +558,7 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 		maxidx = std::max<size_t>(maxidx, ordered[i].index_count);
 	}
 	unsigned int smem = unsigned((maxfit + 15) & ~size_t(15));
-	int sms = 0;
-	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
+	const int sms = s.sms;
 
 	// device metadata: descriptors, results, the ticket, the attribute maps; descriptors and
 	// maps go up in one copy from pinned staging

@@ -2817,6 +2817,8 @@ Simplifier::Simplifier(int device) : device_(device)
 	int sms = 0, per_sm = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
+	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&solve_per_sm_, kSolvePositions, kThreads, 0));
+	cudaDeviceGetAttribute(&clock_khz_, cudaDevAttrClockRate, device);
 	sms_ = sms;
 	coop_blocks_ = unsigned(std::max(1, sms * std::max(per_sm, 1)));
 	tuning_ = Tuning::fromEnvironment();
@@ -3623,9 +3625,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			sa.max_rounds = unsigned(V + 2);
 			sa.sc = w.sc;
 			// co-resident blocks of this kernel (its own register count), as many as the pass kernel's at most
-			int per_sm = 0;
-			MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kSolvePositions, kThreads, 0));
-			unsigned int resident = unsigned(std::max(1, per_sm * sms_));
+			unsigned int resident = unsigned(std::max(1, solve_per_sm_ * sms_));
 			unsigned int blocks = std::max(1u, std::min(std::min(perform_blocks_, resident), gV));
 			MO_CUDA_CHECK(cudaMemsetAsync(w.sc->bar, 0, sizeof(unsigned int) * 3, stream));
 			void* params[] = {&sa};
@@ -3654,8 +3654,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	float rerr;
 	memcpy(&rerr, &result_error_bits, 4);
 	{
-		int khz = 0;
-		cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device_);
+		const int khz = clock_khz_;
 		readScalars();
 		for (int i = 0; i < 8; ++i)
 			rr.perform_phase_ms[i] = khz ? float(double(hs->phase_cycles[i]) / khz) : 0.f;

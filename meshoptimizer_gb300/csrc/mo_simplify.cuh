@@ -151,6 +151,8 @@ private:
 	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative pass kernel (occupancy)
 	unsigned int perform_blocks_ = 1;
 	int sms_ = 1;
+	int solve_per_sm_ = 1; // resident blocks of the position solve kernel per SM
+	int clock_khz_ = 0;    // SM clock for the phase counters (queried once: the query costs ~0.6 ms)
 	Tuning tuning_;
 	// The device-resident pass loop's executable graph, kept for the next run of the same shape:
 	// the graph holds workspace pointers (fixed by the arena base and the layout's sizes) and
