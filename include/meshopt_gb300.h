@@ -218,11 +218,11 @@ MESHOPTGPU_API void meshoptgpu_setBatchConfig(int threads, unsigned int smem_byt
 
 /* Drop-in calls (meshopt_simplify, meshopt_simplifyWithAttributes, meshoptgpu_simplifyDevice)
  * on meshes with at most max_index_count indices run on the batch kernel as a batch of one,
- * where one CTA does the whole simplification: below about 8k triangles that is faster than
+ * where one CTA does the whole simplification: below about 5k triangles that is faster than
  * the multi-CTA pass loop, whose cost per call is fixed by its launches and host reads. Results
  * are identical either way. Such calls record no pass statistics, phase times or round trace
  * (meshoptgpu_setTiming(1) keeps every call on the single-mesh path). Per calling thread;
- * default 24000, 0 disables. */
+ * default 15000, 0 disables. */
 MESHOPTGPU_API void meshoptgpu_setDropinBatchLimit(size_t max_index_count);
 
 /* The single-mesh path runs its pass loop (src/simplifier.cpp:2493-2541) on the device: one

@@ -566,7 +566,10 @@ def set_batch_config(threads=0, smem_bytes=0):
     load().meshoptgpu_setBatchConfig(int(threads), int(smem_bytes))
 
 
-def set_dropin_batch_limit(max_index_count=24000):
+DROPIN_BATCH_LIMIT = 15000  # the library's default
+
+
+def set_dropin_batch_limit(max_index_count=DROPIN_BATCH_LIMIT):
     """Drop-in calls on meshes with at most this many indices run on the batch kernel (0: never)."""
     load().meshoptgpu_setDropinBatchLimit(int(max_index_count))
 

@@ -99,8 +99,9 @@ struct ThreadState
 	int sms = 1;                    // the device's SM count
 	unsigned int batch_smem = 0;    // 0: default budget
 	// drop-in calls with at most this many indices run on the batch kernel as a batch of one
-	// (measured crossover on GB300: about 8k triangles, with or without attributes)
-	size_t dropin_batch_limit = 24000;
+	// (measured crossover on GB300: about 5k triangles; 4.4k-triangle heightfield 1.09 ms batched
+	// against 1.18 ms on the pass loop, 7.9k triangles 2.01 against 1.47 ms)
+	size_t dropin_batch_limit = 15000;
 	// drop-in copies of positions and attributes on streams of their own (another copy engine;
 	// the attributes are waited for only where they are first read)
 	cudaStream_t copy_stream[2] = {nullptr, nullptr};

@@ -24,7 +24,9 @@ def built():
 
     build.build()
     mg.load()
-    mg.set_dropin_batch_limit(24000)
+    mg.set_dropin_batch_limit(24000)  # every seeded case up to 24000 indices on the batch kernel
+    yield
+    mg.set_dropin_batch_limit()
 
 
 def _routed(call):

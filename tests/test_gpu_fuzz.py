@@ -64,7 +64,7 @@ def _check(port, case, batch_limit):
     try:
         got, err = mg.simplify(idx, pos, target, error, options, attributes=attrs, weights=weights, lock=lock)
     finally:
-        mg.set_dropin_batch_limit(24000)
+        mg.set_dropin_batch_limit()
     assert np.array_equal(got, ref), (options, target, error, len(idx))
     assert np.float32(err) == np.float32(ref_err) or abs(err - ref_err) <= 1e-6 * max(1.0, abs(ref_err))
 
