@@ -40,4 +40,35 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 	__syncthreads();
 }
 
+// A grid barrier that a cooperative launch passes once, leaving its two words zero for the next
+// launch: bar[0] counts arrivals, bar[1] departures, and the last block to depart clears both
+// (by then no block polls bar[0] any more).
+__device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int* err)
+{
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		volatile unsigned int* count = bar;
+		__threadfence();
+		atomicAdd(bar, 1u);
+		unsigned int spins = 0;
+		while (*count < gridDim.x)
+		{
+			if (++spins > kBarrierSpinLimit)
+			{
+				atomicOr(err, 1u);
+				break;
+			}
+			__nanosleep(32);
+		}
+		__threadfence();
+		if (atomicAdd(bar + 1, 1u) == gridDim.x - 1)
+		{
+			atomicExch(bar, 0u);
+			atomicExch(bar + 1, 0u);
+		}
+	}
+	__syncthreads();
+}
+
 } // namespace mogpu

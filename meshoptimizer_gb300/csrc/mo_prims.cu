@@ -5,8 +5,12 @@
 // between); each radix pass reads the pairs twice (histogram + scatter) and writes them
 // once. Tiles are sized so that a grid of a few thousand blocks covers the 152 SMs.
 #include "mo_common.cuh"
+#include "mo_grid.cuh"
 #include "mo_prims.cuh"
 #include "mo_probe.cuh"
+
+#include <algorithm>
+#include <atomic>
 
 namespace mogpu
 {
@@ -71,12 +75,69 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(const unsigned int* i
 		*total = base + btotal;
 }
 
+// The whole scan in one cooperative launch: block b reduces its run of consecutive tiles into
+// sums[b]; after the grid barrier each block adds up the sums before it and scans its tiles
+// again, writing the prefixes. in and out may alias: a block writes only elements it has read.
+__global__ void __launch_bounds__(kScanThreads) kScanCoop(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total,
+    unsigned int* sums, unsigned int* bar, unsigned int* err, bool aligned)
+{
+	__shared__ unsigned int smem[kScanThreads / 32 + 1];
+	const size_t tiles = (n + kScanTile - 1) / kScanTile;
+	const size_t per = (tiles + gridDim.x - 1) / gridDim.x;
+	const size_t t0 = min(tiles, (size_t)blockIdx.x * per), t1 = min(tiles, t0 + per);
+	unsigned int s = 0;
+	for (size_t t = t0; t < t1; ++t)
+	{
+		const uint4 v = loadTile4(in, n, t * kScanTile + (size_t)threadIdx.x * kScanItems, aligned);
+		s += v.x + v.y + v.z + v.w;
+	}
+	unsigned int part;
+	blockExclusiveScan<kScanThreads>(s, smem, &part);
+	if (threadIdx.x == 0)
+		sums[blockIdx.x] = part;
+	gridBarrierOnce(bar, err);
+	unsigned int before = 0;
+	for (unsigned int j = threadIdx.x; j < blockIdx.x; j += kScanThreads)
+		before += __ldcg(sums + j);
+	unsigned int base;
+	blockExclusiveScan<kScanThreads>(before, smem, &base);
+	for (size_t t = t0; t < t1; ++t)
+	{
+		const size_t i = t * kScanTile + (size_t)threadIdx.x * kScanItems;
+		const uint4 v = loadTile4(in, n, i, aligned);
+		__syncthreads(); // every thread has read the previous scan's shared words
+		unsigned int tile_total;
+		const unsigned int pre = base + blockExclusiveScan<kScanThreads>(v.x + v.y + v.z + v.w, smem, &tile_total);
+		uint4 o;
+		o.x = pre;
+		o.y = o.x + v.x;
+		o.z = o.y + v.y;
+		o.w = o.z + v.z;
+		if (aligned && i + 3 < n)
+			*reinterpret_cast<uint4*>(out + i) = o;
+		else
+		{
+			if (i + 0 < n)
+				out[i + 0] = o.x;
+			if (i + 1 < n)
+				out[i + 1] = o.y;
+			if (i + 2 < n)
+				out[i + 2] = o.z;
+			if (i + 3 < n)
+				out[i + 3] = o.w;
+		}
+		base += tile_total;
+	}
+	if (total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+		*total = base;
+}
+
 size_t roundWords(size_t w)
 {
 	return (w + 63) & ~size_t(63);
 }
 
-void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream)
+void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream, ScanSync sync)
 {
 	size_t tiles = (n + kScanTile - 1) / kScanTile;
 	bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
@@ -85,9 +146,22 @@ void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int
 		MO_LAUNCH(kScanApply, 1, kScanThreads, 0, stream, in, out, n, nullptr, total, aligned);
 		return;
 	}
+	const unsigned int cap = sync.bar ? coopScanCapacity() : 0u;
+	if (cap)
+	{
+		// consecutive tiles per block, then as few blocks as that needs
+		const size_t per = (tiles + cap - 1) / cap;
+		const unsigned int blocks = unsigned((tiles + per - 1) / per);
+		unsigned int* sums = scratch;
+		cudaEvent_t e0 = probeBegin("kScanCoop", stream);
+		void* params[] = {(void*)&in, (void*)&out, (void*)&n, (void*)&total, (void*)&sums, (void*)&sync.bar, (void*)&sync.err, (void*)&aligned};
+		MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kScanCoop, dim3(blocks), dim3(kScanThreads), params, 0, stream));
+		probeEnd(e0, stream);
+		return;
+	}
 	unsigned int* sums = scratch;
 	MO_LAUNCH(kScanReduce, (unsigned)tiles, kScanThreads, 0, stream, in, n, sums, aligned);
-	scanLevel(sums, sums, tiles, nullptr, scratch + roundWords(tiles), stream);
+	scanLevel(sums, sums, tiles, nullptr, scratch + roundWords(tiles), stream, ScanSync());
 	MO_LAUNCH(kScanApply, (unsigned)tiles, kScanThreads, 0, stream, in, out, n, sums, total, aligned);
 }
 
@@ -210,6 +284,27 @@ __global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int
 
 } // namespace
 
+constexpr int kMaxDevices = 64;
+constexpr unsigned int kCoopScanBlocksPerSM = 4; // at most this many per SM (occupancy permitting)
+
+unsigned int coopScanCapacity()
+{
+	static std::atomic<unsigned int> cache[kMaxDevices];
+	int dev = 0;
+	MO_CUDA_CHECK(cudaGetDevice(&dev));
+	if (dev < 0 || dev >= kMaxDevices)
+		return 0;
+	unsigned int c = cache[dev].load(std::memory_order_relaxed);
+	if (c)
+		return c;
+	int sms = 0, occ = 0;
+	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kScanCoop, kScanThreads, 0));
+	c = unsigned(std::max(1, sms)) * std::min(unsigned(std::max(1, occ)), kCoopScanBlocksPerSM);
+	cache[dev].store(c, std::memory_order_relaxed);
+	return c;
+}
+
 size_t scanScratchWords(size_t n)
 {
 	size_t words = 64;
@@ -222,7 +317,8 @@ size_t scanScratchWords(size_t n)
 	return words;
 }
 
-void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream)
+void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream,
+    ScanSync sync)
 {
 	if (n == 0)
 	{
@@ -230,7 +326,7 @@ void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned
 			MO_CUDA_CHECK(cudaMemsetAsync(total, 0, sizeof(unsigned int), stream));
 		return;
 	}
-	scanLevel(in, out, n, total, scratch, stream);
+	scanLevel(in, out, n, total, scratch, stream, sync);
 	MO_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -242,7 +338,8 @@ size_t radixScratchWords(size_t n)
 }
 
 void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
-    unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream, const unsigned int* n_dev)
+    unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream, const unsigned int* n_dev,
+    ScanSync sync)
 {
 	if (n == 0)
 		return;
@@ -269,7 +366,7 @@ void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, un
 		unsigned int* vd = to_out ? vals_out : vals_tmp;
 		int shift = p * 8;
 		MO_LAUNCH(kRadixHist, tiles, kSortThreads, 0, stream, ks, n, n_dev, shift, hist, tiles);
-		scanExclusive(hist, hist, size_t(tiles) * kSortBins, nullptr, sscratch, stream);
+		scanExclusive(hist, hist, size_t(tiles) * kSortBins, nullptr, sscratch, stream, sync);
 		MO_LAUNCH(kRadixScatter, tiles, kSortThreads, 0, stream, ks, vs, kd, vd, n, n_dev, shift, hist, tiles);
 		ks = kd;
 		vs = vd;

@@ -77,9 +77,25 @@ __device__ __forceinline__ unsigned int blockExclusiveScan(unsigned int v, unsig
 // scratch words needed by scanExclusive for n elements
 size_t scanScratchWords(size_t n);
 
+// Single-launch mode of scanExclusive (and of radixSortPairs' histogram scans): a scan over
+// more than one tile runs as one cooperative kernel (reduce, one grid barrier, apply) instead
+// of a reduce and an apply launch per level. bar: two device words, zero before the first
+// scan, which every scan leaves zero; err: set to 1 if the barrier's bounded wait gave up.
+// A caller gives each stream that scans concurrently words of its own.
+struct ScanSync
+{
+	unsigned int* bar = nullptr;
+	unsigned int* err = nullptr;
+};
+
+// Blocks a single-launch scan may use on the current device (all resident at once); queried
+// once per device and cached. Call it outside stream capture before the first such scan.
+unsigned int coopScanCapacity();
+
 // out[i] = sum(in[0..i)) for i < n; if total != nullptr, *total (device) = sum(in[0..n)).
 // in and out may alias. scratch: scanScratchWords(n) words of device memory.
-void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream);
+void scanExclusive(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total, unsigned int* scratch, cudaStream_t stream,
+    ScanSync sync = ScanSync());
 
 // scratch words needed by radixSortPairs for n pairs
 size_t radixScratchWords(size_t n);
@@ -92,7 +108,7 @@ size_t radixScratchWords(size_t n);
 // launches can be recorded once and replayed for any count up to n.
 void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
     unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream,
-    const unsigned int* n_dev = nullptr);
+    const unsigned int* n_dev = nullptr, ScanSync sync = ScanSync());
 
 inline unsigned int gridFor(size_t n, int threads)
 {

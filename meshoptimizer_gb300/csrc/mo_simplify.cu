@@ -109,6 +109,8 @@ struct Scalars
 	unsigned int solve_pending[3];      // update mode: position-solve candidates left, rotating by round
 	unsigned int solve_rounds;
 	unsigned int max_degree[2];         // corners of the busiest vertex: raw, remapped
+	unsigned int scan_bar[2];           // the single-launch scans' barrier words (left zero by each scan)
+	unsigned int scan_error;            // a single-launch scan's barrier gave up waiting
 };
 
 static_assert(sizeof(Scalars) <= kPinnedBytes, "the scalars block must fit the pinned readback buffer");
@@ -1047,40 +1049,48 @@ __device__ __forceinline__ bool pickEdge(unsigned int i0, unsigned int i1, const
 	return true;
 }
 
-// lv: counts of the live pass; the grid covers the first pass's triangles and the slots past
-// the live count are cleared, so the scan over the full range is the scan of the live one
-__global__ void kPickCount(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
-    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, unsigned int* __restrict__ cnt, const PassLive* lv)
+// candidates per block of kThreads triangles (the scan runs over blocks, not triangles). lv:
+// counts of the live pass; the grid covers the first pass's triangles and blocks past the live
+// count write zero, so the scan over the full range is the scan of the live one
+__global__ void __launch_bounds__(kThreads) kPickCount(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap,
+    const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
+    unsigned int* __restrict__ bcnt, const PassLive* lv)
 {
-	size_t t = gtid();
+	__shared__ unsigned int sm[kThreads / 32 + 1];
 	if (lv)
 	{
 		if (lv->stop)
 			return;
-		if (t < tris && t >= lv->tris)
-			cnt[t] = 0;
 		res = lv->res;
 		tris = lv->tris;
 	}
-	if (t >= tris)
-		return;
-	unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
+	const size_t t = gtid();
 	unsigned int c = 0;
-#pragma unroll
-	for (int e = 0; e < 3; ++e)
+	if (t < tris)
 	{
-		unsigned int v0, v1, bd;
-		c += pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0, v1, bd);
+		const unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
+#pragma unroll
+		for (int e = 0; e < 3; ++e)
+		{
+			unsigned int v0, v1, bd;
+			c += pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0, v1, bd);
+		}
 	}
-	cnt[t] = c;
+	unsigned int total;
+	blockExclusiveScan<kThreads>(c, sm, &total);
+	if (threadIdx.x == 0)
+		bcnt[blockIdx.x] = total;
 }
 
 // emits the candidates of every triangle whose prefix leaves room for three more
-// (the capacity check at :1319-1320 stops at the first triangle that does not)
-__global__ void kPickEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
-    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, const unsigned int* __restrict__ offs, Scalars* sc,
-    unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr, const PassLive* lv)
+// (the capacity check at :1319-1320 stops at the first triangle that does not); a triangle's
+// prefix is its block's scanned count plus the block-local prefix
+__global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap,
+    const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
+    const unsigned int* __restrict__ boffs, Scalars* sc, unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr,
+    const PassLive* lv)
 {
+	__shared__ unsigned int sm[kThreads / 32 + 1];
 	if (lv)
 	{
 		if (lv->stop)
@@ -1088,28 +1098,39 @@ __global__ void kPickEmit(const unsigned int* __restrict__ res, size_t tris, con
 		res = lv->res;
 		tris = lv->tris;
 	}
-	size_t t = gtid();
+	const size_t t = gtid();
+	unsigned int v0[3], v1[3], bd[3];
+	bool ok[3] = {false, false, false};
+	unsigned int c = 0;
+	if (t < tris)
+	{
+		const unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
+#pragma unroll
+		for (int e = 0; e < 3; ++e)
+		{
+			ok[e] = pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0[e], v1[e], bd[e]);
+			c += ok[e];
+		}
+	}
+	unsigned int total;
+	const unsigned int pre = blockExclusiveScan<kThreads>(c, sm, &total);
 	if (t >= tris)
 		return;
-	unsigned int o = offs[t];
+	unsigned int o = boffs[blockIdx.x] + pre;
 	if ((size_t)o + 3 > sc->capacity)
 	{
 		atomicMin(&sc->pick_trunc, o);
 		return;
 	}
-	unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
 #pragma unroll
 	for (int e = 0; e < 3; ++e)
-	{
-		unsigned int v0, v1, bd;
-		if (pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0, v1, bd))
+		if (ok[e])
 		{
-			cv0[o] = v0;
-			cv1[o] = v1;
-			cerr[o] = bd;
+			cv0[o] = v0[e];
+			cv1[o] = v1[e];
+			cerr[o] = bd[e];
 			o++;
 		}
-	}
 }
 
 // ---------------------------------------------------------------- pass: rank
@@ -2421,7 +2442,7 @@ __global__ void kPassEnd(Scalars* sc, cudaGraphConditionalHandle handle, unsigne
 	lv.iterations++;
 	if (!lv.stop)
 	{
-		if (sc->grid_error)
+		if (sc->grid_error || sc->scan_error)
 			lv.stop = 1; // reported by the host after the loop
 		else
 		{
@@ -2823,6 +2844,7 @@ Simplifier::Simplifier(int device) : device_(device)
 	coop_blocks_ = unsigned(std::max(1, sms * std::max(per_sm, 1)));
 	tuning_ = Tuning::fromEnvironment();
 	perform_blocks_ = std::min(coop_blocks_, unsigned(std::max(1, sms * tuning_.perform_blocks_per_sm)));
+	coopScanCapacity(); // cached now: the pass loop's scans may first run while it is recorded
 }
 
 void Simplifier::dropLoopGraph()
@@ -2985,7 +3007,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	auto readScalars = [&]() {
 		MO_CUDA_CHECK(cudaMemcpyAsync(hs, w.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
 		MO_CUDA_CHECK(cudaStreamSynchronize(stream));
+		if (hs->scan_error)
+			throw std::runtime_error("grid barrier wait limit reached in a scan");
 	};
+	// scans and sorts of this run: one cooperative launch per scan (the run's stream is the only
+	// one that uses these words)
+	const ScanSync ss{w.sc->scan_bar, &w.sc->scan_error};
 
 	cudaEvent_t ev[16];
 	bool timed = times != nullptr;
@@ -3019,7 +3046,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	{
 		MO_LAUNCH(kHashInsert, gV, kThreads, 0, stream, w.pos_raw, V, w.table, w.hash_mask, w.slot, &w.sc->probe_fail);
 		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.flags);
-		scanExclusive(w.flags, w.flags, V, &w.sc->dup_count, w.scratch, stream);
+		scanExclusive(w.flags, w.flags, V, &w.sc->dup_count, w.scratch, stream, ss);
 	}
 	// vertex -> corner lists in corner order: raw (classification, attribute quadrics) and
 	// remapped (position quadrics). Their offsets and largest degrees come before the host read
@@ -3027,11 +3054,11 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 	if (I)
 		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt);
-	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream);
+	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream, ss);
 	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 	if (I)
 		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt);
-	scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream);
+	scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream, ss);
 	if (V)
 	{
 		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_raw, V, &w.sc->max_degree[0]);
@@ -3049,7 +3076,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		// rebuild the dup flags (the scan consumed them) into cnt, then compact
 		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.cnt);
 		MO_LAUNCH(kCompactFlagged, gV, kThreads, 0, stream, w.cnt, w.flags, w.remap, V, w.keys_b, w.vals_b);
-		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.ckey, w.cv0, D, bitsFor(V), w.scratch, stream);
+		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.ckey, w.cv0, D, bitsFor(V), w.scratch, stream, nullptr, ss);
 		MO_LAUNCH(kWedgeLink, gridFor(D, kThreads), kThreads, 0, stream, w.keys_a, w.vals_a, D, w.wedge);
 	}
 
@@ -3073,12 +3100,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	else
 	{
 		// a vertex with many corners: stable radix sorts by vertex
-		radixSortPairs(w.res0, nullptr, w.keys_a, w.csr_raw, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
+		radixSortPairs(w.res0, nullptr, w.keys_a, w.csr_raw, w.keys_b, w.vals_b, I, vbits, w.scratch, stream, nullptr, ss);
 		if (D)
 		{
 			if (I)
 				MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.ckey);
-			radixSortPairs(w.ckey, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream);
+			radixSortPairs(w.ckey, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream, nullptr, ss);
 		}
 	}
 	const unsigned int* off_rm = D ? w.off_rm : w.off_raw;
@@ -3142,14 +3169,14 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		if (I)
 			MO_LAUNCH(kUnionEdges, gridFor(I / 3, kThreads), kThreads, 0, stream, w.res0, I / 3, w.remap, w.parent);
 		MO_LAUNCH(kComponentRoots, gV, kThreads, 0, stream, V, w.remap, w.parent, w.flags);
-		scanExclusive(w.flags, w.fill, V, &w.sc->dup_count, w.scratch, stream);
+		scanExclusive(w.flags, w.fill, V, &w.sc->dup_count, w.scratch, stream, ss);
 		MO_LAUNCH(kComponentIds, gV, kThreads, 0, stream, V, w.remap, w.parent, w.fill, w.comp);
 		readScalars();
 		comp_count = hs->dup_count;
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (comp_count + 1) * 4, stream));
 		MO_LAUNCH(kCountKeys, gV, kThreads, 0, stream, w.comp, nullptr, V, w.cnt);
-		scanExclusive(w.cnt, w.off_rm, comp_count + 1, nullptr, w.scratch, stream);
-		radixSortPairs(w.comp, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, V, bitsFor(comp_count ? comp_count - 1 : 0), w.scratch, stream);
+		scanExclusive(w.cnt, w.off_rm, comp_count + 1, nullptr, w.scratch, stream, ss);
+		radixSortPairs(w.comp, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, V, bitsFor(comp_count ? comp_count - 1 : 0), w.scratch, stream, nullptr, ss);
 		MO_LAUNCH(kMeasureComponents, gridFor(comp_count, kThreads), kThreads, 0, stream, comp_count, w.off_rm, w.vals_a, w.pos, w.comp_err);
 	}
 	if (V)
@@ -3233,7 +3260,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		if (T)
 		{
 			MO_LAUNCH(kPruneCount, gT, kThreads, 0, stream, res, T, w.comp, w.comp_err, cutoff, w.blkcnt, &w.sc->done);
-			scanExclusive(w.blkcnt, w.blkcnt, gT, &w.sc->tri_total, w.scratch, stream);
+			scanExclusive(w.blkcnt, w.blkcnt, gT, &w.sc->tri_total, w.scratch, stream, ss);
 			MO_LAUNCH(kPruneEmit, gT, kThreads, 0, stream, res, T, w.comp, w.comp_err, cutoff, w.blkcnt, res_next);
 		}
 		else
@@ -3328,16 +3355,16 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, cs));
 				MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, cs));
 				MO_LAUNCH(kCountKeys, gI, kThreads, 0, cs, nullptr, w.remap, I, w.cnt, lv);
-				scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs);
+				scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs, ss);
 				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, w.fill, w.adj, lv);
 				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
-				scanExclusive(w.tcnt, w.tcnt, T0, &w.sc->pick_total, w.scratch, cs);
+				scanExclusive(w.tcnt, w.tcnt, gT0, &w.sc->pick_total, w.scratch, cs, ss);
 				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
 				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, lv);
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
 				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 				    w.attr, w.aq, w.ag, ac, lv);
-				radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count);
+				radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count, ss);
 				MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr,
 				    w.skind, w.status, lv);
 				PerformArgs pa;
@@ -3435,14 +3462,14 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 		MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
 		MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
-		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream);
+		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream, ss);
 		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[3], stream));
 
 		// pick
 		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, nullptr);
-		scanExclusive(w.tcnt, w.tcnt, T, &w.sc->pick_total, w.scratch, stream);
+		scanExclusive(w.tcnt, w.tcnt, gT, &w.sc->pick_total, w.scratch, stream, ss);
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, stream));
 		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, nullptr);
 		readScalars();
@@ -3458,7 +3485,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		    w.ag, ac, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
-		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream);
+		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream, nullptr, ss);
 		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr, w.skind,
 		    w.status, nullptr);
 		if (timed)
@@ -3601,7 +3628,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			MO_LAUNCH(kMarkUpdate, gridFor(result_count, kThreads), kThreads, 0, stream, res, result_count, w.remap, w.vupdate);
 			MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
 		}
-		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream);
+		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream, ss);
 		if (T)
 			MO_LAUNCH(kAdjFill, gridFor(T, kThreads), kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj, nullptr);
 		MO_CUDA_CHECK(cudaMemcpyAsync(w.pos_new, w.pos, V * sizeof(float4), cudaMemcpyDeviceToDevice, stream));

@@ -118,6 +118,14 @@ def test_fractal_heightfield(port):
     _compare_with_oracle(port, c["indices"], c["positions"], c["target"], c["error"], 0)
 
 
+def test_fractal_heightfield_full(port):
+    """The largest single-mesh workload at its full size: the 3163 x 3163 fractal terrain
+    (19,996,488 triangles, 1%, 12 passes), bit-exact with every pass's counters (the oracle
+    takes about 15 s of one host core)."""
+    c = W.config_fractal_3163()
+    _compare_with_oracle(port, c["indices"], c["positions"], c["target"], c["error"], 0)
+
+
 def test_patches_lock_border(port):
     for g, (idx, pos) in enumerate(W.sphere_patches(24, seed=5, levels=5)):
         _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.5), 2e-2, mg.SimplifyLockBorder)
