@@ -193,23 +193,26 @@ __global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* _
 	hist[(size_t)threadIdx.x * tiles + blockIdx.x] = sh[threadIdx.x];
 }
 
-// Stable scatter: elements are ranked in index order (sub-round j holds elements
-// j*256 .. j*256+255 of the tile; within it, warp w and lane l give the order), so equal
-// digits keep their input order; tiles are laid out by the digit-major scanned histogram.
-// The tile is first put in digit order in shared memory and then written out front to back,
-// so each digit's elements of the tile leave as one contiguous run (coalesced stores).
-__global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
+// Stable scatter. Warp w ranks the tile's elements w*512 .. w*512+511, 32 at a time (lane order
+// within each step, steps in order), against per-warp digit counters in shared memory; the warp
+// counters of each digit are then turned into offsets in warp order. So equal digits keep their
+// input order, and the tile is put in digit order in shared memory with one block barrier per
+// phase, then written out front to back: each digit's elements of the tile leave as one
+// contiguous run (coalesced stores) at the position the digit-major scanned histogram gives.
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortWarpSpan = kSortTile / kSortWarps; // consecutive elements per warp
+
+__global__ void __launch_bounds__(kSortThreads, 3) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
     unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, size_t n, const unsigned int* n_dev, int shift, const unsigned int* __restrict__ hist,
     unsigned int tiles)
 {
 	// vin == nullptr stands for the identity values 0..n-1
 	n = liveCount(n, n_dev);
-	__shared__ unsigned int base[kSortBins];  // next tile-local slot per digit
-	__shared__ unsigned int lbase[kSortBins]; // tile-local start per digit
-	__shared__ unsigned int gbase[kSortBins]; // global position of the tile's first element per digit
-	// per warp and digit: the sub-round's count, then its first slot; zero between sub-rounds
-	__shared__ unsigned int wcnt[kSortThreads / 32][kSortBins];
+	__shared__ unsigned int lbase[kSortBins];              // tile-local start per digit
+	__shared__ unsigned int gbase[kSortBins];              // global position of the tile's first element per digit
+	__shared__ unsigned int wcnt[kSortWarps][kSortBins];   // per warp and digit: count, then offset within the digit
 	__shared__ unsigned int sk[kSortTile], sv[kSortTile];
+	__shared__ unsigned int scan_smem[kSortWarps + 1];
 
 	const unsigned int t = threadIdx.x, w = t >> 5, lane = t & 31;
 	const size_t tile0 = (size_t)blockIdx.x * kSortTile;
@@ -224,51 +227,64 @@ __global__ void __launch_bounds__(kSortThreads) kRadixScatter(const unsigned int
 		const unsigned int next = at + 1 < (size_t)kSortBins * tiles ? hist[at + 1] : (unsigned int)n;
 		gbase[t] = g;
 		unsigned int total;
-		unsigned int l = blockExclusiveScan<kSortThreads>(next - g, wcnt[0], &total);
-		__syncthreads();
-		lbase[t] = l;
-		base[t] = l;
+		lbase[t] = blockExclusiveScan<kSortThreads>(next - g, scan_smem, &total);
 	}
 #pragma unroll
-	for (int q = 0; q < kSortThreads / 32; ++q)
+	for (int q = 0; q < kSortWarps; ++q)
 		wcnt[q][t] = 0;
 	__syncthreads();
 
-	for (int j = 0; j < kSortItems; ++j)
-	{
-		size_t i = tile0 + (size_t)j * kSortThreads + t;
-		bool valid = i < n;
-		unsigned int k = valid ? __ldg(kin + i) : 0u;
-		unsigned int v = valid ? (vin ? __ldg(vin + i) : (unsigned int)i) : 0u;
-		unsigned int d = valid ? ((k >> shift) & 0xFFu) : (0x100u + lane);
-		unsigned int peers = __match_any_sync(0xffffffffu, d);
-		unsigned int rank = __popc(peers & ((1u << lane) - 1u));
-		bool leader = valid && lane == (unsigned)(__ffs(peers) - 1);
-		if (leader)
-			wcnt[w][d] = __popc(peers);
-		__syncthreads();
-		{
-			// counts to first slots, in warp order; entries without elements stay zero
-			unsigned int run = base[t];
+	// rank within the warp: the digit's count before this element among the warp's elements
+	constexpr int kSteps = kSortWarpSpan / 32;
+	unsigned int kr[kSteps], rr[kSteps];
+	const size_t w0 = tile0 + (size_t)w * kSortWarpSpan + lane;
 #pragma unroll
-			for (int q = 0; q < kSortThreads / 32; ++q)
-			{
-				unsigned int c = wcnt[q][t];
-				if (c)
-					wcnt[q][t] = run;
-				run += c;
-			}
-			base[t] = run;
-		}
-		__syncthreads();
-		unsigned int lp = valid ? wcnt[w][d] + rank : 0u;
-		__syncwarp();
-		if (leader)
-			wcnt[w][d] = 0; // only this warp's lanes read it
-		if (valid)
+	for (int j = 0; j < kSteps; ++j)
+	{
+		const size_t i = w0 + (size_t)j * 32;
+		kr[j] = i < n ? __ldg(kin + i) : 0u;
+	}
+#pragma unroll
+	for (int j = 0; j < kSteps; ++j)
+	{
+		const bool valid = w0 + (size_t)j * 32 < n;
+		const unsigned int d = valid ? ((kr[j] >> shift) & 0xFFu) : (0x100u + lane);
+		const unsigned int peers = __match_any_sync(0xffffffffu, d);
+		const unsigned int leader = __ffs(peers) - 1;
+		unsigned int before = 0;
+		if (valid && lane == leader)
 		{
-			sk[lp] = k;
-			sv[lp] = v;
+			before = wcnt[w][d];
+			wcnt[w][d] = before + __popc(peers);
+		}
+		before = __shfl_sync(0xffffffffu, before, leader);
+		rr[j] = before + __popc(peers & ((1u << lane) - 1u));
+		__syncwarp();
+	}
+	__syncthreads();
+	{
+		// warp counts of digit t to offsets within the digit, in warp order
+		unsigned int run = 0;
+#pragma unroll
+		for (int q = 0; q < kSortWarps; ++q)
+		{
+			const unsigned int c = wcnt[q][t];
+			wcnt[q][t] = run;
+			run += c;
+		}
+	}
+	__syncthreads();
+	// the values are loaded only now (fewer registers live through the ranking)
+#pragma unroll
+	for (int j = 0; j < kSteps; ++j)
+	{
+		const size_t i = w0 + (size_t)j * 32;
+		if (i < n)
+		{
+			const unsigned int d = (kr[j] >> shift) & 0xFFu;
+			const unsigned int lp = lbase[d] + wcnt[w][d] + rr[j];
+			sk[lp] = kr[j];
+			sv[lp] = vin ? __ldg(vin + i) : (unsigned int)i;
 		}
 	}
 	__syncthreads();

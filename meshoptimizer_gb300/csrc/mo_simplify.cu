@@ -1087,8 +1087,7 @@ __global__ void __launch_bounds__(kThreads) kPickCount(const unsigned int* __res
 // prefix is its block's scanned count plus the block-local prefix
 __global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap,
     const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
-    const unsigned int* __restrict__ boffs, Scalars* sc, unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr,
-    const PassLive* lv)
+    const unsigned int* __restrict__ boffs, Scalars* sc, uint4* __restrict__ crec, const PassLive* lv)
 {
 	__shared__ unsigned int sm[kThreads / 32 + 1];
 	if (lv)
@@ -1125,21 +1124,20 @@ __global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __rest
 #pragma unroll
 	for (int e = 0; e < 3; ++e)
 		if (ok[e])
-		{
-			cv0[o] = v0[e];
-			cv1[o] = v1[e];
-			cerr[o] = bd[e];
-			o++;
-		}
+			crec[o++] = make_uint4(v0[e], v1[e], bd[e], 0u);
 }
 
 // ---------------------------------------------------------------- pass: rank
 
-// rankEdgeCollapses :1374-1450, one candidate per thread; also writes the 12-bit sort key
-__global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int* __restrict__ cv1, unsigned int* __restrict__ cerr,
-    unsigned int* __restrict__ ckey, const float4* __restrict__ pos, const Quadric* __restrict__ vq, const unsigned int* __restrict__ remap,
-    const unsigned int* __restrict__ wedge, const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop,
-    const unsigned int* __restrict__ loopback, const float* __restrict__ attr, const Quadric* __restrict__ aq, const float4* __restrict__ ag, int ac,
+// rankEdgeCollapses :1374-1450, one candidate per thread. The candidate {v0, v1, bidi} becomes,
+// in place, {i0, i1, error bits, kind of i0} with the cheaper direction first; its decision
+// record {r0, r1, begin and end of r0's adjacency} and the 12-bit sort key are written beside
+// it. These vertex gathers run here, in candidate (triangle) order, where neighbouring
+// candidates share vertices, rather than after the sort.
+__global__ void kRank(size_t count, uint4* __restrict__ crec, uint4* __restrict__ cring, unsigned int* __restrict__ ckey,
+    const float4* __restrict__ pos, const Quadric* __restrict__ vq, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge,
+    const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
+    const unsigned int* __restrict__ adj_off, const float* __restrict__ attr, const Quadric* __restrict__ aq, const float4* __restrict__ ag, int ac,
     const PassLive* lv)
 {
 	if (lv)
@@ -1151,12 +1149,14 @@ __global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int
 	size_t c = gtid();
 	if (c >= count)
 		return;
-	unsigned int i0 = cv0[c], i1 = cv1[c];
-	bool bidi = cerr[c] != 0;
+	const uint4 cand = crec[c];
+	const unsigned int i0 = cand.x, i1 = cand.y;
+	const bool bidi = cand.z != 0;
+	const unsigned int ra = remap[i0], rb = remap[i1];
 	V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1);
 
-	float ei = qerror(ldquadric(vq, remap[i0]), p1);
-	float ej = bidi ? qerror(ldquadric(vq, remap[i1]), p0) : FLT_MAX;
+	float ei = qerror(ldquadric(vq, ra), p1);
+	float ej = bidi ? qerror(ldquadric(vq, rb), p0) : FLT_MAX;
 
 	if (ac)
 	{
@@ -1189,21 +1189,21 @@ __global__ void kRank(size_t count, unsigned int* __restrict__ cv0, unsigned int
 		}
 	}
 
-	bool rev = bidi & (ej < ei);
-	cv0[c] = rev ? i1 : i0;
-	cv1[c] = rev ? i0 : i1;
+	const bool rev = bidi & (ej < ei);
+	const unsigned int s0 = rev ? i1 : i0, s1 = rev ? i0 : i1;
+	const unsigned int r0 = rev ? rb : ra, r1 = rev ? ra : rb;
 	float err = ej < ei ? ej : ei;
 	unsigned int bits = __float_as_uint(err);
-	cerr[c] = bits;
+	crec[c] = make_uint4(s0, s1, bits, kind[s0]);
+	cring[c] = make_uint4(r0, r1, adj_off[r0], adj_off[r0 + 1]);
 	ckey[c] = sortKey(bits);
 }
 
-// sorted record: {r0, r1, begin and end of r0's adjacency} for the decision rounds, the raw
-// endpoints {i0, i1} for commits, plus error bits and source kind
-__global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ order, const unsigned int* __restrict__ cv0, const unsigned int* __restrict__ cv1,
-    const unsigned int* __restrict__ cerr, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
-    const unsigned int* __restrict__ adj_off, uint4* __restrict__ srec, uint2* __restrict__ sidx, unsigned int* __restrict__ serr,
-    unsigned char* __restrict__ skind, unsigned char* __restrict__ status, const PassLive* lv)
+// the ranked candidates in sorted order: the decision record {r0, r1, adjacency range of r0}
+// for the rounds, the raw endpoints {i0, i1} for commits, the error bits and the source kind
+__global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ order, const uint4* __restrict__ crec, const uint4* __restrict__ cring,
+    uint4* __restrict__ srec, uint2* __restrict__ sidx, unsigned int* __restrict__ serr, unsigned char* __restrict__ skind,
+    unsigned char* __restrict__ status, const PassLive* lv)
 {
 	if (lv)
 	{
@@ -1214,13 +1214,12 @@ __global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ ord
 	size_t k = gtid();
 	if (k >= count)
 		return;
-	unsigned int c = order[k];
-	unsigned int i0 = cv0[c], i1 = cv1[c];
-	unsigned int r0 = remap[i0];
-	srec[k] = make_uint4(r0, remap[i1], adj_off[r0], adj_off[r0 + 1]);
-	sidx[k] = make_uint2(i0, i1);
-	serr[k] = cerr[c];
-	skind[k] = kind[i0];
+	const unsigned int c = order[k];
+	const uint4 a = crec[c];
+	srec[k] = cring[c];
+	sidx[k] = make_uint2(a.x, a.y);
+	serr[k] = a.z;
+	skind[k] = (unsigned char)a.w;
 	status[k] = kUndecided;
 }
 
@@ -2663,7 +2662,8 @@ struct Work
 	unsigned int *res0, *res1;
 	unsigned int *adj_off, *fill;
 	uint2* adj;
-	unsigned int *cv0, *cv1, *cerr, *ckey;
+	uint4 *crec, *cring; // candidates (pick, then rank in place) and their decision records
+	unsigned int* ckey;
 	uint4* srec;
 	uint2* sidx;
 	unsigned int* serr;
@@ -2746,9 +2746,8 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = f
 	w.adj_off = c.take<unsigned int>(Vp + 1);
 	w.fill = c.take<unsigned int>(Vp);
 	w.adj = c.take<uint2>(I + 1);
-	w.cv0 = c.take<unsigned int>(big);
-	w.cv1 = c.take<unsigned int>(cap);
-	w.cerr = c.take<unsigned int>(cap);
+	w.crec = c.take<uint4>(big);
+	w.cring = c.take<uint4>(cap);
 	w.ckey = c.take<unsigned int>(big);
 	w.srec = c.take<uint4>(cap);
 	w.sidx = c.take<uint2>(cap);
@@ -3076,7 +3075,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		// rebuild the dup flags (the scan consumed them) into cnt, then compact
 		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.cnt);
 		MO_LAUNCH(kCompactFlagged, gV, kThreads, 0, stream, w.cnt, w.flags, w.remap, V, w.keys_b, w.vals_b);
-		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.ckey, w.cv0, D, bitsFor(V), w.scratch, stream, nullptr, ss);
+		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.ckey, reinterpret_cast<unsigned int*>(w.crec), D, bitsFor(V), w.scratch, stream, nullptr, ss);
 		MO_LAUNCH(kWedgeLink, gridFor(D, kThreads), kThreads, 0, stream, w.keys_a, w.vals_a, D, w.wedge);
 	}
 
@@ -3360,13 +3359,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
 				scanExclusive(w.tcnt, w.tcnt, gT0, &w.sc->pick_total, w.scratch, cs, ss);
 				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
-				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, lv);
+				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.crec, lv);
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
-				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
-				    w.attr, w.aq, w.ag, ac, lv);
+				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+				    w.adj_off, w.attr, w.aq, w.ag, ac, lv);
 				radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count, ss);
-				MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr,
-				    w.skind, w.status, lv);
+				MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.crec, w.cring, w.srec, w.sidx, w.serr, w.skind, w.status, lv);
 				PerformArgs pa;
 				pa.count = 0;
 				pa.srec = w.srec;
@@ -3471,7 +3469,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, nullptr);
 		scanExclusive(w.tcnt, w.tcnt, gT, &w.sc->pick_total, w.scratch, stream, ss);
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, stream));
-		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.cv0, w.cv1, w.cerr, nullptr);
+		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.crec, nullptr);
 		readScalars();
 		const size_t C = std::min<size_t>(hs->pick_total, hs->pick_trunc);
 		if (timed)
@@ -3481,13 +3479,12 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		const unsigned int gC = gridFor(C, kThreads);
 
 		// rank + sort
-		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.cv0, w.cv1, w.cerr, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback, w.attr, w.aq,
-		    w.ag, ac, nullptr);
+		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.crec, w.cring, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback, w.adj_off,
+		    w.attr, w.aq, w.ag, ac, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
 		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream, nullptr, ss);
-		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.cv0, w.cv1, w.cerr, w.remap, w.kind, w.adj_off, w.srec, w.sidx, w.serr, w.skind,
-		    w.status, nullptr);
+		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.crec, w.cring, w.srec, w.sidx, w.serr, w.skind, w.status, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
