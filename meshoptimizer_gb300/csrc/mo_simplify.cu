@@ -995,8 +995,30 @@ __global__ void kCapacity(size_t index_count, Scalars* sc)
 
 // ---------------------------------------------------------------- pass: adjacency
 
+// corners per vertex of the current index buffer, welded by remap; each corner keeps the count
+// before it as its slot in its vertex's list, so the fill below needs no atomics. lv: the live
+// pass's buffer and count, and the slots go to its next buffer (free until the compaction)
+__global__ void kCountCorners(const unsigned int* __restrict__ res, size_t n, const unsigned int* __restrict__ remap, unsigned int* __restrict__ cnt,
+    unsigned int* __restrict__ slot, const PassLive* lv)
+{
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		res = lv->res;
+		n = lv->indices;
+		slot = lv->res_next;
+	}
+	size_t i = gtid();
+	if (i >= n)
+		return;
+	slot[i] = atomicAdd(&cnt[remap[res[i]]], 1u);
+}
+
+// half-edges {next, prev} of every vertex in its list (the order within a list is arbitrary: the
+// flip test and the one-ring checks do not depend on it)
 __global__ void kAdjFill(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ off,
-    unsigned int* __restrict__ fill, uint2* __restrict__ adj, const PassLive* lv)
+    const unsigned int* __restrict__ slot, uint2* __restrict__ adj, const PassLive* lv)
 {
 	if (lv)
 	{
@@ -1004,17 +1026,15 @@ __global__ void kAdjFill(const unsigned int* __restrict__ res, size_t tris, cons
 			return;
 		res = lv->res;
 		tris = lv->tris;
+		slot = lv->res_next;
 	}
 	size_t t = gtid();
 	if (t >= tris)
 		return;
-	unsigned int v[3] = {remap[res[t * 3 + 0]], remap[res[t * 3 + 1]], remap[res[t * 3 + 2]]};
+	const unsigned int v[3] = {remap[res[t * 3 + 0]], remap[res[t * 3 + 1]], remap[res[t * 3 + 2]]};
 #pragma unroll
 	for (int c = 0; c < 3; ++c)
-	{
-		unsigned int s = off[v[c]] + atomicAdd(&fill[v[c]], 1u);
-		adj[s] = make_uint2(v[c == 2 ? 0 : c + 1], v[c == 0 ? 2 : c - 1]);
-	}
+		adj[off[v[c]] + slot[t * 3 + c]] = make_uint2(v[c == 2 ? 0 : c + 1], v[c == 0 ? 2 : c - 1]);
 }
 
 // ---------------------------------------------------------------- pass: pick
@@ -3352,10 +3372,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			{
 				const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads), gC = gridFor(capn, kThreads);
 				MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, cs));
-				MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, cs));
-				MO_LAUNCH(kCountKeys, gI, kThreads, 0, cs, nullptr, w.remap, I, w.cnt, lv);
+				MO_LAUNCH(kCountCorners, gI, kThreads, 0, cs, nullptr, I, w.remap, w.cnt, nullptr, lv);
 				scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs, ss);
-				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, w.fill, w.adj, lv);
+				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, nullptr, w.adj, lv);
 				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
 				scanExclusive(w.tcnt, w.tcnt, gT0, &w.sc->pick_total, w.scratch, cs, ss);
 				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
@@ -3458,10 +3477,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 
 		// adjacency of the current result, welded by remap
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
-		MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
-		MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
+		MO_LAUNCH(kCountCorners, gridFor(result_count, kThreads), kThreads, 0, stream, res, result_count, w.remap, w.cnt, res_next, nullptr);
 		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream, ss);
-		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj, nullptr);
+		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, res_next, w.adj, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[3], stream));
 
@@ -3618,16 +3636,16 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		const size_t T = result_count / 3;
 		MO_CUDA_CHECK(cudaMemsetAsync(w.vupdate, 0, V, stream));
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
-		MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
 		MO_CUDA_CHECK(cudaMemsetAsync(w.sc->solve_pending, 0, sizeof(w.sc->solve_pending), stream));
+		unsigned int* slot = res == w.res0 ? w.res1 : w.res0; // the index buffer the result is not in
 		if (result_count)
 		{
 			MO_LAUNCH(kMarkUpdate, gridFor(result_count, kThreads), kThreads, 0, stream, res, result_count, w.remap, w.vupdate);
-			MO_LAUNCH(kCountKeys, gridFor(result_count, kThreads), kThreads, 0, stream, res, w.remap, result_count, w.cnt);
+			MO_LAUNCH(kCountCorners, gridFor(result_count, kThreads), kThreads, 0, stream, res, result_count, w.remap, w.cnt, slot, nullptr);
 		}
 		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream, ss);
 		if (T)
-			MO_LAUNCH(kAdjFill, gridFor(T, kThreads), kThreads, 0, stream, res, T, w.remap, w.adj_off, w.fill, w.adj, nullptr);
+			MO_LAUNCH(kAdjFill, gridFor(T, kThreads), kThreads, 0, stream, res, T, w.remap, w.adj_off, slot, w.adj, nullptr);
 		MO_CUDA_CHECK(cudaMemcpyAsync(w.pos_new, w.pos, V * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
 		const unsigned int gV = gridFor(V, kThreads);
 		MO_LAUNCH(kSolveList, gV, kThreads, 0, stream, V, w.vupdate, w.remap, w.kind, w.sdone, w.slist1, &w.sc->solve_pending[1]);
