@@ -366,24 +366,25 @@ __global__ void kCompactFlagged(const unsigned int* __restrict__ flags, const un
 
 // ---------------------------------------------------------------- setup: CSR
 
-// lv (device-resident pass loop, else nullptr): the index buffer and count come from it
+// slot (optional): each element keeps the count before it, its place in its key's list.
+// bad (optional): keys of vcount or more are not counted and set it (the index validation)
 __global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ cnt,
-    const PassLive* lv = nullptr)
+    unsigned int* __restrict__ slot = nullptr, size_t vcount = 0, unsigned int* bad = nullptr)
 {
-	if (lv)
-	{
-		if (lv->stop)
-			return;
-		idx = lv->res;
-		n = lv->indices;
-	}
 	size_t i = gtid();
 	if (i >= n)
 		return;
 	unsigned int v = idx[i];
+	if (bad && v >= vcount)
+	{
+		atomicOr(bad, 1u);
+		return;
+	}
 	if (remap)
 		v = remap[v];
-	atomicAdd(&cnt[v], 1u);
+	const unsigned int before = atomicAdd(&cnt[v], 1u);
+	if (slot)
+		slot[i] = before;
 }
 
 // the largest count of corners[v] = off[v+1] - off[v]
@@ -407,10 +408,11 @@ __global__ void kMaxDegree(const unsigned int* __restrict__ off, size_t n, unsig
 	}
 }
 
-// vertex -> corner lists: every corner into its vertex's range (arbitrary order within it), then
-// each range sorted by corner index, which is the order a stable sort by vertex gives
+// vertex -> corner lists: every corner into its vertex's range at the slot its count gave it
+// (arbitrary order within the range), then each range sorted by corner index, which is the
+// order a stable sort by vertex gives
 __global__ void kCornerFill(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, const unsigned int* __restrict__ off,
-    unsigned int* fill, unsigned int* __restrict__ csr)
+    const unsigned int* __restrict__ slot, unsigned int* __restrict__ csr)
 {
 	size_t p = gtid();
 	if (p >= n)
@@ -418,7 +420,7 @@ __global__ void kCornerFill(const unsigned int* __restrict__ idx, const unsigned
 	unsigned int v = idx[p];
 	if (remap)
 		v = remap[v];
-	csr[off[v] + atomicAdd(&fill[v], 1u)] = (unsigned int)p;
+	csr[off[v] + slot[p]] = (unsigned int)p;
 }
 
 // insertion sort of each vertex's corners (only used when no vertex has more than
@@ -3054,8 +3056,6 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 
 	// ---- setup
 	const unsigned int gV = gridFor(V, kThreads), gI = gridFor(I, kThreads);
-	if (I)
-		MO_LAUNCH(kValidateIndices, gI, kThreads, 0, stream, w.res0, I, V, &w.sc->bad_index);
 	if (V)
 		MO_LAUNCH(kGatherPositions, gV, kThreads, 0, stream, m.positions, m.positions_stride / 4, V, w.pos_raw);
 
@@ -3070,13 +3070,18 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// vertex -> corner lists in corner order: raw (classification, attribute quadrics) and
 	// remapped (position quadrics). Their offsets and largest degrees come before the host read
 	// below, which decides how the lists are filled.
+	// each corner's slot in its lists: raw in res1, remapped in serr (both free until the passes)
+	unsigned int* const slot_raw = w.res1;
+	unsigned int* const slot_rm = w.serr;
 	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
+	// the counts also validate the indices (the first kernels that read them); the host read
+	// below reports a bad index before anything else uses the lists
 	if (I)
-		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt);
+		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt, slot_raw, V, &w.sc->bad_index);
 	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream, ss);
 	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 	if (I)
-		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt);
+		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt, slot_rm, V, &w.sc->bad_index);
 	scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream, ss);
 	if (V)
 	{
@@ -3105,13 +3110,11 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		// few corners per vertex: fill and sort each list in place
 		if (I && V)
 		{
-			MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
-			MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, nullptr, I, w.off_raw, w.fill, w.csr_raw);
+			MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, nullptr, I, w.off_raw, slot_raw, w.csr_raw);
 			MO_LAUNCH(kCornerSort, gV, kThreads, 0, stream, w.off_raw, V, w.csr_raw);
 			if (D)
 			{
-				MO_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, V * 4, stream));
-				MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, w.remap, I, w.off_rm, w.fill, w.csr_rm);
+				MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, w.remap, I, w.off_rm, slot_rm, w.csr_rm);
 				MO_LAUNCH(kCornerSort, gV, kThreads, 0, stream, w.off_rm, V, w.csr_rm);
 			}
 		}
