@@ -973,11 +973,14 @@ __global__ void kFillAttributeQuadrics(const unsigned int* __restrict__ idx, con
 			ag[(size_t)v * count + k] = G[k];
 }
 
-// boundEdgeCollapses :1292-1308 numerator: sum of degrees of manifold and seam vertices
-__global__ void kDualCount(const unsigned int* __restrict__ off, const unsigned char* __restrict__ kind, size_t n, unsigned long long* dual)
+// boundEdgeCollapses :1292-1308 numerator: sum of degrees of manifold and seam vertices (one
+// global add per block: the adds all go to one address)
+__global__ void __launch_bounds__(kThreads) kDualCount(const unsigned int* __restrict__ off, const unsigned char* __restrict__ kind, size_t n,
+    unsigned long long* dual)
 {
+	__shared__ unsigned int wsum[kThreads / 32];
 	size_t i = gtid();
-	unsigned long long d = 0;
+	unsigned int d = 0;
 	if (i < n)
 	{
 		unsigned char k = kind[i];
@@ -985,8 +988,17 @@ __global__ void kDualCount(const unsigned int* __restrict__ off, const unsigned 
 	}
 	for (int o = 16; o > 0; o >>= 1)
 		d += __shfl_down_sync(0xffffffffu, d, o);
-	if ((threadIdx.x & 31) == 0 && d)
-		atomicAdd(dual, d);
+	if ((threadIdx.x & 31) == 0)
+		wsum[threadIdx.x >> 5] = d;
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		unsigned long long b = 0;
+		for (int q = 0; q < kThreads / 32; ++q)
+			b += wsum[q];
+		if (b)
+			atomicAdd(dual, b);
+	}
 }
 
 __global__ void kCapacity(size_t index_count, Scalars* sc)
@@ -1071,12 +1083,29 @@ __device__ __forceinline__ bool pickEdge(unsigned int i0, unsigned int i1, const
 	return true;
 }
 
-// candidates per block of kThreads triangles (the scan runs over blocks, not triangles). lv:
-// counts of the live pass; the grid covers the first pass's triangles and blocks past the live
-// count write zero, so the scan over the full range is the scan of the live one
+// a triangle's picked edges as 3 bits each (bit 0: a candidate, bit 1: bidirectional, bit 2:
+// from the edge's second vertex), so the emit needs no vertex gathers
+__device__ __forceinline__ unsigned int pickCode(const unsigned int a[3], const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind,
+    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback)
+{
+	unsigned int code = 0;
+#pragma unroll
+	for (int e = 0; e < 3; ++e)
+	{
+		unsigned int v0, v1, bd;
+		if (pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0, v1, bd))
+			code |= (1u | (bd << 1) | ((v0 != a[e]) << 2)) << (3 * e);
+	}
+	return code;
+}
+
+// candidates per block of kThreads triangles (the scan runs over blocks, not triangles) and
+// each triangle's pick code. lv: counts of the live pass; the grid covers the first pass's
+// triangles and blocks past the live count write zero, so the scan over the full range is the
+// scan of the live one
 __global__ void __launch_bounds__(kThreads) kPickCount(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap,
     const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
-    unsigned int* __restrict__ bcnt, const PassLive* lv)
+    unsigned int* __restrict__ bcnt, unsigned short* __restrict__ codes, const PassLive* lv)
 {
 	__shared__ unsigned int sm[kThreads / 32 + 1];
 	if (lv)
@@ -1091,12 +1120,9 @@ __global__ void __launch_bounds__(kThreads) kPickCount(const unsigned int* __res
 	if (t < tris)
 	{
 		const unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
-#pragma unroll
-		for (int e = 0; e < 3; ++e)
-		{
-			unsigned int v0, v1, bd;
-			c += pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0, v1, bd);
-		}
+		const unsigned int code = pickCode(a, remap, kind, loop, loopback);
+		codes[t] = (unsigned short)code;
+		c = __popc(code & 0x49u);
 	}
 	unsigned int total;
 	blockExclusiveScan<kThreads>(c, sm, &total);
@@ -1107,8 +1133,7 @@ __global__ void __launch_bounds__(kThreads) kPickCount(const unsigned int* __res
 // emits the candidates of every triangle whose prefix leaves room for three more
 // (the capacity check at :1319-1320 stops at the first triangle that does not); a triangle's
 // prefix is its block's scanned count plus the block-local prefix
-__global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap,
-    const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
+__global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __restrict__ res, size_t tris, const unsigned short* __restrict__ codes,
     const unsigned int* __restrict__ boffs, Scalars* sc, uint4* __restrict__ crec, const PassLive* lv)
 {
 	__shared__ unsigned int sm[kThreads / 32 + 1];
@@ -1120,21 +1145,9 @@ __global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __rest
 		tris = lv->tris;
 	}
 	const size_t t = gtid();
-	unsigned int v0[3], v1[3], bd[3];
-	bool ok[3] = {false, false, false};
-	unsigned int c = 0;
-	if (t < tris)
-	{
-		const unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
-#pragma unroll
-		for (int e = 0; e < 3; ++e)
-		{
-			ok[e] = pickEdge(a[e], a[e == 2 ? 0 : e + 1], remap, kind, loop, loopback, v0[e], v1[e], bd[e]);
-			c += ok[e];
-		}
-	}
+	const unsigned int code = t < tris ? codes[t] : 0u;
 	unsigned int total;
-	const unsigned int pre = blockExclusiveScan<kThreads>(c, sm, &total);
+	const unsigned int pre = blockExclusiveScan<kThreads>(__popc(code & 0x49u), sm, &total);
 	if (t >= tris)
 		return;
 	unsigned int o = boffs[blockIdx.x] + pre;
@@ -1143,10 +1156,17 @@ __global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __rest
 		atomicMin(&sc->pick_trunc, o);
 		return;
 	}
+	const unsigned int a[3] = {res[t * 3 + 0], res[t * 3 + 1], res[t * 3 + 2]};
 #pragma unroll
 	for (int e = 0; e < 3; ++e)
-		if (ok[e])
-			crec[o++] = make_uint4(v0[e], v1[e], bd[e], 0u);
+	{
+		const unsigned int f = (code >> (3 * e)) & 7u;
+		if (f & 1u)
+		{
+			const unsigned int x = a[e], y = a[e == 2 ? 0 : e + 1];
+			crec[o++] = (f & 4u) ? make_uint4(y, x, 0u, 0u) : make_uint4(x, y, (f >> 1) & 1u, 0u);
+		}
+	}
 }
 
 // ---------------------------------------------------------------- pass: rank
@@ -3034,6 +3054,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// scans and sorts of this run: one cooperative launch per scan (the run's stream is the only
 	// one that uses these words)
 	const ScanSync ss{w.sc->scan_bar, &w.sc->scan_error};
+	// per-triangle pick codes live in the decision-record array, which rank fills only after the pick
+	unsigned short* const pick_codes = reinterpret_cast<unsigned short*>(w.cring);
 
 	cudaEvent_t ev[16];
 	bool timed = times != nullptr;
@@ -3378,10 +3400,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				MO_LAUNCH(kCountCorners, gI, kThreads, 0, cs, nullptr, I, w.remap, w.cnt, nullptr, lv);
 				scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs, ss);
 				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, nullptr, w.adj, lv);
-				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, lv);
+				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, pick_codes, lv);
 				scanExclusive(w.tcnt, w.tcnt, gT0, &w.sc->pick_total, w.scratch, cs, ss);
 				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
-				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.crec, lv);
+				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, pick_codes, w.tcnt, w.sc, w.crec, lv);
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
 				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 				    w.adj_off, w.attr, w.aq, w.ag, ac, lv);
@@ -3487,10 +3509,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			MO_CUDA_CHECK(cudaEventRecord(ev[3], stream));
 
 		// pick
-		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, nullptr);
+		MO_LAUNCH(kPickCount, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, pick_codes, nullptr);
 		scanExclusive(w.tcnt, w.tcnt, gT, &w.sc->pick_total, w.scratch, stream, ss);
 		MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, stream));
-		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, w.remap, w.kind, w.loop, w.loopback, w.tcnt, w.sc, w.crec, nullptr);
+		MO_LAUNCH(kPickEmit, gT, kThreads, 0, stream, res, T, pick_codes, w.tcnt, w.sc, w.crec, nullptr);
 		readScalars();
 		const size_t C = std::min<size_t>(hs->pick_total, hs->pick_trunc);
 		if (timed)
