@@ -366,25 +366,34 @@ __global__ void kCompactFlagged(const unsigned int* __restrict__ flags, const un
 
 // ---------------------------------------------------------------- setup: CSR
 
-// slot (optional): each element keeps the count before it, its place in its key's list.
-// bad (optional): keys of vcount or more are not counted and set it (the index validation)
-__global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ cnt,
-    unsigned int* __restrict__ slot = nullptr, size_t vcount = 0, unsigned int* bad = nullptr)
+__global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ cnt)
 {
 	size_t i = gtid();
 	if (i >= n)
 		return;
 	unsigned int v = idx[i];
-	if (bad && v >= vcount)
+	if (remap)
+		v = remap[v];
+	atomicAdd(&cnt[v], 1u);
+}
+
+// the corners of every vertex, raw and welded by remap, each corner keeping its slot in both
+// lists; an index of vcount or more is not counted and sets bad
+__global__ void kCountCornerLists(const unsigned int* __restrict__ idx, size_t n, const unsigned int* __restrict__ remap, size_t vcount,
+    unsigned int* __restrict__ cnt_raw, unsigned int* __restrict__ cnt_rm, unsigned int* __restrict__ slot_raw, unsigned int* __restrict__ slot_rm,
+    unsigned int* bad)
+{
+	size_t i = gtid();
+	if (i >= n)
+		return;
+	const unsigned int v = idx[i];
+	if (v >= vcount)
 	{
 		atomicOr(bad, 1u);
 		return;
 	}
-	if (remap)
-		v = remap[v];
-	const unsigned int before = atomicAdd(&cnt[v], 1u);
-	if (slot)
-		slot[i] = before;
+	slot_raw[i] = atomicAdd(&cnt_raw[v], 1u);
+	slot_rm[i] = atomicAdd(&cnt_rm[remap[v]], 1u);
 }
 
 // the largest count of corners[v] = off[v+1] - off[v]
@@ -3095,16 +3104,15 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// each corner's slot in its lists: raw in res1, remapped in serr (both free until the passes)
 	unsigned int* const slot_raw = w.res1;
 	unsigned int* const slot_rm = w.serr;
-	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
-	// the counts also validate the indices (the first kernels that read them); the host read
-	// below reports a bad index before anything else uses the lists
+	// both lists' counts in one pass over the indices, in the offset arrays themselves (scanned in
+	// place); the count also validates the indices (the first kernel that reads them), and the
+	// host read below reports a bad index before anything else uses the lists
+	MO_CUDA_CHECK(cudaMemsetAsync(w.off_raw, 0, (V + 1) * 4, stream));
+	MO_CUDA_CHECK(cudaMemsetAsync(w.off_rm, 0, (V + 1) * 4, stream));
 	if (I)
-		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, nullptr, I, w.cnt, slot_raw, V, &w.sc->bad_index);
-	scanExclusive(w.cnt, w.off_raw, V + 1, nullptr, w.scratch, stream, ss);
-	MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
-	if (I)
-		MO_LAUNCH(kCountKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cnt, slot_rm, V, &w.sc->bad_index);
-	scanExclusive(w.cnt, w.off_rm, V + 1, nullptr, w.scratch, stream, ss);
+		MO_LAUNCH(kCountCornerLists, gI, kThreads, 0, stream, w.res0, I, w.remap, V, w.off_raw, w.off_rm, slot_raw, slot_rm, &w.sc->bad_index);
+	scanExclusive(w.off_raw, w.off_raw, V + 1, nullptr, w.scratch, stream, ss);
+	scanExclusive(w.off_rm, w.off_rm, V + 1, nullptr, w.scratch, stream, ss);
 	if (V)
 	{
 		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_raw, V, &w.sc->max_degree[0]);
