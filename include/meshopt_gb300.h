@@ -235,6 +235,15 @@ MESHOPTGPU_API void meshoptgpu_setDropinBatchLimit(size_t max_index_count);
 MESHOPTGPU_API int meshoptgpu_setDeviceLoop(int enabled);
 MESHOPTGPU_API int meshoptgpu_getBatchThreads(void);
 
+/* Failure-path check of the cooperative kernels' grid barriers (no reference counterpart):
+ * launches `blocks` blocks (2 .. the resident limit) where one block never arrives at the
+ * barrier (once != 0: the single-use barrier of the one-launch scans), so the others' bounded
+ * waits run out after wait_limit polls (1 .. 2^20, about 32 ns or more each) and record the
+ * error flag the pass kernel's host reads as "grid barrier wait limit reached". *timed_out
+ * receives that flag (1 expected). Nothing faults or hangs; the context stays usable.
+ * Returns a meshoptgpu_Status* value. */
+MESHOPTGPU_API int meshoptgpu_probeBarrierWait(int once, unsigned int blocks, unsigned int wait_limit, unsigned int* timed_out);
+
 /* ---- serving: continuous batching of simplify requests ---- */
 
 typedef struct meshoptgpu_Server meshoptgpu_Server;

@@ -52,6 +52,7 @@ EXPORTS = [
     "meshoptgpu_getLastRoundTrace",
     "meshoptgpu_optimizeVertexFetchRemapDevice", "meshoptgpu_optimizeVertexFetchDevice", "meshoptgpu_generatePositionRemapDevice",
     "meshoptgpu_simplifyGroups", "meshoptgpu_buildMeshletsFlexGroups", "meshoptgpu_setDropinBatchLimit", "meshoptgpu_setDeviceLoop",
+    "meshoptgpu_probeBarrierWait",
 ]
 
 
@@ -142,6 +143,8 @@ def load():
     lib.meshoptgpu_simplifyWithUpdateDevice.argtypes = [vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp, vp]
     lib.meshoptgpu_setDeviceLoop.restype = C.c_int
     lib.meshoptgpu_setDeviceLoop.argtypes = [C.c_int]
+    lib.meshoptgpu_probeBarrierWait.restype = C.c_int
+    lib.meshoptgpu_probeBarrierWait.argtypes = [C.c_int, C.c_uint, C.c_uint, C.POINTER(C.c_uint)]
     lib.meshoptgpu_simplifyGroups.restype = C.c_int
     lib.meshoptgpu_simplifyGroups.argtypes = [vp, vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, vp, vp, vp, f32, u32, vp, vp, vp]
     lib.meshoptgpu_buildMeshletsFlexGroups.restype = C.c_int
@@ -572,6 +575,13 @@ DROPIN_BATCH_LIMIT = 15000  # the library's default
 def set_dropin_batch_limit(max_index_count=DROPIN_BATCH_LIMIT):
     """Drop-in calls on meshes with at most this many indices run on the batch kernel (0: never)."""
     load().meshoptgpu_setDropinBatchLimit(int(max_index_count))
+
+
+def probe_barrier_wait(once=False, blocks=8, wait_limit=4096):
+    """meshoptgpu_probeBarrierWait: (status, timed_out) of a grid barrier that one block never reaches."""
+    flag = C.c_uint(0)
+    st = int(load().meshoptgpu_probeBarrierWait(int(bool(once)), int(blocks), int(wait_limit), C.byref(flag)))
+    return st, int(flag.value)
 
 
 def set_device_loop(enabled=True):

@@ -1574,6 +1574,25 @@ int meshoptgpu_setDeviceLoop(int enabled)
 	}
 }
 
+int meshoptgpu_probeBarrierWait(int once, unsigned int blocks, unsigned int wait_limit, unsigned int* timed_out)
+{
+	try
+	{
+		ThreadState& s = state();
+		s.ensure();
+		if (blocks < 2 || blocks > coopScanCapacity() || wait_limit == 0 || wait_limit > (1u << 20) || !timed_out)
+			throw std::invalid_argument("probeBarrierWait: blocks must be 2..resident blocks, wait_limit 1..2^20, timed_out non-null");
+		*timed_out = probeBarrierWait(once, blocks, wait_limit, s.stream);
+		setStatus(meshoptgpu_StatusOk, "");
+		return meshoptgpu_StatusOk;
+	}
+	catch (const std::exception& e)
+	{
+		setStatus(statusOf(e), e.what());
+		return statusOf(e);
+	}
+}
+
 int meshoptgpu_getBatchThreads(void)
 {
 	ThreadState& s = state();

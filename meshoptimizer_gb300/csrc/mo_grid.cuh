@@ -16,7 +16,7 @@ constexpr unsigned int kBarrierSpinLimit = 1u << 25; // x >= 32 ns sleep: second
 // when the count reaches (i + 1) * gridDim.x: no block can arrive at barrier i + 1 before every
 // block has arrived at barrier i, so an arrival that reads old = n belongs to barrier n / G.
 // Waiting blocks poll the count itself, so the last arrival releases them with its own add.
-__device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err)
+__device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err, unsigned int limit = kBarrierSpinLimit)
 {
 	__syncthreads();
 	if (threadIdx.x == 0)
@@ -28,7 +28,7 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 		unsigned int spins = 0;
 		while ((int)(*count - target) < 0)
 		{
-			if (++spins > kBarrierSpinLimit)
+			if (++spins > limit)
 			{
 				atomicOr(err, 1u);
 				break;
@@ -43,7 +43,7 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 // A grid barrier that a cooperative launch passes once, leaving its two words zero for the next
 // launch: bar[0] counts arrivals, bar[1] departures, and the last block to depart clears both
 // (by then no block polls bar[0] any more).
-__device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int* err)
+__device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int* err, unsigned int limit = kBarrierSpinLimit)
 {
 	__syncthreads();
 	if (threadIdx.x == 0)
@@ -54,7 +54,7 @@ __device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int*
 		unsigned int spins = 0;
 		while (*count < gridDim.x)
 		{
-			if (++spins > kBarrierSpinLimit)
+			if (++spins > limit)
 			{
 				atomicOr(err, 1u);
 				break;

@@ -300,6 +300,42 @@ __global__ void __launch_bounds__(kSortThreads, 3) kRadixScatter(const unsigned 
 
 } // namespace
 
+// The bounded waits of both grid barriers, made to run out: block 0 never arrives, so every
+// other block waits `limit` times, records the error and leaves. Nothing faults or hangs.
+__global__ void kBarrierWaitProbe(unsigned int* words, unsigned int limit, int once)
+{
+	if (blockIdx.x == 0)
+		return;
+	if (once)
+		gridBarrierOnce(words, words + 2, limit);
+	else
+		gridBarrier(words, words + 2, limit);
+}
+
+unsigned int probeBarrierWait(int once, unsigned int blocks, unsigned int limit, cudaStream_t stream)
+{
+	unsigned int* words = nullptr;
+	MO_CUDA_CHECK(cudaMalloc(&words, 4 * sizeof(unsigned int)));
+	unsigned int err = 0;
+	try
+	{
+		MO_CUDA_CHECK(cudaMemsetAsync(words, 0, 4 * sizeof(unsigned int), stream));
+		void* params[] = {(void*)&words, (void*)&limit, (void*)&once};
+		cudaEvent_t e0 = probeBegin("kBarrierWaitProbe", stream);
+		MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kBarrierWaitProbe, dim3(blocks), dim3(kScanThreads), params, 0, stream));
+		probeEnd(e0, stream);
+		MO_CUDA_CHECK(cudaMemcpyAsync(&err, words + 2, sizeof(err), cudaMemcpyDeviceToHost, stream));
+		MO_CUDA_CHECK(cudaStreamSynchronize(stream));
+	}
+	catch (...)
+	{
+		cudaFree(words);
+		throw;
+	}
+	MO_CUDA_CHECK(cudaFree(words));
+	return err;
+}
+
 constexpr int kMaxDevices = 64;
 constexpr unsigned int kCoopScanBlocksPerSM = 4; // at most this many per SM (occupancy permitting)
 

@@ -88,6 +88,11 @@ struct ScanSync
 	unsigned int* err = nullptr;
 };
 
+// Runs the grid barrier (once != 0: the single-use one) with one of `blocks` blocks never
+// arriving and a wait limit of `limit` polls; returns the error flag the waiting blocks set
+// (1 when the bounded wait ran out, as it must). For tests of the failure path.
+unsigned int probeBarrierWait(int once, unsigned int blocks, unsigned int limit, cudaStream_t stream);
+
 // Blocks a single-launch scan may use on the current device (all resident at once); queried
 // once per device and cached. Call it outside stream capture before the first such scan.
 unsigned int coopScanCapacity();
