@@ -146,7 +146,9 @@ void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int
 		MO_LAUNCH(kScanApply, 1, kScanThreads, 0, stream, in, out, n, nullptr, total, aligned);
 		return;
 	}
-	const unsigned int cap = sync.bar ? coopScanCapacity() : 0u;
+	unsigned int cap = sync.bar ? coopScanCapacity() : 0u;
+	if (cap && sync.max_blocks)
+		cap = std::min(cap, sync.max_blocks);
 	if (cap)
 	{
 		// consecutive tiles per block, then as few blocks as that needs

@@ -86,6 +86,8 @@ struct ScanSync
 {
 	unsigned int* bar = nullptr;
 	unsigned int* err = nullptr;
+	unsigned int max_blocks = 0; // at most this many blocks (0: as many as are resident at once), so
+	                             // concurrent callers on other streams can be resident beside it
 };
 
 // Runs the grid barrier (once != 0: the single-use one) with one of `blocks` blocks never

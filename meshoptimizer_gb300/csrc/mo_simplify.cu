@@ -3062,7 +3062,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	};
 	// scans and sorts of this run: one cooperative launch per scan (the run's stream is the only
 	// one that uses these words)
-	const ScanSync ss{w.sc->scan_bar, &w.sc->scan_error};
+	ScanSync ss;
+	ss.bar = w.sc->scan_bar;
+	ss.err = &w.sc->scan_error;
+	ss.max_blocks = tuning_.perform_grid_cap > 0 ? unsigned(tuning_.perform_grid_cap) : 0u; // the pass kernel's share of the GPU
 	// per-triangle pick codes live in the decision-record array, which rank fills only after the pick
 	unsigned short* const pick_codes = reinterpret_cast<unsigned short*>(w.cring);
 
