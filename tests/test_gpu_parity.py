@@ -273,3 +273,25 @@ def test_high_degree_fan(port):
     idx = np.array([[0, 1 + i, 1 + (i + 1) % n] for i in range(n)], np.uint32).reshape(-1)
     for opt in (0, mg.SimplifyLockBorder):
         _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.3), 1.0, opt)
+
+
+@pytest.mark.parametrize("ac", [9, 17, 32])
+def test_wide_attribute_sets(port, ac):
+    """Attribute counts past 8 and 16 (the wider quadric fill instantiations) up to the
+    reference's limit of 32 (`kMaxAttributes`, src/simplifier.cpp:665), some weights zero, on
+    the single-mesh path and on the batch kernel."""
+    rng = np.random.default_rng(ac)
+    idx, pos = W.heightfield(20, seed=ac, amp=0.05)
+    attrs = rng.random((len(pos), ac)).astype(np.float32)
+    weights = rng.choice(np.array([0.0, 0.1, 0.5, 1.0], np.float32), size=ac)
+    weights[0] = 1.0
+    target = W.target_count(len(idx), 0.2)
+    ref, ref_err = port.simplify("port", idx, pos, target, 5e-2, 0, attributes=attrs, weights=weights)
+    for limit in (0, 1 << 30):  # the pass loop, then the batch kernel (a batch of one)
+        mg.set_dropin_batch_limit(limit)
+        try:
+            out, err = mg.simplify(idx, pos, target, 5e-2, 0, attributes=attrs, weights=weights)
+        finally:
+            mg.set_dropin_batch_limit(0)
+        assert np.array_equal(out, ref), limit
+        assert close(err, ref_err)
