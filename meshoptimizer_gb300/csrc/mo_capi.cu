@@ -235,6 +235,14 @@ size_t align256(size_t v)
 	return (v + 255) & ~size_t(255);
 }
 
+// host bytes of `count` records of `stride` bytes of which the first `used` are read: the last
+// record ends after its used bytes, as the reference reads it (an interleaved array may end
+// there, and a copy of whole strides would read, or write back, past the caller's buffer)
+size_t stridedExtent(size_t count, size_t stride, size_t used)
+{
+	return count ? (count - 1) * stride + used : 0;
+}
+
 struct HostCopy
 {
 	void* dst;
@@ -311,7 +319,8 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		// large meshes on the single-mesh path: positions and attributes on their own copy
 		// streams; the setup waits for the positions at once and for the attributes where it
 		// first reads them
-		const size_t attr_bytes = d_attr ? vertex_count * vertex_attributes_stride : 0;
+		const size_t pos_bytes = stridedExtent(vertex_count, vertex_positions_stride, 12);
+		const size_t attr_bytes = d_attr ? stridedExtent(vertex_count, vertex_attributes_stride, attribute_count * 4) : 0;
 		split = attr_bytes >= (size_t(1) << 20) && index_count > s.dropin_batch_limit;
 		if (index_count)
 			MO_CUDA_CHECK(cudaMemcpyAsync(d_idx, indices, index_count * 4, cudaMemcpyHostToDevice, st));
@@ -319,7 +328,7 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		{
 			s.ensureCopyStreams();
 			if (vertex_count)
-				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, vertex_count * vertex_positions_stride, cudaMemcpyHostToDevice, s.copy_stream[0]));
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, pos_bytes, cudaMemcpyHostToDevice, s.copy_stream[0]));
 			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[0], s.copy_stream[0]));
 			MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, attr_bytes, cudaMemcpyHostToDevice, s.copy_stream[1]));
 			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[1], s.copy_stream[1]));
@@ -328,7 +337,7 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		else
 		{
 			if (vertex_count)
-				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, vertex_count * vertex_positions_stride, cudaMemcpyHostToDevice, st));
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, pos_bytes, cudaMemcpyHostToDevice, st));
 			if (d_attr)
 				MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, attr_bytes, cudaMemcpyHostToDevice, st));
 		}
@@ -392,8 +401,8 @@ size_t updateHost(unsigned int* indices, size_t index_count, float* vertex_posit
 	{
 		ThreadState& s = state();
 		s.ensure();
-		const size_t pbytes = vertex_count * vertex_positions_stride;
-		const size_t abytes = attribute_count ? vertex_count * vertex_attributes_stride : 0;
+		const size_t pbytes = stridedExtent(vertex_count, vertex_positions_stride, 12);
+		const size_t abytes = attribute_count ? stridedExtent(vertex_count, vertex_attributes_stride, attribute_count * 4) : 0;
 		const char* P = reinterpret_cast<const char*>(vertex_positions);
 		const char* A = reinterpret_cast<const char*>(vertex_attributes);
 		const bool joint = abytes && A < P + pbytes && P < A + abytes;
@@ -1052,8 +1061,9 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		{
 			const meshoptgpu_BatchMesh& m = meshes[i];
 			off_idx[i] = place(m.indices, m.index_count * 4, false);
-			off_pos[i] = place(m.vertex_positions, m.vertex_count * m.vertex_positions_stride, true);
-			off_attr[i] = m.attribute_count ? place(m.vertex_attributes, m.vertex_count * m.vertex_attributes_stride, true) : ~size_t(0);
+			off_pos[i] = place(m.vertex_positions, stridedExtent(m.vertex_count, m.vertex_positions_stride, 12), true);
+			off_attr[i] = m.attribute_count ? place(m.vertex_attributes, stridedExtent(m.vertex_count, m.vertex_attributes_stride, m.attribute_count * 4), true)
+			                                : ~size_t(0);
 			off_lock[i] = place(m.vertex_lock, m.vertex_count, true);
 			off_out[i] = out_words;
 			out_words += m.index_count;
@@ -1639,7 +1649,7 @@ float meshopt_simplifyScale(const float* vertex_positions, size_t vertex_count, 
 		s.ensure();
 		float* d_pos = static_cast<float*>(s.inputs.ensure(align256(vertex_count * vertex_positions_stride) + 256));
 		if (vertex_count)
-			MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, vertex_count * vertex_positions_stride, cudaMemcpyHostToDevice, s.stream));
+			MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, stridedExtent(vertex_count, vertex_positions_stride, 12), cudaMemcpyHostToDevice, s.stream));
 		float r = s.simplifier->scale(d_pos, vertex_count, vertex_positions_stride, s.stream);
 		setStatus(meshoptgpu_StatusOk, "");
 		return r;

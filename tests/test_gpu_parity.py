@@ -295,3 +295,29 @@ def test_wide_attribute_sets(port, ac):
             mg.set_dropin_batch_limit(0)
         assert np.array_equal(out, ref), limit
         assert close(err, ref_err)
+
+
+@pytest.mark.parametrize("ac", [2, 5])
+def test_interleaved_vertex_buffer_max_stride(port, ac):
+    """Positions and attributes interleaved in one 256-byte vertex record (the largest stride
+    the reference accepts, src/simplifier.cpp:2349-2354), as real vertex formats lay them out:
+    positions at byte 0, attributes at byte 12, both read with stride 256."""
+    rng = np.random.default_rng(100 + ac)
+    idx, pos = W.heightfield(24, seed=ac, amp=0.05)
+    V = len(pos)
+    buf = rng.random((V, 64)).astype(np.float32)  # 64 floats = 256 bytes per vertex
+    buf[:, 0:3] = pos
+    attrs = np.ascontiguousarray(buf[:, 3:3 + ac])
+    weights = np.linspace(1.0, 0.25, ac).astype(np.float32)
+    target = W.target_count(len(idx), 0.25)
+    ref, ref_err = port.simplify("port", idx, pos, target, 2e-2, 0, attributes=attrs, weights=weights)
+    for limit in (0, 1 << 30):  # the pass loop, then the batch kernel (a batch of one)
+        mg.set_dropin_batch_limit(limit)
+        try:
+            out = np.zeros(len(idx), np.uint32)
+            n, err = mg.simplify_raw(out, idx, len(idx), buf, V, 256, target, 2e-2, 0, attributes=buf[:, 3:], attributes_stride=256,
+                                     weights=weights, attribute_count=ac)
+        finally:
+            mg.set_dropin_batch_limit(0)
+        assert np.array_equal(out[:n], ref), limit
+        assert close(err, ref_err)
