@@ -195,16 +195,17 @@ __global__ void __launch_bounds__(kSortThreads) kRadixHist(const unsigned int* _
 	hist[(size_t)threadIdx.x * tiles + blockIdx.x] = sh[threadIdx.x];
 }
 
-// Stable scatter. Warp w ranks the tile's elements w*512 .. w*512+511, 32 at a time (lane order
-// within each step, steps in order), against per-warp digit counters in shared memory; the warp
-// counters of each digit are then turned into offsets in warp order. So equal digits keep their
+// Stable scatter. Warp w ranks the tile's kSortWarpSpan consecutive elements from w*kSortWarpSpan
+// on, 32 at a time (lane order within each step, steps in order), against per-warp digit
+// counters in shared memory; the warp counters of each digit are then turned into offsets in
+// warp order. So equal digits keep their
 // input order, and the tile is put in digit order in shared memory with one block barrier per
 // phase, then written out front to back: each digit's elements of the tile leave as one
 // contiguous run (coalesced stores) at the position the digit-major scanned histogram gives.
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortWarpSpan = kSortTile / kSortWarps; // consecutive elements per warp
 
-__global__ void __launch_bounds__(kSortThreads, 3) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
+__global__ void __launch_bounds__(kSortThreads, 5) kRadixScatter(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
     unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, size_t n, const unsigned int* n_dev, int shift, const unsigned int* __restrict__ hist,
     unsigned int tiles)
 {

@@ -26,8 +26,8 @@ constexpr int kScanItems = 4;                               // one uint4 per thr
 constexpr int kScanTile = kScanThreads * kScanItems;        // 1024 elements per block
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;        // 4096 pairs per block
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;        // 2048 pairs per block
 constexpr int kSortBins = 256;
 
 __device__ __forceinline__ unsigned int laneId()
