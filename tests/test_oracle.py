@@ -166,3 +166,34 @@ def test_meshlet_optimize_port_matches_golden(port):
             assert np.array_equal(t, c[f"opt{level}_meshlet_triangles"]), (c["name"], level)
             checked += 1
     assert checked >= 100
+
+
+def test_port_matches_reference_library_fuzz(port):
+    """Where the reference library was built from its own sources (oracle/_ref, this container
+    only), the port against it on fuzzed meshes: lattice soups with duplicates and degenerate
+    triangles, every option bit, attributes with zero weights and lock flags."""
+    if not port.available("ref"):
+        pytest.skip("the reference library is built only where the reference sources are present")
+    rng = np.random.default_rng(2024)
+    bits = [1 << b for b in range(7)]  # meshoptimizer.h:469-481: LockBorder, Sparse, ErrorAbsolute, Prune, Regularize, Permissive, RegularizeLight
+    for _ in range(150):
+        V = int(rng.integers(4, 120))
+        pos = rng.integers(0, int(rng.integers(2, 9)), size=(V, 3)).astype(np.float32)
+        idx = rng.integers(0, V, size=3 * int(rng.integers(1, 200))).astype(np.uint32)
+        options = 0
+        for b in bits:
+            if rng.random() < 0.3:
+                options |= b
+        attrs = weights = lock = None
+        if rng.random() < 0.5:
+            ac = int(rng.integers(1, 5))
+            attrs = rng.random((V, ac)).astype(np.float32)
+            weights = rng.choice(np.array([0.0, 0.5, 1.0], np.float32), size=ac)
+        if rng.random() < 0.4:
+            lock = rng.choice(np.array([0, 0, 1, 2, 4, 6], np.uint8), size=V)
+        target = int(rng.integers(0, len(idx) // 3 + 1)) * 3
+        error = float(rng.choice([1e-2, 0.1, float(np.finfo(np.float32).max)]))
+        a = port.simplify("port", idx, pos, target, error, options, attributes=attrs, weights=weights, lock=lock)
+        b = port.simplify("ref", idx, pos, target, error, options, attributes=attrs, weights=weights, lock=lock)
+        assert np.array_equal(a[0], b[0]), (options, target, error)
+        assert np.float32(a[1]) == np.float32(b[1])
