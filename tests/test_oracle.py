@@ -197,3 +197,38 @@ def test_port_matches_reference_library_fuzz(port):
         b = port.simplify("ref", idx, pos, target, error, options, attributes=attrs, weights=weights, lock=lock)
         assert np.array_equal(a[0], b[0]), (options, target, error)
         assert np.float32(a[1]) == np.float32(b[1])
+
+
+def test_meshlet_port_matches_reference_fuzz():
+    """Where the reference's clusterizer was built from its sources (this container only), the
+    meshlet port against it on fuzzed groups: random subsets of a noisy heightfield and lattice
+    soups, random parameter sets within the reference's asserts, and the per-meshlet reorder."""
+    import meshlets as ML
+    from meshoptimizer_gb300 import workloads as W
+
+    if not (ML.available("port") and ML.available("reference")):
+        pytest.skip("the reference clusterizer is built only where the reference sources are present")
+    rng = np.random.default_rng(77)
+    for _ in range(40):
+        if rng.random() < 0.5:
+            idx, pos = W.heightfield(int(rng.integers(4, 40)), seed=int(rng.integers(0, 1 << 30)), amp=float(rng.uniform(0.0, 0.3)))
+            tri = idx.reshape(-1, 3)
+            idx = tri[rng.random(len(tri)) < rng.uniform(0.3, 1.0)].reshape(-1).astype(np.uint32)
+        else:
+            V = int(rng.integers(8, 200))
+            pos = rng.random((V, 3)).astype(np.float32)
+            idx = rng.integers(0, V, size=3 * int(rng.integers(1, 300))).astype(np.uint32)
+        max_v = int(rng.choice([16, 64, 128, 255]))
+        max_t = int(rng.choice([8, 64, 124, 256, 512]))
+        min_t = int(rng.integers(1, max_t + 1))
+        cone = float(rng.choice([0.0, 0.25, 0.5]))
+        split = float(rng.choice([0.0, 2.0]))
+        a = ML.build_meshlets_flex(idx, pos, max_v, min_t, max_t, cone, split, kind="port")
+        b = ML.build_meshlets_flex(idx, pos, max_v, min_t, max_t, cone, split, kind="reference")
+        for x, y in zip(a, b):
+            assert np.array_equal(np.asarray(x), np.asarray(y)), (max_v, min_t, max_t, cone, split)
+        level = int(rng.choice([0, 1, 3]))
+        oa = ML.optimize_meshlets(*a, level, kind="port")
+        ob = ML.optimize_meshlets(*b, level, kind="reference")
+        for x, y in zip(oa, ob):
+            assert np.array_equal(np.asarray(x), np.asarray(y)), ("optimize", level)
