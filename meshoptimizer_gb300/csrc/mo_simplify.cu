@@ -36,7 +36,6 @@ namespace
 constexpr int kThreads = 256;
 constexpr int kStopTile = 1024; // sorted candidates per block in the stop-rule scan
 constexpr size_t kPinnedBytes = 16384; // host readback buffer of the scalars block
-constexpr unsigned int kApplyTile = 4096; // sorted positions compacted per block step in the apply phase
 constexpr unsigned int kStageChunk = 2048; // candidates of a block taken through the decision stages at a time
 constexpr unsigned int kStageItems = 4;    // candidates per thread in the first decision stage
 
@@ -1182,10 +1181,11 @@ __global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __rest
 
 // rankEdgeCollapses :1374-1450, one candidate per thread. The candidate {v0, v1, bidi} becomes,
 // in place, {i0, i1, error bits, kind of i0} with the cheaper direction first; its decision
-// record {r0, r1, begin and end of r0's adjacency} and the 12-bit sort key are written beside
-// it. These vertex gathers run here, in candidate (triangle) order, where neighbouring
-// candidates share vertices, rather than after the sort.
-__global__ void kRank(size_t count, uint4* __restrict__ crec, uint4* __restrict__ cring, unsigned int* __restrict__ ckey,
+// record {r0, r1, begin and end of r0's adjacency}, its error bits and its kind are written
+// beside it. Candidates stay in pick (triangle) order from here on: the sort only gives each
+// its sorted position, and the decision rounds walk pick order, where neighbouring candidates
+// share vertices.
+__global__ void kRank(size_t count, uint4* __restrict__ crec, uint4* __restrict__ cring, unsigned int* __restrict__ cerr, unsigned char* __restrict__ ckind,
     const float4* __restrict__ pos, const Quadric* __restrict__ vq, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge,
     const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback,
     const unsigned int* __restrict__ adj_off, const float* __restrict__ attr, const Quadric* __restrict__ aq, const float4* __restrict__ ag, int ac,
@@ -1245,44 +1245,205 @@ __global__ void kRank(size_t count, uint4* __restrict__ crec, uint4* __restrict_
 	const unsigned int r0 = rev ? rb : ra, r1 = rev ? ra : rb;
 	float err = ej < ei ? ej : ei;
 	unsigned int bits = __float_as_uint(err);
-	crec[c] = make_uint4(s0, s1, bits, kind[s0]);
+	const unsigned char ks = kind[s0];
+	crec[c] = make_uint4(s0, s1, bits, ks);
 	cring[c] = make_uint4(r0, r1, adj_off[r0], adj_off[r0 + 1]);
-	ckey[c] = sortKey(bits);
+	cerr[c] = bits;
+	ckind[c] = ks;
 }
 
-// the ranked candidates in sorted order: the decision record {r0, r1, adjacency range of r0}
-// for the rounds, the raw endpoints {i0, i1} for commits, the error bits and the source kind
-__global__ void kGatherSorted(size_t count, const unsigned int* __restrict__ order, const uint4* __restrict__ crec, const uint4* __restrict__ cring,
-    uint4* __restrict__ srec, uint2* __restrict__ sidx, unsigned int* __restrict__ serr, unsigned char* __restrict__ skind,
-    unsigned char* __restrict__ status, const PassLive* lv)
+// ---------------------------------------------------------------- pass: sort
+//
+// sortEdgeCollapses (:1452-1496) is a stable counting sort on the 12-bit key of each candidate's
+// error (2560 bins). It runs as one here: a 2560-bin histogram per tile of candidates, one
+// exclusive scan over the bin-major histogram matrix (which gives, for every tile and bin, the
+// sorted position of the tile's first candidate with that key), and a stable scatter. The
+// scatter gives each candidate its sorted position (rank, in pick order) and writes, at that
+// position, the error bits and kind that the stop rules read in sorted order.
+constexpr unsigned int kKeyBins = 2560;
+constexpr unsigned int kKeyWarps = kThreads / 32;
+constexpr size_t kKeyScatterSmem = kKeyBins * sizeof(unsigned int) + size_t(kKeyWarps) * kKeyBins * sizeof(unsigned short);
+
+constexpr size_t kKeyTargetTiles = 4 * 152; // sort tiles wanted for the largest count: four per SM of a GB300
+
+// candidates per thread of a sort tile (8, 16, 32 or 64): the smallest that keeps the tile count
+// near kKeyTargetTiles for the largest count the sort will see (the histogram matrix, 2560 words
+// per tile, stays a few MB), with no fewer than eight per thread
+unsigned int keySortItems(size_t n)
 {
+	const size_t per_tile = (n + kKeyTargetTiles - 1) / kKeyTargetTiles;
+	unsigned int items = 8;
+	while (items < 64 && size_t(items) * kThreads < per_tile)
+		items *= 2;
+	return items;
+}
+
+unsigned int keySortTiles(size_t n, unsigned int items)
+{
+	const size_t tile = size_t(items) * kThreads;
+	return unsigned(std::max<size_t>(1, (n + tile - 1) / tile));
+}
+
+// scratch words of sortCandidates for any count up to n: the histogram matrix and its scan. A
+// count below 64 per thread has at most kKeyTargetTiles tiles (and at most one per 2048
+// candidates); one at 64 per thread has one per 16384.
+size_t keySortScratchWords(size_t n)
+{
+	const size_t tiles = std::max(std::min((n + 2047) / 2048, kKeyTargetTiles), size_t(keySortTiles(n, 64)));
+	const size_t m = std::max<size_t>(tiles, 1) * kKeyBins;
+	return ((m + 63) & ~size_t(63)) + scanScratchWords(m);
+}
+
+__global__ void __launch_bounds__(kThreads) kKeyHist(const unsigned int* __restrict__ cerr, size_t n, unsigned int items, unsigned int* __restrict__ hist,
+    unsigned int tiles, const PassLive* lv)
+{
+	__shared__ unsigned int sh[kKeyBins];
 	if (lv)
 	{
 		if (lv->stop)
 			return;
-		count = lv->count;
+		n = lv->count;
 	}
-	size_t k = gtid();
-	if (k >= count)
+	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
+		sh[b] = 0;
+	__syncthreads();
+	const size_t t0 = (size_t)blockIdx.x * items * kThreads + threadIdx.x;
+	for (unsigned int j0 = 0; j0 < items; j0 += 8)
+	{
+		unsigned int kb[8];
+#pragma unroll
+		for (unsigned int q = 0; q < 8; ++q)
+		{
+			const size_t i = t0 + (size_t)(j0 + q) * kThreads;
+			kb[q] = i < n ? sortKey(__ldg(cerr + i)) : kKeyBins;
+		}
+#pragma unroll
+		for (unsigned int q = 0; q < 8; ++q)
+			if (kb[q] < kKeyBins)
+				atomicAdd(&sh[kb[q]], 1u);
+	}
+	__syncthreads();
+	// tiles past the live count write zeros, so the scan over the whole matrix is the live one's
+	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
+		hist[(size_t)b * tiles + blockIdx.x] = sh[b];
+}
+
+// Stable scatter of one tile. Warp w takes the tile's 32 * items consecutive candidates from
+// w * 32 * items on, 32 at a time in order; equal keys among the 32 are ranked by lane
+// (match_any), against per-warp key counters. The first walk counts, the counters of each key are
+// turned into offsets in warp order, and the second walk places every candidate after the
+// earlier ones of its key: equal keys keep pick order, as the reference's counting sort keeps
+// collapse order.
+__global__ void __launch_bounds__(kThreads) kKeyScatter(const unsigned int* __restrict__ cerr, const unsigned char* __restrict__ ckind, size_t n,
+    unsigned int items, const unsigned int* __restrict__ hist, unsigned int tiles, unsigned int* __restrict__ rank, unsigned int* __restrict__ serr,
+    unsigned char* __restrict__ skind, const PassLive* lv)
+{
+	extern __shared__ __align__(16) unsigned char key_smem[];
+	unsigned int* gbase = reinterpret_cast<unsigned int*>(key_smem);               // sorted position of the tile's first candidate per key
+	unsigned short* wcnt = reinterpret_cast<unsigned short*>(gbase + kKeyBins);   // per warp and key: count, then offset in the tile
+	if (lv)
+	{
+		if (lv->stop)
+			return;
+		n = lv->count;
+	}
+	const size_t tile0 = (size_t)blockIdx.x * items * kThreads;
+	if (tile0 >= n)
 		return;
-	const unsigned int c = order[k];
-	const uint4 a = crec[c];
-	srec[k] = cring[c];
-	sidx[k] = make_uint2(a.x, a.y);
-	serr[k] = a.z;
-	skind[k] = (unsigned char)a.w;
-	status[k] = kUndecided;
+	const unsigned int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
+	{
+		gbase[b] = hist[(size_t)b * tiles + blockIdx.x];
+#pragma unroll
+		for (unsigned int q = 0; q < kKeyWarps; ++q)
+			wcnt[q * kKeyBins + b] = 0;
+	}
+	__syncthreads();
+	unsigned short* mine = wcnt + w * kKeyBins;
+	const size_t w0 = tile0 + (size_t)w * 32 * items + lane;
+	for (unsigned int s0 = 0; s0 < items; s0 += 8)
+	{
+		unsigned int kb[8];
+#pragma unroll
+		for (unsigned int q = 0; q < 8; ++q)
+		{
+			const size_t i = w0 + (size_t)(s0 + q) * 32;
+			kb[q] = i < n ? sortKey(__ldg(cerr + i)) : kKeyBins + lane;
+		}
+#pragma unroll
+		for (unsigned int q = 0; q < 8; ++q)
+		{
+			const unsigned int peers = __match_any_sync(0xffffffffu, kb[q]);
+			if (kb[q] < kKeyBins && lane == __ffs(peers) - 1)
+				mine[kb[q]] += (unsigned short)__popc(peers);
+			__syncwarp();
+		}
+	}
+	__syncthreads();
+	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
+	{
+		unsigned int run = 0;
+#pragma unroll
+		for (unsigned int q = 0; q < kKeyWarps; ++q)
+		{
+			const unsigned int c = wcnt[q * kKeyBins + b];
+			wcnt[q * kKeyBins + b] = (unsigned short)run;
+			run += c;
+		}
+	}
+	__syncthreads();
+	for (unsigned int s0 = 0; s0 < items; s0 += 8)
+	{
+		unsigned int eb[8];
+		unsigned char kd[8];
+#pragma unroll
+		for (unsigned int q = 0; q < 8; ++q)
+		{
+			const size_t i = w0 + (size_t)(s0 + q) * 32;
+			eb[q] = i < n ? __ldg(cerr + i) : 0u;
+			kd[q] = i < n ? __ldg(ckind + i) : (unsigned char)0;
+		}
+#pragma unroll
+		for (unsigned int q = 0; q < 8; ++q)
+		{
+			const size_t i = w0 + (size_t)(s0 + q) * 32;
+			const bool valid = i < n;
+			const unsigned int key = valid ? sortKey(eb[q]) : kKeyBins + lane;
+			const unsigned int peers = __match_any_sync(0xffffffffu, key);
+			const unsigned int leader = __ffs(peers) - 1;
+			unsigned int before = 0;
+			if (valid && lane == leader)
+			{
+				before = mine[key];
+				mine[key] = (unsigned short)(before + __popc(peers));
+			}
+			before = __shfl_sync(0xffffffffu, before, leader);
+			if (valid)
+			{
+				const unsigned int pos = gbase[key] + before + __popc(peers & ((1u << lane) - 1u));
+				rank[i] = pos;
+				serr[pos] = eb[q];
+				skind[pos] = kd[q];
+			}
+			__syncwarp();
+		}
+	}
 }
 
 // ---------------------------------------------------------------- pass: perform
 //
-// kPerform runs, in one cooperative launch per pass, everything from the sorted candidates
-// to the next pass's index buffer: the decision rounds (performEdgeCollapses :1498-1636 made
-// order-free), the stop rules as a prefix scan over sorted order, the collapse_remap writes
-// and quadric merges of the committed prefix (:1574-1616, updateQuadrics :1638-1673), the
-// loop remap (:1845-1864) and the order-preserving index compaction (:1811-1843). Phases are
-// separated by grid barriers (mo_grid.cuh); data written by other blocks in an earlier phase
-// is read through L2 (ld.global.cg).
+// kPerform runs, in one cooperative launch per pass, everything from the ranked candidates to
+// the next pass's index buffer: the decision rounds (performEdgeCollapses :1498-1636 made
+// order-free), the stop rules as a prefix scan over sorted order, the collapse_remap writes and
+// quadric merges of the committed prefix (:1574-1616, updateQuadrics :1638-1673), the loop remap
+// (:1845-1864) and the order-preserving index compaction (:1811-1843). Phases are separated by
+// grid barriers (mo_grid.cuh); data written by other blocks in an earlier phase is read through
+// L2 (ld.global.cg).
+//
+// Candidates are identified by their sorted position k (the serial order of the reference's
+// loop), but the rounds visit them in pick order c, where k = rank[c]: pick order follows the
+// index buffer, so the candidates a warp takes share vertices, and their per-vertex gathers and
+// mark atomics fall on a few cache sectors instead of one each.
 
 __device__ __forceinline__ unsigned long long roundTag(unsigned int round)
 {
@@ -1296,10 +1457,13 @@ __device__ __forceinline__ bool earlierThan(unsigned long long v, unsigned long 
 
 struct PerformArgs
 {
-	// sorted candidates
+	// candidates in pick order: {i0, i1, error bits, kind of i0}, {r0, r1, adjacency range of r0}
+	// and the sorted position of each
 	unsigned int count;
-	const uint4* srec; // {r0, r1, adjacency begin of r0, adjacency end of r0}
-	const uint2* sidx; // {i0, i1}
+	const uint4* crec;
+	const uint4* cring;
+	const unsigned int* rank;
+	// by sorted position
 	const unsigned char* skind;
 	const unsigned int* serr;
 	unsigned char* status;
@@ -1308,9 +1472,10 @@ struct PerformArgs
 	unsigned long long* minT[2];
 	unsigned long long* minS[2];
 	unsigned char* touched;
-	unsigned long long* moved; // (sorted index of the commit that moved the vertex << 32) | target; ~0: not moved
+	unsigned long long* moved; // (sorted position of the commit that moved the vertex << 32) | target; ~0: not moved
 	unsigned int* cr;
-	unsigned int* list[2];
+	unsigned int* list[2];     // undecided candidates (pick order), one region per block
+	unsigned int* commits;     // committed candidates (pick order), one region per block
 	// mesh
 	const unsigned int* adj_off;
 	const uint2* adj;
@@ -1344,17 +1509,17 @@ struct PerformArgs
 // Decision rule: candidate k is decided once nothing earlier in sorted order can change its
 // outcome:
 //  * an earlier candidate already committed on one of its endpoints -> locked (final: any
-//    commit seen on an endpoint has a smaller sorted index);
+//    commit seen on an endpoint has a smaller sorted position);
 //  * otherwise it waits until it is the earliest undecided candidate on both endpoints (minT)
 //    and no undecided earlier candidate moves a vertex of its one-ring (minS); then the flip
 //    test runs against the one-ring as moved by earlier commits only (moving commit < k).
 
 // the commit of a decided candidate: r0 moves to its target and both endpoints lock
-__device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int k, unsigned int r0, unsigned int r1)
+__device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int c, unsigned int k, unsigned int r0, unsigned int r1)
 {
-	uint2 ii = __ldg(a.sidx + k);
-	const unsigned int i0 = ii.x, i1 = ii.y;
-	unsigned char kd = __ldg(a.skind + k);
+	const uint4 cd = __ldg(a.crec + c);
+	const unsigned int i0 = cd.x, i1 = cd.y;
+	const unsigned char kd = (unsigned char)cd.w;
 	unsigned int target;
 	if (kd == kComplex)
 		target = complexTarget(r0, i1, a.remap, a.loop, a.loopback);
@@ -1373,9 +1538,10 @@ __device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int k, 
 	a.status[k] = kCommit;
 }
 
-// The rule runs in three stages per round, each over the candidates the stage before left (so
-// lanes stay busy): the lock flags and endpoint marks (in the rounds loop), then the one-ring's
-// marks (ringWaits), then the flip test and the commit (flipOrCommit).
+// The rule runs in four stages per round, each over the candidates the stage before left (so
+// lanes stay busy): the lock flags and endpoint marks (in the rounds loop), the one-ring's marks
+// (ringWaits), the flip test and the commit (flipOrCommit), and last the candidates that still
+// wait: locked at once if a commit of this round took an endpoint, else marked for the next round.
 
 // no undecided earlier candidate may move a vertex of the one-ring (its sources): true if one does
 __device__ __forceinline__ bool ringWaits(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
@@ -1412,8 +1578,8 @@ __device__ __forceinline__ bool ringWaits(const PerformArgs& a, unsigned int k, 
 
 // flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232), then
 // the commit; the neighbours' own positions are loaded with their moved records (a moved
-// neighbour's target position is loaded after)
-__device__ __forceinline__ void flipOrCommit(const PerformArgs& a, unsigned int k, const uint4& rec)
+// neighbour's target position is loaded after). Returns true if the candidate committed.
+__device__ __forceinline__ bool flipOrCommit(const PerformArgs& a, unsigned int c, unsigned int k, const uint4& rec)
 {
 	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
 	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
@@ -1445,11 +1611,12 @@ __device__ __forceinline__ void flipOrCommit(const PerformArgs& a, unsigned int 
 			if (triFlip(pa, pb, v0, v1))
 			{
 				a.status[k] = kSkipFlip;
-				return;
+				return false;
 			}
 		}
 	}
-	commitOne(a, k, r0, r1);
+	commitOne(a, c, k, r0, r1);
+	return true;
 }
 
 __device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
@@ -1591,14 +1758,15 @@ __device__ void applyComplexCommit(const PerformArgs& a, unsigned int r0, unsign
 	}
 }
 
-__device__ void applyCommit(const PerformArgs& a, unsigned int k, unsigned int& errbits, unsigned int& derrbits)
+// the commit of candidate c (pick order)
+__device__ void applyCommit(const PerformArgs& a, unsigned int c, unsigned int& errbits, unsigned int& derrbits)
 {
-	uint4 rec = __ldg(a.srec + k);
-	uint2 ii = __ldg(a.sidx + k);
-	const unsigned int r0 = rec.x, r1 = rec.y, i0 = ii.x, i1 = ii.y;
-	unsigned char kd = __ldg(a.skind + k);
-	float e = __uint_as_float(__ldg(a.serr + k));
-	errbits = e == e ? __float_as_uint(e) : 0u;
+	const uint4 rec = __ldg(a.cring + c);
+	const uint4 cd = __ldg(a.crec + c);
+	const unsigned int r0 = rec.x, r1 = rec.y, i0 = cd.x, i1 = cd.y;
+	const unsigned char kd = (unsigned char)cd.w;
+	const float e = __uint_as_float(cd.z);
+	errbits = e == e ? cd.z : 0u;
 	if (kd == kComplex)
 	{
 		applyComplexCommit(a, r0, r1, i0, i1, derrbits);
@@ -1698,8 +1866,9 @@ struct PhaseClock
 
 __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(PerformArgs a)
 {
-	__shared__ unsigned int s_app[33];
-	__shared__ unsigned int s_stage[2][kStageChunk]; // candidates passed to the next decision stage
+	__shared__ unsigned int s_app[4];
+	__shared__ unsigned int s_stage[3][kStageChunk]; // candidates passed to stage B, to stage C, and kept for stage D
+	__shared__ unsigned int s_commits;               // this block's commits so far
 	PhaseClock pc;
 	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
 	if (timer)
@@ -1745,14 +1914,38 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 	unsigned int carryT = 0, carryF = 0, carryM = prev_err;
 	unsigned int windows = 0;
 
+	// block b's candidates are the pick-order tiles b, b + G, b + 2G, ... of blockDim each; its
+	// undecided and committed candidates live in its own region of the lists
+	const unsigned int stride = G * blockDim.x;
+	const unsigned int tiles = (count + stride - 1) / stride;
+	const size_t region = (size_t)blockIdx.x * tiles * blockDim.x;
+	unsigned int* const commits = a.commits + region;
+	if (threadIdx.x == 0)
+		s_commits = 0;
+
+	// warp-aggregated append of the lanes whose flag is set to dst at the shared counter
+	auto append = [&](bool flag, unsigned int v, unsigned int* counter, unsigned int* dst) {
+		unsigned int m = __ballot_sync(0xffffffffu, flag);
+		if (m)
+		{
+			unsigned int leader = __ffs(m) - 1, o = 0;
+			if (lane == leader)
+				o = atomicAdd(counter, __popc(m));
+			o = __shfl_sync(0xffffffffu, o, leader);
+			if (flag)
+				dst[o + __popc(m & ((1u << lane) - 1u))] = v;
+		}
+	};
+
 	for (;;)
 	{
-		// ---- decision rounds over the window [K0, K1)
+		// ---- decision rounds over the sorted window [K0, K1)
 		++windows;
-		for (size_t x = gtid(); x < K1 - K0; x += gthreads)
+		for (size_t c = gtid(); c < count; c += gthreads)
 		{
-			unsigned int k = K0 + (unsigned int)x;
-			markCandidate(a, k, __ldg(a.srec + k), round + 1);
+			const unsigned int k = __ldg(a.rank + c);
+			if (k >= K0 && k < K1)
+				markCandidate(a, k, __ldg(a.cring + c), round + 1);
 		}
 		if (gtid() == 0)
 			sc->act_count[(round + 2) % 3] = 0; // appended to by the window's first round
@@ -1760,17 +1953,12 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		if (timer)
 			pc.lap(windows == 1 ? kPhInit : kPhMarks);
 
-		// the first round walks the window grid-stride (block b takes every G-th tile of blockDim
-		// candidates), so the earliest candidates, which most others wait on, are decided first;
-		// every block keeps the candidates it left undecided in its own region of the lists,
-		// compacted with shared-memory atomics, and walks that region in the later rounds; only
-		// the per-round total crosses blocks (one global add per block, read after the barrier)
-		const unsigned int wlen = K1 - K0;
-		const unsigned int stride = G * blockDim.x;
-		const unsigned int tiles = (wlen + stride - 1) / stride;
-		const size_t region = (size_t)blockIdx.x * tiles * blockDim.x;
+		// the first round walks the block's tiles and takes the window's candidates among them;
+		// the block keeps the candidates it left undecided in its region of the lists, compacted
+		// with shared-memory atomics, and walks that region in the later rounds; only the
+		// per-round total crosses blocks (one global add per block, read after the barrier)
 		unsigned int nb = tiles * blockDim.x; // this block's undecided candidates (slots in the first round)
-		unsigned int n = wlen;                // all blocks'
+		unsigned int n = K1 - K0;             // all blocks'
 		bool first = true;
 		unsigned int guard = 0;
 		while (n)
@@ -1788,24 +1976,11 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 				sc->act_count[(round + 2) % 3] = 0;
 			if (threadIdx.x == 0)
 				s_app[0] = 0;
-			// warp-aggregated append of the lanes whose flag is set to dst at the shared counter
-			auto append = [&](bool flag, unsigned int k, unsigned int* counter, unsigned int* dst) {
-				unsigned int m = __ballot_sync(0xffffffffu, flag);
-				if (m)
-				{
-					unsigned int leader = __ffs(m) - 1, o = 0;
-					if (lane == leader)
-						o = atomicAdd(counter, __popc(m));
-					o = __shfl_sync(0xffffffffu, o, leader);
-					if (flag)
-						dst[o + __popc(m & ((1u << lane) - 1u))] = k;
-				}
-			};
 			for (unsigned int c0 = 0; c0 < nb; c0 += kStageChunk)
 			{
 				const unsigned int c1 = min(nb, c0 + kStageChunk);
 				if (threadIdx.x == 0)
-					s_app[1] = 0, s_app[2] = 0;
+					s_app[1] = 0, s_app[2] = 0, s_app[3] = 0;
 				__syncthreads();
 				// stage A: lock flags and endpoint marks; kStageItems candidates per thread, their
 				// loads issued together
@@ -1813,23 +1988,27 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 				const unsigned long long* minT = a.minT[round & 1];
 				for (unsigned int base = c0; base < c1; base += blockDim.x * kStageItems)
 				{
-					unsigned int kk[kStageItems];
+					unsigned int cc[kStageItems], kk[kStageItems];
 					bool ok[kStageItems];
 #pragma unroll
 					for (unsigned int q = 0; q < kStageItems; ++q)
 					{
 						const unsigned int x = base + q * blockDim.x + threadIdx.x;
 						const unsigned int g = (x - threadIdx.x) * G + blockIdx.x * blockDim.x + threadIdx.x;
-						ok[q] = x < c1 && (!first || g < wlen);
-						kk[q] = ok[q] ? (first ? K0 + g : __ldcg(cur + x)) : 0u;
+						ok[q] = x < c1 && (!first || g < count);
+						cc[q] = ok[q] ? (first ? g : __ldcg(cur + x)) : 0u;
 					}
 					uint2 ends[kStageItems];
 #pragma unroll
 					for (unsigned int q = 0; q < kStageItems; ++q)
 					{
-						uint4 rec = ok[q] ? __ldg(a.srec + kk[q]) : make_uint4(0, 0, 0, 0);
+						kk[q] = ok[q] ? __ldg(a.rank + cc[q]) : 0u;
+						const uint4 rec = ok[q] ? __ldg(a.cring + cc[q]) : make_uint4(0, 0, 0, 0);
 						ends[q] = make_uint2(rec.x, rec.y);
 					}
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+						ok[q] = ok[q] && (!first || (kk[q] >= K0 && kk[q] < K1));
 					unsigned char t[kStageItems];
 					unsigned long long m0[kStageItems], m1[kStageItems];
 #pragma unroll
@@ -1848,15 +2027,8 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 						const bool pass = ok[q] && !t[q] && !keep;
 						if (locked)
 							a.status[kk[q]] = kSkipLocked;
-						if (keep)
-						{
-							unsigned long long key = roundTag(round + 1) | kk[q];
-							atomicMin(&a.minT[(round + 1) & 1][ends[q].x], key);
-							atomicMin(&a.minT[(round + 1) & 1][ends[q].y], key);
-							atomicMin(&a.minS[(round + 1) & 1][ends[q].x], key);
-						}
-						append(keep, kk[q], &s_app[0], next);
-						append(pass, kk[q], &s_app[1], s_stage[0]);
+						append(keep, cc[q], &s_app[3], s_stage[2]);
+						append(pass, cc[q], &s_app[1], s_stage[0]);
 					}
 				}
 				__syncthreads();
@@ -1866,26 +2038,56 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 				{
 					const unsigned int x = base + threadIdx.x;
 					bool keep = false, pass = false;
-					unsigned int k = 0;
+					unsigned int c = 0;
 					if (x < nB)
 					{
-						k = s_stage[0][x];
-						uint4 rec = __ldg(a.srec + k);
-						keep = ringWaits(a, k, rec, round);
+						c = s_stage[0][x];
+						keep = ringWaits(a, __ldg(a.rank + c), __ldg(a.cring + c), round);
 						pass = !keep;
-						if (keep)
-							markCandidate(a, k, rec, round + 1);
 					}
-					append(keep, k, &s_app[0], next);
-					append(pass, k, &s_app[2], s_stage[1]);
+					append(keep, c, &s_app[3], s_stage[2]);
+					append(pass, c, &s_app[2], s_stage[1]);
 				}
 				__syncthreads();
 				// stage C: the flip test and the commit
 				const unsigned int nC = s_app[2];
-				for (unsigned int x = threadIdx.x; x < nC; x += blockDim.x)
+				for (unsigned int base = 0; base < nC; base += blockDim.x)
 				{
-					const unsigned int k = s_stage[1][x];
-					flipOrCommit(a, k, __ldg(a.srec + k));
+					const unsigned int x = base + threadIdx.x;
+					bool committed = false;
+					unsigned int c = 0;
+					if (x < nC)
+					{
+						c = s_stage[1][x];
+						committed = flipOrCommit(a, c, __ldg(a.rank + c), __ldg(a.cring + c));
+					}
+					append(committed, c, &s_commits, commits);
+				}
+				__syncthreads();
+				// stage D: the candidates that wait. A commit of this round (this block's, or another's
+				// whose write is already seen) on an endpoint locks one now: that commit is earlier,
+				// so the lock is final, and the candidates waiting on this one need not wait a round
+				// more for it. The others mark their endpoints for the next round.
+				const unsigned int nD = s_app[3];
+				for (unsigned int base = 0; base < nD; base += blockDim.x)
+				{
+					const unsigned int x = base + threadIdx.x;
+					bool keep = false;
+					unsigned int c = 0;
+					if (x < nD)
+					{
+						c = s_stage[2][x];
+						const unsigned int k = __ldg(a.rank + c);
+						const uint4 rec = __ldg(a.cring + c);
+						if (__ldcg(a.touched + rec.x) | __ldcg(a.touched + rec.y))
+							a.status[k] = kSkipLocked;
+						else
+						{
+							keep = true;
+							markCandidate(a, k, rec, round + 1);
+						}
+					}
+					append(keep, c, &s_app[0], next);
 				}
 				__syncthreads();
 			}
@@ -2001,47 +2203,28 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		return;
 
 	// ---- apply the committed prefix. Commits are independent (no two share an endpoint), so
-	// any order gives the same result. Sorted order is cut into slices of blockDim positions and
-	// block b takes slices b, b + G, b + 2G, ...: commits are densest at the front of sorted
-	// order, and interleaving spreads them evenly over the blocks. Each block compacts the commits
-	// of 16 slices at a time in shared memory, so every lane applies a commit.
+	// any order gives the same result: each block applies its own commits (pick order, so their
+	// quadric rows are near one another) whose sorted position is inside the prefix. The
+	// decisions of the prefix are counted over sorted order.
 	const unsigned long long cutv = __ldcg(&sc->cut);
 	const unsigned int cut = cutv == ~0ull ? count : (unsigned int)(cutv >> 2);
 	unsigned int nd = 0, ns = 0, ni = 0, em = 0, dm = 0;
+	for (size_t k = gtid(); k < cut; k += gthreads)
 	{
-		constexpr unsigned int per = kApplyTile / kThreads; // slices per block step
-		__shared__ unsigned int clist[kApplyTile];
-		const unsigned int slices = (cut + kThreads - 1) / kThreads;
-		for (unsigned int s0 = blockIdx.x; s0 < slices; s0 += G * per)
+		const unsigned char st = __ldcg(a.status + k);
+		nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
+	}
+	{
+		const unsigned int mc = s_commits; // every append to it was followed by a block barrier
+		for (unsigned int x = threadIdx.x; x < mc; x += blockDim.x)
 		{
-			unsigned int mine = 0, mask = 0;
-			for (unsigned int q = 0; q < per; ++q)
-			{
-				unsigned int s = s0 + q * G;
-				unsigned int k = s * kThreads + threadIdx.x;
-				if (s < slices && k < cut)
-				{
-					unsigned char st = __ldcg(a.status + k);
-					nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
-					mine += st == kCommit;
-					mask |= (st == kCommit ? 1u : 0u) << q;
-				}
-			}
-			unsigned int off = mine, d1 = 0, d2 = 0;
-			uint3 tot = blockScan3(off, d1, d2, sm);
-			for (; mask; mask &= mask - 1)
-			{
-				unsigned int q = __ffs(mask) - 1;
-				clist[off++] = (s0 + q * G) * kThreads + threadIdx.x;
-			}
-			__syncthreads();
-			for (unsigned int x = threadIdx.x; x < tot.x; x += blockDim.x)
+			const unsigned int c = commits[x];
+			if (__ldg(a.rank + c) < cut)
 			{
 				unsigned int eb = 0, db = 0;
-				applyCommit(a, clist[x], eb, db);
+				applyCommit(a, c, eb, db);
 				em = max(em, eb), dm = max(dm, db);
 			}
-			__syncthreads();
 		}
 	}
 	{
@@ -2713,13 +2896,13 @@ struct Work
 	unsigned int *res0, *res1;
 	unsigned int *adj_off, *fill;
 	uint2* adj;
-	uint4 *crec, *cring; // candidates (pick, then rank in place) and their decision records
-	unsigned int* ckey;
-	uint4* srec;
-	uint2* sidx;
-	unsigned int* serr;
-	unsigned char *skind, *status;
-	unsigned int *act0, *act1;
+	uint4 *crec, *cring; // candidates in pick order (pick, then rank in place) and their decision records
+	unsigned int* cerr;   // their error bits (setup: scratch of the duplicate and corner sorts)
+	unsigned char* ckind; // their kinds
+	unsigned int* rank;   // their sorted positions
+	unsigned int* serr;   // error bits by sorted position (setup: each corner's slot in its remapped list)
+	unsigned char *skind, *status; // kinds and decisions by sorted position
+	unsigned int *act0, *act1, *commits;
 	unsigned long long *minT, *minS;
 	unsigned char* touched;
 	unsigned long long* moved;
@@ -2799,14 +2982,15 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = f
 	w.adj = c.take<uint2>(I + 1);
 	w.crec = c.take<uint4>(big);
 	w.cring = c.take<uint4>(cap);
-	w.ckey = c.take<unsigned int>(big);
-	w.srec = c.take<uint4>(cap);
-	w.sidx = c.take<uint2>(cap);
+	w.cerr = c.take<unsigned int>(big);
+	w.ckind = c.take<unsigned char>(cap);
+	w.rank = c.take<unsigned int>(cap);
 	w.serr = c.take<unsigned int>(cap);
 	w.skind = c.take<unsigned char>(cap);
 	w.status = c.take<unsigned char>(cap);
 	w.act0 = c.take<unsigned int>(cap + kListSlack); // per-block regions of whole tiles
 	w.act1 = c.take<unsigned int>(cap + kListSlack);
+	w.commits = c.take<unsigned int>(cap + kListSlack);
 	w.minT = c.take<unsigned long long>(2 * Vp);
 	w.minS = c.take<unsigned long long>(2 * Vp);
 	w.touched = c.take<unsigned char>(Vp);
@@ -2817,7 +3001,7 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = f
 	w.cr = c.take<unsigned int>(Vp);
 	w.blk = c.take<uint4>(std::max<size_t>(cap / kStopTile + 2, 8192)); // >= blocks of any cooperative launch
 	w.blkcnt = c.take<unsigned int>(T / kThreads + 2);
-	size_t sw = std::max(std::max(scanScratchWords(I + Vp + 2), radixScratchWords(big)), scanScratchWords(T + 2));
+	size_t sw = std::max(std::max(scanScratchWords(I + Vp + 2), radixScratchWords(big)), std::max(scanScratchWords(T + 2), keySortScratchWords(cap)));
 	w.scratch = c.take<unsigned int>(sw);
 	const size_t Vs = solve ? Vp : 0;
 	w.vg = (solve && ac) ? c.take<float4>(Vp) : nullptr;
@@ -2835,6 +3019,22 @@ int bitsFor(size_t maxval)
 	while (b < 32 && (size_t(1) << b) <= maxval)
 		++b;
 	return b;
+}
+
+// The pass's counting sort (kKeyHist, scan, kKeyScatter) of up to n candidates: their sorted
+// positions into w.rank, the error bits and kinds by sorted position into w.serr and w.skind. lv:
+// the device-resident loop's live count (the grids cover n), else nullptr.
+void sortCandidates(const Work& w, size_t n, cudaStream_t stream, const PassLive* lv, ScanSync ss)
+{
+	if (n == 0)
+		return;
+	const unsigned int items = keySortItems(n), tiles = keySortTiles(n, items);
+	const size_t m = size_t(tiles) * kKeyBins;
+	unsigned int* hist = w.scratch;
+	unsigned int* sscratch = w.scratch + ((m + 63) & ~size_t(63));
+	MO_LAUNCH(kKeyHist, tiles, kThreads, 0, stream, w.cerr, n, items, hist, tiles, lv);
+	scanExclusive(hist, hist, m, nullptr, sscratch, stream, ss);
+	MO_LAUNCH(kKeyScatter, tiles, kThreads, kKeyScatterSmem, stream, w.cerr, w.ckind, n, items, hist, tiles, w.rank, w.serr, w.skind, lv);
 }
 
 } // namespace
@@ -2889,6 +3089,7 @@ Simplifier::Simplifier(int device) : device_(device)
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&solve_per_sm_, kSolvePositions, kThreads, 0));
+	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
 	cudaDeviceGetAttribute(&clock_khz_, cudaDevAttrClockRate, device);
 	sms_ = sms;
 	coop_blocks_ = unsigned(std::max(1, sms * std::max(per_sm, 1)));
@@ -3133,7 +3334,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		// rebuild the dup flags (the scan consumed them) into cnt, then compact
 		MO_LAUNCH(kHashRemap, gV, kThreads, 0, stream, w.table, w.slot, V, w.remap, w.wedge, w.cnt);
 		MO_LAUNCH(kCompactFlagged, gV, kThreads, 0, stream, w.cnt, w.flags, w.remap, V, w.keys_b, w.vals_b);
-		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.ckey, reinterpret_cast<unsigned int*>(w.crec), D, bitsFor(V), w.scratch, stream, nullptr, ss);
+		radixSortPairs(w.keys_b, w.vals_b, w.keys_a, w.vals_a, w.cerr, reinterpret_cast<unsigned int*>(w.crec), D, bitsFor(V), w.scratch, stream, nullptr, ss);
 		MO_LAUNCH(kWedgeLink, gridFor(D, kThreads), kThreads, 0, stream, w.keys_a, w.vals_a, D, w.wedge);
 	}
 
@@ -3159,8 +3360,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		if (D)
 		{
 			if (I)
-				MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.ckey);
-			radixSortPairs(w.ckey, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream, nullptr, ss);
+				MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cerr);
+			radixSortPairs(w.cerr, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream, nullptr, ss);
 		}
 	}
 	const unsigned int* off_rm = D ? w.off_rm : w.off_raw;
@@ -3370,7 +3571,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 
 		LaunchProbe& lp = probe();
 		const bool reuse = loop_.exec && loop_.base == arena_.base() && loop_.I == I && loop_.V == V && loop_.ac == ac && loop_.solve == solve &&
-		                   loop_.blocks == blocks;
+		                   loop_.blocks == blocks && loop_.scan_blocks == ss.max_blocks;
 		if (!reuse)
 		{
 			dropLoopGraph();
@@ -3416,14 +3617,14 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
 				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, pick_codes, w.tcnt, w.sc, w.crec, lv);
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
-				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 				    w.adj_off, w.attr, w.aq, w.ag, ac, lv);
-				radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, capn, 12, w.scratch, cs, &w.sc->live.count, ss);
-				MO_LAUNCH(kGatherSorted, gC, kThreads, 0, cs, capn, w.vals_a, w.crec, w.cring, w.srec, w.sidx, w.serr, w.skind, w.status, lv);
+				sortCandidates(w, capn, cs, lv, ss);
 				PerformArgs pa;
 				pa.count = 0;
-				pa.srec = w.srec;
-				pa.sidx = w.sidx;
+				pa.crec = w.crec;
+				pa.cring = w.cring;
+				pa.rank = w.rank;
 				pa.skind = w.skind;
 				pa.serr = w.serr;
 				pa.status = w.status;
@@ -3437,6 +3638,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				pa.cr = w.cr;
 				pa.list[0] = w.act0;
 				pa.list[1] = w.act1;
+				pa.commits = w.commits;
 				pa.adj_off = w.adj_off;
 				pa.adj = w.adj;
 				pa.pos = w.pos;
@@ -3488,6 +3690,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			loop_.ac = ac;
 			loop_.solve = solve;
 			loop_.blocks = blocks;
+			loop_.scan_blocks = ss.max_blocks;
 		}
 		MO_CUDA_CHECK(cudaGraphLaunch(loop_.exec, stream));
 		readScalars();
@@ -3533,12 +3736,11 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		const unsigned int gC = gridFor(C, kThreads);
 
 		// rank + sort
-		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.crec, w.cring, w.ckey, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback, w.adj_off,
-		    w.attr, w.aq, w.ag, ac, nullptr);
+		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+		    w.adj_off, w.attr, w.aq, w.ag, ac, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
-		radixSortPairs(w.ckey, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, C, 12, w.scratch, stream, nullptr, ss);
-		MO_LAUNCH(kGatherSorted, gC, kThreads, 0, stream, C, w.vals_a, w.crec, w.cring, w.srec, w.sidx, w.serr, w.skind, w.status, nullptr);
+		sortCandidates(w, C, stream, nullptr, ss);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 
@@ -3547,8 +3749,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		{
 			PerformArgs pa;
 			pa.count = unsigned(C);
-			pa.srec = w.srec;
-			pa.sidx = w.sidx;
+			pa.crec = w.crec;
+			pa.cring = w.cring;
+			pa.rank = w.rank;
 			pa.skind = w.skind;
 			pa.serr = w.serr;
 			pa.status = w.status;
@@ -3562,6 +3765,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.cr = w.cr;
 			pa.list[0] = w.act0;
 			pa.list[1] = w.act1;
+			pa.commits = w.commits;
 			pa.adj_off = w.adj_off;
 			pa.adj = w.adj;
 			pa.pos = w.pos;

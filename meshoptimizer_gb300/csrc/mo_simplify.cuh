@@ -164,6 +164,7 @@ private:
 		int ac = 0;
 		bool solve = false;
 		unsigned int blocks = 0;
+		unsigned int scan_blocks = 0;         // the one-launch scans' grid cap recorded in the body (0: none)
 		unsigned long long body_launches = 0; // kernels one replay of the body launches
 		cudaGraph_t graph = nullptr;
 		cudaGraphExec_t exec = nullptr;
