@@ -39,17 +39,42 @@ sys.path.insert(0, ROOT)
 
 from meshoptimizer_gb300 import workloads as W  # noqa: E402
 
-# Algorithmic bytes of the dominant kernel, kPerform (one cooperative launch per pass), from
-# the per-pass counters the library reports:
-#   decision rounds   29 B per active candidate (id 4, record 16, status 1, touched 2, append 4, pad 2)
-#   stop-rule scan    12 B per evaluated candidate (status, kind, error bits, read twice)
-#   per-vertex init   9 B per vertex (touched, moved_by, collapse_remap)
-#   apply             164 B per committed collapse (record 16, two quadrics read 96, one written 48, remap 4)
-#   loop remap        16 B per vertex (loop and loopback read and written)
-#   compaction        24 B per input triangle (indices read twice) + 12 B per kept triangle
-def kperform_bytes(p, vertices, next_triangles):
-    return (29 * p["active"] + 12 * p["evaluated"] + 9 * vertices + 164 * p["done"] + 16 * vertices
-            + 24 * p["triangles"] + 12 * next_triangles)
+# Algorithmic bytes of the dominant kernel, kPerform (one cooperative launch per pass): the
+# compulsory traffic of a pass, every array it must touch read (and written where it changes)
+# once, from the per-pass counters the library reports:
+#   candidate records  42 B per evaluated candidate (pick records 16 + 16, sorted position 4,
+#                      error bits 4, kind 1, decision 1): every candidate up to the stop cut
+#                      is decided
+#   per-vertex state   52 B per vertex (endpoint marks 16, one-ring marks 16, collapse_remap 4,
+#                      position 16)
+#   adjacency          24 B per triangle (three 8-byte corner records, read by the ring walks)
+#   apply              144 B per committed collapse (position quadrics: source read, target read
+#                      and written), plus 144 + 48 a with a attributes (attribute quadric and a
+#                      gradients: source read, target read and written)
+#   loop remap         16 B per vertex (loop and loopback read and written)
+#   compaction         12 B per input triangle + 12 B per kept triangle
+def kperform_bytes(p, vertices, next_triangles, attributes=0):
+    apply = 144 + (144 + 48 * attributes if attributes else 0)
+    return (42 * p["evaluated"] + 52 * vertices + 24 * p["triangles"] + apply * p["done"] + 16 * vertices
+            + 12 * p["triangles"] + 12 * next_triangles)
+
+
+KPERFORM_BYTES_DEFINITION = ("kperform_bytes(): 42 B per evaluated candidate, 52 B per vertex (marks, remap, position), "
+                             "24 B per triangle (adjacency), 144 B per commit + (144 + 48 a) B with a attributes, "
+                             "16 B per vertex (loops), 12 B per triangle in + 12 B per triangle kept")
+
+
+# Per-pass byte model of the whole pass (attribute path included), for the per-phase GB/s of
+# the stress line: adjacency 12 B per input triangle (indices) + 24 B per triangle
+# (corner records written) + 8 B per vertex (counts and offsets); pick 12 B per triangle + 12 B per
+# candidate written; rank 12 B per candidate read + 37 B per candidate written + 56 B per vertex of
+# gathered rows (+ 16 a + 48 with attributes); sort 8 B per candidate read twice + 13 B written;
+# perform as kperform_bytes.
+def pass_phase_bytes(p, vertices, next_triangles, attributes=0):
+    T, Cn = p["triangles"], p["candidates"]
+    rank_rows = 56 + (48 + 16 * attributes if attributes else 0)
+    return {"adjacency": 36 * T + 8 * vertices, "pick": 12 * T + 12 * Cn, "rank": 49 * Cn + rank_rows * vertices,
+            "sort": 29 * Cn, "perform": kperform_bytes(p, vertices, next_triangles, attributes)}
 
 
 WORKLOADS = {
@@ -162,7 +187,11 @@ def bench_groups(args, mg, torch, seed_offset=0):
         exact = exact and all(np.array_equal(a, r[0]) for a, r in zip(batched_out, ref))
         cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
                "sample": f"all {len(meshes)} groups once, independent groups split statically over {threads} threads"}
-    return _groups_line(args, mg, meshes, tris, out_tris, total_ms, tt, h2d, d2h, plain_gpu, cpu, exact, clocks, launches)
+    line = _groups_line(args, mg, meshes, tris, out_tris, total_ms, tt, h2d, d2h, plain_gpu, cpu, exact, clocks, launches)
+    line["error_vs_fp64_oracle"] = None
+    if not args.no_cpu_baseline:
+        line["error_vs_fp64_oracle"] = fp64_statement(meshes, [(len(o) // 3, float(e)) for o, e in zip(batched_out, errs)])
+    return line
 
 
 def _groups_plain(args, mg, torch, meshes, raw_descs, stream, batched_out, host_res):
@@ -307,7 +336,7 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
     gv = dmv.cpu().numpy().view(np.uint32)
     gt = dmt.cpu().numpy()
 
-    cpu, exact, cl_cpu, cl_exact = None, None, None, None
+    cpu, exact, cl_cpu, cl_exact, fp64 = None, None, None, None, None
     if not args.no_cpu_baseline:
         import concurrent.futures as cf
 
@@ -335,6 +364,9 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
                 exact = exact and int(counts[g]) == len(o) and np.array_equal(out[int(off[g]):int(off[g]) + len(o)], o) and float(errs[g]) == e
         cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtris/s", "cores": threads, "kind": "port",
                "sample": f"the whole level once: lockBoundary restatement, then all {len(groups)} groups split statically over {threads} threads"}
+        fp64 = fp64_statement([dict(indices=groups[g], positions=pos, target=int(targets[g]), error=error, options=options, attributes=attr,
+                                    weights=w, lock=ref_locks) for g in range(len(groups))],
+                              [(int(counts[g]) // 3, float(errs[g])) for g in range(len(groups))])
 
         def cl_work(gs):
             res = []
@@ -367,7 +399,7 @@ def bench_clod_level(args, mg, torch, levels=9, group_tris=1024):
                    "batch_threads_per_cta": mg.batch_threads(), "l2": "flushed between steps (512 MiB write, outside the timed events)"},
         "e2e": {"value": round(tris * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(idx.nbytes), "ms_per_step": round(1e3 * tt / args.steps, 3)},
-        "cpu_baseline": cpu, "bit_exact_vs_oracle": exact, "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "cpu_baseline": cpu, "bit_exact_vs_oracle": exact, "error_vs_fp64_oracle": fp64, "clocks": clocks.summary(), "gpu_launches": int(launches),
         "clusterize": {"metric": "simplified Mtris/s clusterized (bit-exact)", "value": round(stris / (cl_ms / 1e3) / 1e6, 4), "unit": "Mtris/s",
                        "ms_per_step": round(cl_ms, 3), "meshlets": int(mcounts.sum()),
                        "config": {"function": "meshopt_buildMeshletsFlex per group, then meshopt_optimizeMeshletLevel(1) per meshlet (meshoptgpu_buildMeshletsFlexGroups)", "input_tris": stris,
@@ -390,10 +422,11 @@ def bench_serving(args, mg, torch):
     pool_size = 96
     sizes = W.lognormal_sizes(pool_size, seed=4, median=20000.0, sigma=1.0)
     dev = torch.device("cuda", 0)
-    pool = []
+    pool, pool_host = [], []
     for i, t in enumerate(sizes):
         n = int(round((t / 2) ** 0.5)) + 1
         idx, pos = W.heightfield(n, seed=1000 + i, amp=0.05)
+        pool_host.append((idx, pos))
         pool.append((torch.from_numpy(idx.view(np.int32)).to(dev), torch.from_numpy(pos).to(dev), len(idx), len(pos)))
     n_req = args.requests
     rng = random.Random(7)
@@ -444,14 +477,28 @@ def bench_serving(args, mg, torch):
         plain_res = plain_res or res
     # the served results equal the plain (single-mesh path, alone) results request by request
     same = plain_res is not None and all(a[1] == b[1] and a[2] == b[2] for a, b in zip(served_res, plain_res))
+    # per rate that both arms ran: served delivers more input Mtris/s, and its p99 is lower
+    beats = [{"rate_per_s": a["rate_per_s"], "mtris_s": a["mtris_s"] > b["mtris_s"], "p99": a["p99_ms"] < b["p99_ms"]}
+             for a, b in zip(served, plain)]
+    fp64 = None
+    if not getattr(args, "no_cpu_baseline", False):
+        # a sample of the served results (the first requests of the first rate) against the FP64 oracle
+        k = min(400, n_req)
+        cases = []
+        for i in range(k):
+            m, target = reqs[i]
+            cases.append(dict(indices=pool_host[m][0], positions=pool_host[m][1], target=target, error=1e-2, options=0))
+        fp64 = fp64_statement(cases, [(served_res[i][1] // 3, served_res[i][2]) for i in range(k)],
+                              sample=f"the first {k} requests of the {rates[0]:g} req/s run")
     line = {
         "metric": "input Mtris/s simplified (bit-exact); p50/p99 request latency", "value": served[0]["mtris_s"], "unit": "Mtris/s", "n_gpus": 1,
         "steps": n_req, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "serving_poisson", "requests_per_rate": n_req, "pool_meshes": pool_size, "tris": "lognormal median 20k sigma 1 [1k,1M]",
                    "ratio": "U[0.1,0.5]", "target_error": 1e-2, "memory_budget_gb": 40, "request_input_tris": total_tris,
                    "single_mesh_workers": args.serve_workers, "pass_kernel_grid_cap": args.serve_blocks or 64,
-                   "batch_kernel_max_index_count": args.serve_large or 30000},
-        "served": served, "plain": plain, "served_equals_plain": bool(same),
+                   "batch_kernel_max_index_count": args.serve_large or 30000,
+                   "plain": "one request at a time on the single-mesh GPU path, in arrival order"},
+        "served": served, "plain": plain, "served_equals_plain": bool(same), "served_beats_plain": beats, "error_vs_fp64_oracle": fp64,
     }
     return line
 
@@ -593,6 +640,215 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def fp64_statement(cases, results, threads=None, sample=None):
+    """The FP32 results' error stated against the FP64 oracle (the same driver in double).
+
+    cases: dicts with indices, positions, target, error, options (and attributes, weights, lock);
+    results: the GPU's (output triangles, result error) for each case, in order."""
+    import concurrent.futures as cf
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    if not oracle.available("port"):
+        oracle.build(with_reference=False)
+    oracle.load("port")
+
+    def one(c):
+        out64, e64, _ = oracle.simplify("port", c["indices"], c["positions"], c["target"], c["error"], c["options"],
+                                        attributes=c.get("attributes"), weights=c.get("weights"), lock=c.get("lock"), fp64=True)
+        return len(out64) // 3, e64
+
+    with cf.ThreadPoolExecutor(threads or os.cpu_count() or 1) as ex:
+        ref = list(ex.map(one, cases))
+    rel, same, t32, t64 = [], 0, 0, 0
+    for (tris32, e32), (tris64, e64) in zip(results, ref):
+        d = abs(float(e32) - e64)
+        rel.append(d / e64 if e64 > 0 else (0.0 if d == 0 else float("inf")))
+        same += int(tris32 == tris64)
+        t32 += int(tris32)
+        t64 += tris64
+    out = {"results": len(cases), "max_relative_difference": float(max(rel)) if rel else 0.0,
+           "median_relative_difference": float(statistics.median(rel)) if rel else 0.0,
+           "output_tris_equal": same, "fp32_output_tris": t32, "fp64_output_tris": t64}
+    if sample:
+        out["sample"] = sample
+    return out
+
+
+def bench_single(args, mg, torch, c, dist=None, world=1, rank=0, local=0, roofline=True, e2e_leg=True, cpu_leg=True, per_pass=False):
+    """One complete simplification of one mesh per step: device-resident value, roofline of the
+    pass kernel, drop-in e2e, CPU baseline, bit-exactness and the FP64 statement."""
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    idx = torch.from_numpy(c["indices"].view(np.int32)).to(dev)
+    pos = torch.from_numpy(c["positions"]).to(dev)
+    has_attr = c.get("attributes") is not None
+    attr = torch.from_numpy(c["attributes"]).to(dev) if has_attr else None
+    out = torch.empty_like(idx)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    V = pos.shape[0]
+    ac = attr.shape[1] if has_attr else 0
+    ac_used = int(np.count_nonzero(np.asarray(c["weights"]) > 0)) if has_attr else 0
+
+    def step():
+        return mg.simplify_device(out.data_ptr(), idx.data_ptr(), idx.numel(), pos.data_ptr(), V, 12, c["target"], c["error"], c["options"],
+                                  d_attributes=attr.data_ptr() if has_attr else 0, attributes_stride=4 * ac,
+                                  weights=c.get("weights"), stream=stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 0)):
+        n_out, err = step()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = mg.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            n_out, err = step()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = mg.launch_count() - launches0
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+
+    # per-launch CUDA-event timing of the roofline kernel: the same steps replayed with the
+    # host-driven pass loop (events cannot be recorded inside the device-resident loop's graph)
+    k_launches = k_ms = host_loop_ms = 0
+    if roofline:
+        mg.set_device_loop(False)
+        step()
+        mg.set_kernel_profile(args.kernel)
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for i in range(args.steps):
+            flush.zero_()
+            kev[i][0].record(stream)
+            step()
+            kev[i][1].record(stream)
+        torch.cuda.synchronize()
+        k_launches, k_ms = mg.kernel_profile()
+        mg.set_kernel_profile(None)
+        mg.set_device_loop(True)
+        host_loop_ms = sum(a.elapsed_time(b) for a, b in kev)
+    from meshoptimizer_gb300 import replicas
+
+    rate, secs, _ = replicas.aggregate(total_ms / 1e3, float(c["tris"] * args.steps), dist=dist, device=dev)
+    total_ms = secs * 1e3
+    value = rate / 1e6
+    gpu_out = out[:n_out].cpu().numpy().view(np.uint32)
+
+    # per-pass and per-phase view of one more run (not timed for the value)
+    mg.set_timing(True)
+    step()
+    phases = mg.last_phase_times()
+    passes = mg.last_pass_stats()
+    pass_phases = mg.last_pass_phase_times()
+    trace = mg.last_round_trace()
+    mg.set_timing(False)
+
+    # end to end through the drop-in C ABI with pinned host buffers
+    e2e = None
+    if e2e_leg:
+        h_idx = torch.from_numpy(c["indices"].view(np.int32)).pin_memory()
+        h_pos = torch.from_numpy(c["positions"]).pin_memory()
+        h_attr = torch.from_numpy(c["attributes"]).pin_memory() if has_attr else None
+        h_out = torch.empty(len(c["indices"]), dtype=torch.int32).pin_memory()
+        n_idx, n_pos = h_idx.numpy().view(np.uint32), h_pos.numpy()
+        n_attr = h_attr.numpy() if has_attr else None
+        n_outb = h_out.numpy().view(np.uint32)
+
+        def e2e_step():
+            if has_attr:
+                return mg.simplify_raw(n_outb, n_idx, len(n_idx), n_pos, V, 12, c["target"], c["error"], c["options"], attributes=n_attr,
+                                       attributes_stride=4 * ac, weights=c["weights"], attribute_count=ac)
+            return mg.simplify_raw(n_outb, n_idx, len(n_idx), n_pos, V, 12, c["target"], c["error"], c["options"])
+
+        for _ in range(max(args.warmup, 0)):
+            e2e_step()
+        tt = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            n_e2e, _ = e2e_step()
+            tt += time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([tt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tt = float(t.item())
+        assert np.array_equal(n_outb[:n_e2e], gpu_out), "drop-in and device-resident results differ"
+        h2d = c["indices"].nbytes + c["positions"].nbytes + (c["attributes"].nbytes if has_attr else 0)
+        d2h = n_e2e * 4
+        e2e = {"value": round(world * c["tris"] * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * tt / args.steps, 3)}
+
+    if rank != 0:
+        return None
+
+    # roofline of the selected kernel: algorithmic bytes over its measured launch time
+    peak, peak_kind = measured_peak()
+    roof = None
+    nxt = [p["triangles"] for p in passes[1:]] + [int(n_out) // 3]
+    if k_launches:
+        avg_ms = k_ms / k_launches
+        bytes_run = sum(kperform_bytes(p, V, t, ac_used) for p, t in zip(passes, nxt))
+        bytes_per_launch = bytes_run / max(len(passes), 1)
+        achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0
+        roof = {"bound": "hbm", "kernel": args.kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
+                "avg_launch_us": round(1e3 * avg_ms, 2), "launches": k_launches,
+                "algorithmic_bytes_per_launch": int(bytes_per_launch), "unit_definition": KPERFORM_BYTES_DEFINITION,
+                "share_of_step": round(k_ms / host_loop_ms, 4) if host_loop_ms else None,
+                "kernel_timing": "CUDA events around every launch on its stream, over the same steps replayed with the host-driven "
+                                 "pass loop (the timed steps run the device-resident loop, whose graph cannot hold events)"}
+        tr = kernel_traffic(args.kernel, c["name"])
+        if tr:
+            roof["traffic"] = tr["dram_bytes_per_launch"]
+            roof["traffic_source"] = tr["source"]
+
+    cpu = bit_exact = fp64 = None
+    if cpu_leg:
+        mt, runs, secs_cpu, ref_out, ref_err = cpu_baseline(c)
+        bit_exact = bool(np.array_equal(ref_out, gpu_out)) and abs(ref_err - err) <= 1e-6 * max(abs(ref_err), 1e-30)
+        fp64 = fp64_statement([c], [(int(n_out) // 3, err)], threads=1)
+        fp64["fp32_result_error"] = err
+        cpu = {"value": round(mt, 4), "unit": "Mtris/s", "cores": 1, "kind": "port",
+               "sample": f"{runs} full simplification(s) of {c['name']} in {secs_cpu:.1f} s, single thread (the simplifier has no threading)"}
+
+    line = {
+        "metric": "input Mtris/s simplified (bit-exact)", "value": round(value, 4), "unit": "Mtris/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": c["name"], "input_tris": c["tris"], "output_tris": int(n_out) // 3, "target_index_count": c["target"],
+                   "target_error": c["error"], "options": c["options"], "attributes": ac, "result_error": err,
+                   "l2": "flushed between steps (512 MiB write, outside the timed events)", "parallelism": f"replicas{world}"},
+        "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact, "error_vs_fp64_oracle": fp64,
+        "clocks": clocks.summary(), "gpu_launches": int(launches),
+        "phases_ms": {k: round(v, 3) for k, v in phases.items()},
+        "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active", "windows")} for p in passes],
+        "round_trace_us": [[n, round(t, 1)] for n, t in trace[:64]],
+    }
+    if per_pass:
+        # per pass: CUDA-event time of each phase (host-driven loop, timing on) and the phase's
+        # algorithmic bytes over it
+        rows = []
+        for p, t, ph in zip(passes, nxt, pass_phases):
+            b = pass_phase_bytes(p, V, t, ac_used)
+            rows.append({"triangles": p["triangles"], "candidates": p["candidates"], "rounds": p["rounds"],
+                         "ms": {k: round(v, 3) for k, v in ph.items()},
+                         "gb_s": {k: round(b[k] / (ph[k] / 1e3) / 1e9, 1) if ph[k] > 0 else None for k in b},
+                         "algorithmic_mb": {k: round(b[k] / 1e6, 2) for k in b}})
+        line["per_pass"] = rows
+        line["per_pass_definition"] = ("ms: CUDA events around each phase of each pass (host-driven pass loop); gb_s: the phase's "
+                                       "algorithmic bytes (pass_phase_bytes in bench.py) over that time, against the measured "
+                                       f"{peak} GB/s copy bandwidth")
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -603,11 +859,11 @@ def main():
     ap.add_argument("--kernel", default="kPerform", help="kernel whose CUDA-event time gives the roofline line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched-groups and serving summaries of the default line")
+    ap.add_argument("--no-extras", action="store_true", help="skip the groups, serving, cluster-LOD and heightfield summaries of the default line")
     ap.add_argument("--no-plain", action="store_true", help="groups: skip the separate one-call-per-group comparison leg")
     ap.add_argument("--requests", type=int, default=10000, help="serving: requests per arrival rate")
-    ap.add_argument("--rates", default="250,500,1000,2000", help="serving: Poisson arrival rates (requests/s)")
-    ap.add_argument("--plain-rates", type=int, default=2, help="serving: how many of the rates also run the plain path")
+    ap.add_argument("--rates", default="500,1000,2000,4000", help="serving: Poisson arrival rates (requests/s)")
+    ap.add_argument("--plain-rates", type=int, default=4, help="serving: how many of the rates also run the plain path")
     ap.add_argument("--serve-workers", type=int, default=16, help="serving: concurrent single-mesh workers")
     ap.add_argument("--serve-blocks", type=int, default=0, help="serving: pass-kernel grid cap per request (0: server default)")
     ap.add_argument("--serve-large", type=int, default=0, help="serving: index count above which requests skip the batch kernel (0: default)")
@@ -645,174 +901,28 @@ def main():
         print(json.dumps(bench_clod_level(args, mg, torch)))
         return
     c = load_workload(args.workload)
-    dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
-    idx = torch.from_numpy(c["indices"].view(np.int32)).to(dev)
-    pos = torch.from_numpy(c["positions"]).to(dev)
-    has_attr = c.get("attributes") is not None
-    attr = torch.from_numpy(c["attributes"]).to(dev) if has_attr else None
-    out = torch.empty_like(idx)
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    V = pos.shape[0]
-    ac = attr.shape[1] if has_attr else 0
-
-    def step():
-        return mg.simplify_device(out.data_ptr(), idx.data_ptr(), idx.numel(), pos.data_ptr(), V, 12, c["target"], c["error"], c["options"],
-                                  d_attributes=attr.data_ptr() if has_attr else 0, attributes_stride=4 * ac,
-                                  weights=c.get("weights"), stream=stream.cuda_stream)
-
-    for _ in range(max(args.warmup, 0)):
-        n_out, err = step()
-
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    launches0 = mg.launch_count()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        for i in range(args.steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            n_out, err = step()
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    launches = mg.launch_count() - launches0
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
-
-    # per-launch CUDA-event timing of the roofline kernel: the same steps replayed with the
-    # host-driven pass loop (events cannot be recorded inside the device-resident loop's graph)
-    mg.set_device_loop(False)
-    step()
-    mg.set_kernel_profile(args.kernel)
-    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for i in range(args.steps):
-        flush.zero_()
-        kev[i][0].record(stream)
-        step()
-        kev[i][1].record(stream)
-    torch.cuda.synchronize()
-    k_launches, k_ms = mg.kernel_profile()
-    mg.set_kernel_profile(None)
-    mg.set_device_loop(True)
-    host_loop_ms = sum(a.elapsed_time(b) for a, b in kev)
-    from meshoptimizer_gb300 import replicas
-
-    rate, secs, _ = replicas.aggregate(total_ms / 1e3, float(c["tris"] * args.steps), dist=dist, device=dev)
-    total_ms = secs * 1e3
-    value = rate / 1e6
-    gpu_out = out[:n_out].cpu().numpy().view(np.uint32)
-
-    # per-pass and per-phase view of one more run (not timed for the value)
-    mg.set_timing(True)
-    step()
-    phases = mg.last_phase_times()
-    passes = mg.last_pass_stats()
-    trace = mg.last_round_trace()
-    mg.set_timing(False)
-
-    # end to end through the drop-in C ABI with pinned host buffers
-    e2e = None
-    if not args.no_e2e:
-        h_idx = torch.from_numpy(c["indices"].view(np.int32)).pin_memory()
-        h_pos = torch.from_numpy(c["positions"]).pin_memory()
-        h_attr = torch.from_numpy(c["attributes"]).pin_memory() if has_attr else None
-        h_out = torch.empty(len(c["indices"]), dtype=torch.int32).pin_memory()
-        n_idx, n_pos = h_idx.numpy().view(np.uint32), h_pos.numpy()
-        n_attr = h_attr.numpy() if has_attr else None
-        n_outb = h_out.numpy().view(np.uint32)
-
-        def e2e_step():
-            if has_attr:
-                return mg.simplify_raw(n_outb, n_idx, len(n_idx), n_pos, V, 12, c["target"], c["error"], c["options"], attributes=n_attr,
-                                       attributes_stride=4 * ac, weights=c["weights"], attribute_count=ac)
-            return mg.simplify_raw(n_outb, n_idx, len(n_idx), n_pos, V, 12, c["target"], c["error"], c["options"])
-
-        for _ in range(max(args.warmup, 0)):
-            e2e_step()
-        tt = 0.0
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            n_e2e, _ = e2e_step()
-            tt += time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([tt], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tt = float(t.item())
-        assert np.array_equal(n_outb[:n_e2e], gpu_out), "drop-in and device-resident results differ"
-        h2d = c["indices"].nbytes + c["positions"].nbytes + (c["attributes"].nbytes if has_attr else 0)
-        d2h = n_e2e * 4
-        e2e = {"value": round(world * c["tris"] * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1e3 * tt / args.steps, 3)}
-
+    line = bench_single(args, mg, torch, c, dist=dist, world=world, rank=rank, local=local, e2e_leg=not args.no_e2e,
+                        cpu_leg=not args.no_cpu_baseline, per_pass=args.workload.startswith("fractal"))
     if rank != 0:
+        if dist:
+            dist.destroy_process_group()
         return
-
-    # roofline of the selected kernel: algorithmic bytes over its measured launch time
-    peak, peak_kind = measured_peak()
-    roofline = None
-    if k_launches:
-        avg_ms = k_ms / k_launches
-        nxt = [p["triangles"] for p in passes[1:]] + [int(n_out) // 3]
-        bytes_run = sum(kperform_bytes(p, V, t) for p, t in zip(passes, nxt))
-        bytes_per_launch = bytes_run / max(len(passes), 1)
-        achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0
-        roofline = {"bound": "hbm", "kernel": args.kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
-                    "avg_launch_us": round(1e3 * avg_ms, 2), "launches": k_launches,
-                    "algorithmic_bytes_per_launch": int(bytes_per_launch),
-                    "unit_definition": "kperform_bytes(): rounds 29 B/active candidate, stop 12 B/evaluated, apply 164 B/commit, "
-                                       "25 B/vertex, 24 B/triangle + 12 B/kept triangle",
-                    "share_of_step": round(k_ms / host_loop_ms, 4) if host_loop_ms else None,
-                    "kernel_timing": "CUDA events around every launch on its stream, over the same steps replayed with the host-driven "
-                                     "pass loop (the timed steps run the device-resident loop, whose graph cannot hold events)"}
-        tr = kernel_traffic(args.kernel, c["name"])
-        if tr:
-            roofline["traffic"] = tr["dram_bytes_per_launch"]
-            roofline["traffic_source"] = tr["source"]
-
-    cpu = None
-    bit_exact = None
-    fp64 = None
-    if not args.no_cpu_baseline:
-        mt, runs, secs, ref_out, ref_err = cpu_baseline(c)
-        bit_exact = bool(np.array_equal(ref_out, gpu_out)) and abs(ref_err - err) <= 1e-6 * max(abs(ref_err), 1e-30)
-        import oracle
-
-        # the FP32 path's result error stated against the FP64 oracle (same driver in double)
-        out64, err64, _ = oracle.simplify("port", c["indices"], c["positions"], c["target"], c["error"], c["options"],
-                                          attributes=c.get("attributes"), weights=c.get("weights"), fp64=True)
-        fp64 = {"fp32_result_error": err, "fp64_result_error": err64, "relative_difference": abs(err - err64) / err64 if err64 else 0.0,
-                "fp64_output_tris": len(out64) // 3}
-        cpu = {"value": round(mt, 4), "unit": "Mtris/s", "cores": 1, "kind": "port",
-               "sample": f"{runs} full simplification(s) of {c['name']} in {secs:.1f} s, single thread (the simplifier has no threading)"}
-
-    line = {
-        "metric": "input Mtris/s simplified (bit-exact)", "value": round(value, 4), "unit": "Mtris/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": c["name"], "input_tris": c["tris"], "output_tris": int(n_out) // 3, "target_index_count": c["target"],
-                   "target_error": c["error"], "options": c["options"], "attributes": ac, "result_error": err,
-                   "l2": "flushed between steps (512 MiB write, outside the timed events)", "parallelism": f"replicas{world}"},
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact, "error_vs_fp64_oracle": fp64,
-        "clocks": clocks.summary(), "gpu_launches": int(launches),
-        "phases_ms": {k: round(v, 3) for k, v in phases.items()},
-        "passes": [{k: p[k] for k in ("triangles", "candidates", "evaluated", "done", "rounds", "active", "windows")} for p in passes],
-        "round_trace_us": [[n, round(t, 1)] for n, t in trace[:64]],
-    }
     if not args.no_extras and world == 1:
         g = bench_groups(argparse.Namespace(steps=3, warmup=3, no_cpu_baseline=args.no_cpu_baseline), mg, torch)
         line["batched_groups"] = {k: g[k] for k in ("value", "unit", "ms_per_step", "e2e", "plain_gpu", "cpu_baseline",
-                                                   "bit_exact_vs_plain_and_oracle")}
+                                                   "bit_exact_vs_plain_and_oracle", "error_vs_fp64_oracle")}
         line["batched_groups"]["config"] = g["config"]
-        sv = bench_serving(argparse.Namespace(requests=2000, rates="500,1000", plain_rates=1, serve_workers=16, serve_blocks=0, serve_large=0,
-                                              serve_batch_workers=0), mg, torch)
-        line["serving"] = {k: sv[k] for k in ("served", "plain", "served_equals_plain", "config")}
+        sv = bench_serving(argparse.Namespace(requests=args.requests, rates=args.rates, plain_rates=args.plain_rates,
+                                              serve_workers=args.serve_workers, serve_blocks=args.serve_blocks, serve_large=args.serve_large,
+                                              serve_batch_workers=args.serve_batch_workers, no_cpu_baseline=args.no_cpu_baseline), mg, torch)
+        line["serving"] = {k: sv[k] for k in ("served", "plain", "served_equals_plain", "served_beats_plain", "error_vs_fp64_oracle", "config")}
         cl = bench_clod_level(argparse.Namespace(steps=3, warmup=3, no_cpu_baseline=args.no_cpu_baseline), mg, torch)
-        line["cluster_lod_level"] = {k: cl[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "cpu_baseline", "bit_exact_vs_oracle", "clusterize", "level_ms")}
+        line["cluster_lod_level"] = {k: cl[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "cpu_baseline", "bit_exact_vs_oracle",
+                                                        "error_vs_fp64_oracle", "clusterize", "level_ms")}
+        hf = bench_single(argparse.Namespace(steps=10, warmup=3, kernel=args.kernel), mg, torch, load_workload("heightfield_256"),
+                          local=local, e2e_leg=True, cpu_leg=not args.no_cpu_baseline)
+        line["heightfield_256"] = {k: hf[k] for k in ("value", "unit", "ms_per_step", "config", "e2e", "roofline", "cpu_baseline",
+                                                      "bit_exact_vs_oracle", "error_vs_fp64_oracle", "phases_ms", "passes")}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

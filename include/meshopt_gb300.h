@@ -26,6 +26,12 @@ extern "C"
 {
 #endif
 
+/* The option and vertex_lock enumerators below are meshoptimizer.h's own (same names and values).
+ * A translation unit that mixes CPU and GPU calls includes meshoptimizer.h first and this header
+ * after it; this header then leaves the enumerators to meshoptimizer.h (its version macro
+ * MESHOPTIMIZER_VERSION marks it as included) and only adds the GPU entry points. */
+#ifndef MESHOPTIMIZER_VERSION
+
 /* Option bits: same values as meshoptimizer.h:466-482. */
 enum
 {
@@ -45,6 +51,8 @@ enum
 	meshopt_SimplifyVertex_Protect = 1 << 1,
 	meshopt_SimplifyVertex_Priority = 1 << 2,
 };
+
+#endif /* MESHOPTIMIZER_VERSION */
 
 /* Replaces meshopt_simplify, meshoptimizer.h:513 (implementation src/simplifier.cpp:2628). */
 MESHOPTGPU_API size_t meshopt_simplify(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions,
@@ -102,10 +110,15 @@ MESHOPTGPU_API void meshoptgpu_setTiming(int enabled);
 MESHOPTGPU_API int meshoptgpu_getLastRoundTrace(unsigned int* active, float* micros, int max_rounds);
 MESHOPTGPU_API int meshoptgpu_getLastPhaseTimes(float* out16);
 
+/* With timing enabled, the CUDA-event time (ms) of each pass of the calling thread's last
+ * single-mesh call, five values per pass: adjacency, pick, rank, sort, perform. Copies up to
+ * max_passes rows; returns the number of passes recorded. */
+MESHOPTGPU_API int meshoptgpu_getLastPassPhaseTimes(float* out, int max_passes);
+
 /* meshoptimizer.h:560 (src/simplifier.cpp:2642): simplifies indices in place and writes the
  * optimal positions (and attributes) of the vertices the result uses back into the caller's
- * buffers. Same results as the reference. Prune and the debug bit are not implemented here
- * (they return meshoptgpu_StatusUnsupported with the buffers unchanged). */
+ * buffers. Same results as the reference, for every option bit (Prune and the internal debug
+ * bit included). */
 MESHOPTGPU_API size_t meshopt_simplifyWithUpdate(unsigned int* indices, size_t index_count, float* vertex_positions, size_t vertex_count,
     size_t vertex_positions_stride, float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
     const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error);
@@ -318,11 +331,12 @@ MESHOPTGPU_API int meshoptgpu_generatePositionRemapDevice(unsigned int* destinat
 
 /* Allocation-free mesh extent. No counterpart in the reference: it is the device-pointer
  * form of meshopt_simplifyScale for callers that must not allocate device memory while they
- * run (work recorded into a CUDA graph, a frame loop with a fixed memory budget, a plugin
- * whose host owns all allocations). It writes the extent (the value meshopt_simplifyScale
- * returns) to the device float *extent, reading positions that are already on the device,
- * enqueued on `stream` without synchronising; it calls no cudaMalloc/cudaFree.
- * Its scratch is a fixed 512 KiB device array inside the library (held on every GPU that
+ * run: a renderer's frame loop whose device-memory budget is fixed up front, or a plugin whose
+ * host application owns every device allocation. It writes the extent (the value
+ * meshopt_simplifyScale returns) to the device float *extent, reading positions that are
+ * already on the device, enqueued on `stream` without synchronising; it calls no
+ * cudaMalloc/cudaFree and no allocating library routine.
+ * Its scratch is a fixed 1 MiB device array inside the library (held on every GPU that
  * loads it until exit), which limits vertex_count to 67,108,864; larger counts return
  * meshoptgpu_StatusInvalidArgument. The first call on each device looks up that array's
  * device address: make it before any stream capture. All calls share the array, so calls

@@ -46,7 +46,7 @@ EXPORTS = [
     "meshoptgpu_getLastStatus", "meshoptgpu_getLastMessage", "meshoptgpu_getLastPassStats",
     "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
     "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
-    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc",
+    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc", "meshoptgpu_getLastPassPhaseTimes",
     "meshoptgpu_simplifyBatch", "meshoptgpu_simplifyBatchHost", "meshoptgpu_setBatchConfig", "meshoptgpu_getBatchThreads",
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
@@ -105,6 +105,8 @@ def load():
     lib.meshoptgpu_setTiming.argtypes = [C.c_int]
     lib.meshoptgpu_getLastPhaseTimes.restype = C.c_int
     lib.meshoptgpu_getLastPhaseTimes.argtypes = [vp]
+    lib.meshoptgpu_getLastPassPhaseTimes.restype = C.c_int
+    lib.meshoptgpu_getLastPassPhaseTimes.argtypes = [vp, C.c_int]
     lib.meshoptgpu_simplifyDevice.restype = sz
     lib.meshoptgpu_simplifyDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp, vp]
     lib.meshoptgpu_workspaceBytes.restype = sz
@@ -305,6 +307,15 @@ def last_phase_times():
     return dict(zip(keys, [float(x) for x in out]))
 
 
+def last_pass_phase_times():
+    """With timing on: per pass of the last single-mesh call, CUDA-event ms of its adjacency,
+    pick, rank, sort and perform phases."""
+    out = (C.c_float * (5 * 128))()
+    n = load().meshoptgpu_getLastPassPhaseTimes(C.cast(out, C.c_void_p), 128)
+    keys = ["adjacency", "pick", "rank", "sort", "perform"]
+    return [dict(zip(keys, [float(out[5 * i + j]) for j in range(5)])) for i in range(min(n, 128))]
+
+
 def workspace_bytes(index_count, vertex_count, attribute_count=0):
     return int(load().meshoptgpu_workspaceBytes(index_count, vertex_count, attribute_count))
 
@@ -330,8 +341,9 @@ def kernel_profile():
 def simplify_scale_noalloc(d_extent, d_positions, vertex_count, positions_stride=12, stream=0):
     """meshoptgpu_simplifyScaleNoAlloc: writes the extent to the device float at d_extent.
 
-    For callers that must not allocate device memory while they run (graph capture, fixed
-    budgets); it reads device positions and uses only the library's fixed 512 KiB scratch,
+    For callers that must not allocate device memory while they run (a fixed device-memory
+    budget, a host that owns every allocation); it reads device positions and uses only the
+    library's fixed 1 MiB scratch,
     which limits vertex_count to 67,108,864. Enqueued on `stream` without synchronising.
     Returns the status code (0 on success).
     """

@@ -1695,6 +1695,15 @@ int meshoptgpu_getLastRoundTrace(unsigned int* active, float* micros, int max_ro
 	return n;
 }
 
+int meshoptgpu_getLastPassPhaseTimes(float* out, int max_passes)
+{
+	const RunResult& r = state().last;
+	int n = int(r.pass_phase_ms.size());
+	for (int i = 0; i < n && i < max_passes; ++i)
+		memcpy(out + 5 * i, r.pass_phase_ms[i].data(), 5 * sizeof(float));
+	return n;
+}
+
 void meshoptgpu_setTiming(int enabled)
 {
 	state().timing = enabled != 0;

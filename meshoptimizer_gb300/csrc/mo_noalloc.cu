@@ -1,10 +1,9 @@
 // mo_noalloc.cu - meshoptgpu_simplifyScaleNoAlloc: the mesh extent (what meshopt_simplifyScale
 // returns) computed on device data without allocating anything.
 //
-// Who needs this: code that must not call cudaMalloc/cudaFree while it runs, e.g. work being
-// recorded into a CUDA graph (allocation calls are not allowed while a stream is capturing),
-// a renderer's frame loop whose device-memory budget is fixed up front, or a plugin whose host
-// application owns all device allocations. meshopt_simplifyScale stages the positions in
+// Who needs this: code that must not call cudaMalloc/cudaFree while it runs, e.g. a renderer's
+// frame loop whose device-memory budget is fixed up front, or a plugin whose host application
+// owns all device allocations. meshopt_simplifyScale stages the positions in
 // device scratch that it allocates on first use; this entry point instead reads positions the
 // caller already has on the device and keeps its only scratch, the per-block partial extents,
 // in a fixed file-scope device array.
@@ -25,12 +24,12 @@ namespace
 {
 
 constexpr int kThreads = 256;
-constexpr int kPerThread = 16;
-constexpr size_t kPerBlock = size_t(kThreads) * kPerThread;        // 4096 vertices per block
-constexpr size_t kMaxBlocks = 16384;
+constexpr int kPerThread = 8;
+constexpr size_t kPerBlock = size_t(kThreads) * kPerThread;        // 2048 vertices per block
+constexpr size_t kMaxBlocks = 32768;
 constexpr size_t kMaxVertices = kMaxBlocks * kPerBlock;           // 67,108,864 vertices
 constexpr size_t kTicketWord = kMaxBlocks * 8;                     // after the partials
-constexpr size_t kScratchWords = kTicketWord + 64;                 // 512 KiB + 256 B
+constexpr size_t kScratchWords = kTicketWord + 64;                 // 1 MiB + 256 B
 
 // per block: min xyz, max xyz (as float bits) at [8 * block]; the finished-block ticket at kTicketWord
 static __device__ __align__(256) unsigned int g_scale_scratch[kScratchWords];
@@ -73,18 +72,30 @@ __device__ void blockFold(float (&v)[6], float (*sm)[6])
 				v[j] = j < 3 ? foldMin(v[j], sm[q][j]) : foldMax(v[j], sm[q][j]);
 }
 
-// One launch: every block folds 4096 vertices into its partial; the last block to finish
-// (ticket) folds the partials in block order and writes the extent.
+// One launch: every block folds 2048 vertices into its partial; the last block to finish
+// (ticket) folds the partials in block order and writes the extent. A block first copies the
+// positions of its vertices into shared memory with consecutive threads on consecutive words
+// (coalesced whatever the stride), then each thread folds its 8 consecutive vertices from there
+// in index order.
 __global__ void __launch_bounds__(kThreads) kScaleNoAlloc(const float* __restrict__ pos, size_t stride_f, size_t n, unsigned int* scratch, float* out)
 {
 	__shared__ float sm[kThreads / 32][6];
+	__shared__ float sp[kPerBlock * 3];
 	__shared__ bool last;
 	float v[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
-	size_t begin = blockIdx.x * kPerBlock + size_t(threadIdx.x) * kPerThread;
-	size_t end = begin + kPerThread < n ? begin + kPerThread : n;
-	for (size_t i = begin; i < end; ++i)
+	const size_t base = blockIdx.x * kPerBlock;
+	const unsigned int count = unsigned(n - base < kPerBlock ? n - base : kPerBlock);
+	for (unsigned int w = threadIdx.x; w < count * 3; w += kThreads)
 	{
-		const float* p = pos + i * stride_f;
+		const unsigned int i = w / 3, c = w - i * 3;
+		sp[w] = __ldg(pos + (base + i) * stride_f + c);
+	}
+	__syncthreads();
+	const unsigned int begin = threadIdx.x * kPerThread;
+	const unsigned int end = begin + kPerThread < count ? begin + kPerThread : count;
+	for (unsigned int i = begin; i < end; ++i)
+	{
+		const float* p = sp + i * 3;
 		for (int j = 0; j < 3; ++j)
 		{
 			v[j] = v[j] > p[j] ? p[j] : v[j];

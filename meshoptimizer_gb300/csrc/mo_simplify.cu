@@ -1467,12 +1467,15 @@ struct PerformArgs
 	const unsigned char* skind;
 	const unsigned int* serr;
 	unsigned char* status;
-	// per-vertex decision state; marks alternate by round parity
+	// per-vertex decision state, marks alternating by round parity (a mark is the round's tag in the
+	// high word and the candidate's sorted position in the low word; later rounds have smaller tags):
+	//  * minT[p][v]: the earliest undecided candidate with endpoint v; 0 once a commit took v;
+	//  * minS[2 v + p]: the earliest undecided candidate that moves v; once a commit moved v, the
+	//    pair holds {that commit's sorted position, v's target}, both with tag 0.
+	// A pass leaves both as it found them: the apply phase restores what its commits wrote.
 	unsigned int vcount;
 	unsigned long long* minT[2];
-	unsigned long long* minS[2];
-	unsigned char* touched;
-	unsigned long long* moved; // (sorted position of the commit that moved the vertex << 32) | target; ~0: not moved
+	unsigned long long* minS;
 	unsigned int* cr;
 	unsigned int* list[2];     // undecided candidates (pick order), one region per block
 	unsigned int* commits;     // committed candidates (pick order), one region per block
@@ -1532,91 +1535,87 @@ __device__ __forceinline__ void commitOne(const PerformArgs& a, unsigned int c, 
 	}
 	else
 		target = i1;
-	a.moved[r0] = ((unsigned long long)k << 32) | target;
-	a.touched[r0] = 1;
-	a.touched[r1] = 1;
+	*reinterpret_cast<ulonglong2*>(a.minS + 2 * (size_t)r0) = make_ulonglong2(k, target);
+	a.minT[0][r0] = 0;
+	a.minT[1][r0] = 0;
+	a.minT[0][r1] = 0;
+	a.minT[1][r1] = 0;
 	a.status[k] = kCommit;
 }
 
-// The rule runs in four stages per round, each over the candidates the stage before left (so
-// lanes stay busy): the lock flags and endpoint marks (in the rounds loop), the one-ring's marks
-// (ringWaits), the flip test and the commit (flipOrCommit), and last the candidates that still
+// The rule runs in three stages per round, each over the candidates the stage before left (so
+// lanes stay busy): the endpoint marks (in the rounds loop); one walk over the one-ring
+// (ringDecide) for the waits, the flip test and the commit; and last the candidates that still
 // wait: locked at once if a commit of this round took an endpoint, else marked for the next round.
 
-// no undecided earlier candidate may move a vertex of the one-ring (its sources): true if one does
-__device__ __forceinline__ bool ringWaits(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
-{
-	const unsigned int r0 = rec.x, b = rec.z, e = rec.w;
-	const unsigned long long tag = roundTag(round);
-	const unsigned long long* minS = a.minS[round & 1];
-	for (unsigned int j = b; j < e; j += 4)
-	{
-		uint2 ed[4];
-#pragma unroll
-		for (int q = 0; q < 4; ++q)
-			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r0, r0);
-		unsigned long long sx[4], sy[4];
-#pragma unroll
-		for (int q = 0; q < 4; ++q)
-		{
-			sx[q] = __ldcg(minS + ed[q].x);
-			sy[q] = __ldcg(minS + ed[q].y);
-		}
-		bool wait = false;
-#pragma unroll
-		for (int q = 0; q < 4; ++q)
-			wait |= earlierThan(sx[q], tag, k) | earlierThan(sy[q], tag, k);
-		if (wait)
-			return true;
-	}
-	return false;
-}
-
-#ifndef MO_FLIP_BATCH
-#define MO_FLIP_BATCH 2
+#ifndef MO_RING_BATCH
+#define MO_RING_BATCH 2
 #endif
 
-// flip test against the one-ring as moved by earlier commits (hasTriangleFlips :1201-1232), then
-// the commit; the neighbours' own positions are loaded with their moved records (a moved
-// neighbour's target position is loaded after). Returns true if the candidate committed.
-__device__ __forceinline__ bool flipOrCommit(const PerformArgs& a, unsigned int c, unsigned int k, const uint4& rec)
+enum
+{
+	kRingWaits = 0,
+	kRingFlip = 1,
+	kRingCommit = 2,
+};
+
+// One walk over the one-ring of r0. If an undecided earlier candidate moves a vertex of it, the
+// candidate waits. Otherwise the flip test (hasTriangleFlips :1201-1232) sees the one-ring as
+// moved by earlier commits only, and the candidate is rejected or commits. The whole ring is
+// checked for waits before a flip decides anything: a wait means an earlier decision is still
+// open that may move a vertex the test reads.
+__device__ __forceinline__ int ringDecide(const PerformArgs& a, unsigned int c, unsigned int k, const uint4& rec, unsigned int round)
 {
 	const unsigned int r0 = rec.x, r1 = rec.y, b = rec.z, e = rec.w;
-	V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
-	constexpr int FB = MO_FLIP_BATCH;
+	const unsigned long long tag = roundTag(round);
+	const unsigned int p = round & 1;
+	const V3 v0 = ldpos(a.pos, r0), v1 = ldpos(a.pos, r1);
+	bool flip = false;
+	constexpr int FB = MO_RING_BATCH;
 	for (unsigned int j = b; j < e; j += FB)
 	{
 		uint2 ed[FB];
-		unsigned long long mx[FB], my[FB];
+		ulonglong2 sx[FB], sy[FB];
 		float4 px[FB], py[FB];
 #pragma unroll
 		for (int q = 0; q < FB; ++q)
 		{
-			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r1, r1);
-			mx[q] = __ldcg(a.moved + ed[q].x);
-			my[q] = __ldcg(a.moved + ed[q].y);
+			ed[q] = j + q < e ? __ldg(a.adj + j + q) : make_uint2(r1, r1); // r1 is in the ring already
+			sx[q] = __ldcg(reinterpret_cast<const ulonglong2*>(a.minS) + ed[q].x);
+			sy[q] = __ldcg(reinterpret_cast<const ulonglong2*>(a.minS) + ed[q].y);
 			px[q] = __ldg(a.pos + ed[q].x);
 			py[q] = __ldg(a.pos + ed[q].y);
 		}
+		bool wait = false;
+#pragma unroll
+		for (int q = 0; q < FB; ++q)
+			wait |= earlierThan(p ? sx[q].y : sx[q].x, tag, k) | earlierThan(p ? sy[q].y : sy[q].x, tag, k);
+		if (wait)
+			return kRingWaits;
+		if (flip)
+			continue;
 #pragma unroll
 		for (int q = 0; q < FB; ++q)
 		{
-			bool mvx = (unsigned int)(mx[q] >> 32) < k, mvy = (unsigned int)(my[q] >> 32) < k;
-			unsigned int va = mvx ? (unsigned int)mx[q] : ed[q].x;
-			unsigned int vb = mvy ? (unsigned int)my[q] : ed[q].y;
+			// moved by an earlier commit: the pair holds {commit, target} with tag 0
+			const bool mvx = (sx[q].x >> 32) == 0 && (unsigned int)sx[q].x < k;
+			const bool mvy = (sy[q].x >> 32) == 0 && (unsigned int)sy[q].x < k;
+			const unsigned int va = mvx ? (unsigned int)sx[q].y : ed[q].x;
+			const unsigned int vb = mvy ? (unsigned int)sy[q].y : ed[q].y;
 			if (va == r1 || vb == r1 || va == vb)
 				continue;
-			V3 pa = mvx ? ldpos(a.pos, va) : V3{px[q].x, px[q].y, px[q].z};
-			V3 pb = mvy ? ldpos(a.pos, vb) : V3{py[q].x, py[q].y, py[q].z};
-			if (triFlip(pa, pb, v0, v1))
-			{
-				a.status[k] = kSkipFlip;
-				return false;
-			}
+			const V3 pa = mvx ? ldpos(a.pos, va) : V3{px[q].x, px[q].y, px[q].z};
+			const V3 pb = mvy ? ldpos(a.pos, vb) : V3{py[q].x, py[q].y, py[q].z};
+			flip |= triFlip(pa, pb, v0, v1);
 		}
 	}
+	if (flip)
+	{
+		a.status[k] = kSkipFlip;
+		return kRingFlip;
+	}
 	commitOne(a, c, k, r0, r1);
-	return true;
+	return kRingCommit;
 }
 
 __device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int k, const uint4& rec, unsigned int round)
@@ -1624,7 +1623,7 @@ __device__ __forceinline__ void markCandidate(const PerformArgs& a, unsigned int
 	unsigned long long key = roundTag(round) | k;
 	atomicMin(&a.minT[round & 1][rec.x], key);
 	atomicMin(&a.minT[round & 1][rec.y], key);
-	atomicMin(&a.minS[round & 1][rec.x], key);
+	atomicMin(&a.minS[2 * (size_t)rec.x + (round & 1)], key);
 }
 
 // per sorted candidate: triangles removed if committed, flip rejection, committed error
@@ -1867,7 +1866,7 @@ struct PhaseClock
 __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(PerformArgs a)
 {
 	__shared__ unsigned int s_app[4];
-	__shared__ unsigned int s_stage[3][kStageChunk]; // candidates passed to stage B, to stage C, and kept for stage D
+	__shared__ unsigned int s_stage[2][kStageChunk]; // candidates passed to stage B, and kept for stage C (wait)
 	__shared__ unsigned int s_commits;               // this block's commits so far
 	PhaseClock pc;
 	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
@@ -1902,11 +1901,7 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 	}
 
 	for (size_t i = gtid(); i < a.vcount; i += gthreads)
-	{
-		a.touched[i] = 0;
-		a.moved[i] = ~0ull;
 		a.cr[i] = (unsigned int)i;
-	}
 
 	unsigned int round = round_base;
 	unsigned long long active_sum = 0;
@@ -1980,10 +1975,9 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 			{
 				const unsigned int c1 = min(nb, c0 + kStageChunk);
 				if (threadIdx.x == 0)
-					s_app[1] = 0, s_app[2] = 0, s_app[3] = 0;
+					s_app[1] = 0, s_app[3] = 0;
 				__syncthreads();
-				// stage A: lock flags and endpoint marks; kStageItems candidates per thread, their
-				// loads issued together
+				// stage A: endpoint marks; kStageItems candidates per thread, their loads issued together
 				const unsigned long long tag = roundTag(round);
 				const unsigned long long* minT = a.minT[round & 1];
 				for (unsigned int base = c0; base < c1; base += blockDim.x * kStageItems)
@@ -2009,85 +2003,85 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 #pragma unroll
 					for (unsigned int q = 0; q < kStageItems; ++q)
 						ok[q] = ok[q] && (!first || (kk[q] >= K0 && kk[q] < K1));
-					unsigned char t[kStageItems];
 					unsigned long long m0[kStageItems], m1[kStageItems];
 #pragma unroll
 					for (unsigned int q = 0; q < kStageItems; ++q)
 					{
-						t[q] = ok[q] ? (unsigned char)(__ldcg(a.touched + ends[q].x) | __ldcg(a.touched + ends[q].y)) : (unsigned char)0;
-						m0[q] = ok[q] ? __ldcg(minT + ends[q].x) : 0ull;
-						m1[q] = ok[q] ? __ldcg(minT + ends[q].y) : 0ull;
+						m0[q] = ok[q] ? __ldcg(minT + ends[q].x) : 1ull;
+						m1[q] = ok[q] ? __ldcg(minT + ends[q].y) : 1ull;
 					}
 #pragma unroll
 					for (unsigned int q = 0; q < kStageItems; ++q)
 					{
 						const unsigned long long mine = tag | kk[q];
-						const bool locked = ok[q] && t[q];
-						const bool keep = ok[q] && !t[q] && (m0[q] != mine || m1[q] != mine);
-						const bool pass = ok[q] && !t[q] && !keep;
+						const bool taken = m0[q] == 0 || m1[q] == 0; // a commit took an endpoint
+						const bool locked = ok[q] && taken;
+						const bool keep = ok[q] && !taken && (m0[q] != mine || m1[q] != mine);
+						const bool pass = ok[q] && !taken && !keep;
 						if (locked)
 							a.status[kk[q]] = kSkipLocked;
-						append(keep, cc[q], &s_app[3], s_stage[2]);
+						append(keep, cc[q], &s_app[3], s_stage[1]);
 						append(pass, cc[q], &s_app[1], s_stage[0]);
 					}
 				}
 				__syncthreads();
-				// stage B: the one-ring's marks
+				// stage B: the one-ring's marks, the flip test and the commit, in one walk
 				const unsigned int nB = s_app[1];
 				for (unsigned int base = 0; base < nB; base += blockDim.x)
 				{
 					const unsigned int x = base + threadIdx.x;
-					bool keep = false, pass = false;
+					int r = kRingFlip;
 					unsigned int c = 0;
 					if (x < nB)
 					{
 						c = s_stage[0][x];
-						keep = ringWaits(a, __ldg(a.rank + c), __ldg(a.cring + c), round);
-						pass = !keep;
+						r = ringDecide(a, c, __ldg(a.rank + c), __ldg(a.cring + c), round);
 					}
-					append(keep, c, &s_app[3], s_stage[2]);
-					append(pass, c, &s_app[2], s_stage[1]);
+					append(r == kRingWaits, c, &s_app[3], s_stage[1]);
+					append(r == kRingCommit, c, &s_commits, commits);
 				}
 				__syncthreads();
-				// stage C: the flip test and the commit
-				const unsigned int nC = s_app[2];
-				for (unsigned int base = 0; base < nC; base += blockDim.x)
-				{
-					const unsigned int x = base + threadIdx.x;
-					bool committed = false;
-					unsigned int c = 0;
-					if (x < nC)
-					{
-						c = s_stage[1][x];
-						committed = flipOrCommit(a, c, __ldg(a.rank + c), __ldg(a.cring + c));
-					}
-					append(committed, c, &s_commits, commits);
-				}
-				__syncthreads();
-				// stage D: the candidates that wait. A commit of this round (this block's, or another's
+				// stage C: the candidates that wait. A commit of this round (this block's, or another's
 				// whose write is already seen) on an endpoint locks one now: that commit is earlier,
 				// so the lock is final, and the candidates waiting on this one need not wait a round
 				// more for it. The others mark their endpoints for the next round.
 				const unsigned int nD = s_app[3];
-				for (unsigned int base = 0; base < nD; base += blockDim.x)
+				for (unsigned int base = 0; base < nD; base += blockDim.x * kStageItems)
 				{
-					const unsigned int x = base + threadIdx.x;
-					bool keep = false;
-					unsigned int c = 0;
-					if (x < nD)
+					unsigned int cc[kStageItems], kk[kStageItems];
+					uint2 ends[kStageItems];
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
 					{
-						c = s_stage[2][x];
-						const unsigned int k = __ldg(a.rank + c);
-						const uint4 rec = __ldg(a.cring + c);
-						if (__ldcg(a.touched + rec.x) | __ldcg(a.touched + rec.y))
-							a.status[k] = kSkipLocked;
-						else
-						{
-							keep = true;
-							markCandidate(a, k, rec, round + 1);
-						}
+						const unsigned int x = base + q * blockDim.x + threadIdx.x;
+						cc[q] = x < nD ? s_stage[1][x] : ~0u;
+						kk[q] = cc[q] != ~0u ? __ldg(a.rank + cc[q]) : 0u;
+						const uint4 rec = cc[q] != ~0u ? __ldg(a.cring + cc[q]) : make_uint4(0, 0, 0, 0);
+						ends[q] = make_uint2(rec.x, rec.y);
 					}
-					append(keep, c, &s_app[0], next);
+					unsigned long long m0[kStageItems], m1[kStageItems];
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+					{
+						m0[q] = cc[q] != ~0u ? __ldcg(minT + ends[q].x) : 1ull;
+						m1[q] = cc[q] != ~0u ? __ldcg(minT + ends[q].y) : 1ull;
+					}
+#pragma unroll
+					for (unsigned int q = 0; q < kStageItems; ++q)
+					{
+						const bool valid = cc[q] != ~0u;
+						const bool taken = m0[q] == 0 || m1[q] == 0;
+						if (valid && taken)
+							a.status[kk[q]] = kSkipLocked;
+						if (valid && !taken)
+						{
+							const unsigned long long key = roundTag(round + 1) | kk[q];
+							atomicMin(&a.minT[(round + 1) & 1][ends[q].x], key);
+							atomicMin(&a.minT[(round + 1) & 1][ends[q].y], key);
+							atomicMin(&a.minS[2 * (size_t)ends[q].x + ((round + 1) & 1)], key);
+						}
+						append(valid && !taken, cc[q], &s_app[0], next);
+					}
 				}
 				__syncthreads();
 			}
@@ -2215,10 +2209,17 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
 	}
 	{
+		// every commit of the pass, inside the prefix or not, also restores the marks it wrote
 		const unsigned int mc = s_commits; // every append to it was followed by a block barrier
 		for (unsigned int x = threadIdx.x; x < mc; x += blockDim.x)
 		{
 			const unsigned int c = commits[x];
+			const uint4 rec = __ldg(a.cring + c);
+			a.minT[0][rec.x] = ~0ull;
+			a.minT[1][rec.x] = ~0ull;
+			a.minT[0][rec.y] = ~0ull;
+			a.minT[1][rec.y] = ~0ull;
+			*reinterpret_cast<ulonglong2*>(a.minS + 2 * (size_t)rec.x) = make_ulonglong2(~0ull, ~0ull);
 			if (__ldg(a.rank + c) < cut)
 			{
 				unsigned int eb = 0, db = 0;
@@ -2904,8 +2905,7 @@ struct Work
 	unsigned char *skind, *status; // kinds and decisions by sorted position
 	unsigned int *act0, *act1, *commits;
 	unsigned long long *minT, *minS;
-	unsigned char* touched;
-	unsigned long long* moved;
+	unsigned char* touched; // setup scratch (the permissive kinds)
 	unsigned int* cr;
 	unsigned int *comp, *parent;
 	float* comp_err;
@@ -2994,7 +2994,6 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = f
 	w.minT = c.take<unsigned long long>(2 * Vp);
 	w.minS = c.take<unsigned long long>(2 * Vp);
 	w.touched = c.take<unsigned char>(Vp);
-	w.moved = c.take<unsigned long long>(Vp);
 	w.comp = c.take<unsigned int>(Vp);
 	w.parent = c.take<unsigned int>(Vp + 1);
 	w.comp_err = c.take<float>(Vp + 1);
@@ -3631,10 +3630,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				pa.vcount = unsigned(V);
 				pa.minT[0] = w.minT;
 				pa.minT[1] = w.minT + (V + 1);
-				pa.minS[0] = w.minS;
-				pa.minS[1] = w.minS + (V + 1);
-				pa.touched = w.touched;
-				pa.moved = w.moved;
+				pa.minS = w.minS;
 				pa.cr = w.cr;
 				pa.list[0] = w.act0;
 				pa.list[1] = w.act1;
@@ -3758,10 +3754,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			pa.vcount = unsigned(V);
 			pa.minT[0] = w.minT;
 			pa.minT[1] = w.minT + (V + 1);
-			pa.minS[0] = w.minS;
-			pa.minS[1] = w.minS + (V + 1);
-			pa.touched = w.touched;
-			pa.moved = w.moved;
+			pa.minS = w.minS;
 			pa.cr = w.cr;
 			pa.list[0] = w.act0;
 			pa.list[1] = w.act1;
@@ -3841,11 +3834,13 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			prune(vertex_error);
 		if (timed)
 		{
-			acc_adj += elapsed(2, 3);
-			acc_pick += elapsed(3, 4);
-			acc_rank += elapsed(4, 5);
-			acc_sort += elapsed(5, 6);
-			acc_perf += elapsed(6, 7);
+			const std::array<float, 5> ph = {elapsed(2, 3), elapsed(3, 4), elapsed(4, 5), elapsed(5, 6), elapsed(6, 7)};
+			acc_adj += ph[0];
+			acc_pick += ph[1];
+			acc_rank += ph[2];
+			acc_sort += ph[3];
+			acc_perf += ph[4];
+			rr.pass_phase_ms.push_back(ph);
 		}
 	}
 

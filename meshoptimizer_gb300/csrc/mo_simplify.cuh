@@ -5,6 +5,7 @@
 #include <stddef.h>
 
 #include <algorithm>
+#include <array>
 #include <vector>
 
 #include "mo_prims.cuh"
@@ -72,6 +73,8 @@ struct RunResult
 	float perform_phase_ms[8] = {};
 	// decision rounds of the run in order: active candidates and duration (microseconds)
 	std::vector<std::pair<unsigned int, float>> round_trace;
+	// with timing on: CUDA-event times (ms) of each pass's adjacency, pick, rank, sort and perform
+	std::vector<std::array<float, 5>> pass_phase_ms;
 };
 
 // Device timings of the phases of one run (milliseconds, from CUDA events).

@@ -66,10 +66,16 @@ class SetupDump(C.Structure):
     ]
 
 
+def reference_root() -> str:
+    """Where the reference's sources are: $REFERENCE_ROOT, else a `reference` checkout beside
+    this repository. Only the build of the reference library and fixture generation read it."""
+    return os.environ.get("REFERENCE_ROOT") or os.path.join(os.path.dirname(HERE), "..", "reference")
+
+
 def build(with_reference: bool = True) -> None:
     """Compile the port and, where the reference sources exist, the reference library."""
     subprocess.run(["make", "-s", "-C", HERE, "libmo_oracle.so"], check=True)
-    ref_root = os.environ.get("REFERENCE_ROOT", "/root/reference")
+    ref_root = reference_root()
     if with_reference and os.path.isfile(os.path.join(ref_root, "src", "simplifier.cpp")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE_ROOT={ref_root}"], check=True)
         if os.path.isfile(os.path.join(ref_root, "demo", "clusterlod.h")):

@@ -47,7 +47,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 from meshoptimizer_gb300 import workloads as W  # noqa: E402
 
-REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT") or os.path.join(ROOT, "..", "reference")
 TESTS_CPP = os.path.join(REFERENCE_ROOT, "demo", "tests.cpp")
 
 
