@@ -225,7 +225,8 @@ def _groups_line(args, mg, meshes, tris, out_tris, total_ms, tt, h2d, d2h, plain
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "cluster_groups_4096", "groups": len(meshes), "input_tris": tris, "output_tris": out_tris,
                    "tris_per_group": "200-512", "options": "LockBorder", "target": "50%", "target_error": 2e-2,
-                   "batch_threads_per_cta": mg.batch_threads(), "l2": "flushed between steps (512 MiB write, outside the timed events)"},
+                   "batch_threads_per_cta": mg.batch_threads(), "batch_smem_kib": mg.tuning(max(len(m["indices"]) for m in meshes))["batch_smem_kib"],
+                   "l2": "flushed between steps (512 MiB write, outside the timed events)"},
         "e2e": {"value": round(tris * args.steps / tt / 1e6, 4), "unit": "Mtris/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": round(1e3 * tt / args.steps, 3)},
         "plain_gpu": plain_gpu,
@@ -698,6 +699,7 @@ def bench_single(args, mg, torch, c, dist=None, world=1, rank=0, local=0, roofli
 
     for _ in range(max(args.warmup, 0)):
         n_out, err = step()
+    tuned = mg.tuning(idx.numel(), ac_used)  # the first warm-up call tuned this size class's launch shape
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = mg.launch_count()
@@ -825,7 +827,8 @@ def bench_single(args, mg, torch, c, dist=None, world=1, rank=0, local=0, roofli
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": c["name"], "input_tris": c["tris"], "output_tris": int(n_out) // 3, "target_index_count": c["target"],
                    "target_error": c["error"], "options": c["options"], "attributes": ac, "result_error": err,
-                   "l2": "flushed between steps (512 MiB write, outside the timed events)", "parallelism": f"replicas{world}"},
+                   "l2": "flushed between steps (512 MiB write, outside the timed events)", "parallelism": f"replicas{world}",
+                   "autotuned": {"perform_blocks_per_sm": tuned["perform_blocks_per_sm"], "sort_items_per_thread": tuned["sort_items"]}},
         "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "bit_exact_vs_oracle": bit_exact, "error_vs_fp64_oracle": fp64,
         "clocks": clocks.summary(), "gpu_launches": int(launches),
         "phases_ms": {k: round(v, 3) for k, v in phases.items()},

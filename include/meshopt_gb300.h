@@ -225,18 +225,33 @@ MESHOPTGPU_API int meshoptgpu_buildMeshletsFlexGroups(unsigned int* meshlets, un
     float cone_weight, float split_factor, int optimize_level, void* stream);
 
 /* Batch launch shape: threads per CTA (128, 256 or 512; 0 = autotune, the default) and the
- * shared-memory budget per CTA in bytes (0 = default). The autotuner times each thread count
- * on the first batch of a size class and keeps the fastest for that class. */
+ * shared-memory budget per CTA in bytes (0 = autotune, the default). The autotuner times every
+ * open pair of thread count and budget (64, 104 and 160 KiB) on the first batch of a size class
+ * and keeps the fastest for that class. */
 MESHOPTGPU_API void meshoptgpu_setBatchConfig(int threads, unsigned int smem_bytes);
 
 /* Drop-in calls (meshopt_simplify, meshopt_simplifyWithAttributes, meshoptgpu_simplifyDevice)
  * on meshes with at most max_index_count indices run on the batch kernel as a batch of one,
- * where one CTA does the whole simplification: below about 5k triangles that is faster than
- * the multi-CTA pass loop, whose cost per call is fixed by its launches and host reads. Results
- * are identical either way. Such calls record no pass statistics, phase times or round trace
- * (meshoptgpu_setTiming(1) keeps every call on the single-mesh path). Per calling thread;
- * default 15000, 0 disables. */
+ * where one CTA does the whole simplification: for small meshes that is faster than the
+ * multi-CTA pass loop, whose cost per call is fixed by its launches. Results are identical
+ * either way. Such calls record no pass statistics, phase times or round trace
+ * (meshoptgpu_setTiming(1) keeps every call on the single-mesh path). Per calling thread.
+ * The default, (size_t)-1, leaves the route to the autotuner: up to 3000 indices the batch
+ * kernel, above 98304 the single-mesh path, and in between whichever the first repeatable call
+ * of the size class timed faster on its own mesh. 0 sends every call to the single-mesh path.
+ *
+ * The single-mesh path's launch shape (pass-kernel blocks per SM, the pass sort's tile) is
+ * autotuned the same way, per size class of the mesh: the first repeatable call (destination
+ * not aliasing indices, no update mode, Prune or debug bit) times the candidates on its own
+ * mesh. MESHOPTGPU_AUTOTUNE=0 in the environment turns both tuners off (fixed defaults). */
 MESHOPTGPU_API void meshoptgpu_setDropinBatchLimit(size_t max_index_count);
+
+/* The autotuner's choices for meshes of index_count indices (with attributes or not), on the
+ * current device: out4[0] pass-kernel blocks per SM, out4[1] pass sort candidates per thread
+ * (0: chosen by count), out4[2] drop-in route (1 batch kernel, 0 single-mesh path, -1 not
+ * tuned), out4[3] the batch kernel's shared-memory budget (KiB) for the largest size class
+ * tuned so far (0: none). Returns 1 if the single-mesh shape is tuned for that size class. */
+MESHOPTGPU_API int meshoptgpu_getTuning(size_t index_count, size_t attribute_count, int* out4);
 
 /* The single-mesh path runs its pass loop (src/simplifier.cpp:2493-2541) on the device: one
  * pass is recorded into a CUDA graph as the body of a WHILE conditional node and replayed

@@ -46,7 +46,7 @@ EXPORTS = [
     "meshoptgpu_getLastStatus", "meshoptgpu_getLastMessage", "meshoptgpu_getLastPassStats",
     "meshoptgpu_setTiming", "meshoptgpu_getLastPhaseTimes", "meshoptgpu_simplifyDevice",
     "meshoptgpu_workspaceBytes", "meshoptgpu_releaseThreadResources", "meshoptgpu_getLaunchCount",
-    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc", "meshoptgpu_getLastPassPhaseTimes",
+    "meshoptgpu_setKernelProfile", "meshoptgpu_getKernelProfile", "meshoptgpu_simplifyScaleNoAlloc", "meshoptgpu_getLastPassPhaseTimes", "meshoptgpu_getTuning",
     "meshoptgpu_simplifyBatch", "meshoptgpu_simplifyBatchHost", "meshoptgpu_setBatchConfig", "meshoptgpu_getBatchThreads",
     "meshoptgpu_serverCreate", "meshoptgpu_serverDestroy", "meshoptgpu_serverSubmit", "meshoptgpu_serverWait", "meshoptgpu_serverStats",
     "meshoptgpu_getLastRoundTrace",
@@ -107,6 +107,8 @@ def load():
     lib.meshoptgpu_getLastPhaseTimes.argtypes = [vp]
     lib.meshoptgpu_getLastPassPhaseTimes.restype = C.c_int
     lib.meshoptgpu_getLastPassPhaseTimes.argtypes = [vp, C.c_int]
+    lib.meshoptgpu_getTuning.restype = C.c_int
+    lib.meshoptgpu_getTuning.argtypes = [sz, sz, vp]
     lib.meshoptgpu_simplifyDevice.restype = sz
     lib.meshoptgpu_simplifyDevice.argtypes = [vp, vp, sz, vp, sz, sz, vp, sz, vp, sz, vp, sz, f32, u32, vp, vp]
     lib.meshoptgpu_workspaceBytes.restype = sz
@@ -314,6 +316,17 @@ def last_pass_phase_times():
     n = load().meshoptgpu_getLastPassPhaseTimes(C.cast(out, C.c_void_p), 128)
     keys = ["adjacency", "pick", "rank", "sort", "perform"]
     return [dict(zip(keys, [float(out[5 * i + j]) for j in range(5)])) for i in range(min(n, 128))]
+
+
+def tuning(index_count, attribute_count=0):
+    """The autotuner's choices for meshes of index_count indices: pass-kernel blocks per SM, pass
+    sort candidates per thread (0: by count), drop-in route (batch / single / None) and the batch
+    kernel's shared-memory budget in KiB (largest size class tuned so far); None if untuned."""
+    out = (C.c_int * 4)()
+    found = load().meshoptgpu_getTuning(int(index_count), int(attribute_count), C.cast(out, C.c_void_p))
+    route = {1: "batch", 0: "single"}.get(int(out[2]))
+    return {"perform_blocks_per_sm": int(out[0]) if found else None, "sort_items": int(out[1]) if found else None,
+            "dropin_route": route, "batch_smem_kib": int(out[3]) or None}
 
 
 def workspace_bytes(index_count, vertex_count, attribute_count=0):
@@ -581,11 +594,12 @@ def set_batch_config(threads=0, smem_bytes=0):
     load().meshoptgpu_setBatchConfig(int(threads), int(smem_bytes))
 
 
-DROPIN_BATCH_LIMIT = 15000  # the library's default
+DROPIN_BATCH_LIMIT = 2 ** 64 - 1  # the library's default: the route is autotuned per size class
 
 
 def set_dropin_batch_limit(max_index_count=DROPIN_BATCH_LIMIT):
-    """Drop-in calls on meshes with at most this many indices run on the batch kernel (0: never)."""
+    """Drop-in calls on meshes with at most this many indices run on the batch kernel (0: never;
+    the default leaves the route to the autotuner)."""
     load().meshoptgpu_setDropinBatchLimit(int(max_index_count))
 
 

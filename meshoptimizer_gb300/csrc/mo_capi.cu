@@ -19,8 +19,10 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <thread>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -98,10 +100,10 @@ struct ThreadState
 	int batch_threads = 0;          // 0: autotune
 	int sms = 1;                    // the device's SM count
 	unsigned int batch_smem = 0;    // 0: default budget
-	// drop-in calls with at most this many indices run on the batch kernel as a batch of one
-	// (measured crossover on GB300: about 5k triangles; 4.4k-triangle heightfield 1.09 ms batched
-	// against 1.18 ms on the pass loop, 7.9k triangles 2.01 against 1.47 ms)
-	size_t dropin_batch_limit = 15000;
+	// drop-in calls with at most this many indices run on the batch kernel as a batch of one;
+	// (size_t)-1: the autotuner picks the route per size class (see routeAndRun)
+	size_t dropin_batch_limit = ~size_t(0);
+	bool autotune = true; // the single-mesh path's launch shape and the drop-in route are timed per size class
 	// drop-in copies of positions and attributes on streams of their own (another copy engine;
 	// the attributes are waited for only where they are first read)
 	cudaStream_t copy_stream[2] = {nullptr, nullptr};
@@ -153,6 +155,8 @@ struct ThreadState
 		MO_CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
 		MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 		simplifier.reset(new Simplifier(dev));
+		const char* at = getenv("MESHOPTGPU_AUTOTUNE");
+		autotune = !(at && atoi(at) == 0) && !getenv("MESHOPTGPU_PERFORM_BLOCKS_PER_SM");
 	}
 };
 
@@ -286,9 +290,14 @@ void parallelCopies(const std::vector<HostCopy>& copies)
 		th.join();
 }
 
-// Runs a small mesh (device pointers) on the batch kernel when the calling thread's drop-in
-// limit and the mesh's options allow; returns false to leave it to the single-mesh path.
+// Runs a small mesh (device pointers) on the batch kernel when the mesh's options allow; returns
+// false to leave it to the single-mesh path.
 bool smallMeshOnBatch(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st);
+
+// A drop-in or device call's simplification (device pointers): on the batch kernel or the
+// single-mesh path, as the calling thread's drop-in limit or the autotuner decides; the result
+// in d_out and s.last.
+void routeAndRun(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st, bool allow_batch);
 
 size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions, size_t vertex_count,
     size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
@@ -359,8 +368,7 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		m.target_error = target_error;
 		m.options = options;
 		m.attributes_ready = split ? s.copy_done[1] : nullptr;
-		if (split || !smallMeshOnBatch(s, m, d_out, st))
-			s.last = s.simplifier->run(m, d_out, st, s.timing ? &s.times : nullptr);
+		routeAndRun(s, m, d_out, st, !split);
 		if (s.last.index_count)
 			MO_CUDA_CHECK(cudaMemcpyAsync(destination, d_out, s.last.index_count * 4, cudaMemcpyDeviceToHost, st));
 		MO_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -468,8 +476,11 @@ const size_t kBatchSlabTotal = size_t(16) << 30; // global slabs for meshes beyo
 struct BatchTuner
 {
 	std::mutex lock;
-	std::map<int, int> threads; // size class -> fastest threads per CTA
+	std::map<int, std::pair<int, size_t>> shape; // size class -> fastest (threads per CTA, shared-memory budget per CTA)
 } g_tuner;
+
+// the shared-memory budgets the batch autotuner times (two, two and one CTAs of 256 threads per SM)
+const size_t kBatchSmemBudgets[3] = {64 * 1024, kBatchSmemDefault, 160 * 1024};
 
 int sizeClass(size_t max_index_count)
 {
@@ -555,19 +566,27 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 	std::iota(perm.begin(), perm.end(), 0u);
 	std::stable_sort(perm.begin(), perm.end(), [&](unsigned int a, unsigned int b) { return descs[a].index_count > descs[b].index_count; });
 	std::vector<BatchDesc> ordered(n);
-	size_t budget = s.batch_smem ? s.batch_smem : kBatchSmemDefault;
-	size_t maxfit = 0, maxslab = 0, maxidx = 0;
+	size_t maxidx = 0;
 	for (size_t i = 0; i < n; ++i)
 	{
 		ordered[i] = descs[perm[i]];
-		size_t ws = descWorkspace(ordered[i], false);
-		if (ws <= budget)
-			maxfit = std::max(maxfit, ws);
-		else
-			maxslab = std::max(maxslab, descWorkspace(ordered[i], true));
 		maxidx = std::max<size_t>(maxidx, ordered[i].index_count);
 	}
-	unsigned int smem = unsigned((maxfit + 15) & ~size_t(15));
+	// a budget's dynamic shared memory (the largest mesh that fits it) and slab size (the largest
+	// that does not): meshes whose workspace fits the launch's shared memory run there
+	auto footprint = [&](size_t budget, unsigned int& smem, size_t& maxslab) {
+		size_t maxfit = 0;
+		maxslab = 0;
+		for (const BatchDesc& d : ordered)
+		{
+			const size_t ws = descWorkspace(d, false);
+			if (ws <= budget)
+				maxfit = std::max(maxfit, ws);
+			else
+				maxslab = std::max(maxslab, descWorkspace(d, true));
+		}
+		smem = unsigned((maxfit + 15) & ~size_t(15));
+	};
 	const int sms = s.sms;
 
 	// device metadata: descriptors, results, the ticket, the attribute maps; descriptors and
@@ -594,7 +613,10 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 	bool full = false;
 	for (const BatchDesc& d : ordered)
 		full = full || batchNeedsFull(d);
-	auto launch = [&](int threads) {
+	auto launch = [&](int threads, size_t budget) {
+		unsigned int smem = 0;
+		size_t maxslab = 0;
+		footprint(budget, smem, maxslab);
 		int per_sm = std::max(1, batchBlocksPerSM(threads, smem, full));
 		unsigned int blocks = unsigned(std::min<size_t>(size_t(per_sm) * sms, n));
 		if (maxslab)
@@ -604,40 +626,59 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 	};
 
 	int threads = s.batch_threads;
-	if (threads == 0)
+	size_t budget = s.batch_smem ? s.batch_smem : kBatchSmemDefault;
+	if (threads == 0 || s.batch_smem == 0)
 	{
+		// the block size and the shared-memory budget the caller left open are autotuned per size
+		// class: the first batch of a class times every candidate pair on its own meshes
+		// (identical results) and keeps the fastest
 		int cls = sizeClass(maxidx);
+		bool known = false;
 		{
 			std::lock_guard<std::mutex> g(g_tuner.lock);
-			auto it = g_tuner.threads.find(cls);
-			if (it != g_tuner.threads.end())
-				threads = it->second;
+			auto it = g_tuner.shape.find(cls);
+			if (it != g_tuner.shape.end())
+			{
+				threads = threads ? threads : it->second.first;
+				budget = s.batch_smem ? budget : it->second.second;
+				known = true;
+			}
 		}
-		if (threads == 0)
+		if (!known)
 		{
-			// autotune: time each block size on this batch (identical results), keep the fastest
 			cudaEvent_t e0, e1;
 			MO_CUDA_CHECK(cudaEventCreate(&e0));
 			MO_CUDA_CHECK(cudaEventCreate(&e1));
 			float best = 1e30f;
+			int best_t = threads ? threads : 256;
+			size_t best_b = budget;
 			for (int t : {128, 256, 512})
 			{
-				MO_CUDA_CHECK(cudaEventRecord(e0, st));
-				launch(t);
-				MO_CUDA_CHECK(cudaEventRecord(e1, st));
-				MO_CUDA_CHECK(cudaEventSynchronize(e1));
-				float ms = 0;
-				MO_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
-				if (ms < best)
-					best = ms, threads = t;
+				if (threads && t != threads)
+					continue;
+				for (size_t b : kBatchSmemBudgets)
+				{
+					if (s.batch_smem && b != s.batch_smem)
+						continue;
+					MO_CUDA_CHECK(cudaEventRecord(e0, st));
+					launch(t, b);
+					MO_CUDA_CHECK(cudaEventRecord(e1, st));
+					MO_CUDA_CHECK(cudaEventSynchronize(e1));
+					float ms = 0;
+					MO_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+					if (ms < best)
+						best = ms, best_t = t, best_b = b;
+				}
 			}
 			cudaEventDestroy(e0);
 			cudaEventDestroy(e1);
+			threads = best_t;
+			budget = best_b;
 			std::lock_guard<std::mutex> g(g_tuner.lock);
-			g_tuner.threads[cls] = threads;
+			g_tuner.shape[cls] = std::make_pair(threads, budget);
 		}
 	}
-	launch(threads);
+	launch(threads, budget);
 	std::vector<BatchResult> tmp(n);
 	MO_CUDA_CHECK(cudaMemcpyAsync(tmp.data(), d_res, n * sizeof(BatchResult), cudaMemcpyDeviceToHost, st));
 	MO_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -650,8 +691,7 @@ void runBatch(ThreadState& s, std::vector<BatchDesc>& descs, const AttrMaps& map
 // batch kernel's option set unless the mesh may take the single-mesh path
 bool smallMeshOnBatch(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st)
 {
-	if (s.timing || m.index_count == 0 || m.index_count > s.dropin_batch_limit || (m.options & ~kBatchOptions) ||
-	    m.vertex_count >= (size_t(1) << 32))
+	if (s.timing || m.index_count == 0 || (m.options & ~kBatchOptions) || m.vertex_count >= (size_t(1) << 32))
 		return false;
 	meshoptgpu_BatchMesh bm{};
 	bm.index_count = m.index_count;
@@ -676,6 +716,162 @@ bool smallMeshOnBatch(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cu
 	s.last.index_count = res[0].index_count;
 	s.last.result_error = res[0].result_error;
 	return true;
+}
+
+// ---------------------------------------------------------------- autotuning of the single-mesh path
+//
+// Per size class of the mesh (its index count's bit length, and whether it has attributes), the
+// first call that can be repeated (its destination does not alias its indices, no update mode,
+// Prune or debug bit) times the candidates on the call's own mesh and keeps the fastest for the
+// class; the results are identical whatever the choice, so the call returns the last candidate's.
+// Later calls of the class take the choice. Tuned:
+//  * the pass kernels' launch shape: pass-kernel blocks per SM (the resident maximum and one and
+//    two fewer), then the pass sort's tile (4, 8 or 16 candidates per thread) at the best;
+//  * the drop-in route for meshes between kDropinBatchAlways and kDropinSingleAlways indices: the
+//    batch kernel (one CTA does the whole mesh) or the single-mesh path (multi-CTA pass loop).
+constexpr size_t kTuneMinIndices = 3000;       // below: the default shape (nothing to gain)
+constexpr size_t kDropinBatchAlways = 3000;    // up to here drop-in calls take the batch kernel
+constexpr size_t kDropinSingleAlways = 98304;  // above here the single-mesh path
+constexpr size_t kDropinDefault = 15000;       // the route of calls that cannot be timed
+
+struct ShapeTuner
+{
+	std::mutex lock;
+	std::map<std::tuple<int, int, int>, std::pair<int, unsigned int>> shape; // -> (blocks per SM, sort items)
+	std::map<std::tuple<int, int, int>, bool> batch;                         // -> batch kernel faster
+} g_shapes;
+
+std::tuple<int, int, int> shapeKey(const ThreadState& s, const MeshDesc& m)
+{
+	return std::make_tuple(s.device, sizeClass(m.index_count), m.attribute_count ? 1 : 0);
+}
+
+bool repeatable(const ThreadState& s, const MeshDesc& m, const unsigned int* d_out)
+{
+	return s.autotune && !s.timing && static_cast<const void*>(d_out) != static_cast<const void*>(m.indices) &&
+	       !(m.options & (kOptPrune | kOptInternalDebug | kOptInternalSolve)) && m.index_count > m.target_index_count;
+}
+
+float timedMs(cudaStream_t st, const std::function<void()>& f, int reps)
+{
+	cudaEvent_t e0, e1;
+	MO_CUDA_CHECK(cudaEventCreate(&e0));
+	MO_CUDA_CHECK(cudaEventCreate(&e1));
+	float best = 1e30f;
+	for (int r = 0; r < reps; ++r)
+	{
+		MO_CUDA_CHECK(cudaEventRecord(e0, st));
+		f();
+		MO_CUDA_CHECK(cudaEventRecord(e1, st));
+		MO_CUDA_CHECK(cudaEventSynchronize(e1));
+		float ms = 0;
+		MO_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+		best = std::min(best, ms);
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return best;
+}
+
+// the single-mesh path with its size class's tuned launch shape (tuning it first if it has none)
+void runSingle(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st)
+{
+	Simplifier& sp = *s.simplifier;
+	if (!s.autotune)
+	{
+		s.last = sp.run(m, d_out, st, s.timing ? &s.times : nullptr);
+		return;
+	}
+	const auto key = shapeKey(s, m);
+	{
+		std::lock_guard<std::mutex> g(g_shapes.lock);
+		auto it = g_shapes.shape.find(key);
+		if (it != g_shapes.shape.end())
+		{
+			sp.setPassShape(it->second.first, it->second.second);
+			s.last = sp.run(m, d_out, st, s.timing ? &s.times : nullptr);
+			return;
+		}
+	}
+	const int top = std::max(1, sp.performBlocksPerSMMax());
+	if (!repeatable(s, m, d_out) || m.index_count < kTuneMinIndices)
+	{
+		sp.setPassShape(top, 0);
+		s.last = sp.run(m, d_out, st, s.timing ? &s.times : nullptr);
+		return;
+	}
+	const int reps = 2; // the faster of two runs per candidate
+	auto trial = [&](int bps, unsigned int items) {
+		sp.setPassShape(bps, items);
+		return timedMs(st, [&]() { s.last = sp.run(m, d_out, st); }, reps);
+	};
+	int best_bps = top;
+	float best = 1e30f;
+	for (int bps = top; bps >= std::max(1, top - 2); --bps)
+	{
+		const float ms = trial(bps, 0);
+		if (ms < best)
+			best = ms, best_bps = bps;
+	}
+	unsigned int best_items = 0;
+	for (unsigned int items : {4u, 8u, 16u})
+	{
+		const float ms = trial(best_bps, items);
+		if (ms < best)
+			best = ms, best_items = items;
+	}
+	sp.setPassShape(best_bps, best_items);
+	std::lock_guard<std::mutex> g(g_shapes.lock);
+	g_shapes.shape[key] = std::make_pair(best_bps, best_items);
+}
+
+void routeAndRun(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st, bool allow_batch)
+{
+	const bool batchable = allow_batch && !s.timing && m.index_count && !(m.options & ~kBatchOptions) && m.vertex_count < (size_t(1) << 32);
+	if (!batchable)
+	{
+		runSingle(s, m, d_out, st);
+		return;
+	}
+	if (s.dropin_batch_limit != ~size_t(0) || !s.autotune)
+	{
+		// a fixed limit: the caller's (meshoptgpu_setDropinBatchLimit), or the default
+		const size_t limit = s.dropin_batch_limit != ~size_t(0) ? s.dropin_batch_limit : kDropinDefault;
+		if (m.index_count > limit || !smallMeshOnBatch(s, m, d_out, st))
+			runSingle(s, m, d_out, st);
+		return;
+	}
+	if (m.index_count <= kDropinBatchAlways && smallMeshOnBatch(s, m, d_out, st))
+		return;
+	if (m.index_count > kDropinSingleAlways)
+	{
+		runSingle(s, m, d_out, st);
+		return;
+	}
+	const auto key = shapeKey(s, m);
+	int route = -1; // 1: batch kernel, 0: single-mesh path
+	{
+		std::lock_guard<std::mutex> g(g_shapes.lock);
+		auto it = g_shapes.batch.find(key);
+		if (it != g_shapes.batch.end())
+			route = it->second ? 1 : 0;
+	}
+	if (route < 0 && !repeatable(s, m, d_out))
+		route = m.index_count <= kDropinDefault ? 1 : 0;
+	if (route < 0)
+	{
+		// each route once untimed (its own first-call tuning), then each timed
+		smallMeshOnBatch(s, m, d_out, st);
+		runSingle(s, m, d_out, st);
+		const float tb = timedMs(st, [&]() { smallMeshOnBatch(s, m, d_out, st); }, 2);
+		const float ts = timedMs(st, [&]() { runSingle(s, m, d_out, st); }, 2);
+		std::lock_guard<std::mutex> g(g_shapes.lock);
+		g_shapes.batch[key] = tb < ts;
+		return; // d_out and s.last hold the single-mesh path's result, identical to the batch kernel's
+	}
+	if (route == 1 && smallMeshOnBatch(s, m, d_out, st))
+		return;
+	runSingle(s, m, d_out, st);
 }
 
 std::string checkBatchMesh(const meshoptgpu_BatchMesh& m, bool any_option = false)
@@ -1609,7 +1805,39 @@ int meshoptgpu_getBatchThreads(void)
 	if (s.batch_threads)
 		return s.batch_threads;
 	std::lock_guard<std::mutex> g(g_tuner.lock);
-	return g_tuner.threads.empty() ? 0 : g_tuner.threads.rbegin()->second;
+	return g_tuner.shape.empty() ? 0 : g_tuner.shape.rbegin()->second.first;
+}
+
+int meshoptgpu_getTuning(size_t index_count, size_t attribute_count, int* out4)
+{
+	if (!out4)
+		return 0;
+	int dev = 0;
+	cudaGetDevice(&dev);
+	const auto key = std::make_tuple(dev, sizeClass(index_count), attribute_count ? 1 : 0);
+	int found = 0;
+	out4[0] = out4[1] = 0;
+	out4[2] = -1;
+	out4[3] = 0;
+	{
+		std::lock_guard<std::mutex> g(g_shapes.lock);
+		auto it = g_shapes.shape.find(key);
+		if (it != g_shapes.shape.end())
+		{
+			out4[0] = it->second.first;
+			out4[1] = int(it->second.second);
+			found = 1;
+		}
+		auto jt = g_shapes.batch.find(key);
+		if (jt != g_shapes.batch.end())
+			out4[2] = jt->second ? 1 : 0;
+	}
+	{
+		std::lock_guard<std::mutex> g(g_tuner.lock);
+		if (!g_tuner.shape.empty())
+			out4[3] = int(g_tuner.shape.rbegin()->second.second / 1024);
+	}
+	return found;
 }
 
 } // extern "C"
@@ -1754,8 +1982,7 @@ size_t meshoptgpu_simplifyDevice(unsigned int* destination, const unsigned int* 
 		m.target_index_count = target_index_count;
 		m.target_error = target_error;
 		m.options = options;
-		if (!smallMeshOnBatch(s, m, destination, st))
-			s.last = s.simplifier->run(m, destination, st, s.timing ? &s.times : nullptr);
+		routeAndRun(s, m, destination, st, true);
 		if (result_error)
 			*result_error = s.last.result_error;
 		setStatus(meshoptgpu_StatusOk, "");

@@ -43,9 +43,11 @@ __global__ void __launch_bounds__(kScanThreads) kScanReduce(const unsigned int* 
 }
 
 __global__ void __launch_bounds__(kScanThreads) kScanApply(const unsigned int* in, unsigned int* out, size_t n, const unsigned int* __restrict__ tileoffs,
-    unsigned int* total, bool aligned)
+    unsigned int* total, bool aligned, const unsigned int* n_dev = nullptr)
 {
 	__shared__ unsigned int smem[kScanThreads / 32 + 1];
+	if (n_dev && *n_dev < n)
+		n = *n_dev;
 	size_t i = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
 	uint4 v = loadTile4(in, n, i, aligned);
 	unsigned int s = v.x + v.y + v.z + v.w;
@@ -79,9 +81,11 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(const unsigned int* i
 // sums[b]; after the grid barrier each block adds up the sums before it and scans its tiles
 // again, writing the prefixes. in and out may alias: a block writes only elements it has read.
 __global__ void __launch_bounds__(kScanThreads) kScanCoop(const unsigned int* in, unsigned int* out, size_t n, unsigned int* total,
-    unsigned int* sums, unsigned int* bar, unsigned int* err, bool aligned)
+    unsigned int* sums, unsigned int* bar, unsigned int* err, bool aligned, const unsigned int* n_dev)
 {
 	__shared__ unsigned int smem[kScanThreads / 32 + 1];
+	if (n_dev && *n_dev < n)
+		n = *n_dev; // the live count; the grid covers n
 	const size_t tiles = (n + kScanTile - 1) / kScanTile;
 	const size_t per = (tiles + gridDim.x - 1) / gridDim.x;
 	const size_t t0 = min(tiles, (size_t)blockIdx.x * per), t1 = min(tiles, t0 + per);
@@ -143,12 +147,14 @@ void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int
 	bool aligned = ((uintptr_t)in % 16 == 0) && ((uintptr_t)out % 16 == 0);
 	if (tiles <= 1)
 	{
-		MO_LAUNCH(kScanApply, 1, kScanThreads, 0, stream, in, out, n, nullptr, total, aligned);
+		MO_LAUNCH(kScanApply, 1, kScanThreads, 0, stream, in, out, n, nullptr, total, aligned, sync.n_dev);
 		return;
 	}
 	unsigned int cap = sync.bar ? coopScanCapacity() : 0u;
 	if (cap && sync.max_blocks)
 		cap = std::min(cap, sync.max_blocks);
+	if (sync.n_dev && !cap)
+		throw std::invalid_argument("scanExclusive: a device-side count needs the single-launch mode");
 	if (cap)
 	{
 		// consecutive tiles per block, then as few blocks as that needs
@@ -156,7 +162,8 @@ void scanLevel(const unsigned int* in, unsigned int* out, size_t n, unsigned int
 		const unsigned int blocks = unsigned((tiles + per - 1) / per);
 		unsigned int* sums = scratch;
 		cudaEvent_t e0 = probeBegin("kScanCoop", stream);
-		void* params[] = {(void*)&in, (void*)&out, (void*)&n, (void*)&total, (void*)&sums, (void*)&sync.bar, (void*)&sync.err, (void*)&aligned};
+		void* params[] = {(void*)&in, (void*)&out, (void*)&n, (void*)&total, (void*)&sums, (void*)&sync.bar, (void*)&sync.err, (void*)&aligned,
+		                  (void*)&sync.n_dev};
 		MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kScanCoop, dim3(blocks), dim3(kScanThreads), params, 0, stream));
 		probeEnd(e0, stream);
 		return;

@@ -88,6 +88,8 @@ struct ScanSync
 	unsigned int* err = nullptr;
 	unsigned int max_blocks = 0; // at most this many blocks (0: as many as are resident at once), so
 	                             // concurrent callers on other streams can be resident beside it
+	const unsigned int* n_dev = nullptr; // optional: the live element count on the device (at most n),
+	                                     // read by the kernels; needs the single-launch mode
 };
 
 // Runs the grid barrier (once != 0: the single-use one) with one of `blocks` blocks never

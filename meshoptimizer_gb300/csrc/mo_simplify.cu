@@ -55,6 +55,8 @@ struct PassLive
 	unsigned int passes;
 	unsigned int iterations;
 	unsigned int target;      // target_index_count
+	unsigned int sort_items;  // candidates per thread of the sort's tiles
+	unsigned int sort_cells;  // cells of the pass's live sort histogram matrix
 	float error_limit;        // squared, in the rescaled space (:2489-2491)
 	double window_factor;     // this pass's first decision window, in units of the triangle goal / 2
 	double window_base;       // its smallest value
@@ -1259,43 +1261,36 @@ __global__ void kRank(size_t count, uint4* __restrict__ crec, uint4* __restrict_
 // exclusive scan over the bin-major histogram matrix (which gives, for every tile and bin, the
 // sorted position of the tile's first candidate with that key), and a stable scatter. The
 // scatter gives each candidate its sorted position (rank, in pick order) and writes, at that
-// position, the error bits and kind that the stop rules read in sorted order.
+// position, the error bits and kind that the stop rules read in sorted order. The matrix has one
+// column per live tile (its row stride is the live tile count), so its scan covers the live
+// candidates only.
 constexpr unsigned int kKeyBins = 2560;
 constexpr unsigned int kKeyWarps = kThreads / 32;
 constexpr size_t kKeyScatterSmem = kKeyBins * sizeof(unsigned int) + size_t(kKeyWarps) * kKeyBins * sizeof(unsigned short);
 
-constexpr size_t kKeyTargetTiles = 4 * 152; // sort tiles wanted for the largest count: four per SM of a GB300
-
-// candidates per thread of a sort tile (8, 16, 32 or 64): the smallest that keeps the tile count
-// near kKeyTargetTiles for the largest count the sort will see (the histogram matrix, 2560 words
-// per tile, stays a few MB), with no fewer than eight per thread
-unsigned int keySortItems(size_t n)
+// candidates per thread of a sort tile, by the largest count the sort sees: small counts take
+// small tiles (more blocks for a short sort), large ones 4096-candidate tiles (a smaller matrix)
+inline unsigned int keySortItems(size_t n)
 {
-	const size_t per_tile = (n + kKeyTargetTiles - 1) / kKeyTargetTiles;
-	unsigned int items = 8;
-	while (items < 64 && size_t(items) * kThreads < per_tile)
-		items *= 2;
-	return items;
+	return n <= (size_t(1) << 19) ? 4u : (n <= (size_t(1) << 21) ? 8u : 16u);
 }
 
-unsigned int keySortTiles(size_t n, unsigned int items)
+__host__ __device__ inline unsigned int keySortTiles(size_t n, unsigned int items)
 {
 	const size_t tile = size_t(items) * kThreads;
-	return unsigned(std::max<size_t>(1, (n + tile - 1) / tile));
+	return unsigned((n + tile - 1) / tile);
 }
 
-// scratch words of sortCandidates for any count up to n: the histogram matrix and its scan. A
-// count below 64 per thread has at most kKeyTargetTiles tiles (and at most one per 2048
-// candidates); one at 64 per thread has one per 16384.
+// scratch words of sortCandidates for any count up to n and any tile: the histogram matrix (at
+// most one column per 1024 candidates) and its scan
 size_t keySortScratchWords(size_t n)
 {
-	const size_t tiles = std::max(std::min((n + 2047) / 2048, kKeyTargetTiles), size_t(keySortTiles(n, 64)));
-	const size_t m = std::max<size_t>(tiles, 1) * kKeyBins;
+	const size_t m = std::max<size_t>(keySortTiles(n, 4), 1) * kKeyBins;
 	return ((m + 63) & ~size_t(63)) + scanScratchWords(m);
 }
 
-__global__ void __launch_bounds__(kThreads) kKeyHist(const unsigned int* __restrict__ cerr, size_t n, unsigned int items, unsigned int* __restrict__ hist,
-    unsigned int tiles, const PassLive* lv)
+template <unsigned int ITEMS>
+__global__ void __launch_bounds__(kThreads) kKeyHist(const unsigned int* __restrict__ cerr, size_t n, unsigned int* __restrict__ hist, const PassLive* lv)
 {
 	__shared__ unsigned int sh[kKeyBins];
 	if (lv)
@@ -1304,39 +1299,39 @@ __global__ void __launch_bounds__(kThreads) kKeyHist(const unsigned int* __restr
 			return;
 		n = lv->count;
 	}
+	const unsigned int tiles = keySortTiles(n, ITEMS);
+	if (blockIdx.x >= tiles)
+		return;
 	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
 		sh[b] = 0;
 	__syncthreads();
-	const size_t t0 = (size_t)blockIdx.x * items * kThreads + threadIdx.x;
-	for (unsigned int j0 = 0; j0 < items; j0 += 8)
+	const size_t t0 = (size_t)blockIdx.x * ITEMS * kThreads + threadIdx.x;
+	unsigned int kb[ITEMS];
+#pragma unroll
+	for (unsigned int q = 0; q < ITEMS; ++q)
 	{
-		unsigned int kb[8];
-#pragma unroll
-		for (unsigned int q = 0; q < 8; ++q)
-		{
-			const size_t i = t0 + (size_t)(j0 + q) * kThreads;
-			kb[q] = i < n ? sortKey(__ldg(cerr + i)) : kKeyBins;
-		}
-#pragma unroll
-		for (unsigned int q = 0; q < 8; ++q)
-			if (kb[q] < kKeyBins)
-				atomicAdd(&sh[kb[q]], 1u);
+		const size_t i = t0 + (size_t)q * kThreads;
+		kb[q] = i < n ? sortKey(__ldg(cerr + i)) : kKeyBins;
 	}
+#pragma unroll
+	for (unsigned int q = 0; q < ITEMS; ++q)
+		if (kb[q] < kKeyBins)
+			atomicAdd(&sh[kb[q]], 1u);
 	__syncthreads();
-	// tiles past the live count write zeros, so the scan over the whole matrix is the live one's
 	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
 		hist[(size_t)b * tiles + blockIdx.x] = sh[b];
 }
 
-// Stable scatter of one tile. Warp w takes the tile's 32 * items consecutive candidates from
-// w * 32 * items on, 32 at a time in order; equal keys among the 32 are ranked by lane
-// (match_any), against per-warp key counters. The first walk counts, the counters of each key are
-// turned into offsets in warp order, and the second walk places every candidate after the
-// earlier ones of its key: equal keys keep pick order, as the reference's counting sort keeps
-// collapse order.
+// Stable scatter of one tile. Warp w takes the tile's 32 * ITEMS consecutive candidates from
+// w * 32 * ITEMS on, 32 at a time in order; equal keys among the 32 are ranked by lane
+// (match_any) against per-warp key counters, and each candidate keeps its key and its rank within
+// the warp in registers. The warp counters of each key are then turned into offsets in warp
+// order, and every candidate is placed after the earlier ones of its key: equal keys keep pick
+// order, as the reference's counting sort keeps collapse order.
+template <unsigned int ITEMS>
 __global__ void __launch_bounds__(kThreads) kKeyScatter(const unsigned int* __restrict__ cerr, const unsigned char* __restrict__ ckind, size_t n,
-    unsigned int items, const unsigned int* __restrict__ hist, unsigned int tiles, unsigned int* __restrict__ rank, unsigned int* __restrict__ serr,
-    unsigned char* __restrict__ skind, const PassLive* lv)
+    const unsigned int* __restrict__ hist, unsigned int* __restrict__ rank, unsigned int* __restrict__ serr, unsigned char* __restrict__ skind,
+    const PassLive* lv)
 {
 	extern __shared__ __align__(16) unsigned char key_smem[];
 	unsigned int* gbase = reinterpret_cast<unsigned int*>(key_smem);               // sorted position of the tile's first candidate per key
@@ -1347,10 +1342,19 @@ __global__ void __launch_bounds__(kThreads) kKeyScatter(const unsigned int* __re
 			return;
 		n = lv->count;
 	}
-	const size_t tile0 = (size_t)blockIdx.x * items * kThreads;
-	if (tile0 >= n)
+	const unsigned int tiles = keySortTiles(n, ITEMS);
+	if (blockIdx.x >= tiles)
 		return;
+	const size_t tile0 = (size_t)blockIdx.x * ITEMS * kThreads;
 	const unsigned int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const size_t w0 = tile0 + (size_t)w * 32 * ITEMS + lane;
+	unsigned int eb[ITEMS];
+#pragma unroll
+	for (unsigned int q = 0; q < ITEMS; ++q)
+	{
+		const size_t i = w0 + (size_t)q * 32;
+		eb[q] = i < n ? __ldg(cerr + i) : 0u;
+	}
 	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
 	{
 		gbase[b] = hist[(size_t)b * tiles + blockIdx.x];
@@ -1360,24 +1364,23 @@ __global__ void __launch_bounds__(kThreads) kKeyScatter(const unsigned int* __re
 	}
 	__syncthreads();
 	unsigned short* mine = wcnt + w * kKeyBins;
-	const size_t w0 = tile0 + (size_t)w * 32 * items + lane;
-	for (unsigned int s0 = 0; s0 < items; s0 += 8)
+	unsigned short rk[ITEMS]; // rank among the warp's candidates of the same key
+#pragma unroll
+	for (unsigned int q = 0; q < ITEMS; ++q)
 	{
-		unsigned int kb[8];
-#pragma unroll
-		for (unsigned int q = 0; q < 8; ++q)
+		const bool valid = w0 + (size_t)q * 32 < n;
+		const unsigned int key = valid ? sortKey(eb[q]) : kKeyBins + lane;
+		const unsigned int peers = __match_any_sync(0xffffffffu, key);
+		const unsigned int leader = __ffs(peers) - 1;
+		unsigned int before = 0;
+		if (valid && lane == leader)
 		{
-			const size_t i = w0 + (size_t)(s0 + q) * 32;
-			kb[q] = i < n ? sortKey(__ldg(cerr + i)) : kKeyBins + lane;
+			before = mine[key];
+			mine[key] = (unsigned short)(before + __popc(peers));
 		}
-#pragma unroll
-		for (unsigned int q = 0; q < 8; ++q)
-		{
-			const unsigned int peers = __match_any_sync(0xffffffffu, kb[q]);
-			if (kb[q] < kKeyBins && lane == __ffs(peers) - 1)
-				mine[kb[q]] += (unsigned short)__popc(peers);
-			__syncwarp();
-		}
+		before = __shfl_sync(0xffffffffu, before, leader);
+		rk[q] = (unsigned short)(before + __popc(peers & ((1u << lane) - 1u)));
+		__syncwarp();
 	}
 	__syncthreads();
 	for (unsigned int b = threadIdx.x; b < kKeyBins; b += kThreads)
@@ -1392,40 +1395,17 @@ __global__ void __launch_bounds__(kThreads) kKeyScatter(const unsigned int* __re
 		}
 	}
 	__syncthreads();
-	for (unsigned int s0 = 0; s0 < items; s0 += 8)
+#pragma unroll
+	for (unsigned int q = 0; q < ITEMS; ++q)
 	{
-		unsigned int eb[8];
-		unsigned char kd[8];
-#pragma unroll
-		for (unsigned int q = 0; q < 8; ++q)
+		const size_t i = w0 + (size_t)q * 32;
+		if (i < n)
 		{
-			const size_t i = w0 + (size_t)(s0 + q) * 32;
-			eb[q] = i < n ? __ldg(cerr + i) : 0u;
-			kd[q] = i < n ? __ldg(ckind + i) : (unsigned char)0;
-		}
-#pragma unroll
-		for (unsigned int q = 0; q < 8; ++q)
-		{
-			const size_t i = w0 + (size_t)(s0 + q) * 32;
-			const bool valid = i < n;
-			const unsigned int key = valid ? sortKey(eb[q]) : kKeyBins + lane;
-			const unsigned int peers = __match_any_sync(0xffffffffu, key);
-			const unsigned int leader = __ffs(peers) - 1;
-			unsigned int before = 0;
-			if (valid && lane == leader)
-			{
-				before = mine[key];
-				mine[key] = (unsigned short)(before + __popc(peers));
-			}
-			before = __shfl_sync(0xffffffffu, before, leader);
-			if (valid)
-			{
-				const unsigned int pos = gbase[key] + before + __popc(peers & ((1u << lane) - 1u));
-				rank[i] = pos;
-				serr[pos] = eb[q];
-				skind[pos] = kd[q];
-			}
-			__syncwarp();
+			const unsigned int key = sortKey(eb[q]);
+			const unsigned int pos = gbase[key] + mine[key] + rk[q];
+			rank[i] = pos;
+			serr[pos] = eb[q];
+			skind[pos] = __ldg(ckind + i);
 		}
 	}
 }
@@ -2655,6 +2635,7 @@ __global__ void kPassPrep(Scalars* sc)
 		lv.stop = 1;
 		return;
 	}
+	lv.sort_cells = keySortTiles(C, lv.sort_items) * kKeyBins;
 	unsigned long long goal = (unsigned long long)(lv.indices - lv.target) / 3;
 	lv.goal = goal;
 	double wf = lv.window_factor * double(goal / 2) + 4096.0;
@@ -3020,20 +3001,34 @@ int bitsFor(size_t maxval)
 	return b;
 }
 
-// The pass's counting sort (kKeyHist, scan, kKeyScatter) of up to n candidates: their sorted
-// positions into w.rank, the error bits and kinds by sorted position into w.serr and w.skind. lv:
-// the device-resident loop's live count (the grids cover n), else nullptr.
-void sortCandidates(const Work& w, size_t n, cudaStream_t stream, const PassLive* lv, ScanSync ss)
+// The pass's counting sort (kKeyHist, scan, kKeyScatter) of up to n candidates, in tiles of
+// items * 256 (items: 4, 8 or 16): their sorted positions into w.rank, the error bits and kinds by
+// sorted position into w.serr and w.skind. lv: the device-resident loop's live state (the grids
+// cover n; the kernels and the scan take the live count from it, whose sort_items must equal
+// items), else nullptr.
+void sortCandidates(const Work& w, size_t n, cudaStream_t stream, const PassLive* lv, ScanSync ss, unsigned int items)
 {
 	if (n == 0)
 		return;
-	const unsigned int items = keySortItems(n), tiles = keySortTiles(n, items);
+	const unsigned int tiles = keySortTiles(n, items);
 	const size_t m = size_t(tiles) * kKeyBins;
 	unsigned int* hist = w.scratch;
 	unsigned int* sscratch = w.scratch + ((m + 63) & ~size_t(63));
-	MO_LAUNCH(kKeyHist, tiles, kThreads, 0, stream, w.cerr, n, items, hist, tiles, lv);
+	if (lv)
+		ss.n_dev = &lv->sort_cells;
+	if (items == 4)
+		MO_LAUNCH(kKeyHist<4>, tiles, kThreads, 0, stream, w.cerr, n, hist, lv);
+	else if (items == 8)
+		MO_LAUNCH(kKeyHist<8>, tiles, kThreads, 0, stream, w.cerr, n, hist, lv);
+	else
+		MO_LAUNCH(kKeyHist<16>, tiles, kThreads, 0, stream, w.cerr, n, hist, lv);
 	scanExclusive(hist, hist, m, nullptr, sscratch, stream, ss);
-	MO_LAUNCH(kKeyScatter, tiles, kThreads, kKeyScatterSmem, stream, w.cerr, w.ckind, n, items, hist, tiles, w.rank, w.serr, w.skind, lv);
+	if (items == 4)
+		MO_LAUNCH(kKeyScatter<4>, tiles, kThreads, kKeyScatterSmem, stream, w.cerr, w.ckind, n, hist, w.rank, w.serr, w.skind, lv);
+	else if (items == 8)
+		MO_LAUNCH(kKeyScatter<8>, tiles, kThreads, kKeyScatterSmem, stream, w.cerr, w.ckind, n, hist, w.rank, w.serr, w.skind, lv);
+	else
+		MO_LAUNCH(kKeyScatter<16>, tiles, kThreads, kKeyScatterSmem, stream, w.cerr, w.ckind, n, hist, w.rank, w.serr, w.skind, lv);
 }
 
 } // namespace
@@ -3088,7 +3083,9 @@ Simplifier::Simplifier(int device) : device_(device)
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&solve_per_sm_, kSolvePositions, kThreads, 0));
-	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
+	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
+	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
+	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
 	cudaDeviceGetAttribute(&clock_khz_, cudaDevAttrClockRate, device);
 	sms_ = sms;
 	coop_blocks_ = unsigned(std::max(1, sms * std::max(per_sm, 1)));
@@ -3554,6 +3551,8 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		init.indices = unsigned(I);
 		init.tris = unsigned(T0);
 		init.target = unsigned(m.target_index_count);
+		const unsigned int sort_items = sort_items_ ? sort_items_ : keySortItems(capn);
+		init.sort_items = sort_items;
 		init.window_factor = tuning_.window_factor;
 		init.window_base = tuning_.window_factor;
 		MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->live, &init, sizeof(init), cudaMemcpyHostToDevice, stream));
@@ -3570,7 +3569,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 
 		LaunchProbe& lp = probe();
 		const bool reuse = loop_.exec && loop_.base == arena_.base() && loop_.I == I && loop_.V == V && loop_.ac == ac && loop_.solve == solve &&
-		                   loop_.blocks == blocks && loop_.scan_blocks == ss.max_blocks;
+		                   loop_.blocks == blocks && loop_.sort_items == sort_items && loop_.scan_blocks == ss.max_blocks;
 		if (!reuse)
 		{
 			dropLoopGraph();
@@ -3618,7 +3617,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
 				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 				    w.adj_off, w.attr, w.aq, w.ag, ac, lv);
-				sortCandidates(w, capn, cs, lv, ss);
+				sortCandidates(w, capn, cs, lv, ss, sort_items);
 				PerformArgs pa;
 				pa.count = 0;
 				pa.crec = w.crec;
@@ -3686,6 +3685,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			loop_.ac = ac;
 			loop_.solve = solve;
 			loop_.blocks = blocks;
+			loop_.sort_items = sort_items;
 			loop_.scan_blocks = ss.max_blocks;
 		}
 		MO_CUDA_CHECK(cudaGraphLaunch(loop_.exec, stream));
@@ -3736,7 +3736,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		    w.adj_off, w.attr, w.aq, w.ag, ac, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
-		sortCandidates(w, C, stream, nullptr, ss);
+		sortCandidates(w, C, stream, nullptr, ss, sort_items_ ? sort_items_ : keySortItems(C));
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[6], stream));
 

@@ -153,6 +153,7 @@ private:
 	                                 // the legacy default stream, which cannot capture)
 	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative pass kernel (occupancy)
 	unsigned int perform_blocks_ = 1;
+	unsigned int sort_items_ = 0;    // candidates per thread of the pass sort's tiles (0: by count)
 	int sms_ = 1;
 	int solve_per_sm_ = 1; // resident blocks of the position solve kernel per SM
 	int clock_khz_ = 0;    // SM clock for the phase counters (queried once: the query costs ~0.6 ms)
@@ -167,6 +168,7 @@ private:
 		int ac = 0;
 		bool solve = false;
 		unsigned int blocks = 0;
+		unsigned int sort_items = 0;
 		unsigned int scan_blocks = 0;         // the one-launch scans' grid cap recorded in the body (0: none)
 		unsigned long long body_launches = 0; // kernels one replay of the body launches
 		cudaGraph_t graph = nullptr;
@@ -180,6 +182,20 @@ public:
 		tuning_ = t;
 		perform_blocks_ = std::min(coop_blocks_, unsigned(std::max(1, sms_ * t.perform_blocks_per_sm)));
 	}
+	// The launch shape of the pass kernels an autotuner picks: pass-kernel blocks per SM, and the
+	// pass sort's candidates per thread (4, 8 or 16; 0: chosen by the candidate count). Results do
+	// not depend on either.
+	void setPassShape(int perform_blocks_per_sm, unsigned int sort_items)
+	{
+		Tuning t = tuning_;
+		t.perform_blocks_per_sm = perform_blocks_per_sm;
+		setTuning(t);
+		sort_items_ = (sort_items == 4 || sort_items == 8 || sort_items == 16) ? sort_items : 0;
+	}
+	int performBlocksPerSM() const { return tuning_.perform_blocks_per_sm; }
+	// resident blocks per SM of the pass kernel at most (its register count)
+	int performBlocksPerSMMax() const { return int(coop_blocks_ / unsigned(std::max(1, sms_))); }
+	unsigned int sortItems() const { return sort_items_; }
 	const Tuning& tuning() const { return tuning_; }
 };
 
