@@ -304,17 +304,20 @@ __device__ __forceinline__ void addAttributeQuadric(Quadric& Qacc, float4* Gacc,
 	qadd(Qacc, Q);
 }
 
+// one attribute's term of quadricError's attribute sum (src/simplifier.cpp:784-798), added to r in
+// attribute order
+__device__ __forceinline__ void qattrStep(float& r, float a, const float4& g4, const V3& v, float w)
+{
+	float g = v.x * g4.x + v.y * g4.y + v.z * g4.z + g4.w;
+	r += a * (a * w - 2 * g);
+}
+
 // quadricError with attributes (src/simplifier.cpp:784-798): position error plus the attribute terms
 __device__ __forceinline__ float qerrorAttr(const Quadric& Q, const float4* __restrict__ G, int count, const V3& v, const float* __restrict__ va)
 {
 	float r = qeval(Q, v);
 	for (int k = 0; k < count; ++k)
-	{
-		float a = va[k];
-		float4 g4 = G[k];
-		float g = v.x * g4.x + v.y * g4.y + v.z * g4.z + g4.w;
-		r += a * (a * Q.w - 2 * g);
-	}
+		qattrStep(r, va[k], G[k], v, Q.w);
 	return fabsf(r);
 }
 

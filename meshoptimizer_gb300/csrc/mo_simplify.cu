@@ -1033,10 +1033,22 @@ __global__ void kCountCorners(const unsigned int* __restrict__ res, size_t n, co
 		n = lv->indices;
 		slot = lv->res_next;
 	}
-	size_t i = gtid();
-	if (i >= n)
-		return;
-	slot[i] = atomicAdd(&cnt[remap[res[i]]], 1u);
+	const size_t i = gtid();
+	if (i - (threadIdx.x & 31) >= n)
+		return; // the whole warp is past the corners
+	// corners of the same vertex among the warp's 32 (neighbouring triangles share vertices) take
+	// their slots with one atomic add; a list's order is arbitrary anyway
+	const unsigned int lane = threadIdx.x & 31;
+	const bool valid = i < n;
+	const unsigned int v = valid ? remap[res[i]] : ~lane; // past the end: a key no vertex has
+	const unsigned int peers = __match_any_sync(0xffffffffu, v);
+	const unsigned int leader = __ffs(peers) - 1;
+	unsigned int base = 0;
+	if (valid && lane == leader)
+		base = atomicAdd(&cnt[v], __popc(peers));
+	base = __shfl_sync(0xffffffffu, base, leader);
+	if (valid)
+		slot[i] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // half-edges {next, prev} of every vertex in its list (the order within a list is arbitrary: the
@@ -1452,7 +1464,7 @@ struct PerformArgs
 	//  * minT[p][v]: the earliest undecided candidate with endpoint v; 0 once a commit took v;
 	//  * minS[2 v + p]: the earliest undecided candidate that moves v; once a commit moved v, the
 	//    pair holds {that commit's sorted position, v's target}, both with tag 0.
-	// A pass leaves both as it found them: the apply phase restores what its commits wrote.
+	// Every pass starts by setting both to ~0 for all vertices.
 	unsigned int vcount;
 	unsigned long long* minT[2];
 	unsigned long long* minS;
@@ -1880,8 +1892,16 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		error_limit = lv->error_limit;
 	}
 
+	// per-vertex state of the pass, streamed: collapse_remap, and both parities of both marks (the
+	// marks the window's candidates set below come after the barrier)
 	for (size_t i = gtid(); i < a.vcount; i += gthreads)
+	{
 		a.cr[i] = (unsigned int)i;
+		a.minT[0][i] = ~0ull;
+		a.minT[1][i] = ~0ull;
+		reinterpret_cast<ulonglong2*>(a.minS)[i] = make_ulonglong2(~0ull, ~0ull);
+	}
+	gridBarrier(sc->bar, &sc->grid_error);
 
 	unsigned int round = round_base;
 	unsigned long long active_sum = 0;
@@ -2189,17 +2209,10 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		nd += st == kCommit, ns += st == kSkipLocked, ni += st == kSkipFlip;
 	}
 	{
-		// every commit of the pass, inside the prefix or not, also restores the marks it wrote
 		const unsigned int mc = s_commits; // every append to it was followed by a block barrier
 		for (unsigned int x = threadIdx.x; x < mc; x += blockDim.x)
 		{
 			const unsigned int c = commits[x];
-			const uint4 rec = __ldg(a.cring + c);
-			a.minT[0][rec.x] = ~0ull;
-			a.minT[1][rec.x] = ~0ull;
-			a.minT[0][rec.y] = ~0ull;
-			a.minT[1][rec.y] = ~0ull;
-			*reinterpret_cast<ulonglong2*>(a.minS + 2 * (size_t)rec.x) = make_ulonglong2(~0ull, ~0ull);
 			if (__ldg(a.rank + c) < cut)
 			{
 				unsigned int eb = 0, db = 0;
@@ -3535,8 +3548,6 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	int passes = 0;
 	double window_factor = tuning_.window_factor; // the host loop's first-window factor, as kPassEnd adapts it
 	unsigned int round_base = 0; // decision rounds are numbered across the run (mark tags never repeat)
-	MO_CUDA_CHECK(cudaMemsetAsync(w.minT, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
-	MO_CUDA_CHECK(cudaMemsetAsync(w.minS, 0xFF, 2 * (V + 1) * sizeof(unsigned long long), stream));
 
 	// ---- the pass loop on the device: one pass recorded into the body of a WHILE conditional
 	// node, replayed until kPassEnd ends it
