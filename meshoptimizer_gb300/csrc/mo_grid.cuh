@@ -42,7 +42,9 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 
 // A grid barrier that a cooperative launch passes once, leaving its two words zero for the next
 // launch: bar[0] counts arrivals, bar[1] departures, and the last block to depart clears both
-// (by then no block polls bar[0] any more).
+// (by then no block polls bar[0] any more). A launch whose wait ran out leaves them nonzero: the
+// owner clears them before it uses them again (the simplifier clears its words, with the rest of
+// its scalars, at the start of every call, and a call whose barrier ran out reports an error).
 __device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int* err, unsigned int limit = kBarrierSpinLimit)
 {
 	__syncthreads();

@@ -100,6 +100,8 @@ __global__ void __launch_bounds__(kScanThreads) kScanCoop(const unsigned int* in
 	if (threadIdx.x == 0)
 		sums[blockIdx.x] = part;
 	gridBarrierOnce(bar, err);
+	if (__ldcg(err))
+		return; // a barrier wait ran out: no block writes prefixes from incomplete sums
 	unsigned int before = 0;
 	for (unsigned int j = threadIdx.x; j < blockIdx.x; j += kScanThreads)
 		before += __ldcg(sums + j);

@@ -111,6 +111,7 @@ struct Scalars
 	unsigned int solve_rounds;
 	unsigned int max_degree[2];         // corners of the busiest vertex: raw, remapped
 	unsigned int scan_bar[2];           // the single-launch scans' barrier words (left zero by each scan)
+	unsigned int scan_bar2[2];          // those of the scans on the pass loop's second branch (the pick)
 	unsigned int scan_error;            // a single-launch scan's barrier gave up waiting
 };
 
@@ -1054,7 +1055,7 @@ __global__ void kCountCorners(const unsigned int* __restrict__ res, size_t n, co
 // half-edges {next, prev} of every vertex in its list (the order within a list is arbitrary: the
 // flip test and the one-ring checks do not depend on it)
 __global__ void kAdjFill(const unsigned int* __restrict__ res, size_t tris, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ off,
-    const unsigned int* __restrict__ slot, uint2* __restrict__ adj, const PassLive* lv)
+    const unsigned int* __restrict__ slot, uint2* __restrict__ adj, const PassLive* lv, size_t adj_cap)
 {
 	if (lv)
 	{
@@ -1070,7 +1071,11 @@ __global__ void kAdjFill(const unsigned int* __restrict__ res, size_t tris, cons
 	const unsigned int v[3] = {remap[res[t * 3 + 0]], remap[res[t * 3 + 1]], remap[res[t * 3 + 2]]};
 #pragma unroll
 	for (int c = 0; c < 3; ++c)
-		adj[off[v[c]] + slot[t * 3 + c]] = make_uint2(v[c == 2 ? 0 : c + 1], v[c == 0 ? 2 : c - 1]);
+	{
+		const size_t at = size_t(off[v[c]]) + slot[t * 3 + c];
+		if (at < adj_cap) // in range whenever the offsets' scan completed
+			adj[at] = make_uint2(v[c == 2 ? 0 : c + 1], v[c == 0 ? 2 : c - 1]);
+	}
 }
 
 // ---------------------------------------------------------------- pass: pick
@@ -1416,8 +1421,11 @@ __global__ void __launch_bounds__(kThreads) kKeyScatter(const unsigned int* __re
 			const unsigned int key = sortKey(eb[q]);
 			const unsigned int pos = gbase[key] + mine[key] + rk[q];
 			rank[i] = pos;
-			serr[pos] = eb[q];
-			skind[pos] = __ldg(ckind + i);
+			if (pos < n) // in range whenever the histogram scan completed
+			{
+				serr[pos] = eb[q];
+				skind[pos] = __ldg(ckind + i);
+			}
 		}
 	}
 }
@@ -2906,6 +2914,7 @@ struct Work
 	uint4* blk;
 	unsigned int* blkcnt;
 	unsigned int* scratch;
+	unsigned int* scratch2; // the pick's block-count scan, beside the adjacency scan in the pass loop
 	unsigned int hash_mask;
 	// the update mode only
 	float4* vg;              // volume gradients (with attributes)
@@ -2996,6 +3005,7 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = f
 	w.blkcnt = c.take<unsigned int>(T / kThreads + 2);
 	size_t sw = std::max(std::max(scanScratchWords(I + Vp + 2), radixScratchWords(big)), std::max(scanScratchWords(T + 2), keySortScratchWords(cap)));
 	w.scratch = c.take<unsigned int>(sw);
+	w.scratch2 = c.take<unsigned int>(scanScratchWords(T / kThreads + 2));
 	const size_t Vs = solve ? Vp : 0;
 	w.vg = (solve && ac) ? c.take<float4>(Vp) : nullptr;
 	w.pos_new = c.take<float4>(Vs);
@@ -3092,6 +3102,9 @@ Simplifier::Simplifier(int device) : device_(device)
 	MO_CUDA_CHECK(cudaSetDevice(device));
 	MO_CUDA_CHECK(cudaMallocHost(&pinned_, kPinnedBytes));
 	MO_CUDA_CHECK(cudaStreamCreateWithFlags(&capture_, cudaStreamNonBlocking));
+	MO_CUDA_CHECK(cudaStreamCreateWithFlags(&capture2_, cudaStreamNonBlocking));
+	MO_CUDA_CHECK(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+	MO_CUDA_CHECK(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
 	int sms = 0, per_sm = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
@@ -3121,6 +3134,12 @@ Simplifier::~Simplifier()
 	dropLoopGraph();
 	if (capture_)
 		cudaStreamDestroy(capture_);
+	if (capture2_)
+		cudaStreamDestroy(capture2_);
+	if (fork_)
+		cudaEventDestroy(fork_);
+	if (join_)
+		cudaEventDestroy(join_);
 	if (pinned_)
 		cudaFreeHost(pinned_);
 }
@@ -3617,14 +3636,23 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			try
 			{
 				const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads), gC = gridFor(capn, kThreads);
+				// the pick (its own scan scratch and barrier words) and the adjacency are independent:
+				// two branches of the body, joined before the rank
+				cudaStream_t cs2 = capture2_;
+				ScanSync ss2 = ss;
+				ss2.bar = w.sc->scan_bar2;
+				MO_CUDA_CHECK(cudaEventRecord(fork_, cs));
+				MO_CUDA_CHECK(cudaStreamWaitEvent(cs2, fork_, 0));
+				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs2, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, pick_codes, lv);
+				scanExclusive(w.tcnt, w.tcnt, gT0, &w.sc->pick_total, w.scratch2, cs2, ss2);
+				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs2));
+				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs2, nullptr, T0, pick_codes, w.tcnt, w.sc, w.crec, lv);
+				MO_CUDA_CHECK(cudaEventRecord(join_, cs2));
 				MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, cs));
 				MO_LAUNCH(kCountCorners, gI, kThreads, 0, cs, nullptr, I, w.remap, w.cnt, nullptr, lv);
 				scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, cs, ss);
-				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, nullptr, w.adj, lv);
-				MO_LAUNCH(kPickCount, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.kind, w.loop, w.loopback, w.tcnt, pick_codes, lv);
-				scanExclusive(w.tcnt, w.tcnt, gT0, &w.sc->pick_total, w.scratch, cs, ss);
-				MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->pick_trunc, 0xFF, 4, cs));
-				MO_LAUNCH(kPickEmit, gT0, kThreads, 0, cs, nullptr, T0, pick_codes, w.tcnt, w.sc, w.crec, lv);
+				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, nullptr, w.adj, lv, I);
+				MO_CUDA_CHECK(cudaStreamWaitEvent(cs, join_, 0));
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
 				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 				    w.adj_off, w.attr, w.aq, w.ag, ac, lv);
@@ -3725,7 +3753,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (V + 1) * 4, stream));
 		MO_LAUNCH(kCountCorners, gridFor(result_count, kThreads), kThreads, 0, stream, res, result_count, w.remap, w.cnt, res_next, nullptr);
 		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream, ss);
-		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, res_next, w.adj, nullptr);
+		MO_LAUNCH(kAdjFill, gT, kThreads, 0, stream, res, T, w.remap, w.adj_off, res_next, w.adj, nullptr, I);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[3], stream));
 
@@ -3891,7 +3919,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		}
 		scanExclusive(w.cnt, w.adj_off, V + 1, nullptr, w.scratch, stream, ss);
 		if (T)
-			MO_LAUNCH(kAdjFill, gridFor(T, kThreads), kThreads, 0, stream, res, T, w.remap, w.adj_off, slot, w.adj, nullptr);
+			MO_LAUNCH(kAdjFill, gridFor(T, kThreads), kThreads, 0, stream, res, T, w.remap, w.adj_off, slot, w.adj, nullptr, I);
 		MO_CUDA_CHECK(cudaMemcpyAsync(w.pos_new, w.pos, V * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
 		const unsigned int gV = gridFor(V, kThreads);
 		MO_LAUNCH(kSolveList, gV, kThreads, 0, stream, V, w.vupdate, w.remap, w.kind, w.sdone, w.slist1, &w.sc->solve_pending[1]);

@@ -149,6 +149,8 @@ private:
 	DeviceArena arena_;
 	DeviceArena sparse_arena_; // compact copy of a sparse subset
 	unsigned int* pinned_ = nullptr; // small pinned readback buffer
+	cudaStream_t capture2_ = nullptr; // records the pass body's second branch (the pick)
+	cudaEvent_t fork_ = nullptr, join_ = nullptr; // the branch's fork and join while recording
 	cudaStream_t capture_ = nullptr; // records the device-resident pass loop (the caller's stream may be
 	                                 // the legacy default stream, which cannot capture)
 	unsigned int coop_blocks_ = 1;   // resident blocks of the cooperative pass kernel (occupancy)
