@@ -41,12 +41,13 @@ from meshoptimizer_gb300 import workloads as W  # noqa: E402
 
 # Algorithmic bytes of the dominant kernel, kPerform (one cooperative launch per pass): the
 # compulsory traffic of a pass, every array it must touch read (and written where it changes)
-# once, from the per-pass counters the library reports:
+# once, from the per-pass counters the library reports (T triangles of the pass, V vertices of
+# the buffer; a mesh of T triangles uses about T / 2 of them):
 #   candidate records  42 B per evaluated candidate (pick records 16 + 16, sorted position 4,
 #                      error bits 4, kind 1, decision 1): every candidate up to the stop cut
 #                      is decided
-#   per-vertex state   52 B per vertex (endpoint marks 16, one-ring marks 16, collapse_remap 4,
-#                      position 16)
+#   per-vertex reset   36 B per vertex (collapse_remap 4, both parities of both marks 32)
+#   positions          8 B per triangle (16 B per used vertex, read by the ring walks)
 #   adjacency          24 B per triangle (three 8-byte corner records, read by the ring walks)
 #   apply              144 B per committed collapse (position quadrics: source read, target read
 #                      and written), plus 144 + 48 a with a attributes (attribute quadric and a
@@ -55,25 +56,26 @@ from meshoptimizer_gb300 import workloads as W  # noqa: E402
 #   compaction         12 B per input triangle + 12 B per kept triangle
 def kperform_bytes(p, vertices, next_triangles, attributes=0):
     apply = 144 + (144 + 48 * attributes if attributes else 0)
-    return (42 * p["evaluated"] + 52 * vertices + 24 * p["triangles"] + apply * p["done"] + 16 * vertices
-            + 12 * p["triangles"] + 12 * next_triangles)
+    T = p["triangles"]
+    return (42 * p["evaluated"] + 36 * vertices + 8 * T + 24 * T + apply * p["done"] + 16 * vertices + 12 * T + 12 * next_triangles)
 
 
-KPERFORM_BYTES_DEFINITION = ("kperform_bytes(): 42 B per evaluated candidate, 52 B per vertex (marks, remap, position), "
-                             "24 B per triangle (adjacency), 144 B per commit + (144 + 48 a) B with a attributes, "
-                             "16 B per vertex (loops), 12 B per triangle in + 12 B per triangle kept")
+KPERFORM_BYTES_DEFINITION = ("kperform_bytes(): 42 B per evaluated candidate, 52 B per vertex (reset of remap and marks, loops), "
+                             "44 B per triangle (positions, adjacency, indices in), 12 B per kept triangle, "
+                             "144 B per commit + (144 + 48 a) B with a attributes")
 
 
 # Per-pass byte model of the whole pass (attribute path included), for the per-phase GB/s of
-# the stress line: adjacency 12 B per input triangle (indices) + 24 B per triangle
-# (corner records written) + 8 B per vertex (counts and offsets); pick 12 B per triangle + 12 B per
-# candidate written; rank 12 B per candidate read + 37 B per candidate written + 56 B per vertex of
-# gathered rows (+ 16 a + 48 with attributes); sort 8 B per candidate read twice + 13 B written;
-# perform as kperform_bytes.
+# the stress line: adjacency 12 B per input triangle (indices) + 24 B per triangle (corner records
+# written) + 8 B per vertex (counts and offsets); pick 12 B per triangle + 12 B per candidate
+# written; rank 12 B per candidate read + 37 B per candidate written + the rows of the used
+# vertices (T / 2 of them: position 16, position quadric 48, remap 4, kind 1, adjacency offsets 8,
+# and 48 + 20 a with attributes); sort 8 B per candidate read twice + 13 B written; perform as
+# kperform_bytes.
 def pass_phase_bytes(p, vertices, next_triangles, attributes=0):
     T, Cn = p["triangles"], p["candidates"]
-    rank_rows = 56 + (48 + 16 * attributes if attributes else 0)
-    return {"adjacency": 36 * T + 8 * vertices, "pick": 12 * T + 12 * Cn, "rank": 49 * Cn + rank_rows * vertices,
+    rows = 77 + (48 + 20 * attributes if attributes else 0)
+    return {"adjacency": 36 * T + 8 * vertices, "pick": 12 * T + 12 * Cn, "rank": 49 * Cn + rows * (T // 2),
             "sort": 29 * Cn, "perform": kperform_bytes(p, vertices, next_triangles, attributes)}
 
 
