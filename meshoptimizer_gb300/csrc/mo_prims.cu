@@ -401,6 +401,44 @@ size_t radixScratchWords(size_t n)
 	return h + scanScratchWords(tiles * kSortBins);
 }
 
+// A sort of at most kSmallSortMax pairs in one block: each pair becomes the 64-bit word
+// (key digits << 32 | input position), and a bitonic network sorts the words in shared memory.
+// Distinct positions make the order total, so equal keys keep their input order: the result is
+// the stable order the digit passes give. The key digits are the low `mask` bits the digit
+// passes would look at; keys and values are read back from the input by position.
+constexpr unsigned int kSmallSortMax = 4096;
+constexpr unsigned int kSmallSortThreads = 1024;
+
+__global__ void __launch_bounds__(kSmallSortThreads) kSmallSortPairs(const unsigned int* __restrict__ kin, const unsigned int* __restrict__ vin,
+    unsigned int* __restrict__ kout, unsigned int* __restrict__ vout, unsigned int n, unsigned int mask)
+{
+	__shared__ unsigned long long s[kSmallSortMax];
+	unsigned int m = 1;
+	while (m < n)
+		m <<= 1;
+	for (unsigned int i = threadIdx.x; i < m; i += blockDim.x)
+		s[i] = i < n ? ((unsigned long long)(__ldg(kin + i) & mask) << 32) | i : ~0ull;
+	__syncthreads();
+	for (unsigned int k = 2; k <= m; k <<= 1)
+		for (unsigned int j = k >> 1; j > 0; j >>= 1)
+		{
+			for (unsigned int t = threadIdx.x; t < m / 2; t += blockDim.x)
+			{
+				const unsigned int lo = 2 * t - (t & (j - 1)), hi = lo + j; // the pair t of this step, lo's bit j clear
+				const unsigned long long a = s[lo], b = s[hi];
+				if ((a > b) == ((lo & k) == 0))
+					s[lo] = b, s[hi] = a;
+			}
+			__syncthreads();
+		}
+	for (unsigned int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		const unsigned int src = (unsigned int)s[i];
+		kout[i] = __ldg(kin + src);
+		vout[i] = vin ? __ldg(vin + src) : src;
+	}
+}
+
 void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
     unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream, const unsigned int* n_dev,
     ScanSync sync)
@@ -414,6 +452,12 @@ void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, un
 			throw std::invalid_argument("radixSortPairs: a device count needs at least one digit pass");
 		MO_CUDA_CHECK(cudaMemcpyAsync(keys_out, keys_in, n * 4, cudaMemcpyDeviceToDevice, stream));
 		MO_CUDA_CHECK(cudaMemcpyAsync(vals_out, vals_in, n * 4, cudaMemcpyDeviceToDevice, stream));
+		return;
+	}
+	if (!n_dev && n <= kSmallSortMax)
+	{
+		const unsigned int mask = passes >= 4 ? ~0u : (1u << (8 * passes)) - 1u;
+		MO_LAUNCH(kSmallSortPairs, 1, kSmallSortThreads, 0, stream, keys_in, vals_in, keys_out, vals_out, (unsigned int)n, mask);
 		return;
 	}
 	unsigned int tiles = unsigned((n + kSortTile - 1) / kSortTile);

@@ -114,7 +114,9 @@ size_t radixScratchWords(size_t n);
 // (keys_out, vals_out); keys_tmp/vals_tmp are ping-pong buffers of n elements. Input
 // arrays are left unchanged only when the pass count is even; callers treat them as scratch.
 // n_dev (optional): the live count on the device (<= n), read by the kernels, so that the
-// launches can be recorded once and replayed for any count up to n.
+// launches can be recorded once and replayed for any count up to n. Up to 4,096 pairs with a
+// host count sort in one single-block launch instead of the digit passes (the same order).
+// The outputs must not alias the inputs.
 void radixSortPairs(const unsigned int* keys_in, const unsigned int* vals_in, unsigned int* keys_out, unsigned int* vals_out,
     unsigned int* keys_tmp, unsigned int* vals_tmp, size_t n, int bits, unsigned int* scratch, cudaStream_t stream,
     const unsigned int* n_dev = nullptr, ScanSync sync = ScanSync());

@@ -109,7 +109,7 @@ struct Scalars
 	PassStats pstats[kMaxPassStats];    // its per-pass counters
 	unsigned int solve_pending[3];      // update mode: position-solve candidates left, rotating by round
 	unsigned int solve_rounds;
-	unsigned int max_degree[2];         // corners of the busiest vertex: raw, remapped
+	unsigned int max_degree;            // corners of the busiest vertex
 	unsigned int scan_bar[2];           // the single-launch scans' barrier words (left zero by each scan)
 	unsigned int scan_bar2[2];          // those of the scans on the pass loop's second branch (the pick)
 	unsigned int scan_error;            // a single-launch scan's barrier gave up waiting
@@ -379,23 +379,31 @@ __global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned 
 	atomicAdd(&cnt[v], 1u);
 }
 
-// the corners of every vertex, raw and welded by remap, each corner keeping its slot in both
-// lists; an index of vcount or more is not counted and sets bad
-__global__ void kCountCornerLists(const unsigned int* __restrict__ idx, size_t n, const unsigned int* __restrict__ remap, size_t vcount,
-    unsigned int* __restrict__ cnt_raw, unsigned int* __restrict__ cnt_rm, unsigned int* __restrict__ slot_raw, unsigned int* __restrict__ slot_rm,
-    unsigned int* bad)
+// the corners of every vertex, each corner keeping its slot in its vertex's list; an index of
+// vcount or more is not counted and sets bad
+__global__ void kCountCornerLists(const unsigned int* __restrict__ idx, size_t n, size_t vcount, unsigned int* __restrict__ cnt,
+    unsigned int* __restrict__ slot, unsigned int* bad)
 {
-	size_t i = gtid();
-	if (i >= n)
-		return;
-	const unsigned int v = idx[i];
-	if (v >= vcount)
-	{
+	const size_t i = gtid();
+	if (i - (threadIdx.x & 31) >= n)
+		return; // the whole warp is past the corners
+	// corners of one vertex among the warp's 32 take their slots with one atomic add (the lists
+	// are sorted afterwards, so the order the slots give is arbitrary)
+	const unsigned int lane = threadIdx.x & 31;
+	unsigned int v = i < n ? idx[i] : ~0u;
+	if (i < n && v >= vcount)
 		atomicOr(bad, 1u);
-		return;
-	}
-	slot_raw[i] = atomicAdd(&cnt_raw[v], 1u);
-	slot_rm[i] = atomicAdd(&cnt_rm[remap[v]], 1u);
+	const bool valid = v < vcount;
+	if (!valid)
+		v = ~lane; // a key no vertex has, distinct per lane
+	const unsigned int peers = __match_any_sync(0xffffffffu, v);
+	const unsigned int leader = __ffs(peers) - 1;
+	unsigned int base = 0;
+	if (valid && lane == leader)
+		base = atomicAdd(&cnt[v], __popc(peers));
+	base = __shfl_sync(0xffffffffu, base, leader);
+	if (valid)
+		slot[i] = base + __popc(peers & ((1u << lane) - 1u));
 }
 
 // the largest count of corners[v] = off[v+1] - off[v]
@@ -483,13 +491,6 @@ __global__ void kIota(unsigned int* __restrict__ out, size_t n)
 	size_t i = gtid();
 	if (i < n)
 		out[i] = (unsigned int)i;
-}
-
-__global__ void kRemapKeys(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ remap, size_t n, unsigned int* __restrict__ keys)
-{
-	size_t i = gtid();
-	if (i < n)
-		keys[i] = remap[idx[i]];
 }
 
 __device__ __forceinline__ void cornerNeighbours(const unsigned int* __restrict__ idx, unsigned int p, unsigned int& next, unsigned int& prev)
@@ -792,11 +793,72 @@ __global__ void kSparseOut(const unsigned int* __restrict__ in, size_t n, const 
 // Per primary vertex r, in the order the reference accumulates into vertex_quadrics[r]:
 // face quadrics of its faces in face order (fillFaceQuadrics :1057-1082), then the point
 // quadric (fillVertexQuadrics :1084-1106), then border/seam edge quadrics in (face, edge,
-// i0-then-i1) order (fillEdgeQuadrics :1108-1157). `off/csr` is the remapped vertex -> corner
-// list with corners in increasing order.
+// i0-then-i1) order (fillEdgeQuadrics :1108-1157). The corners of r's position group in
+// increasing order are r's own list (`off/csr`, vertex -> corner lists with corners in
+// increasing order) when r is its only wedge, else the merge of its wedges' lists.
+
+// the border/seam edges of face f (vertices tv, kinds tk) that end at r's group, folded into Q
+__device__ __forceinline__ void foldEdges(Quadric& Q, unsigned int r, const unsigned int (&tv)[3], const unsigned char (&tk)[3], const float4* __restrict__ pos,
+    const unsigned int* __restrict__ remap, const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback)
+{
+#pragma unroll
+	for (int ed = 0; ed < 3; ++ed)
+	{
+		const int ne = ed == 2 ? 0 : ed + 1, pe = ed == 0 ? 2 : ed - 1;
+		unsigned int i0 = tv[ed], i1 = tv[ne];
+		unsigned char k0 = tk[ed], k1 = tk[ne];
+		bool b0 = k0 == kBorder || k0 == kSeam, b1 = k1 == kBorder || k1 == kSeam;
+		if (!b0 && !b1)
+			continue;
+		if (b0 && loop[i0] != i1)
+			continue;
+		if (b1 && loopback[i1] != i0)
+			continue;
+		bool to0 = remap[i0] == r, to1 = remap[i1] == r;
+		if (!to0 && !to1)
+			continue;
+		unsigned int i2 = tv[pe];
+		float weight = (k0 == kBorder || k1 == kBorder) ? 10.f : 0.5f;
+		V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1), p2 = ldpos(pos, i2);
+		Quadric E = qedge(p0, p1, p2, weight);
+		Quadric T = qtriangle(p0, p1, p2, weight);
+		T.w = 0;
+		qadd(E, T);
+		if (to0)
+			qadd(Q, E);
+		if (to1)
+			qadd(Q, E);
+	}
+}
+
+// the smallest corner above `after` (or any, when first) among the lists of r's wedges; ~0u past
+// the last. Each list is sorted, so a binary search per wedge finds its candidate.
+__device__ unsigned int nextGroupCorner(unsigned int r, unsigned int after, bool first, const unsigned int* __restrict__ wedge,
+    const unsigned int* __restrict__ off, const unsigned int* __restrict__ csr)
+{
+	unsigned int best = ~0u, v = r;
+	do
+	{
+		unsigned int lo = off[v], hi = off[v + 1];
+		while (lo < hi)
+		{
+			const unsigned int mid = (lo + hi) / 2;
+			if (first || csr[mid] > after)
+				hi = mid;
+			else
+				lo = mid + 1;
+		}
+		if (lo < off[v + 1])
+			best = min(best, csr[lo]);
+		v = wedge[v];
+	} while (v != r);
+	return best;
+}
+
 __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsigned int* __restrict__ off, const unsigned int* __restrict__ csr, size_t n,
-    const float4* __restrict__ pos, const unsigned int* __restrict__ remap, const unsigned char* __restrict__ kind, const unsigned int* __restrict__ loop,
-    const unsigned int* __restrict__ loopback, const unsigned char* __restrict__ lock, float factor, Quadric* __restrict__ vq, float4* __restrict__ vg)
+    const float4* __restrict__ pos, const unsigned int* __restrict__ remap, const unsigned int* __restrict__ wedge, const unsigned char* __restrict__ kind,
+    const unsigned int* __restrict__ loop, const unsigned int* __restrict__ loopback, const unsigned char* __restrict__ lock, float factor,
+    Quadric* __restrict__ vq, float4* __restrict__ vg)
 {
 	size_t vi = gtid();
 	if (vi >= n)
@@ -809,37 +871,54 @@ __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsign
 			vg[r] = make_float4(0.f, 0.f, 0.f, 0.f);
 		return;
 	}
+	const bool single = wedge[r] == r;
 	unsigned int b = off[r], e = off[r + 1];
 	Quadric Q = qzero();
 	float4 G = make_float4(0.f, 0.f, 0.f, 0.f); // volume gradient (update mode with attributes), the same face order
-	// corners in groups of kFillBatch: the group's loads are issued together (past the end the
-	// last corner is loaded again), then its faces fold in corner order
-	for (unsigned int j = b; j < e; j += kFillBatch)
+	if (single)
 	{
-		uint3 t[kFillBatch];
-#pragma unroll
-		for (unsigned int q = 0; q < kFillBatch; ++q)
+		// corners in groups of kFillBatch: the group's loads are issued together (past the end the
+		// last corner is loaded again), then its faces fold in corner order
+		for (unsigned int j = b; j < e; j += kFillBatch)
 		{
-			unsigned int f = csr[min(j + q, e - 1)] / 3;
-			t[q] = make_uint3(idx[f * 3 + 0], idx[f * 3 + 1], idx[f * 3 + 2]);
-		}
-		V3 p[kFillBatch][3];
+			uint3 t[kFillBatch];
 #pragma unroll
-		for (unsigned int q = 0; q < kFillBatch; ++q)
-		{
-			p[q][0] = ldpos(pos, t[q].x);
-			p[q][1] = ldpos(pos, t[q].y);
-			p[q][2] = ldpos(pos, t[q].z);
-		}
-#pragma unroll
-		for (unsigned int q = 0; q < kFillBatch; ++q)
-			if (j + q < e)
+			for (unsigned int q = 0; q < kFillBatch; ++q)
 			{
-				Quadric F = qtriangle(p[q][0], p[q][1], p[q][2], 1.f);
-				qadd(Q, F);
-				if (vg)
-					gadd(G, qvolumeGrad(p[q][0], p[q][1], p[q][2]));
+				unsigned int f = csr[min(j + q, e - 1)] / 3;
+				t[q] = make_uint3(idx[f * 3 + 0], idx[f * 3 + 1], idx[f * 3 + 2]);
 			}
+			V3 p[kFillBatch][3];
+#pragma unroll
+			for (unsigned int q = 0; q < kFillBatch; ++q)
+			{
+				p[q][0] = ldpos(pos, t[q].x);
+				p[q][1] = ldpos(pos, t[q].y);
+				p[q][2] = ldpos(pos, t[q].z);
+			}
+#pragma unroll
+			for (unsigned int q = 0; q < kFillBatch; ++q)
+				if (j + q < e)
+				{
+					Quadric F = qtriangle(p[q][0], p[q][1], p[q][2], 1.f);
+					qadd(Q, F);
+					if (vg)
+						gadd(G, qvolumeGrad(p[q][0], p[q][1], p[q][2]));
+				}
+		}
+	}
+	else
+	{
+		// a group of several wedges (rare): its corners one at a time, merged from the wedges' lists
+		for (unsigned int c = nextGroupCorner(r, 0, true, wedge, off, csr); c != ~0u; c = nextGroupCorner(r, c, false, wedge, off, csr))
+		{
+			const unsigned int f = c / 3;
+			const V3 p0 = ldpos(pos, idx[f * 3 + 0]), p1 = ldpos(pos, idx[f * 3 + 1]), p2 = ldpos(pos, idx[f * 3 + 2]);
+			Quadric F = qtriangle(p0, p1, p2, 1.f);
+			qadd(Q, F);
+			if (vg)
+				gadd(G, qvolumeGrad(p0, p1, p2));
+		}
 	}
 	if (vg)
 		vg[r] = G;
@@ -848,60 +927,57 @@ __global__ void kFillQuadrics(const unsigned int* __restrict__ idx, const unsign
 	V3 p = ldpos(pos, r);
 	Quadric P = qpoint(p.x, p.y, p.z, w);
 	qadd(Q, P);
-
-	unsigned int lastf = ~0u;
-	for (unsigned int j = b; j < e; j += kFillBatch)
+	// edge quadrics need an open edge at the vertex or a wedge of it: a manifold vertex is a
+	// single wedge with no open edge (kinds only move away from manifold after classification)
+	if (kind[r] == kManifold)
 	{
-		unsigned int fs[kFillBatch];
-		unsigned int tv[kFillBatch][3];
-		unsigned char tk[kFillBatch][3];
-#pragma unroll
-		for (unsigned int q = 0; q < kFillBatch; ++q)
+		stquadric(vq, r, Q);
+		return;
+	}
+
+	// a face shows up once per corner it has in the group: its edges fold in once
+	unsigned int lastf = ~0u;
+	if (single)
+	{
+		for (unsigned int j = b; j < e; j += kFillBatch)
 		{
-			fs[q] = csr[min(j + q, e - 1)] / 3;
+			unsigned int fs[kFillBatch];
+			unsigned int tv[kFillBatch][3];
+			unsigned char tk[kFillBatch][3];
 #pragma unroll
-			for (int c = 0; c < 3; ++c)
-				tv[q][c] = idx[fs[q] * 3 + c];
-		}
-#pragma unroll
-		for (unsigned int q = 0; q < kFillBatch; ++q)
-#pragma unroll
-			for (int c = 0; c < 3; ++c)
-				tk[q][c] = kind[tv[q][c]];
-#pragma unroll
-		for (unsigned int q = 0; q < kFillBatch; ++q)
-		{
-			if (j + q >= e || fs[q] == lastf)
-				continue;
-			lastf = fs[q];
-#pragma unroll
-			for (int ed = 0; ed < 3; ++ed)
+			for (unsigned int q = 0; q < kFillBatch; ++q)
 			{
-				const int ne = ed == 2 ? 0 : ed + 1, pe = ed == 0 ? 2 : ed - 1;
-				unsigned int i0 = tv[q][ed], i1 = tv[q][ne];
-				unsigned char k0 = tk[q][ed], k1 = tk[q][ne];
-				bool b0 = k0 == kBorder || k0 == kSeam, b1 = k1 == kBorder || k1 == kSeam;
-				if (!b0 && !b1)
-					continue;
-				if (b0 && loop[i0] != i1)
-					continue;
-				if (b1 && loopback[i1] != i0)
-					continue;
-				bool to0 = remap[i0] == r, to1 = remap[i1] == r;
-				if (!to0 && !to1)
-					continue;
-				unsigned int i2 = tv[q][pe];
-				float weight = (k0 == kBorder || k1 == kBorder) ? 10.f : 0.5f;
-				V3 p0 = ldpos(pos, i0), p1 = ldpos(pos, i1), p2 = ldpos(pos, i2);
-				Quadric E = qedge(p0, p1, p2, weight);
-				Quadric T = qtriangle(p0, p1, p2, weight);
-				T.w = 0;
-				qadd(E, T);
-				if (to0)
-					qadd(Q, E);
-				if (to1)
-					qadd(Q, E);
+				fs[q] = csr[min(j + q, e - 1)] / 3;
+#pragma unroll
+				for (int c = 0; c < 3; ++c)
+					tv[q][c] = idx[fs[q] * 3 + c];
 			}
+#pragma unroll
+			for (unsigned int q = 0; q < kFillBatch; ++q)
+#pragma unroll
+				for (int c = 0; c < 3; ++c)
+					tk[q][c] = kind[tv[q][c]];
+#pragma unroll
+			for (unsigned int q = 0; q < kFillBatch; ++q)
+			{
+				if (j + q >= e || fs[q] == lastf)
+					continue;
+				lastf = fs[q];
+				foldEdges(Q, r, tv[q], tk[q], pos, remap, loop, loopback);
+			}
+		}
+	}
+	else
+	{
+		for (unsigned int c = nextGroupCorner(r, 0, true, wedge, off, csr); c != ~0u; c = nextGroupCorner(r, c, false, wedge, off, csr))
+		{
+			const unsigned int f = c / 3;
+			if (f == lastf)
+				continue;
+			lastf = f;
+			const unsigned int tv[3] = {idx[f * 3 + 0], idx[f * 3 + 1], idx[f * 3 + 2]};
+			const unsigned char tk[3] = {kind[tv[0]], kind[tv[1]], kind[tv[2]]};
+			foldEdges(Q, r, tv, tk, pos, remap, loop, loopback);
 		}
 	}
 	stquadric(vq, r, Q);
@@ -2894,7 +2970,7 @@ struct Work
 	float* attr;
 	Quadric *vq, *aq;
 	float4* ag;
-	unsigned int *off_raw, *csr_raw, *off_rm, *csr_rm, *cnt, *tcnt;
+	unsigned int *off_raw, *csr_raw, *comp_off, *cnt, *tcnt;
 	unsigned int *keys_a, *vals_a, *keys_b, *vals_b;
 	unsigned int *res0, *res1;
 	unsigned int *adj_off, *fill;
@@ -2970,8 +3046,7 @@ size_t layout(Work& w, char* base, size_t I, size_t V, size_t ac, bool solve = f
 	w.ag = c.take<float4>(ac ? Vp * ac : 1);
 	w.off_raw = c.take<unsigned int>(Vp + 1);
 	w.csr_raw = c.take<unsigned int>(I + 1);
-	w.off_rm = c.take<unsigned int>(Vp + 1);
-	w.csr_rm = c.take<unsigned int>(I + 1);
+	w.comp_off = c.take<unsigned int>(Vp + 1);
 	w.cnt = c.take<unsigned int>(Vp + 1);
 	w.tcnt = c.take<unsigned int>(T + 2);
 	w.keys_a = c.take<unsigned int>(big);
@@ -3333,23 +3408,18 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// vertex -> corner lists in corner order: raw (classification, attribute quadrics) and
 	// remapped (position quadrics). Their offsets and largest degrees come before the host read
 	// below, which decides how the lists are filled.
-	// each corner's slot in its lists: raw in res1, remapped in serr (both free until the passes)
+	// each corner's slot in its vertex's list, in res1 (free until the passes)
 	unsigned int* const slot_raw = w.res1;
-	unsigned int* const slot_rm = w.serr;
-	// both lists' counts in one pass over the indices, in the offset arrays themselves (scanned in
-	// place); the count also validates the indices (the first kernel that reads them), and the
-	// host read below reports a bad index before anything else uses the lists
+	// the counts in one pass over the indices, in the offset array itself (scanned in place); the
+	// count also validates the indices (the first kernel that reads them), and the host read
+	// below reports a bad index before anything else uses the lists. A position group's corners
+	// are the merge of its wedges' lists (the quadric fill walks them), so no welded list is built.
 	MO_CUDA_CHECK(cudaMemsetAsync(w.off_raw, 0, (V + 1) * 4, stream));
-	MO_CUDA_CHECK(cudaMemsetAsync(w.off_rm, 0, (V + 1) * 4, stream));
 	if (I)
-		MO_LAUNCH(kCountCornerLists, gI, kThreads, 0, stream, w.res0, I, w.remap, V, w.off_raw, w.off_rm, slot_raw, slot_rm, &w.sc->bad_index);
+		MO_LAUNCH(kCountCornerLists, gI, kThreads, 0, stream, w.res0, I, V, w.off_raw, slot_raw, &w.sc->bad_index);
 	scanExclusive(w.off_raw, w.off_raw, V + 1, nullptr, w.scratch, stream, ss);
-	scanExclusive(w.off_rm, w.off_rm, V + 1, nullptr, w.scratch, stream, ss);
 	if (V)
-	{
-		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_raw, V, &w.sc->max_degree[0]);
-		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_rm, V, &w.sc->max_degree[1]);
-	}
+		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_raw, V, &w.sc->max_degree);
 	// flags now hold offsets; recompute flags from remap in the compaction kernel
 	readScalars();
 	if (hs->bad_index)
@@ -3367,33 +3437,20 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	}
 
 	const int vbits = bitsFor(V ? V - 1 : 0);
-	if (hs->max_degree[0] <= kCornerSortMax && hs->max_degree[1] <= kCornerSortMax)
+	if (hs->max_degree <= kCornerSortMax)
 	{
 		// few corners per vertex: fill and sort each list in place
 		if (I && V)
 		{
 			MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, nullptr, I, w.off_raw, slot_raw, w.csr_raw);
 			MO_LAUNCH(kCornerSort, gV, kThreads, 0, stream, w.off_raw, V, w.csr_raw);
-			if (D)
-			{
-				MO_LAUNCH(kCornerFill, gI, kThreads, 0, stream, w.res0, w.remap, I, w.off_rm, slot_rm, w.csr_rm);
-				MO_LAUNCH(kCornerSort, gV, kThreads, 0, stream, w.off_rm, V, w.csr_rm);
-			}
 		}
 	}
 	else
 	{
-		// a vertex with many corners: stable radix sorts by vertex
+		// a vertex with many corners: a stable radix sort by vertex
 		radixSortPairs(w.res0, nullptr, w.keys_a, w.csr_raw, w.keys_b, w.vals_b, I, vbits, w.scratch, stream, nullptr, ss);
-		if (D)
-		{
-			if (I)
-				MO_LAUNCH(kRemapKeys, gI, kThreads, 0, stream, w.res0, w.remap, I, w.cerr);
-			radixSortPairs(w.cerr, nullptr, w.keys_a, w.csr_rm, w.keys_b, w.vals_b, I, vbits, w.scratch, stream, nullptr, ss);
-		}
 	}
-	const unsigned int* off_rm = D ? w.off_rm : w.off_raw;
-	const unsigned int* csr_rm = D ? w.csr_rm : w.csr_raw;
 
 	// classification
 	if (V)
@@ -3432,7 +3489,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// quadrics
 	float factor = (m.options & kOptRegularizeLight) ? 1e-2f : ((m.options & kOptRegularize) ? 1e-1f : 1e-7f);
 	if (V)
-		MO_LAUNCH(kFillQuadrics, gV, kThreads, 0, stream, w.res0, off_rm, csr_rm, V, w.pos, w.remap, w.kind, w.loop, w.loopback, m.lock, factor, w.vq,
+		MO_LAUNCH(kFillQuadrics, gV, kThreads, 0, stream, w.res0, w.off_raw, w.csr_raw, V, w.pos, w.remap, w.wedge, w.kind, w.loop, w.loopback, m.lock, factor, w.vq,
 		    (solve && ac) ? w.vg : nullptr);
 	if (ac && V)
 	{
@@ -3459,9 +3516,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		comp_count = hs->dup_count;
 		MO_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (comp_count + 1) * 4, stream));
 		MO_LAUNCH(kCountKeys, gV, kThreads, 0, stream, w.comp, nullptr, V, w.cnt);
-		scanExclusive(w.cnt, w.off_rm, comp_count + 1, nullptr, w.scratch, stream, ss);
+		scanExclusive(w.cnt, w.comp_off, comp_count + 1, nullptr, w.scratch, stream, ss);
 		radixSortPairs(w.comp, nullptr, w.keys_a, w.vals_a, w.keys_b, w.vals_b, V, bitsFor(comp_count ? comp_count - 1 : 0), w.scratch, stream, nullptr, ss);
-		MO_LAUNCH(kMeasureComponents, gridFor(comp_count, kThreads), kThreads, 0, stream, comp_count, w.off_rm, w.vals_a, w.pos, w.comp_err);
+		MO_LAUNCH(kMeasureComponents, gridFor(comp_count, kThreads), kThreads, 0, stream, comp_count, w.comp_off, w.vals_a, w.pos, w.comp_err);
 	}
 	if (V)
 		MO_LAUNCH(kDualCount, gV, kThreads, 0, stream, w.off_raw, w.kind, V, &w.sc->dual);
