@@ -568,7 +568,8 @@ class ClockSampler:
 def kernel_traffic(kernel, workload):
     """DRAM bytes per launch of `kernel` on `workload` from a committed ncu summary
     (profiles/traffic.json: dram__bytes_read.sum + dram__bytes_write.sum averaged over the
-    captured launches), or None."""
+    captured launches, cold cache and, where captured, with the cache as the run left it), or
+    None."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.isfile(path):
         return None
@@ -576,7 +577,10 @@ def kernel_traffic(kernel, workload):
         entries = json.load(f)
     for e in entries:
         if e.get("kernel") == kernel and e.get("workload") == workload:
-            return {"dram_bytes_per_launch": int(e["dram_bytes_per_launch"]), "source": e["source"]}
+            out = {"dram_bytes_per_launch": int(e["dram_bytes_per_launch"]), "source": e["source"]}
+            if "dram_bytes_per_launch_in_run" in e:
+                out["dram_bytes_per_launch_in_run"] = int(e["dram_bytes_per_launch_in_run"])
+            return out
     return None
 
 
@@ -835,6 +839,8 @@ def bench_single(args, mg, torch, c, dist=None, world=1, rank=0, local=0, roofli
         tr = kernel_traffic(args.kernel, c["name"])
         if tr:
             roof["traffic"] = tr["dram_bytes_per_launch"]
+            if "dram_bytes_per_launch_in_run" in tr:
+                roof["traffic_in_run"] = tr["dram_bytes_per_launch_in_run"]
             roof["traffic_source"] = tr["source"]
 
     cpu = bit_exact = fp64 = None
