@@ -104,32 +104,32 @@ struct ThreadState
 	// (size_t)-1: the autotuner picks the route per size class (see routeAndRun)
 	size_t dropin_batch_limit = ~size_t(0);
 	bool autotune = true; // the single-mesh path's launch shape and the drop-in route are timed per size class
-	// drop-in copies of positions and attributes on streams of their own (another copy engine;
-	// the attributes are waited for only where they are first read)
-	cudaStream_t copy_stream[2] = {nullptr, nullptr};
-	cudaEvent_t copy_done[2] = {nullptr, nullptr};
+	// drop-in copies on a stream of their own, in the order the setup first reads them:
+	// positions, indices, attributes (one stream takes the whole host link, so a second one would
+	// only slow the first inputs down). Events: positions, attributes, indices copied.
+	cudaStream_t copy_stream = nullptr;
+	cudaEvent_t copy_done[3] = {nullptr, nullptr, nullptr};
 
 	void ensureCopyStreams()
 	{
-		for (int i = 0; i < 2; ++i)
-			if (!copy_stream[i])
-			{
-				MO_CUDA_CHECK(cudaStreamCreateWithFlags(&copy_stream[i], cudaStreamNonBlocking));
+		if (!copy_stream)
+			MO_CUDA_CHECK(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+		for (int i = 0; i < 3; ++i)
+			if (!copy_done[i])
 				MO_CUDA_CHECK(cudaEventCreateWithFlags(&copy_done[i], cudaEventDisableTiming));
-			}
 	}
 
 	void releaseCopyStreams()
 	{
-		for (int i = 0; i < 2; ++i)
+		for (int i = 0; i < 3; ++i)
 		{
 			if (copy_done[i])
 				cudaEventDestroy(copy_done[i]);
-			if (copy_stream[i])
-				cudaStreamDestroy(copy_stream[i]);
 			copy_done[i] = nullptr;
-			copy_stream[i] = nullptr;
 		}
+		if (copy_stream)
+			cudaStreamDestroy(copy_stream);
+		copy_stream = nullptr;
 	}
 
 	~ThreadState()
@@ -299,6 +299,9 @@ bool smallMeshOnBatch(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cu
 // in d_out and s.last.
 void routeAndRun(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st, bool allow_batch);
 
+// the index count above which routeAndRun sends every drop-in call to the single-mesh path
+size_t singlePathAbove(const ThreadState& s);
+
 size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size_t index_count, const float* vertex_positions, size_t vertex_count,
     size_t vertex_positions_stride, const float* vertex_attributes, size_t vertex_attributes_stride, const float* attribute_weights, size_t attribute_count,
     const unsigned char* vertex_lock, size_t target_index_count, float target_error, unsigned int options, float* result_error)
@@ -325,26 +328,30 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		unsigned char* d_lock = vertex_lock ? reinterpret_cast<unsigned char*>(base + b_idx + b_pos + b_attr) : nullptr;
 		unsigned int* d_out = reinterpret_cast<unsigned int*>(base + b_idx + b_pos + b_attr + b_lock);
 		cudaStream_t st = s.stream;
-		// large meshes on the single-mesh path: positions and attributes on their own copy
-		// streams; the setup waits for the positions at once and for the attributes where it
-		// first reads them
+		// large meshes on the single-mesh path: the copies on the copy stream, positions first (the
+		// setup's first kernels read only them), then indices, then attributes; the setup waits for
+		// each where it first reads it
 		const size_t pos_bytes = stridedExtent(vertex_count, vertex_positions_stride, 12);
 		const size_t attr_bytes = d_attr ? stridedExtent(vertex_count, vertex_attributes_stride, attribute_count * 4) : 0;
-		split = attr_bytes >= (size_t(1) << 20) && index_count > s.dropin_batch_limit;
-		if (index_count)
-			MO_CUDA_CHECK(cudaMemcpyAsync(d_idx, indices, index_count * 4, cudaMemcpyHostToDevice, st));
+		split = index_count * 4 + pos_bytes + attr_bytes >= (size_t(1) << 20) && index_count > singlePathAbove(s);
 		if (split)
 		{
 			s.ensureCopyStreams();
 			if (vertex_count)
-				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, pos_bytes, cudaMemcpyHostToDevice, s.copy_stream[0]));
-			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[0], s.copy_stream[0]));
-			MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, attr_bytes, cudaMemcpyHostToDevice, s.copy_stream[1]));
-			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[1], s.copy_stream[1]));
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, pos_bytes, cudaMemcpyHostToDevice, s.copy_stream));
+			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[0], s.copy_stream));
+			if (index_count)
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_idx, indices, index_count * 4, cudaMemcpyHostToDevice, s.copy_stream));
+			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[2], s.copy_stream));
+			if (d_attr)
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_attr, vertex_attributes, attr_bytes, cudaMemcpyHostToDevice, s.copy_stream));
+			MO_CUDA_CHECK(cudaEventRecord(s.copy_done[1], s.copy_stream));
 			MO_CUDA_CHECK(cudaStreamWaitEvent(st, s.copy_done[0], 0));
 		}
 		else
 		{
+			if (index_count)
+				MO_CUDA_CHECK(cudaMemcpyAsync(d_idx, indices, index_count * 4, cudaMemcpyHostToDevice, st));
 			if (vertex_count)
 				MO_CUDA_CHECK(cudaMemcpyAsync(d_pos, vertex_positions, pos_bytes, cudaMemcpyHostToDevice, st));
 			if (d_attr)
@@ -368,12 +375,16 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 		m.target_error = target_error;
 		m.options = options;
 		m.attributes_ready = split ? s.copy_done[1] : nullptr;
+		m.indices_ready = split ? s.copy_done[2] : nullptr;
 		routeAndRun(s, m, d_out, st, !split);
 		if (s.last.index_count)
 			MO_CUDA_CHECK(cudaMemcpyAsync(destination, d_out, s.last.index_count * 4, cudaMemcpyDeviceToHost, st));
 		MO_CUDA_CHECK(cudaStreamSynchronize(st));
-		if (split) // the caller's attribute buffer is read to the end before returning
+		if (split) // the caller's index and attribute buffers are read to the end before returning
+		{
 			MO_CUDA_CHECK(cudaEventSynchronize(s.copy_done[1]));
+			MO_CUDA_CHECK(cudaEventSynchronize(s.copy_done[2]));
+		}
 		if (result_error)
 			*result_error = s.last.result_error;
 		setStatus(meshoptgpu_StatusOk, "");
@@ -386,6 +397,7 @@ size_t simplifyHost(unsigned int* destination, const unsigned int* indices, size
 			ThreadState& s = state();
 			cudaEventSynchronize(s.copy_done[0]);
 			cudaEventSynchronize(s.copy_done[1]);
+			cudaEventSynchronize(s.copy_done[2]);
 		}
 		return failHost(destination, indices, index_count, result_error, statusOf(e), e.what());
 	}
@@ -823,6 +835,13 @@ void runSingle(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStrea
 	sp.setPassShape(best_bps, best_items);
 	std::lock_guard<std::mutex> g(g_shapes.lock);
 	g_shapes.shape[key] = std::make_pair(best_bps, best_items);
+}
+
+size_t singlePathAbove(const ThreadState& s)
+{
+	if (s.dropin_batch_limit != ~size_t(0))
+		return s.dropin_batch_limit;
+	return s.autotune ? kDropinSingleAlways : kDropinDefault;
 }
 
 void routeAndRun(ThreadState& s, const MeshDesc& m, unsigned int* d_out, cudaStream_t st, bool allow_batch)

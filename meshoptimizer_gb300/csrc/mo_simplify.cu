@@ -380,9 +380,10 @@ __global__ void kCountKeys(const unsigned int* __restrict__ idx, const unsigned 
 }
 
 // the corners of every vertex, each corner keeping its slot in its vertex's list; an index of
-// vcount or more is not counted and sets bad
+// vcount or more is not counted and sets bad. The indices are copied to res on the way (the
+// first pass's index buffer).
 __global__ void kCountCornerLists(const unsigned int* __restrict__ idx, size_t n, size_t vcount, unsigned int* __restrict__ cnt,
-    unsigned int* __restrict__ slot, unsigned int* bad)
+    unsigned int* __restrict__ slot, unsigned int* bad, unsigned int* __restrict__ res)
 {
 	const size_t i = gtid();
 	if (i - (threadIdx.x & 31) >= n)
@@ -391,6 +392,8 @@ __global__ void kCountCornerLists(const unsigned int* __restrict__ idx, size_t n
 	// are sorted afterwards, so the order the slots give is arbitrary)
 	const unsigned int lane = threadIdx.x & 31;
 	unsigned int v = i < n ? idx[i] : ~0u;
+	if (i < n)
+		res[i] = v;
 	if (i < n && v >= vcount)
 		atomicOr(bad, 1u);
 	const bool valid = v < vcount;
@@ -3252,6 +3255,8 @@ RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStre
 	unsigned int* total = reinterpret_cast<unsigned int*>(base += b_scan);
 
 	MO_CUDA_CHECK(cudaMemsetAsync(total, 0, 8, stream));
+	if (m.indices_ready)
+		MO_CUDA_CHECK(cudaStreamWaitEvent(stream, m.indices_ready, 0));
 	if (I)
 		MO_LAUNCH(kValidateIndices, gridFor(I, kThreads), kThreads, 0, stream, m.indices, I, V, total + 1);
 	unsigned int hv[2] = {0, 0};
@@ -3288,6 +3293,7 @@ RunResult Simplifier::runSparse(const MeshDesc& m, unsigned int* d_out, cudaStre
 	cm.positions_stride = 12;
 	cm.attributes = ac ? cattr : nullptr;
 	cm.attributes_ready = nullptr;
+	cm.indices_ready = nullptr;
 	cm.attributes_stride = ac * 4;
 	cm.lock = m.lock ? clock : nullptr;
 	cm.options = m.options & ~(kOptSparse | kOptInternalDebug); // debug bits are not produced for sparse subsets (:2602)
@@ -3389,8 +3395,6 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		MO_CUDA_CHECK(cudaEventRecord(ev[0], stream));
 
 	MO_CUDA_CHECK(cudaMemsetAsync(w.sc, 0, sizeof(Scalars), stream));
-	if (I)
-		MO_CUDA_CHECK(cudaMemcpyAsync(w.res0, m.indices, I * 4, cudaMemcpyDeviceToDevice, stream));
 
 	// ---- setup
 	const unsigned int gV = gridFor(V, kThreads), gI = gridFor(I, kThreads);
@@ -3415,8 +3419,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 	// below reports a bad index before anything else uses the lists. A position group's corners
 	// are the merge of its wedges' lists (the quadric fill walks them), so no welded list is built.
 	MO_CUDA_CHECK(cudaMemsetAsync(w.off_raw, 0, (V + 1) * 4, stream));
+	if (m.indices_ready)
+		MO_CUDA_CHECK(cudaStreamWaitEvent(stream, m.indices_ready, 0));
 	if (I)
-		MO_LAUNCH(kCountCornerLists, gI, kThreads, 0, stream, w.res0, I, V, w.off_raw, slot_raw, &w.sc->bad_index);
+		MO_LAUNCH(kCountCornerLists, gI, kThreads, 0, stream, m.indices, I, V, w.off_raw, slot_raw, &w.sc->bad_index, w.res0);
 	scanExclusive(w.off_raw, w.off_raw, V + 1, nullptr, w.scratch, stream, ss);
 	if (V)
 		MO_LAUNCH(kMaxDegree, gV, kThreads, 0, stream, w.off_raw, V, &w.sc->max_degree);

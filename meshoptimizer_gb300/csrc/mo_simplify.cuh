@@ -41,6 +41,8 @@ struct MeshDesc
 	// when set, the attributes are still arriving: the stream waits for this event before it
 	// first reads them (their copy overlaps the setup that does not need them)
 	cudaEvent_t attributes_ready = nullptr;
+	// the same for the indices (their copy overlaps the setup's position-only kernels)
+	cudaEvent_t indices_ready = nullptr;
 };
 
 // Per-pass counters, the same quantities the reference prints under TRACE
