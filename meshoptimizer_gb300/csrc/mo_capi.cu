@@ -254,41 +254,157 @@ struct HostCopy
 	size_t bytes;
 };
 
-// Host memcpy of many pieces, spread over up to 8 threads in contiguous runs of about equal
-// bytes when there is enough to copy (packing a batch into pinned staging and scattering its
-// results are memory-bound host loops).
-void parallelCopies(const std::vector<HostCopy>& copies)
+// Host threads for the batch path's packing and scattering copies (memory-bound host loops),
+// started on first use and kept for the process (never joined: the threads only ever wait for
+// the next job). One job at a time: a caller that finds the pool busy copies on its own thread.
+class CopyPool
 {
-	size_t total = 0;
-	for (const HostCopy& c : copies)
-		total += c.bytes;
-	unsigned int hw = std::max(1u, std::thread::hardware_concurrency());
-	size_t threads = std::min<size_t>(std::min<size_t>(8, hw), total >> 21); // one thread per 2 MiB at least
-	auto run = [&](size_t b, size_t e) {
+public:
+	static CopyPool& get()
+	{
+		static CopyPool* pool = new CopyPool(); // left to the process: no teardown order at exit
+		return *pool;
+	}
+
+	// copies[0, n) in `parts` contiguous runs given by cut (cut[0] = 0, cut[parts] = n); the calling
+	// thread takes the last run. False when the pool is busy (nothing copied).
+	bool run(const HostCopy* copies, const std::vector<size_t>& cut)
+	{
+		std::unique_lock<std::mutex> own(busy_, std::try_to_lock);
+		if (!own.owns_lock())
+			return false;
+		const size_t parts = cut.size() - 1;
+		{
+			std::lock_guard<std::mutex> g(m_);
+			while (workers_.size() + 1 < parts)
+			{
+				const size_t id = workers_.size();
+				workers_.emplace_back([this, id]() { work(id); });
+				workers_.back().detach();
+			}
+			copies_ = copies;
+			cut_ = cut;
+			pending_ = parts - 1;
+			++generation_;
+		}
+		cv_.notify_all();
+		copyRun(copies, cut[parts - 1], cut[parts]);
+		std::unique_lock<std::mutex> g(m_);
+		done_.wait(g, [&]() { return pending_ == 0; });
+		return true;
+	}
+
+	static void copyRun(const HostCopy* copies, size_t b, size_t e)
+	{
 		for (size_t i = b; i < e; ++i)
 			memcpy(copies[i].dst, copies[i].src, copies[i].bytes);
-	};
+	}
+
+private:
+	void work(size_t id)
+	{
+		size_t seen = 0;
+		for (;;)
+		{
+			const HostCopy* copies;
+			size_t b, e;
+			{
+				std::unique_lock<std::mutex> g(m_);
+				cv_.wait(g, [&]() { return generation_ != seen; });
+				seen = generation_;
+				if (id + 1 >= cut_.size() - 1)
+					continue; // this job has fewer runs than workers
+				copies = copies_;
+				b = cut_[id];
+				e = cut_[id + 1];
+			}
+			copyRun(copies, b, e);
+			std::lock_guard<std::mutex> g(m_);
+			if (--pending_ == 0)
+				done_.notify_one();
+		}
+	}
+
+	std::mutex busy_, m_;
+	std::condition_variable cv_, done_;
+	std::vector<std::thread> workers_;
+	const HostCopy* copies_ = nullptr;
+	std::vector<size_t> cut_;
+	size_t generation_ = 0, pending_ = 0;
+};
+
+// Host memcpy of many pieces, spread over up to 16 threads in contiguous runs of about equal
+// bytes when there is enough to copy (one thread per 256 KiB at least: one host thread copies
+// about 10 GB/s, the link to the GPU takes 200).
+void parallelCopies(const HostCopy* copies, size_t n)
+{
+	size_t total = 0;
+	for (size_t i = 0; i < n; ++i)
+		total += copies[i].bytes;
+	const unsigned int hw = std::max(1u, std::thread::hardware_concurrency());
+	const size_t threads = std::min<size_t>(std::min<size_t>(16, hw), total >> 18);
 	if (threads <= 1)
 	{
-		run(0, copies.size());
+		CopyPool::copyRun(copies, 0, n);
 		return;
 	}
 	std::vector<size_t> cut(1, 0);
-	size_t acc = 0, share = total / threads;
-	for (size_t i = 0; i < copies.size() && cut.size() < threads; ++i)
+	size_t acc = 0;
+	const size_t share = total / threads;
+	for (size_t i = 0; i < n && cut.size() < threads; ++i)
 	{
 		acc += copies[i].bytes;
 		if (acc >= share * cut.size())
 			cut.push_back(i + 1);
 	}
-	cut.push_back(copies.size());
-	std::vector<std::thread> pool;
-	for (size_t t = 0; t + 2 < cut.size(); ++t)
-		pool.emplace_back(run, cut[t], cut[t + 1]);
-	run(cut[cut.size() - 2], cut.back());
-	for (std::thread& th : pool)
-		th.join();
+	cut.push_back(n);
+	if (!CopyPool::get().run(copies, cut))
+		CopyPool::copyRun(copies, 0, n);
 }
+
+void parallelCopies(const std::vector<HostCopy>& copies)
+{
+	parallelCopies(copies.data(), copies.size());
+}
+
+// Offsets of distinct (pointer, bytes) keys in insertion order: an open-addressing table over a
+// flat array (no allocation per key), for packing the arrays that meshes of a batch share once.
+class PieceTable
+{
+public:
+	explicit PieceTable(size_t keys)
+	{
+		size_t cap = 16;
+		while (cap < 2 * keys)
+			cap <<= 1;
+		slots_.assign(cap, Slot{nullptr, 0, 0});
+	}
+	// the offset stored for (p, bytes), or ~0 after storing `at` for it
+	size_t findOrInsert(const void* p, size_t bytes, size_t at)
+	{
+		const size_t mask = slots_.size() - 1;
+		size_t h = (reinterpret_cast<uintptr_t>(p) * 0x9E3779B97F4A7C15ull ^ bytes * 0xC2B2AE3D27D4EB4Full) >> 17;
+		for (;; ++h)
+		{
+			Slot& sl = slots_[h & mask];
+			if (!sl.p)
+			{
+				sl = Slot{p, bytes, at};
+				return ~size_t(0);
+			}
+			if (sl.p == p && sl.bytes == bytes)
+				return sl.at;
+		}
+	}
+
+private:
+	struct Slot
+	{
+		const void* p;
+		size_t bytes, at;
+	};
+	std::vector<Slot> slots_;
+};
 
 // Runs a small mesh (device pointers) on the batch kernel when the mesh's options allow; returns
 // false to leave it to the single-mesh path.
@@ -1253,22 +1369,21 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 		// every distinct vertex, attribute and lock array once (meshes of a sparse group share
 		// them); outputs follow all inputs on the device
 		size_t in_bytes = 0, out_words = 0;
-		std::map<std::pair<const void*, size_t>, size_t> shared;
+		PieceTable shared(3 * mesh_count);
 		std::vector<std::pair<const void*, size_t>> pieces; // (source, bytes) in pack order
+		pieces.reserve(2 * mesh_count);
 		auto place = [&](const void* p, size_t bytes, bool dedupe) -> size_t {
 			if (!p || !bytes)
 				return ~size_t(0);
+			const size_t at = in_bytes;
 			if (dedupe)
 			{
-				auto it = shared.find({p, bytes});
-				if (it != shared.end())
-					return it->second;
+				const size_t seen = shared.findOrInsert(p, bytes, at);
+				if (seen != ~size_t(0))
+					return seen;
 			}
-			size_t at = in_bytes;
 			in_bytes = (in_bytes + bytes + 15) & ~size_t(15);
 			pieces.push_back({p, bytes});
-			if (dedupe)
-				shared.emplace(std::make_pair(p, bytes), at);
 			return at;
 		};
 		std::vector<size_t> off_idx(mesh_count), off_pos(mesh_count), off_attr(mesh_count), off_lock(mesh_count), off_out(mesh_count);
@@ -1284,7 +1399,12 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 			out_words += m.index_count;
 		}
 		char* h = static_cast<char*>(s.batch_host.ensure(in_bytes + 16));
+		char* d = static_cast<char*>(s.batch_io.ensure(align256(in_bytes) + out_words * 4 + 256));
+		unsigned int* d_out = reinterpret_cast<unsigned int*>(d + align256(in_bytes));
+		cudaStream_t st = s.stream;
 		{
+			// packed and uploaded in chunks of about a quarter of the bytes (4 MiB at least): the
+			// upload of one chunk runs while the next one is packed
 			std::vector<HostCopy> copies;
 			copies.reserve(pieces.size());
 			size_t at = 0;
@@ -1293,12 +1413,19 @@ int meshoptgpu_simplifyBatchHost(const meshoptgpu_BatchMesh* meshes, size_t mesh
 				copies.push_back(HostCopy{h + at, pc.first, pc.second});
 				at = (at + pc.second + 15) & ~size_t(15);
 			}
-			parallelCopies(copies);
+			const size_t chunk = std::max<size_t>(size_t(4) << 20, in_bytes / 4);
+			for (size_t b = 0; b < copies.size();)
+			{
+				size_t e = b, bytes = 0;
+				while (e < copies.size() && (e == b || bytes < chunk))
+					bytes += copies[e++].bytes;
+				parallelCopies(copies.data() + b, e - b);
+				const size_t lo = static_cast<size_t>(static_cast<char*>(copies[b].dst) - h);
+				const size_t hi = e < copies.size() ? static_cast<size_t>(static_cast<char*>(copies[e].dst) - h) : in_bytes;
+				MO_CUDA_CHECK(cudaMemcpyAsync(d + lo, h + lo, hi - lo, cudaMemcpyHostToDevice, st));
+				b = e;
+			}
 		}
-		char* d = static_cast<char*>(s.batch_io.ensure(align256(in_bytes) + out_words * 4 + 256));
-		unsigned int* d_out = reinterpret_cast<unsigned int*>(d + align256(in_bytes));
-		cudaStream_t st = s.stream;
-		MO_CUDA_CHECK(cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, st));
 		std::vector<BatchDesc> descs(mesh_count);
 		std::vector<int> attr_of(mesh_count);
 		AttrMaps maps;
