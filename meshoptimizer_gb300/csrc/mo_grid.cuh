@@ -12,6 +12,24 @@ namespace mogpu
 
 constexpr unsigned int kBarrierSpinLimit = 1u << 25; // x >= 32 ns sleep: seconds, never reached in a normal run
 
+// an arrival that publishes everything the block wrote before it (the block barrier ahead of it
+// orders the other threads' writes before this thread's release)
+__device__ __forceinline__ unsigned int arriveRelease(unsigned int* p)
+{
+	unsigned int old;
+	asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+	return old;
+}
+
+// a poll that, once it sees the last arrival, makes the other blocks' writes visible to this
+// block (the block barrier after it passes them on to the other threads)
+__device__ __forceinline__ unsigned int pollAcquire(const unsigned int* p)
+{
+	unsigned int v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
 // bar[0] counts the arrivals of all barriers of the launch and is zero before it. Barrier i ends
 // when the count reaches (i + 1) * gridDim.x: no block can arrive at barrier i + 1 before every
 // block has arrived at barrier i, so an arrival that reads old = n belongs to barrier n / G.
@@ -21,12 +39,10 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 	__syncthreads();
 	if (threadIdx.x == 0)
 	{
-		volatile unsigned int* count = bar;
-		__threadfence();
-		const unsigned int old = atomicAdd(bar, 1u);
+		const unsigned int old = arriveRelease(bar);
 		const unsigned int target = (old / gridDim.x + 1) * gridDim.x;
 		unsigned int spins = 0;
-		while ((int)(*count - target) < 0)
+		while ((int)(pollAcquire(bar) - target) < 0)
 		{
 			if (++spins > limit)
 			{
@@ -35,7 +51,6 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 			}
 			__nanosleep(32);
 		}
-		__threadfence();
 	}
 	__syncthreads();
 }
@@ -50,11 +65,9 @@ __device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int*
 	__syncthreads();
 	if (threadIdx.x == 0)
 	{
-		volatile unsigned int* count = bar;
-		__threadfence();
-		atomicAdd(bar, 1u);
+		arriveRelease(bar);
 		unsigned int spins = 0;
-		while (*count < gridDim.x)
+		while (pollAcquire(bar) < gridDim.x)
 		{
 			if (++spins > limit)
 			{
@@ -63,7 +76,6 @@ __device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int*
 			}
 			__nanosleep(32);
 		}
-		__threadfence();
 		if (atomicAdd(bar + 1, 1u) == gridDim.x - 1)
 		{
 			atomicExch(bar, 0u);
