@@ -1920,21 +1920,27 @@ enum
 	kPhEmit = 7,
 };
 
+// kept in shared memory (one thread of one block uses it), so it holds no registers in the
+// kernel's other threads; the round trace's count is kept beside it
 struct PhaseClock
 {
-	long long last;
-	long long acc[8];
-	__device__ void start()
+	long long* s; // [0, 8): cycles per phase, [8]: the last lap's clock, [9]: rounds traced
+	__device__ void start(const Scalars* sc)
 	{
-		last = clock64();
+		s[8] = clock64();
 		for (int i = 0; i < 8; ++i)
-			acc[i] = 0;
+			s[i] = 0;
+		s[9] = sc->trace_count;
+	}
+	__device__ long long last() const
+	{
+		return s[8];
 	}
 	__device__ void lap(int phase)
 	{
 		long long t = clock64();
-		acc[phase] += t - last;
-		last = t;
+		s[phase] += t - s[8];
+		s[8] = t;
 	}
 };
 
@@ -1947,10 +1953,11 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 	__shared__ unsigned int s_app[4];
 	__shared__ unsigned int s_stage[2][kStageChunk]; // candidates passed to stage B, and kept for stage C (wait)
 	__shared__ unsigned int s_commits;               // this block's commits so far
-	PhaseClock pc;
+	__shared__ long long s_clock[10];
+	PhaseClock pc{s_clock};
 	const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
 	if (timer)
-		pc.start();
+		pc.start(a.sc);
 	__shared__ unsigned int sm[3][33];
 	Scalars* sc = a.sc;
 	const unsigned int G = gridDim.x;
@@ -2043,10 +2050,11 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 		unsigned int n = K1 - K0;             // all blocks'
 		bool first = true;
 		unsigned int guard = 0;
+		unsigned int gerr = __ldcg(&sc->grid_error); // read again with each round's total, in one round trip
 		while (n)
 		{
 			++round;
-			if (++guard > count + 1 || __ldcg(&sc->grid_error))
+			if (++guard > count + 1 || gerr)
 				break;
 			active_sum += n;
 			const unsigned int* cur = a.list[round & 1] + region;
@@ -2179,17 +2187,19 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 			gridBarrier(sc->bar, &sc->grid_error);
 			if (timer)
 			{
-				long long before = pc.last;
+				long long before = pc.last();
 				pc.lap(kPhRounds);
-				unsigned int tc = sc->trace_count;
+				const unsigned int tc = (unsigned int)s_clock[9];
 				if (tc < 512)
 				{
 					sc->trace[2 * tc] = n;
-					sc->trace[2 * tc + 1] = (unsigned int)((pc.last - before) >> 4);
+					sc->trace[2 * tc + 1] = (unsigned int)((pc.last() - before) >> 4);
 					sc->trace_count = tc + 1;
+					s_clock[9] = tc + 1;
 				}
 			}
-			unsigned int nn = __ldcg(next_total);
+			const unsigned int nn = __ldcg(next_total);
+			gerr = __ldcg(&sc->grid_error);
 			if (nn >= n)
 			{
 				if (gtid() == 0)
@@ -2334,7 +2344,7 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 	{
 		if (timer)
 			for (int i = 0; i < 8; ++i)
-				atomicAdd(&sc->phase_cycles[i], (unsigned long long)pc.acc[i]);
+				atomicAdd(&sc->phase_cycles[i], (unsigned long long)s_clock[i]);
 		if (gtid() == 0)
 		{
 			sc->rounds = round - round_base;
@@ -2422,7 +2432,7 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 	{
 		pc.lap(kPhEmit);
 		for (int i = 0; i < 8; ++i)
-			atomicAdd(&sc->phase_cycles[i], (unsigned long long)pc.acc[i]);
+			atomicAdd(&sc->phase_cycles[i], (unsigned long long)s_clock[i]);
 	}
 }
 
