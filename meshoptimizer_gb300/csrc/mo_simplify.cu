@@ -397,9 +397,9 @@ __global__ void kCountCornerLists(const unsigned int* __restrict__ idx, size_t n
 	if (i < n && v >= vcount)
 		atomicOr(bad, 1u);
 	const bool valid = v < vcount;
-	if (!valid)
-		v = ~lane; // a key no vertex has, distinct per lane
-	const unsigned int peers = __match_any_sync(0xffffffffu, v);
+	// lanes without a valid corner share a key and are masked out of every group (a vertex id
+	// equal to that key stays correct)
+	const unsigned int peers = __match_any_sync(0xffffffffu, valid ? v : ~0u) & __ballot_sync(0xffffffffu, valid);
 	const unsigned int leader = __ffs(peers) - 1;
 	unsigned int base = 0;
 	if (valid && lane == leader)
@@ -1120,8 +1120,9 @@ __global__ void kCountCorners(const unsigned int* __restrict__ res, size_t n, co
 	// their slots with one atomic add; a list's order is arbitrary anyway
 	const unsigned int lane = threadIdx.x & 31;
 	const bool valid = i < n;
-	const unsigned int v = valid ? remap[res[i]] : ~lane; // past the end: a key no vertex has
-	const unsigned int peers = __match_any_sync(0xffffffffu, v);
+	const unsigned int v = valid ? remap[res[i]] : ~0u;
+	// lanes past the end share a key and are masked out of every group
+	const unsigned int peers = __match_any_sync(0xffffffffu, v) & __ballot_sync(0xffffffffu, valid);
 	const unsigned int leader = __ffs(peers) - 1;
 	unsigned int base = 0;
 	if (valid && lane == leader)
