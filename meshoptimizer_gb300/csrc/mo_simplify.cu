@@ -2255,6 +2255,10 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 			unsigned long long F = (unsigned long long)bb.y + eF;
 			unsigned int M = max(bb.z, eM);
 			const unsigned long long egoal0 = goal / 2;
+			// the error goal moves with the flip count only: the last one read is kept with its
+			// position, and read at all only when the rule's other two terms hold
+			unsigned long long goal_at = ~0ull;
+			float error_goal = FLT_MAX;
 			for (unsigned int k = t0; k < t1; ++k)
 			{
 				float e = __uint_as_float(__ldg(a.serr + k));
@@ -2263,11 +2267,15 @@ __global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(Perf
 					reason = 1;
 				else if (T >= goal)
 					reason = 2;
-				else
+				else if (T > goal / 6 && e > __uint_as_float(M))
 				{
-					unsigned long long eg = egoal0 + F;
-					float error_goal = eg < count ? 1.5f * __uint_as_float(__ldg(a.serr + eg)) : FLT_MAX;
-					if (e > error_goal && e > __uint_as_float(M) && T > goal / 6)
+					const unsigned long long eg = egoal0 + F;
+					if (eg != goal_at)
+					{
+						goal_at = eg;
+						error_goal = eg < count ? 1.5f * __uint_as_float(__ldg(a.serr + eg)) : FLT_MAX;
+					}
+					if (e > error_goal)
 						reason = 3;
 				}
 				if (reason)
