@@ -1945,11 +1945,15 @@ struct PhaseClock
 	}
 };
 
-#ifndef MO_PERFORM_MIN_BLOCKS
-#define MO_PERFORM_MIN_BLOCKS 4 // resident blocks per SM the pass kernel is compiled for (64 registers)
+#ifndef MO_PERFORM_THREADS
+#define MO_PERFORM_THREADS 256 // threads per block of the pass kernel
 #endif
+#ifndef MO_PERFORM_MIN_BLOCKS
+#define MO_PERFORM_MIN_BLOCKS (1024 / MO_PERFORM_THREADS) // resident blocks per SM the pass kernel is compiled for (64 registers)
+#endif
+constexpr unsigned int kPerformThreads = MO_PERFORM_THREADS;
 
-__global__ void __launch_bounds__(kThreads, MO_PERFORM_MIN_BLOCKS) kPerform(PerformArgs a)
+__global__ void __launch_bounds__(kPerformThreads, MO_PERFORM_MIN_BLOCKS) kPerform(PerformArgs a)
 {
 	__shared__ unsigned int s_app[4];
 	__shared__ unsigned int s_stage[2][kStageChunk]; // candidates passed to stage B, and kept for stage C (wait)
@@ -3204,7 +3208,7 @@ Simplifier::Simplifier(int device) : device_(device)
 	MO_CUDA_CHECK(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
 	int sms = 0, per_sm = 0;
 	MO_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kThreads, 0));
+	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kPerform, kPerformThreads, 0));
 	MO_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&solve_per_sm_, kSolvePositions, kThreads, 0));
 	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
 	MO_CUDA_CHECK(cudaFuncSetAttribute(kKeyScatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kKeyScatterSmem)));
@@ -3673,10 +3677,10 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 		const PassLive* lv = &w.sc->live;
 
 		// grid of the pass kernel
-		unsigned int blocks = std::max(1u, std::min(perform_blocks_, gridFor(std::max(std::max(capn, V), T0), kThreads)));
+		unsigned int blocks = std::max(1u, std::min(perform_blocks_, gridFor(std::max(std::max(capn, V), T0), kPerformThreads)));
 		if (tuning_.perform_grid_cap > 0)
 			blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
-		if (size_t(blocks) * kThreads > kListSlack)
+		if (size_t(blocks) * kPerformThreads > kListSlack)
 			throw std::runtime_error("kPerform grid exceeds the candidate list slack");
 
 		LaunchProbe& lp = probe();
@@ -3780,7 +3784,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				pa.live = lv;
 				void* params[] = {&pa};
 				lp.launches++;
-				MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, cs));
+				MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kPerformThreads), params, 0, cs));
 				MO_LAUNCH(kPassEnd, 1, 1, 0, cs, w.sc, handle, unsigned(T0 + 1));
 			}
 			catch (...)
@@ -3908,15 +3912,15 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->cut, 0xFF, 8, stream));
 			MO_CUDA_CHECK(cudaMemsetAsync(&w.sc->done, 0, 12, stream));
 			MO_CUDA_CHECK(cudaMemcpyAsync(&w.sc->result_error_bits, &result_error_bits, 4, cudaMemcpyHostToDevice, stream));
-			unsigned int want = gridFor(std::max(std::max(C, V), T), kThreads);
+			unsigned int want = gridFor(std::max(std::max(C, V), T), kPerformThreads);
 			unsigned int blocks = std::max(1u, std::min(perform_blocks_, want));
 			if (tuning_.perform_grid_cap > 0)
 				blocks = std::min(blocks, unsigned(tuning_.perform_grid_cap));
-			if (size_t(blocks) * kThreads > kListSlack)
+			if (size_t(blocks) * kPerformThreads > kListSlack)
 				throw std::runtime_error("kPerform grid exceeds the candidate list slack");
 			void* params[] = {&pa};
 			cudaEvent_t e0 = probeBegin("kPerform", stream);
-			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kThreads), params, 0, stream));
+			MO_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)kPerform, dim3(blocks), dim3(kPerformThreads), params, 0, stream));
 			probeEnd(e0, stream);
 		}
 		if (timed)
