@@ -10,7 +10,11 @@
 namespace mogpu
 {
 
-constexpr unsigned int kBarrierSpinLimit = 1u << 25; // x >= 32 ns sleep: seconds, never reached in a normal run
+#ifndef MO_BARRIER_SLEEP_NS
+#define MO_BARRIER_SLEEP_NS 32
+#endif
+constexpr unsigned int kBarrierSpinLimit = 1u << 25; // x >= 32 ns sleep (or an L2 round trip): seconds, never reached in a normal run
+constexpr unsigned int kBarrierSleepNs = MO_BARRIER_SLEEP_NS; // between polls
 
 // an arrival that publishes everything the block wrote before it (the block barrier ahead of it
 // orders the other threads' writes before this thread's release)
@@ -49,7 +53,8 @@ __device__ __forceinline__ void gridBarrier(unsigned int* bar, unsigned int* err
 				atomicOr(err, 1u);
 				break;
 			}
-			__nanosleep(32);
+			if (kBarrierSleepNs)
+				__nanosleep(kBarrierSleepNs);
 		}
 	}
 	__syncthreads();
@@ -74,7 +79,8 @@ __device__ __forceinline__ void gridBarrierOnce(unsigned int* bar, unsigned int*
 				atomicOr(err, 1u);
 				break;
 			}
-			__nanosleep(32);
+			if (kBarrierSleepNs)
+				__nanosleep(kBarrierSleepNs);
 		}
 		if (atomicAdd(bar + 1, 1u) == gridDim.x - 1)
 		{

@@ -36,8 +36,14 @@ namespace
 constexpr int kThreads = 256;
 constexpr int kStopTile = 1024; // sorted candidates per block in the stop-rule scan
 constexpr size_t kPinnedBytes = 16384; // host readback buffer of the scalars block
-constexpr unsigned int kStageChunk = 2048; // candidates of a block taken through the decision stages at a time
-constexpr unsigned int kStageItems = 4;    // candidates per thread in the first decision stage
+#ifndef MO_STAGE_CHUNK
+#define MO_STAGE_CHUNK 2048
+#endif
+#ifndef MO_STAGE_ITEMS
+#define MO_STAGE_ITEMS 2
+#endif
+constexpr unsigned int kStageChunk = MO_STAGE_CHUNK; // candidates of a block taken through the decision stages at a time
+constexpr unsigned int kStageItems = MO_STAGE_ITEMS; // candidates per thread in the first decision stage
 
 // State of the device-resident pass loop: the counts each pass's kernels read instead of
 // launch parameters, so that one recorded pass can be replayed until the loop ends.
