@@ -71,7 +71,10 @@ struct PassLive
 // The sorted positions a pass decides before its stop rules cut grow from pass to pass relative to
 // its triangle goal; the next pass's first window is this much larger than the last pass needed,
 // so that it rarely needs a second window (a second window costs a full set of decision rounds).
-constexpr double kWindowMargin = 1.5;
+#ifndef MO_WINDOW_MARGIN
+#define MO_WINDOW_MARGIN 1.5
+#endif
+constexpr double kWindowMargin = MO_WINDOW_MARGIN;
 
 __host__ __device__ inline double nextWindowFactor(double base, unsigned long long goal, unsigned long long evaluated)
 {
