@@ -516,7 +516,10 @@ __device__ __forceinline__ void cornerNeighbours(const unsigned int* __restrict_
 // ---------------------------------------------------------------- setup: classification
 
 constexpr unsigned int kOpenEdgesRegs = 12; // vertices with at most this many corners search in registers
-constexpr unsigned int kFillBatch = 4;      // corners whose loads kFillQuadrics issues together
+#ifndef MO_FILL_BATCH
+#define MO_FILL_BATCH 2
+#endif
+constexpr unsigned int kFillBatch = MO_FILL_BATCH; // corners whose loads kFillQuadrics issues together
 
 // openout (stored in loop) and openinc (stored in loopback) of classifyVertices :370-396,
 // from the vertex's own raw half-edge list: ~0u for none, the unique open neighbour, or the
