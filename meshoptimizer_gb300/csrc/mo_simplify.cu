@@ -1290,6 +1290,11 @@ __global__ void __launch_bounds__(kThreads) kPickEmit(const unsigned int* __rest
 
 // ---------------------------------------------------------------- pass: rank
 
+#ifndef MO_RANK_THREADS
+#define MO_RANK_THREADS 256
+#endif
+constexpr unsigned int kRankThreads = MO_RANK_THREADS; // threads per block of kRank (one candidate each)
+
 // rankEdgeCollapses :1374-1450, one candidate per thread. The candidate {v0, v1, bidi} becomes,
 // in place, {i0, i1, error bits, kind of i0} with the cheaper direction first; its decision
 // record {r0, r1, begin and end of r0's adjacency}, its error bits and its kind are written
@@ -3733,7 +3738,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			lp.capturing = true;
 			try
 			{
-				const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads), gC = gridFor(capn, kThreads);
+				const unsigned int gI = gridFor(I, kThreads), gT0 = gridFor(T0, kThreads);
 				// the pick (its own scan scratch and barrier words) and the adjacency are independent:
 				// two branches of the body, joined before the rank
 				cudaStream_t cs2 = capture2_;
@@ -3752,7 +3757,7 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 				MO_LAUNCH(kAdjFill, gT0, kThreads, 0, cs, nullptr, T0, w.remap, w.adj_off, nullptr, w.adj, lv, I);
 				MO_CUDA_CHECK(cudaStreamWaitEvent(cs, join_, 0));
 				MO_LAUNCH(kPassPrep, 1, 1, 0, cs, w.sc);
-				MO_LAUNCH(kRank, gC, kThreads, 0, cs, capn, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+				MO_LAUNCH(kRank, gridFor(capn, kRankThreads), kRankThreads, 0, cs, capn, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 				    w.adj_off, w.attr, w.aq, w.ag, ac, lv);
 				sortCandidates(w, capn, cs, lv, ss, sort_items);
 				PerformArgs pa;
@@ -3866,10 +3871,9 @@ RunResult Simplifier::run(const MeshDesc& m, unsigned int* d_out, cudaStream_t s
 			MO_CUDA_CHECK(cudaEventRecord(ev[4], stream));
 		if (C == 0)
 			break;
-		const unsigned int gC = gridFor(C, kThreads);
 
 		// rank + sort
-		MO_LAUNCH(kRank, gC, kThreads, 0, stream, C, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
+		MO_LAUNCH(kRank, gridFor(C, kRankThreads), kRankThreads, 0, stream, C, w.crec, w.cring, w.cerr, w.ckind, w.pos, w.vq, w.remap, w.wedge, w.kind, w.loop, w.loopback,
 		    w.adj_off, w.attr, w.aq, w.ag, ac, nullptr);
 		if (timed)
 			MO_CUDA_CHECK(cudaEventRecord(ev[5], stream));
