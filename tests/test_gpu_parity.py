@@ -232,6 +232,22 @@ def test_sparse_subset_of_large_buffer(port):
     _compare_with_oracle(port, tri, pos, W.target_count(len(tri), 0.5), 1e-2, mg.SimplifySparse | mg.SimplifyLockBorder)
 
 
+def test_large_dropin_overlapped_uploads(port):
+    """Drop-in calls above the batch route's size limit copy their inputs on a stream of their own
+    (positions, then indices, then attributes), and the setup waits for each where it first reads
+    it: a whole mesh with attributes and lock flags, and a sparse subset of a larger buffer with
+    attributes (the sparse path reads the indices before anything else), against the oracle."""
+    idx, pos, attr, w = W.octa_sphere(7, seed=41)  # 131,072 triangles
+    rng = np.random.default_rng(41)
+    lock = rng.choice(np.array([0, 0, 0, 0, 1, 2, 4], np.uint8), size=len(pos))
+    _compare_with_oracle(port, idx, pos, W.target_count(len(idx), 0.2), 1e-2, 0, attributes=attr, weights=w, lock=lock)
+    big, bpos = W.heightfield(300, seed=42, amp=0.05)
+    battr = rng.random((len(bpos), 3)).astype(np.float32)
+    sub = big.reshape(-1, 3)[20000:60000].reshape(-1).astype(np.uint32)  # 120,000 indices of 536,406
+    _compare_with_oracle(port, sub, bpos, W.target_count(len(sub), 0.3), 1e-2, mg.SimplifySparse, attributes=battr,
+                         weights=np.array([0.5, 1.0, 0.25], np.float32))
+
+
 @pytest.mark.parametrize("seed", range(10))
 def test_prune(port, seed):
     """Prune: disconnected pieces of different sizes removed in the pass loop and the cleanup loop."""
