@@ -513,24 +513,31 @@ def load_workload(name):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples every 200 ms while running."""
+    """nvidia-smi clock/throttle samples every 25 ms while running; entering waits (up to 3 s)
+    for the first sample, so that the sampling runs before the timed region starts, and the
+    summary keeps the samples stamped between entering and leaving (all of them if none is)."""
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index=0):
         self.device_index = device_index
         self.proc = None
         self.lines = []
+        self.t_enter = self.t_exit = None
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "25",
                                           "-i", str(self.device_index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.time()
+            while not self.lines and self.proc.poll() is None and time.time() - t0 < 3.0:
+                time.sleep(0.005)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.t_enter = time.time()
         return self
 
     def _read(self):
@@ -538,6 +545,7 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self.t_exit = time.time()
         if self.proc:
             self.proc.terminate()
             try:
@@ -548,16 +556,23 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
-            f = [x.strip() for x in l.split(",")]
-            if len(f) < 9:
-                continue
+        rows = [[x.strip() for x in l.split(",")] for l in self.lines]
+        rows = [f for f in rows if len(f) >= 10]
+
+        def stamp(f):
             try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
+                return time.mktime(time.strptime(f[0].split(".")[0], "%Y/%m/%d %H:%M:%S")) + float("0." + f[0].split(".")[1])
+            except (ValueError, IndexError):
+                return None
+
+        inside = [f for f in rows if self.t_enter and self.t_exit and stamp(f) is not None and self.t_enter - 0.05 <= stamp(f) <= self.t_exit + 0.05]
+        for f in inside or rows:
+            try:
+                sm.append(float(f[2]))
+                mx.append(float(f[3]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[5:9]):
+            for n, v in zip(names, f[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         if not sm:
