@@ -164,3 +164,40 @@ def test_batch_rejects_prune():
     with pytest.raises(mg.SimplifyError) as e:
         mg.simplify_batch([dict(indices=idx, positions=pos, target=0, error=1e-2, options=mg.SimplifyPrune)])
     assert e.value.status == mg.STATUS_UNSUPPORTED
+
+
+def test_batch_host_concurrent_callers(port):
+    """Host batches from several threads at once: their packing and scattering copies share one
+    pool of host threads (a caller that finds it busy copies on its own thread), and each thread
+    has its own stream and scratch. Every result equals the same batch called alone, and the
+    first batch's meshes equal the oracle's."""
+    import threading
+
+    sets = [[dict(indices=idx, positions=pos, target=W.target_count(len(idx), 0.5), error=2e-2, options=mg.SimplifyLockBorder)
+             for idx, pos in W.sphere_patches(256, seed=70 + t, levels=7)] for t in range(4)]
+    want = [mg.simplify_batch(ms) for ms in sets]
+    for m, (out, err) in zip(sets[0][:16], want[0][:16]):
+        ref, ref_err = port.simplify("port", m["indices"], m["positions"], m["target"], m["error"], m["options"])
+        assert np.array_equal(out, ref)
+    got = [[] for _ in sets]
+    errors = []
+
+    def run(t):
+        try:
+            for _ in range(3):
+                got[t].append(mg.simplify_batch(sets[t]))
+        except Exception as e:  # reported below, on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(t,)) for t in range(len(sets))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for t, runs in enumerate(got):
+        assert len(runs) == 3
+        for res in runs:
+            for i, ((out, err), (wout, werr)) in enumerate(zip(res, want[t])):
+                assert np.array_equal(out, wout), (t, i)
+                assert err == werr, (t, i)
